@@ -1,0 +1,333 @@
+"""Benchmark of the explicit SPH step: particle-steps/s on one GB300.
+
+Workload (BASELINE configs 3/4): coupled thermo-mechanical Johnson-Cook
+cylinder compression, R = 25 mm, H = 50 mm, dx = 0.5 mm, seeded jittered
+lattice (~0.79M particles), consistent Newton return map, Taylor-Quinney
+plastic heat, platen at -10 m/s.  A "step" is one pass of the Fraser loop
+body over all particles (density, rates + stress, acceleration, integration,
+heat, neighbour rebuild every 5 steps).
+
+`value` is the mixed-precision form (FP32 pair loops / stress / flux, FP64
+positions, velocities, plastic strain, Newton, reductions; MLP warm start
+when trained weights are loaded) with inputs resident in HBM; `plain_fp64`
+is the plain-FP64 form of the same code; `e2e` times the drop-in call
+(create, setters from host arrays, solve, read-back of the output fields)
+with host clocks.  `cpu_baseline` times the FP64 CPU oracle on the host cores.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s, mixed+MLP vs plain FP64 on 1 GB300 at ≤1e-3 rel L2 err"
+UNIT = "particle-steps/s"
+WORKLOAD = "jc_thermomech_compression_R25mm_H50mm_dx0.5mm"
+
+# Algorithmic bytes per particle for each kernel: every per-particle field the
+# kernel reads or writes, once, in the form it is stored (neighbour gathers are
+# served by L1/L2; the neighbour-index list is counted separately).
+BYTES_MODEL = {
+    "mixed": {"density": 128, "stress": 248, "accel": 104, "integrate": 328, "thermal": 96},
+    "fp64": {"density": 120, "stress": 416, "accel": 144, "integrate": 264, "thermal": 112},
+}
+NB_INDEX_BYTES = 4  # per neighbour per pair pass
+KERNEL_IDS = {"density": 1, "stress": 2, "accel": 3, "integrate": 4, "thermal": 5}
+PAIR_KERNELS = ("density", "stress", "accel", "thermal")
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_domain(sc, opts):
+    from weldformgpu_gb300 import Domain_d
+    from weldformgpu_gb300 import scenarios as S
+    return S.load(Domain_d(sc["n"]), sc, opts)
+
+
+def base_options():
+    return {"return_map": 1, "thermal": 1, "taylor_quinney": 0.9, "rebuild_every": 5,
+            "rebuild_current_positions": 1, "rebuild_after_yield": 0, "energy_mode": 1}
+
+
+def per_kernel_ms(d, kernels, reps=1):
+    """Event-timed duration of each kernel kind over `reps` steps each."""
+    out = {}
+    for k in kernels:
+        d.set_option("profile_kernel", KERNEL_IDS[k])
+        _, kms, kl, _ = d.time_steps(reps)
+        out[k] = kms / max(kl, 1)
+    d.set_option("profile_kernel", 0)
+    return out
+
+
+def run_form(sc, form, steps, warmup, mlp_params=None):
+    opts = base_options()
+    opts["precision"] = 1 if form == "mixed" else 0
+    d = build_domain(sc, opts)
+    if mlp_params is not None:
+        d.set_mlp_weights(mlp_params)
+        d.set_option("mlp", 1)
+    d.step(warmup)
+    kernels = ["density", "stress", "accel", "integrate", "thermal"]
+    kms = per_kernel_ms(d, kernels)
+    dominant = max(kms, key=kms.get)
+    d.set_option("profile_kernel", KERNEL_IDS[dominant])
+    it0, c0 = d.get_scalar("newton_iters"), d.get_scalar("newton_calls")
+    with ClockSampler() as clk:
+        elapsed, kernel_ms, kernel_launches, launches = d.time_steps(steps)
+    d.set_option("profile_kernel", 0)
+    it1, c1 = d.get_scalar("newton_iters"), d.get_scalar("newton_calls")
+    fields = {f: d.get_field(f) for f in ("u", "pl_strain", "sigma_eq", "T")}
+    d.close()
+    return dict(elapsed_ms=elapsed, kernel_ms=kernel_ms, kernel_launches=kernel_launches,
+                launches=launches, dominant=dominant, per_kernel_ms=kms, clocks=clk.summary(),
+                newton_iters_per_call=(it1 - it0) / max(c1 - c0, 1.0), fields=fields,
+                steps_done=warmup + len(kernels) + steps)
+
+
+def run_e2e(sc, form, steps, mlp_params=None):
+    """The drop-in call from host buffers, host wall clock around everything."""
+    from weldformgpu_gb300 import Domain_d
+    from weldformgpu_gb300 import scenarios as S
+    opts = base_options()
+    opts["precision"] = 1 if form == "mixed" else 0
+    n = sc["n"]
+    t0 = time.perf_counter()
+    d = S.load(Domain_d(n), sc, opts)
+    if mlp_params is not None:
+        d.set_mlp_weights(mlp_params)
+        d.set_option("mlp", 1)
+    d.step(steps)
+    out = [d.get_field(f) for f in ("u", "pl_strain", "sigma_eq", "T")]
+    d.close()
+    t1 = time.perf_counter()
+    h2d = n * (3 * 8 + 8 + 4 + 1 + 8 + 8)           # x, m, id, not_write, Cs, T
+    d2h = sum(a.nbytes for a in out)
+    return n * steps / (t1 - t0), h2d / steps, d2h / steps
+
+
+def cpu_baseline(sc, budget_s=12.0):
+    """FP64 CPU oracle (all host threads) on the same workload, bounded sample."""
+    from oracle import oracle as O
+    from weldformgpu_gb300 import scenarios as S
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    opts = base_options()
+    d = S.load(O.OracleDomain(sc["n"]), sc, opts)
+    d.step(1)                                      # set-up + neighbour search + 1 step
+    t0 = time.perf_counter()
+    done = 0
+    while True:
+        d.step(1)
+        done += 1
+        if time.perf_counter() - t0 > budget_s or done >= 50:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": sc["n"] * done / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d Fraser steps (after 1 set-up step) of the full %d-particle workload, "
+                      "FP64 oracle (oracle/wf_oracle.c), OpenMP" % (done, sc["n"])}
+
+
+def rel_l2(a, b):
+    den = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / (den if den > 0 else 1.0))
+
+
+def dist_setup(n_gpus):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, None
+    import torch.distributed as dist
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    dist.init_process_group("gloo")
+    return rank, ws, dist
+
+
+def reduce_max(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--small", action="store_true", help="small workload (quick check)")
+    args = ap.parse_args()
+    warmup = max(args.warmup, 3)
+    rank, ws, dist = dist_setup(args.gpus)
+
+    from weldformgpu_gb300 import build as B
+    B.build()
+    from weldformgpu_gb300 import scenarios as S
+    sc = S.jc_compression(R=0.006, H=0.012) if args.small else S.jc_compression()
+    n = sc["n"]
+    config = {"workload": WORKLOAD if not args.small else WORKLOAD + "_small", "particles": n,
+              "dx_m": sc["dx"], "dt_s": sc["dt"], "nnb": 56, "rebuild_every": 5,
+              "return_map": "jc_newton_rtol1e-10", "thermal": "coupled, Taylor-Quinney 0.9",
+              "l2": "inputs larger than L2 (state %.0f MB > 129 MB)" % (n * 1100 / 1e6),
+              "parallelism": "replicas" if ws > 1 else "single"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = cpu_baseline(sc, budget_s=max(5.0, min(30.0, 1.5 * args.steps)))
+        line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT,
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": warmup,
+                "higher_is_better": True, "data": "synthetic", "dtype": "f64",
+                "config": config, "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0},
+                "note": "reference CPU path = the FP64 oracle port (the reference's kernels "
+                        "compiled for the CPU exist only where the reference tree is present)"}
+        print(json.dumps(line))
+        return
+
+    mlp = None
+    mlp_path = os.path.join(ROOT, "weldformgpu_gb300", "mlp_jc_weights.npy")
+    if os.path.exists(mlp_path):
+        mlp = np.load(mlp_path)
+    plain = run_form(sc, "fp64", args.steps, warmup)
+    mixed = run_form(sc, "mixed", args.steps, warmup, mlp)
+    t_mixed = reduce_max(dist, mixed["elapsed_ms"])
+    t_plain = reduce_max(dist, plain["elapsed_ms"])
+    value = ws * n * args.steps / (t_mixed / 1e3)
+    plain_value = ws * n * args.steps / (t_plain / 1e3)
+    errs = {f: rel_l2(mixed["fields"][f] - (20.0 if f == "T" else 0.0),
+                      plain["fields"][f] - (20.0 if f == "T" else 0.0))
+            for f in ("u", "pl_strain", "sigma_eq", "T")}
+    e2e_steps = max(args.steps, 100)
+    e2e_v, h2d, d2h = run_e2e(sc, "mixed", e2e_steps, mlp)
+    e2e_v = reduce_max(dist, e2e_v) * ws if dist else e2e_v
+
+    peak, peak_kind = measured_peaks()
+    dom = mixed["dominant"]
+    per_launch_ms = mixed["kernel_ms"] / max(mixed["kernel_launches"], 1)
+    alg_bytes = BYTES_MODEL["mixed"][dom] * n
+    if dom in PAIR_KERNELS:
+        alg_bytes_idx = alg_bytes + NB_INDEX_BYTES * 56 * n
+    else:
+        alg_bytes_idx = alg_bytes
+    achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            tj = json.load(f)
+        if dom in tj.get("mixed", {}):
+            traffic = tj["mixed"][dom] * n
+    step_bytes = sum(BYTES_MODEL["mixed"].values()) * n
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": warmup, "ms_per_step": t_mixed / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": config,
+        "plain_fp64": {"value": plain_value, "ms_per_step": t_plain / args.steps,
+                       "dominant_kernel": plain["dominant"],
+                       "per_kernel_ms": plain["per_kernel_ms"],
+                       "newton_iters_per_plastic_particle": plain["newton_iters_per_call"]},
+        "speedup_vs_plain_fp64": value / plain_value,
+        "rel_l2_vs_fp64": errs,
+        "mlp_warm_start": mlp is not None,
+        "newton_iters_per_plastic_particle": mixed["newton_iters_per_call"],
+        "per_kernel_ms": mixed["per_kernel_ms"],
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": traffic, "alg_bytes_per_launch": alg_bytes,
+                     "alg_bytes_with_nb_index": alg_bytes_idx,
+                     "achieved_with_nb_index": alg_bytes_idx / (per_launch_ms / 1e3) / 1e9,
+                     "step_achieved_GBs": step_bytes / (t_mixed / args.steps / 1e3) / 1e9},
+        "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "steps": e2e_steps,
+                "note": "create + setters from host arrays + solve + read-back, host clock"},
+        "gpu_launches": mixed["launches"],
+        "clocks": mixed["clocks"],
+    }
+    if rank == 0:
+        line["cpu_baseline"] = cpu_baseline(sc)
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

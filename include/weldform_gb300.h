@@ -1,0 +1,155 @@
+/*
+ * weldform_gb300.h — C ABI of the GB300-native explicit SPH solid-mechanics step.
+ *
+ * The library replaces the device half of WeldFormGPU's `SPH::Domain_d`
+ * (src/cuda/Domain_d.cuh:101-426): the same setters, the same solve entry
+ * points (MechFraserSolve / MechSolve / ThermalSolve) and the same physics,
+ * behind plain C functions that take host pointers and sizes.  Every entry
+ * point names the reference member or host statement it replaces.
+ *
+ * Conventions
+ *   - Every function returns an int status: WF_OK (0) or a negative WF_ERR_*.
+ *     No function exits the process; wf_last_error() describes the failure.
+ *   - Arrays of per-particle vectors are interleaved xyz (like double3[n]);
+ *     symmetric tensors are 6 values per particle in the reference's flat
+ *     order [xx, yy, zz, xy, yz, xz] (src/cuda/tensor3.cu:95-100).
+ *   - Host pointers are only read (or written, for getters) during the call.
+ *   - Particle indices at the ABI are the caller's original indices; the
+ *     library keeps its own cell-sorted order on the device.
+ *   - One handle per host thread; a handle owns one CUDA stream.
+ */
+#ifndef WELDFORM_GB300_H
+#define WELDFORM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WF_OK            0
+#define WF_ERR_ARG      -1   /* bad argument (null pointer, size, unknown name)      */
+#define WF_ERR_CUDA     -2   /* CUDA runtime error                                   */
+#define WF_ERR_STATE    -3   /* call made in the wrong state (e.g. no positions)     */
+#define WF_ERR_ALLOC    -4   /* device or host allocation failed                     */
+#define WF_ERR_NUMERIC  -5   /* a kernel reported NaN/Inf or an overflowed list       */
+#define WF_ERR_IO       -6   /* file could not be opened / parsed                    */
+
+/* Neighbour-list capacity per particle: CUDA_MAX_NEIGHBORS
+ * (src/cuNSearch/src/cuNSearchKernels.cuh:6). */
+#define WF_MAX_NEIGHBORS 70
+
+/* Material model ids: src/cuda/Material.cuh:6-8. */
+#define WF_BILINEAR      0
+#define WF_HOLLOMON      1
+#define WF_JOHNSON_COOK  2
+
+/* Material constants, in the JSON `const[]` order the reference reads
+ * (src/WeldFormGPU.cu:753-792): bilinear const[0] = Et; JC const[] =
+ * [A, B, n, C, eps_0, m, T_m, T_t]; Hollomon const[] = [K, m]. */
+typedef struct wf_material {
+  int32_t model;
+  int32_t reserved;
+  double  E;        /* youngsModulus                                  */
+  double  nu;       /* poissonsRatio                                  */
+  double  sy0;      /* yieldStress0 (initial sigma_y, Hollomon sy0)   */
+  double  Et;       /* bilinear tangent modulus                       */
+  double  K_hol;    /* Hollomon K                                     */
+  double  m_hol;    /* Hollomon exponent m                            */
+  double  A, B, n, C, eps0, m, Tm, Tt;   /* Johnson-Cook             */
+} wf_material;
+
+typedef struct wf_domain wf_domain;
+
+/* ---- lifecycle ------------------------------------------------------- */
+/* Domain_d::SetDimension (src/cuda/Domain_d.cu:19-234): allocates the SoA
+ * arena for `particle_count` particles; solid_part_count = particle_count. */
+int         wf_create(wf_domain** out, int64_t particle_count);
+int         wf_destroy(wf_domain* d);
+const char* wf_last_error(const wf_domain* d);
+const char* wf_version(void);
+
+/* ---- reference setters (src/cuda/Domain_d.cu:307-477) ----------------- */
+int wf_set_h(wf_domain* d, double h);                /* Set_h        :416 */
+int wf_set_density(wf_domain* d, double rho);        /* SetDensity   :458 (rho and rho_0) */
+int wf_set_shear_modulus(wf_domain* d, double G);    /* SetShearModulus :447 */
+int wf_set_sigma_y(wf_domain* d, double sy);         /* SetSigmay    :437 */
+int wf_set_conductivity(wf_domain* d, double k);     /* SetConductivity :427 */
+int wf_set_heat_cap(wf_domain* d, double cp);        /* SetHeatCap   :469 */
+int wf_set_cs(wf_domain* d, const double* cs);       /* SetCs        :331 (per particle) */
+int wf_set_free(wf_domain* d, const uint8_t* is_free);   /* SetFreePart :307 */
+int wf_set_id(wf_domain* d, const int32_t* id);          /* SetID       :317 */
+
+/* ---- public fields the reference's main writes directly --------------- */
+int wf_set_positions(wf_domain* d, const double* x);     /* cudaMemcpy x, WeldFormGPU.cu:704 */
+int wf_set_velocities(wf_domain* d, const double* v);    /* cudaMemcpy v, WeldFormGPU.cu:711 */
+int wf_set_mass(wf_domain* d, const double* m);          /* cudaMemcpy m, WeldFormGPU.cu:822 */
+int wf_set_not_write_surf_id(wf_domain* d, const uint8_t* flags); /* WeldFormGPU.cu:858 */
+int wf_set_solid_count(wf_domain* d, int64_t n_solid);   /* solid_part_count, WeldFormGPU.cu:453 */
+int wf_set_time_step(wf_domain* d, double dt);           /* deltat, WeldFormGPU.cu:906 */
+int wf_set_artificial_viscosity(wf_domain* d, double alpha, double beta); /* Alpha/Beta :292 */
+int wf_set_material(wf_domain* d, const wf_material* mat);    /* materials[0], WeldFormGPU.cu:749-800 */
+int wf_add_velocity_bc(wf_domain* d, int32_t zone_id,
+                       double vx, double vy, double vz);  /* bConds, WeldFormGPU.cu:457-485 */
+int wf_set_temperature(wf_domain* d, const double* T);   /* T (Domain_d::CopyData, Domain_d.cu:490) */
+int wf_set_thermal_bc(wf_domain* d, const int32_t* bc_t); /* BC_T: 0 none, 1 convection */
+int wf_set_convection(wf_domain* d, double h_conv, double T_inf); /* h_conv_double, T_inf */
+
+/* Options with no reference field (precision, return map, rebuild cadence…).
+ * Keys are listed in the library documentation; unknown keys fail. */
+int wf_set_option(wf_domain* d, const char* key, double value);
+
+/* ---- solvers ------------------------------------------------------------ */
+/* Domain_d::MechFraserSolve (src/cuda/SolverFraser.cu:30-409). */
+int wf_mech_fraser_solve(wf_domain* d, double tf, double dt_out);
+/* Domain_d::MechSolve (declared at src/cuda/Domain_d.cuh:310, never
+ * defined): bound to the Fraser loop. */
+int wf_mech_solve(wf_domain* d, double tf, double dt_out);
+/* Domain_d::ThermalSolve (src/cuda/Thermal.cu:188-260). */
+int wf_thermal_solve(wf_domain* d, double tf);
+/* `nsteps` iterations of the Fraser loop body (SolverFraser.cu:164-398). */
+int wf_step(wf_domain* d, int64_t nsteps);
+/* Rebuild the neighbour list now (cuNSearch find_neighbors, cuNSearch.cu:111). */
+int wf_find_neighbors(wf_domain* d);
+
+/* ---- outputs (caller's particle order) --------------------------------- */
+int wf_get_field(wf_domain* d, const char* name, double* out);
+int wf_get_field_i32(wf_domain* d, const char* name, int32_t* out);
+/* counts[n]; lists[n*WF_MAX_NEIGHBORS], neighbour ids in search order. */
+int wf_get_neighbors(wf_domain* d, int32_t* counts, int32_t* lists);
+int wf_get_scalar(wf_domain* d, const char* name, double* out);
+/* Domain_d::WriteCSV (src/cuda/Domain_d.cu:556-587), same columns. */
+int wf_write_csv(wf_domain* d, const char* path);
+
+/* ---- host domain set-up (src/Domain.cpp) --------------------------------- */
+/* Two-call protocol: pass x == NULL to get the particle count, then a buffer
+ * of 3*count doubles.  Return value: the count. */
+/* Domain::AddCylinderLength (src/Domain.cpp:490-573); *mass = pi R^2 Lz rho / N */
+int64_t wf_gen_cylinder(double x0, double y0, double z0, double Rxy, double Lz, double r,
+                        double density, double* x, double* mass);
+/* Domain::AddBoxLength, cubic packing (src/Domain.cpp:296-338) */
+int64_t wf_gen_box(double x0, double y0, double z0, double Lx, double Ly, double Lz, double r,
+                   double density, double* x, double* mass);
+/* Cubic lattice of spacing dx clipped to a cylinder (axis z, base z = 0),
+ * jittered by U[-jitter, jitter]*dx per coordinate from a splitmix64 stream;
+ * no reference counterpart (synthetic benchmark workload). */
+int64_t wf_gen_cylinder_lattice(double R, double H, double dx, double jitter, uint64_t seed,
+                                double* x);
+/* Domain::AssignZone (src/Domain.cpp:989-1005): tags particles inside the
+ * inclusive box [start, end]; returns how many. */
+int64_t wf_assign_zone(const double* x, int64_t n, const double* start, const double* end,
+                       int32_t zone_id, int32_t* id, uint8_t* not_write);
+
+/* ---- measurement -------------------------------------------------------- */
+/* Runs `nsteps` steps on the handle's stream between CUDA events and
+ * returns the elapsed device time; per-kernel event pairs are recorded
+ * around the kernel named by wf_set_option("profile_kernel", id). */
+int wf_time_steps(wf_domain* d, int64_t nsteps, double* elapsed_ms,
+                  double* kernel_ms, int64_t* kernel_launches,
+                  int64_t* total_launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WELDFORM_GB300_H */

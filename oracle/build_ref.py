@@ -1,0 +1,61 @@
+"""Builds oracle/_ref/libwfref.so: the reference's own kernel sources compiled
+for the CPU, used only to pin the oracle (test infrastructure).
+
+The sources are read where they lie in the reference tree (default
+/root/reference, or $WF_REFERENCE_DIR); nothing is copied.  The reference's
+CMake build is not used: two translation units written here
+(ref_domain.cpp, ref_nsearch.cpp) #include the reference's kernel files, and
+cuda_host_shim.h stands in for the CUDA built-ins.  Flags keep IEEE
+semantics (-ffp-contract=off), like the reference's --fmad=false.
+
+Usage: python oracle/build_ref.py   (no-op when the reference tree is absent)
+"""
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT_DIR = os.path.join(HERE, "_ref")
+OUT = os.path.join(OUT_DIR, "libwfref.so")
+
+
+def reference_dir():
+    return os.environ.get("WF_REFERENCE_DIR", "/root/reference")
+
+
+def build(verbose=False):
+    ref = reference_dir()
+    src = os.path.join(ref, "src")
+    if not os.path.isdir(os.path.join(src, "cuda")):
+        return None
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    inc = [
+        "-I" + os.path.join(HERE, "ref_shim"),
+        "-I" + os.path.join(src, "cuda"),
+        "-I" + src,
+        "-I" + os.path.join(src, "cuNSearch", "include"),
+        "-I" + os.path.join(src, "cuNSearch", "src"),
+        "-I" + os.path.join(src, "cuNSearch", "Utils"),
+        "-I" + os.path.join(cuda, "include"),
+        "-I" + os.path.join(cuda, "include", "cccl"),
+    ]
+    flags = ["-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-w",
+             "-DTHRUST_DEVICE_SYSTEM=THRUST_DEVICE_SYSTEM_CPP", "-Wno-cpp"]
+    os.makedirs(OUT_DIR, exist_ok=True)
+    objs = []
+    for tu in ("ref_domain.cpp", "ref_nsearch.cpp"):
+        obj = os.path.join(OUT_DIR, tu.replace(".cpp", ".o"))
+        cmd = ["g++"] + flags + inc + ["-c", os.path.join(HERE, tu), "-o", obj]
+        if verbose:
+            print(" ".join(cmd))
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("building %s failed:\n%s" % (tu, r.stderr))
+        objs.append(obj)
+    subprocess.run(["g++", "-shared", "-o", OUT] + objs + ["-lm"], check=True)
+    return OUT
+
+
+if __name__ == "__main__":
+    out = build(verbose="-v" in sys.argv)
+    print(out or "reference tree not found: oracle/_ref not built")

@@ -1,0 +1,301 @@
+"""Python binding of the CPU oracle (oracle/liboracle.so) and of the
+reference's kernels compiled for the CPU (oracle/_ref/libwfref.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline arm.  The product package never imports this module.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from weldformgpu_gb300 import _abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libwfref.so")
+NB = _abi.WF_MAX_NEIGHBORS
+
+# -O2 and -ffp-contract=off: IEEE double arithmetic with no fused multiply-add,
+# as the reference's --fmad=false build (src/CMakeLists.txt:29).
+CFLAGS = ["-std=gnu11", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared"]
+
+
+def build(force=False):
+    """Compiles oracle/wf_oracle.c into oracle/liboracle.so."""
+    src = os.path.join(HERE, "wf_oracle.c")
+    if (not force and os.path.exists(LIB_PATH)
+            and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src)
+            and os.path.getmtime(LIB_PATH) >= os.path.getmtime(os.path.join(HERE, "wf_oracle.h"))):
+        return LIB_PATH
+    subprocess.run(["gcc"] + CFLAGS + ["-o", LIB_PATH, src, "-lm"], check=True)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        _abi.bind(L, "wfo_", _abi.SIGNATURES)
+        L.wfo_run_stage.restype = C.c_int
+        L.wfo_run_stage.argtypes = [C.c_void_p, C.c_char_p]
+        L.wfo_set_field.restype = C.c_int
+        L.wfo_set_field.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_double)]
+        L.wfo_set_threads.restype = C.c_int
+        L.wfo_set_threads.argtypes = [C.c_int]
+        L.wfo_set_mlp_params.restype = C.c_int
+        L.wfo_set_mlp_params.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        for name in ("wfo_gen_cylinder_ref", "wfo_gen_box_cubic"):
+            fn = getattr(L, name)
+            fn.restype = C.c_int64
+            fn.argtypes = [C.c_double] * 8 + [C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.wfo_gen_cylinder_ref.argtypes = [C.c_double] * 7 + [C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.wfo_gen_cylinder_lattice.restype = C.c_int64
+        L.wfo_gen_cylinder_lattice.argtypes = [C.c_double] * 4 + [C.c_uint64, C.POINTER(C.c_double)]
+        L.wfo_assign_zone.restype = C.c_int64
+        L.wfo_assign_zone.argtypes = [C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double),
+                                      C.POINTER(C.c_double), C.c_int32, C.POINTER(C.c_int32),
+                                      C.POINTER(C.c_uint8)]
+        L.wfo_mlp_forward.restype = C.c_int
+        L.wfo_mlp_forward.argtypes = [C.POINTER(C.c_double)] * 2 + [C.c_int64, C.POINTER(C.c_double)]
+        L.wfo_mlp_loss_grad.restype = C.c_int
+        L.wfo_mlp_loss_grad.argtypes = [C.POINTER(C.c_double)] * 3 + [C.c_int64] + [C.POINTER(C.c_double)] * 2
+        _lib = L
+    return _lib
+
+
+def _p(a, ct=C.c_double):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+def set_threads(n):
+    lib().wfo_set_threads(int(n))
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+class OracleDomain:
+    """Same method names as weldformgpu_gb300.Domain_d, backed by the oracle."""
+
+    def __init__(self, n):
+        self.L = lib()
+        self.h = C.c_void_p()
+        rc = self.L.wfo_create(C.byref(self.h), int(n))
+        if rc:
+            raise OracleError("wfo_create failed (%d)" % rc)
+        self.n = int(n)
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.L.wfo_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def _ck(self, rc, what):
+        if rc != 0:
+            raise OracleError("%s: %s (%s)" % (what, _abi.ERROR_NAMES.get(rc, rc),
+                                               self.L.wfo_last_error(self.h).decode()))
+
+    def __getattr__(self, name):
+        # scalar setters / solvers: forwarded with the prefix
+        fn = getattr(self.L, "wfo_" + name, None)
+        if fn is None:
+            raise AttributeError(name)
+
+        def call(*args):
+            conv = []
+            for a in args:
+                if isinstance(a, np.ndarray):
+                    if a.dtype == np.float64:
+                        conv.append(_p(np.ascontiguousarray(a)))
+                    elif a.dtype == np.int32:
+                        conv.append(_p(np.ascontiguousarray(a), C.c_int32))
+                    elif a.dtype == np.uint8 or a.dtype == np.bool_:
+                        conv.append(_p(np.ascontiguousarray(a, dtype=np.uint8), C.c_uint8))
+                    else:
+                        raise TypeError(a.dtype)
+                elif isinstance(a, str):
+                    conv.append(a.encode())
+                else:
+                    conv.append(a)
+            self._ck(fn(self.h, *conv), name)
+        return call
+
+    def set_material(self, mat):
+        self._ck(self.L.wfo_set_material(self.h, C.byref(mat)), "set_material")
+
+    def set_mlp_params(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        self._ck(self.L.wfo_set_mlp_params(self.h, _p(p)), "set_mlp_params")
+
+    def get_field(self, name):
+        c = _abi.FIELD_COMPONENTS.get(name, 1)
+        out = np.empty(self.n * c, dtype=np.float64)
+        self._ck(self.L.wfo_get_field(self.h, name.encode(), _p(out)), "get_field " + name)
+        return out.reshape(self.n, c) if c > 1 else out
+
+    def set_field(self, name, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64).ravel()
+        self._ck(self.L.wfo_set_field(self.h, name.encode(), _p(a)), "set_field " + name)
+
+    def get_field_i32(self, name):
+        out = np.empty(self.n, dtype=np.int32)
+        self._ck(self.L.wfo_get_field_i32(self.h, name.encode(), _p(out, C.c_int32)), name)
+        return out
+
+    def get_neighbors(self):
+        cnt = np.empty(self.n, dtype=np.int32)
+        lst = np.empty(self.n * NB, dtype=np.int32)
+        self._ck(self.L.wfo_get_neighbors(self.h, _p(cnt, C.c_int32), _p(lst, C.c_int32)),
+                 "get_neighbors")
+        return cnt, lst.reshape(self.n, NB)
+
+    def get_scalar(self, name):
+        out = C.c_double()
+        self._ck(self.L.wfo_get_scalar(self.h, name.encode(), C.byref(out)), name)
+        return out.value
+
+    def run_stage(self, name):
+        self._ck(self.L.wfo_run_stage(self.h, name.encode()), "run_stage " + name)
+
+
+# ---- generators -----------------------------------------------------------
+def gen_cylinder_ref(start, R, L, r, density):
+    """Domain::AddCylinderLength; returns (x[n,3], mass)."""
+    L_ = lib()
+    m = C.c_double()
+    n = L_.wfo_gen_cylinder_ref(start[0], start[1], start[2], R, L, r, density, None, C.byref(m))
+    x = np.empty(3 * n, dtype=np.float64)
+    L_.wfo_gen_cylinder_ref(start[0], start[1], start[2], R, L, r, density, _p(x), C.byref(m))
+    return x.reshape(n, 3), m.value
+
+
+def gen_box_cubic(start, dims, r, density):
+    L_ = lib()
+    m = C.c_double()
+    args = list(start) + list(dims) + [r, density]
+    n = L_.wfo_gen_box_cubic(*args, None, C.byref(m))
+    x = np.empty(3 * n, dtype=np.float64)
+    L_.wfo_gen_box_cubic(*args, _p(x), C.byref(m))
+    return x.reshape(n, 3), m.value
+
+
+def gen_cylinder_lattice(R, H, dx, jitter, seed):
+    L_ = lib()
+    n = L_.wfo_gen_cylinder_lattice(R, H, dx, jitter, seed, None)
+    x = np.empty(3 * n, dtype=np.float64)
+    L_.wfo_gen_cylinder_lattice(R, H, dx, jitter, seed, _p(x))
+    return x.reshape(n, 3)
+
+
+def assign_zone(x, start, end, zone, ids, not_write):
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    s = np.asarray(start, dtype=np.float64)
+    e = np.asarray(end, dtype=np.float64)
+    return lib().wfo_assign_zone(_p(x), len(x), _p(s), _p(e), int(zone), _p(ids, C.c_int32),
+                                 _p(not_write, C.c_uint8))
+
+
+def mlp_forward(params, xin):
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    x = np.ascontiguousarray(xin, dtype=np.float64)
+    y = np.empty(len(x), dtype=np.float64)
+    rc = lib().wfo_mlp_forward(_p(p), _p(x), len(x), _p(y))
+    assert rc == 0
+    return y
+
+
+def mlp_loss_grad(params, xin, target):
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    x = np.ascontiguousarray(xin, dtype=np.float64)
+    t = np.ascontiguousarray(target, dtype=np.float64)
+    g = np.empty_like(p)
+    loss = C.c_double()
+    rc = lib().wfo_mlp_loss_grad(_p(p), _p(x), _p(t), len(x), C.byref(loss), _p(g))
+    assert rc == 0
+    return loss.value, g
+
+
+# ---- the reference compiled for the CPU -------------------------------------
+_ref = None
+
+
+def ref_lib():
+    """oracle/_ref/libwfref.so, or None when it was not built (no reference tree)."""
+    global _ref
+    if _ref is None and os.path.exists(REF_PATH):
+        L = C.CDLL(REF_PATH)
+        L.wfr_neighbors.restype = C.c_int
+        L.wfr_neighbors.argtypes = [C.POINTER(C.c_double), C.c_int64, C.c_double,
+                                    C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+        L.wfr_create.restype = C.c_void_p
+        L.wfr_create.argtypes = [C.c_int64]
+        L.wfr_destroy.argtypes = [C.c_void_p]
+        L.wfr_set_scalars.argtypes = [C.c_void_p] + [C.c_double] * 8
+        L.wfr_set_material.argtypes = [C.c_void_p, C.c_int] + [C.c_double] * 11
+        L.wfr_set_arrays.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                     C.POINTER(C.c_int32), C.POINTER(C.c_double)]
+        L.wfr_add_bc.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double]
+        L.wfr_set_rebuild_every.argtypes = [C.c_void_p, C.c_int]
+        L.wfr_begin.argtypes = [C.c_void_p]
+        L.wfr_step.argtypes = [C.c_void_p, C.c_int64]
+        L.wfr_get.restype = C.c_int
+        L.wfr_get.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_double)]
+        _ref = L
+    return _ref
+
+
+def ref_neighbors(x, h):
+    L = ref_lib()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    n = len(x)
+    cnt = np.empty(n, dtype=np.int32)
+    lst = np.empty(n * NB, dtype=np.int32)
+    L.wfr_neighbors(_p(x), n, h, _p(cnt, C.c_int32), _p(lst, C.c_int32))
+    return cnt, lst.reshape(n, NB)
+
+
+class RefDomain:
+    """The reference's Domain_d kernels, run on the CPU in Fraser-loop order."""
+
+    def __init__(self, n):
+        self.L = ref_lib()
+        self.h = self.L.wfr_create(int(n))
+        self.n = int(n)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.wfr_destroy(self.h)
+            self.h = None
+
+    def setup(self, x, m, ids, h, rho, G, sy, Cs, dt, alpha, beta, mat, T=None):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        m = np.ascontiguousarray(m, dtype=np.float64)
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        Tp = None if T is None else _p(np.ascontiguousarray(T, dtype=np.float64))
+        self.L.wfr_set_scalars(self.h, h, rho, G, sy, Cs, dt, alpha, beta)
+        self.L.wfr_set_material(self.h, mat.model, mat.E, mat.nu, mat.Et, mat.A, mat.B, mat.n,
+                                mat.C, mat.eps0, mat.m, mat.Tm, mat.Tt)
+        self.L.wfr_set_arrays(self.h, _p(x), _p(m), _p(ids, C.c_int32), Tp)
+
+    def add_bc(self, zone, v):
+        self.L.wfr_add_bc(self.h, int(zone), float(v[0]), float(v[1]), float(v[2]))
+
+    def begin(self):
+        self.L.wfr_begin(self.h)
+
+    def step(self, k):
+        self.L.wfr_step(self.h, int(k))
+
+    def get(self, name):
+        c = _abi.FIELD_COMPONENTS.get(name, 1)
+        out = np.empty(self.n * c, dtype=np.float64)
+        rc = self.L.wfr_get(self.h, name.encode(), _p(out))
+        assert rc == 0, name
+        return out.reshape(self.n, c) if c > 1 else out

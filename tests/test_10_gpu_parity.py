@@ -1,0 +1,211 @@
+"""GPU parity: the CUDA path through the C ABI against the oracle and the
+reference's golden vectors.
+
+Tolerances:
+  - neighbour lists: identical sets and identical order (bit-exact);
+  - plain FP64 form, reference radial return: bit-exact (np.array_equal) --
+    the FP64 kernels build with -fmad=false and sum neighbours in the
+    oracle's order;
+  - plain FP64 form with pow/log (Johnson-Cook Newton, convection): 1e-9
+    relative, the benchmark spec's plain-form bound (CUDA's pow/log may differ
+    from glibc's in the last bit);
+  - mixed form: relative L2 error <= 1e-3 per output field against the
+    plain FP64 run of the same pipeline.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests import scenarios as S
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+STATE_FIELDS = ["x", "v", "a", "rho", "drho", "p", "sigma", "shearstress", "strrate", "rotrate",
+                "sigma_eq", "pl_strain", "sigma_y", "eff_strain_rate", "int_energy"]
+
+
+def gpu(sc, options=None):
+    from weldformgpu_gb300 import Domain_d
+    return S.load(Domain_d(sc["n"]), sc, options)
+
+
+def ora(sc, options=None):
+    return S.load(O.OracleDomain(sc["n"]), sc, options)
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, dtype=np.float64).ravel()
+    b = np.asarray(b, dtype=np.float64).ravel()
+    den = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (den if den > 0 else 1.0)
+
+
+def same_lists(c1, l1, c2, l2):
+    if not np.array_equal(c1, c2):
+        return False
+    return all(np.array_equal(l1[i, :c1[i]], l2[i, :c2[i]]) for i in range(len(c1)))
+
+
+def test_neighbors_bit_exact_config1():
+    c1 = S.compression_cylinder(R=0.005, H=0.010)
+    g = gpu(c1)
+    g.find_neighbors()
+    o = ora(c1)
+    o.find_neighbors()
+    assert same_lists(*g.get_neighbors(), *o.get_neighbors())
+    gold = np.load(os.path.join(GOLDEN, "nb_c1.npz"))
+    assert np.array_equal(g.get_field_i32("nb_count"), gold["counts"])
+
+
+def test_neighbors_bit_exact_jittered_lattice():
+    sc = S.compression_cylinder(R=0.004, H=0.006, generator="lattice", jitter=0.01, seed=7)
+    g = gpu(sc)
+    g.find_neighbors()
+    o = ora(sc)
+    o.find_neighbors()
+    assert same_lists(*g.get_neighbors(), *o.get_neighbors())
+
+
+@pytest.mark.parametrize("case,checkpoints", [("bilinear", [1, 600, 1500]), ("jc", [300])])
+def test_fp64_fraser_loop_bit_exact_vs_reference_golden(case, checkpoints):
+    gold = np.load(os.path.join(GOLDEN, "fraser_%s.npz" % case))
+    sc = (S.compression_cylinder() if case == "bilinear"
+          else S.compression_cylinder(material="jc", vz_top=-10.0))
+    g = gpu(sc)
+    done = 0
+    for k in checkpoints:
+        g.step(k - done)
+        done = k
+        for f in STATE_FIELDS:
+            if case == "jc" and f in ("sigma_y", "sigma", "shearstress", "sigma_eq", "pl_strain",
+                                      "x", "v", "a", "rho", "drho", "p", "int_energy"):
+                # pow/log of the JC yield law: CUDA vs glibc may differ in the last bit
+                np.testing.assert_allclose(g.get_field(f), gold["s%d_%s" % (k, f)], rtol=1e-9,
+                                           atol=1e-9 * np.max(np.abs(gold["s%d_%s" % (k, f)])))
+            else:
+                got, ref = g.get_field(f), gold["s%d_%s" % (k, f)]
+                assert np.array_equal(got, ref), "%s step %d %s: max |d| %.3e" % (
+                    case, k, f, np.max(np.abs(got - ref)))
+
+
+def test_fp64_config1_lattice_vs_oracle_with_rebuilds():
+    """BASELINE config 1 (jittered lattice, 0.4h/c, rebuild every 10 steps) for 400 steps."""
+    sc = S.compression_cylinder(R=0.005, H=0.010, generator="lattice", dt_rule="baseline")
+    opts = {"rebuild_every": 10, "rebuild_current_positions": 1, "rebuild_after_yield": 0}
+    g = gpu(sc, opts)
+    o = ora(sc, opts)
+    g.step(400)
+    o.step(400)
+    for f in ("x", "u", "v", "rho", "sigma", "pl_strain", "sigma_eq", "int_energy"):
+        assert np.array_equal(g.get_field(f), o.get_field(f)), f
+
+
+def test_fp64_newton_jc_vs_oracle():
+    sc = S.compression_cylinder(material="jc", vz_top=-10.0)
+    g = gpu(sc, {"return_map": 1})
+    o = ora(sc, {"return_map": 1})
+    g.step(400)
+    o.step(400)
+    assert o.get_field("pl_strain").max() > 0.01
+    for f in ("x", "u", "sigma", "pl_strain", "sigma_eq", "sigma_y"):
+        ref = o.get_field(f)
+        np.testing.assert_allclose(g.get_field(f), ref, rtol=1e-9, atol=1e-9 * np.abs(ref).max())
+    gi = g.get_scalar("newton_iters") / g.get_scalar("newton_calls")
+    oi = o.get_scalar("newton_iters") / o.get_scalar("newton_calls")
+    assert abs(gi - oi) < 0.05 * oi
+
+
+def test_mixed_form_within_1e3_of_fp64_jc_newton():
+    sc = S.compression_cylinder(R=0.004, H=0.008, material="jc", vz_top=-10.0,
+                                generator="lattice", dt_rule="baseline")
+    opts = {"return_map": 1, "rebuild_every": 10, "rebuild_current_positions": 1,
+            "rebuild_after_yield": 0}
+    a = gpu(sc, dict(opts, precision=0))
+    b = gpu(sc, dict(opts, precision=1))
+    a.step(600)
+    b.step(600)
+    assert a.get_field("pl_strain").max() > 0.005
+    for f in ("u", "pl_strain", "sigma_eq"):
+        e = rel_l2(b.get_field(f), a.get_field(f))
+        assert e <= 1e-3, (f, e)
+
+
+def test_heat_fp64_vs_oracle():
+    sc = S.heat_box(n_side=16)
+    from weldformgpu_gb300 import Domain_d
+    g = S.load_heat(Domain_d(sc["n"]), sc)
+    o = S.load_heat(O.OracleDomain(sc["n"]), sc)
+    tf = 40 * sc["dt"]
+    g.thermal_solve(tf)
+    o.thermal_solve(tf)
+    np.testing.assert_allclose(g.get_field("T"), o.get_field("T"), rtol=1e-12)
+
+
+def test_heat_mixed_flux_vs_fp64():
+    sc = S.heat_box(n_side=16)
+    from weldformgpu_gb300 import Domain_d
+    a = S.load_heat(Domain_d(sc["n"]), sc)
+    b = S.load_heat(Domain_d(sc["n"]), sc)
+    b.set_option("precision", 1)
+    tf = 40 * sc["dt"]
+    a.thermal_solve(tf)
+    b.thermal_solve(tf)
+    T0 = sc["T"]
+    assert rel_l2(b.get_field("T") - T0, a.get_field("T") - T0) <= 1e-3
+
+
+def test_coupled_thermomechanical_jc_vs_oracle():
+    sc = S.compression_cylinder(material="jc", vz_top=-10.0)
+    sc["k"], sc["cp"] = 167.0, 896.0
+    opts = {"return_map": 1, "thermal": 1, "taylor_quinney": 0.9}
+    g = gpu(sc, opts)
+    o = ora(sc, opts)
+    g.step(300)
+    o.step(300)
+    To = o.get_field("T")
+    assert To.max() > 20.5                         # plastic work heated the cylinder
+    np.testing.assert_allclose(g.get_field("T"), To, rtol=1e-9)
+    np.testing.assert_allclose(g.get_field("pl_strain"), o.get_field("pl_strain"), rtol=1e-9,
+                               atol=1e-12)
+
+
+def test_reference_api_mech_fraser_solve_bit_exact():
+    """MechFraserSolve(tf, dt_out) through the reference's method names: stale
+    (last-output) positions for the rebuilds, outputs every dt_out."""
+    from weldformgpu_gb300 import Domain_d
+    sc = S.compression_cylinder()
+    d = Domain_d(sc["n"])
+    d.Set_h(sc["h"])
+    d.SetDensity(sc["rho"])
+    d.SetShearModulus(sc["G"])
+    d.SetSigmay(sc["sy"])
+    d.SetCs(np.full(sc["n"], sc["Cs"]))
+    d.SetFreePart(np.ones(sc["n"], np.uint8))
+    d.SetID(sc["ids"])
+    d.set_positions(sc["x"])
+    d.set_mass(sc["m"])
+    d.set_time_step(sc["dt"])
+    d.set_material(sc["mat"])
+    for z, v in sc["bcs"]:
+        d.add_velocity_bc(z, *v)
+    tf, dt_out = 700 * sc["dt"], 64 * sc["dt"]
+    d.MechFraserSolve(tf, dt_out)
+    o = ora(sc)
+    o.mech_fraser_solve(tf, dt_out)
+    for f in ("x", "v", "sigma", "pl_strain"):
+        assert np.array_equal(d.get_field(f), o.get_field(f)), f
+
+
+def test_write_csv_reference_columns(tmp_path):
+    sc = S.compression_cylinder()
+    g = gpu(sc)
+    g.step(3)
+    path = tmp_path / "out.csv"
+    g.WriteCSV(str(path))
+    lines = path.read_text().splitlines()
+    assert lines[0].startswith("ID, X, Y, Z, posX,posY,posZ,Ux, Uy, Uz")
+    assert len(lines) == sc["n"] + 1
+    assert len(lines[1].split(",")) == 29

@@ -1,0 +1,908 @@
+// wf_api.cu — the C ABI (include/weldform_gb300.h) over the device domain.
+//
+// struct wf_domain plays the role of the reference's SPH::Domain_d
+// (src/cuda/Domain_d.cuh:101-426): it owns the per-particle arena, the
+// neighbour lists and the solver state, and runs MechFraserSolve's loop
+// (src/cuda/SolverFraser.cu:30-409) and ThermalSolve (src/cuda/Thermal.cu:188-260)
+// as sequences of kernel launches on one CUDA stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/weldform_gb300.h"
+#include "wf_common.cuh"
+#include "wf_mlp.cuh"
+#include "wf_nsearch.cuh"
+
+#define WF_VERSION "weldform-gb300 0.1 (sm_103a)"
+
+// kernel ids for wf_set_option("profile_kernel", id)
+enum { KID_NONE = 0, KID_DENSITY = 1, KID_STRESS = 2, KID_ACCEL = 3, KID_INTEGRATE = 4,
+       KID_THERMAL = 5, KID_REBUILD = 6 };
+
+struct wf_domain {
+  int64_t n = 0, n_solid = 0, npad = 0;
+  cudaStream_t stream = nullptr;
+  // uniform scalars (the reference's setters fill every particle with one value)
+  double h = 0, rho0 = 0, G = 0, Cs = 0, dt = 0, alpha = 1.0, beta = 0.0;
+  double h_conv = 100.0, T_inf = 0.0;
+  bool h_set = false, rho_set = false, G_set = false, cs_set = false, mat_set = false;
+  bool x_set = false, m_set = false;
+  wf_material mat{};
+  std::vector<int32_t> bc_zone;
+  std::vector<std::array<double, 3>> bc_v;
+  // options
+  int precision = 0, return_map = 0, mlp_on = 0, rebuild_every = 5, rebuild_after_yield = 1;
+  int rebuild_current = 0, thermal = 0, energy_mode = 0, newton_max_iter = 50;
+  int clamp_homologous = 1, profile_kernel = KID_NONE;
+  double chi = 0.0, newton_rtol = 1.0e-10, output_interval = 1.0e300;
+  // device arena
+  Fields F[2]{};
+  int cur = 0;
+  double4* vd2 = nullptr;
+  float4* v32b = nullptr;
+  float* sigr32 = nullptr;
+  float* mlp_w = nullptr;      // device MLP parameters (FP32 master copy, see wf_mlp.cu)
+  int32_t *nb = nullptr, *nbc = nullptr, *inv = nullptr;
+  float4 *pf = nullptr, *pf2 = nullptr;
+  uint32_t *cellid = nullptr, *cell_count = nullptr, *cell_cursor = nullptr, *scan_tmp = nullptr;
+  int64_t cell_cap = 0, scan_cap = 0;
+  int32_t *s_src = nullptr, *s_orig = nullptr;
+  int* d_mm = nullptr;
+  int* d_status = nullptr;     // [0] bits, [1] yield flag, [2..3] newton iters, [4..5] calls
+  int* h_status = nullptr;     // pinned mirror
+  double* d_stage = nullptr;   // staging for ABI copies (6 doubles per particle)
+  // solver state
+  bool started = false, nb_built = false, is_yielding = false, isfirst = true;
+  double time = 0, t_out = 0, dt_out = 0;
+  int64_t step = 0;
+  int ts_i = 0;
+  GridDev grid{};
+  // measurement
+  int64_t launches = 0;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  bool timing = false;         // inside wf_time_steps
+  std::string err;
+};
+
+static int wf_cuda_fail(wf_domain* d, cudaError_t e, const char* what) {
+  if (d) d->err = std::string(what) + ": " + cudaGetErrorString(e);
+  return WF_ERR_CUDA;
+}
+static int wf_fail(wf_domain* d, int code, const std::string& msg) {
+  if (d) d->err = msg;
+  return code;
+}
+
+// ---------------------------------------------------------------------------
+// small utility kernels: scatter/gather between caller order and slot order
+// ---------------------------------------------------------------------------
+namespace {
+__global__ void k_scatter_d(int64_t n, const int32_t* inv, const double* src, int comps,
+                            double* dst, int stride, int off) {
+  int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (o >= n) return;
+  int64_t s = inv[o];
+  for (int c = 0; c < comps; c++) dst[s * stride + off + c] = src[o * comps + c];
+}
+__global__ void k_gather_d(int64_t n, const int32_t* inv, const double* src, int stride, int off,
+                           int comps, double* dst) {
+  int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (o >= n) return;
+  int64_t s = inv[o];
+  for (int c = 0; c < comps; c++) dst[o * comps + c] = src[s * stride + off + c];
+}
+__global__ void k_gather_f(int64_t n, const int32_t* inv, const float* src, int stride, int off,
+                           int comps, double* dst) {
+  int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (o >= n) return;
+  int64_t s = inv[o];
+  for (int c = 0; c < comps; c++) dst[o * comps + c] = (double)src[s * stride + off + c];
+}
+// sigma = -p I + S from the FP32 deviatoric state (mixed form)
+__global__ void k_gather_sigma32(int64_t n, const int32_t* inv, const float* ss32, const double* p,
+                                 double* dst) {
+  int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (o >= n) return;
+  int64_t s = inv[o];
+  for (int c = 0; c < 6; c++) dst[o * 6 + c] = (double)ss32[s * 6 + c] + (c < 3 ? -p[s] : 0.0);
+}
+template <class T>
+__global__ void k_scatter_t(int64_t n, const int32_t* inv, const T* src, T* dst) {
+  int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (o >= n) return;
+  dst[inv[o]] = src[o];
+}
+template <class T>
+__global__ void k_gather_t(int64_t n, const int32_t* inv, const T* src, T* dst) {
+  int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (o >= n) return;
+  dst[o] = src[inv[o]];
+}
+__global__ void k_fill_d(int64_t n, double v, double* dst, int stride, int off) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s < n) dst[s * stride + off] = v;
+}
+__global__ void k_iota(int64_t n, int32_t* a, int32_t* b) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s < n) { a[s] = (int32_t)s; b[s] = (int32_t)s; }
+}
+// neighbour lists in caller ids: lists[o*70+k] = perm[nb[k*npad + inv[o]]]
+__global__ void k_gather_nb(int64_t n, int64_t npad, const int32_t* inv, const int32_t* perm,
+                            const int32_t* nb, const int32_t* cnt, int32_t* ocnt, int32_t* olst) {
+  int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (o >= n) return;
+  int64_t s = inv[o];
+  int c = cnt[s];
+  ocnt[o] = c;
+  for (int k = 0; k < WF_NB; k++) olst[o * WF_NB + k] = k < c ? perm[nb[(int64_t)k * npad + s]] : -1;
+}
+// SetVelKernel (src/cuda/Mechanical.cu:154-163): v = 0 for solid particles
+__global__ void k_setvel0(int64_t n, int64_t n_solid, Fields F) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  if (F.perm[s] < n_solid) {
+    double4 v = F.vd[s];
+    F.vd[s] = make_double4(0.0, 0.0, 0.0, v.w);
+  }
+}
+// FP32 mirrors of the master state for the mixed form
+__global__ void k_mixed_init(int64_t n, Fields F) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  double4 x = F.xm[s], v = F.vd[s];
+  F.p32[s] = make_float4((float)x.x, (float)x.y, (float)x.z, (float)x.w);
+  F.v32[s] = make_float4((float)v.x, (float)v.y, (float)v.z, (float)v.w);
+  for (int c = 0; c < 6; c++) F.ss32[s * 6 + c] = (float)F.ss6[s * 6 + c];
+}
+// FP64 copy of the FP32 deviatoric state (mixed -> plain switch)
+__global__ void k_mixed_to_fp64(int64_t n, Fields F) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  for (int c = 0; c < 6; c++) F.ss6[s * 6 + c] = (double)F.ss32[s * 6 + c];
+}
+inline int nblk(int64_t n, int t = 256) { return (int)((n + t - 1) / t); }
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// allocation
+// ---------------------------------------------------------------------------
+template <class T>
+static cudaError_t dalloc(T** p, int64_t count) {
+  cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (size_t)std::max<int64_t>(count, 1));
+  if (e == cudaSuccess) e = cudaMemset(*p, 0, sizeof(T) * (size_t)std::max<int64_t>(count, 1));
+  return e;
+}
+
+static int alloc_fields(wf_domain* d, Fields& F) {
+  const int64_t n = d->npad;
+  WF_CUDA_OK(dalloc(&F.xm, n)); WF_CUDA_OK(dalloc(&F.vd, n));
+  WF_CUDA_OK(dalloc(&F.u, n)); WF_CUDA_OK(dalloc(&F.a, n));
+  WF_CUDA_OK(dalloc(&F.sig6, 6 * n)); WF_CUDA_OK(dalloc(&F.ss6, 6 * n));
+  WF_CUDA_OK(dalloc(&F.eps6, 6 * n)); WF_CUDA_OK(dalloc(&F.sr6, 6 * n));
+  WF_CUDA_OK(dalloc(&F.rr6, 6 * n));
+  WF_CUDA_OK(dalloc(&F.p, n)); WF_CUDA_OK(dalloc(&F.seq, n)); WF_CUDA_OK(dalloc(&F.eps_p, n));
+  WF_CUDA_OK(dalloc(&F.sy, n)); WF_CUDA_OK(dalloc(&F.eff, n)); WF_CUDA_OK(dalloc(&F.dep, n));
+  WF_CUDA_OK(dalloc(&F.drho, n)); WF_CUDA_OK(dalloc(&F.eint, n));
+  WF_CUDA_OK(dalloc(&F.T, n)); WF_CUDA_OK(dalloc(&F.Ta, n)); WF_CUDA_OK(dalloc(&F.Tb, n));
+  WF_CUDA_OK(dalloc(&F.dTdt, n)); WF_CUDA_OK(dalloc(&F.kT, n)); WF_CUDA_OK(dalloc(&F.cpT, n));
+  WF_CUDA_OK(dalloc(&F.id, n)); WF_CUDA_OK(dalloc(&F.bct, n)); WF_CUDA_OK(dalloc(&F.perm, n));
+  WF_CUDA_OK(dalloc(&F.nw, n)); WF_CUDA_OK(dalloc(&F.xh, n));
+  WF_CUDA_OK(dalloc(&F.p32, n)); WF_CUDA_OK(dalloc(&F.v32, n)); WF_CUDA_OK(dalloc(&F.ss32, 6 * n));
+  return WF_OK;
+}
+
+static void free_fields(Fields& F) {
+  void* ptrs[] = {F.xm, F.vd, F.u, F.a, F.sig6, F.ss6, F.eps6, F.sr6, F.rr6, F.p, F.seq, F.eps_p,
+                  F.sy, F.eff, F.dep, F.drho, F.eint, F.T, F.Ta, F.Tb, F.dTdt, F.kT, F.cpT,
+                  F.id, F.bct, F.perm, F.nw, F.xh, F.p32, F.v32, F.ss32};
+  for (void* p : ptrs) if (p) cudaFree(p);
+  F = Fields{};
+}
+
+// ---------------------------------------------------------------------------
+// parameters
+// ---------------------------------------------------------------------------
+static StepParams make_params(const wf_domain* d) {
+  StepParams P;
+  memset(&P, 0, sizeof P);
+  P.n = d->n;
+  P.n_solid = d->n_solid;
+  P.npad = d->npad;
+  P.h = d->h;
+  P.gkC = 1.0 / (d->h * d->h * d->h * d->h * WF_PI);   // Functions.cu:83 with h_ = h
+  P.dt = d->dt;
+  P.Cs = d->Cs;
+  P.G = d->G;
+  P.rho0 = d->rho0;
+  P.alpha = d->alpha;
+  P.beta = d->beta;
+  P.chi = d->chi;
+  P.h_conv = d->h_conv;
+  P.T_inf = d->T_inf;
+  P.return_map = d->return_map;
+  P.newton_max_iter = d->newton_max_iter;
+  P.newton_rtol = d->newton_rtol;
+  P.clamp_homologous = d->clamp_homologous;
+  P.energy_mode = d->energy_mode;
+  P.inv = d->inv;
+  P.contact = 0;
+  P.ncsid = 0;
+  P.nbc = (int)d->bc_zone.size();
+  for (int b = 0; b < P.nbc; b++) {
+    P.bc_zone[b] = d->bc_zone[b];
+    for (int c = 0; c < 3; c++) P.bc_v[b][c] = d->bc_v[b][c];
+  }
+  P.mlp_on = d->mlp_on;
+  const wf_material& m = d->mat;
+  MatParams& M = P.mat;
+  M.model = m.model;
+  M.E = m.E;
+  M.Et = m.Et;
+  M.Ep = (m.model == WF_BILINEAR) ? m.E * m.Et / (m.E - m.Et) : 0.0;   // WeldFormGPU.cu:755
+  M.K_hol = m.K_hol;
+  M.m_hol = m.m_hol;
+  M.sy0 = m.sy0;
+  if (m.model == WF_HOLLOMON) {                                       // Material.cuh:116-130
+    M.eps0_hol = m.sy0 / m.E;
+    M.eps1_hol = std::pow(m.sy0 / m.K_hol, 1. / m.m_hol);
+  }
+  M.A = m.A; M.B = m.B; M.n = m.n; M.C = m.C; M.eps0 = m.eps0; M.m = m.m; M.Tm = m.Tm; M.Tt = m.Tt;
+  return P;
+}
+
+// ---------------------------------------------------------------------------
+// measurement helpers: optional event pairs around one kernel kind
+// ---------------------------------------------------------------------------
+struct KTimer {
+  wf_domain* d;
+  int kid;
+  bool on;
+  KTimer(wf_domain* d_, int kid_)
+      : d(d_), kid(kid_), on(d_->timing && d_->profile_kernel == kid_) {
+    if (on) {
+      if (d->ev_used + 2 > d->ev_pool.size()) {
+        for (int k = 0; k < 64; k++) {
+          cudaEvent_t e;
+          cudaEventCreate(&e);
+          d->ev_pool.push_back(e);
+        }
+      }
+      cudaEventRecord(d->ev_pool[d->ev_used], d->stream);
+    }
+  }
+  ~KTimer() {
+    if (on) {
+      cudaEventRecord(d->ev_pool[d->ev_used + 1], d->stream);
+      d->ev_used += 2;
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// neighbour rebuild (cuNSearch find_neighbors equivalent) + reorder
+// ---------------------------------------------------------------------------
+static int ensure_cells(wf_domain* d, int64_t ncell) {
+  if (ncell + 1 <= d->cell_cap) return WF_OK;
+  if (d->cell_count) { cudaFree(d->cell_count); cudaFree(d->cell_cursor); cudaFree(d->scan_tmp); }
+  int64_t cap = (ncell + 1) + (ncell + 1) / 4 + 1024;
+  WF_CUDA_OK(dalloc(&d->cell_count, cap));
+  WF_CUDA_OK(dalloc(&d->cell_cursor, cap));
+  d->scan_cap = scan_tmp_words(cap) + 16;
+  WF_CUDA_OK(dalloc(&d->scan_tmp, d->scan_cap));
+  d->cell_cap = cap;
+  return WF_OK;
+}
+
+static int rebuild(wf_domain* d, bool use_current) {
+  KTimer t(d, KID_REBUILD);
+  const int64_t n = d->n;
+  cudaStream_t s = d->stream;
+  Fields& A = d->F[d->cur];
+  Fields& B = d->F[1 - d->cur];
+  launch_prep_positions(n, A, use_current ? 1 : 0, d->pf, s);
+  int mm_init[6] = {INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN};
+  WF_CUDA_OK(cudaMemcpyAsync(d->d_mm, mm_init, sizeof mm_init, cudaMemcpyHostToDevice, s));
+  const float r = (float)(2.0 * d->h);                // SolverFraser.cu:72-82
+  launch_minmax(n, d->pf, r, d->d_mm, s);
+  int mm[6];
+  WF_CUDA_OK(cudaMemcpyAsync(mm, d->d_mm, sizeof mm, cudaMemcpyDeviceToHost, s));
+  WF_CUDA_OK(cudaStreamSynchronize(s));
+  grid_from_minmax(mm, r, &d->grid);
+  const int64_t ncell = (int64_t)d->grid.dim[0] * d->grid.dim[1] * d->grid.dim[2];
+  if (ncell > (int64_t)2000000000) return wf_fail(d, WF_ERR_NUMERIC, "neighbour grid too large");
+  int rc = ensure_cells(d, ncell);
+  if (rc) return rc;
+  WF_CUDA_OK(cudaMemsetAsync(d->cell_count, 0, sizeof(uint32_t) * (ncell + 1), s));
+  WF_CUDA_OK(cudaMemsetAsync(d->cell_cursor, 0, sizeof(uint32_t) * (ncell + 1), s));
+  launch_cell_count(n, d->pf, d->grid, d->cellid, d->cell_count, d->d_status, s);
+  device_exclusive_scan(d->cell_count, ncell + 1, d->scan_tmp, s);
+  launch_cell_scatter(n, d->cellid, d->cell_count, d->cell_cursor, A.perm, d->s_src, d->s_orig, s);
+  launch_cell_sort(ncell, d->cell_count, d->s_src, d->s_orig, s);
+  launch_reorder(n, d->s_src, A, B, d->pf, d->pf2, d->inv, s);
+  d->cur = 1 - d->cur;
+  launch_nblist(n, d->npad, d->pf2, d->grid, d->cell_count, d->nb, d->nbc, d->d_status, s);
+  d->launches += 8;
+  WF_CUDA_OK(cudaGetLastError());
+  d->nb_built = true;
+  return WF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// the Fraser loop (SolverFraser.cu:30-409)
+// ---------------------------------------------------------------------------
+static int check_ready(wf_domain* d) {
+  if (!d->h_set) return wf_fail(d, WF_ERR_STATE, "Set_h not called");
+  if (!d->x_set) return wf_fail(d, WF_ERR_STATE, "positions not set");
+  if (!d->m_set) return wf_fail(d, WF_ERR_STATE, "masses not set");
+  if (!d->rho_set) return wf_fail(d, WF_ERR_STATE, "SetDensity not called");
+  if (!(d->dt > 0)) return wf_fail(d, WF_ERR_STATE, "time step not set");
+  if (!d->mat_set) return wf_fail(d, WF_ERR_STATE, "material not set");
+  if (!d->cs_set) return wf_fail(d, WF_ERR_STATE, "SetCs not called");
+  if (!d->G_set) return wf_fail(d, WF_ERR_STATE, "SetShearModulus not called");
+  return WF_OK;
+}
+
+static int read_status(wf_domain* d) {
+  WF_CUDA_OK(cudaMemcpyAsync(d->h_status, d->d_status, 8 * sizeof(int), cudaMemcpyDeviceToHost,
+                             d->stream));
+  WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+  return WF_OK;
+}
+
+static int solve_begin(wf_domain* d, double dt_out) {
+  int rc = check_ready(d);
+  if (rc) return rc;
+  d->time = 0.0;
+  d->isfirst = true;
+  d->step = 0;
+  d->t_out = dt_out;
+  d->dt_out = dt_out;
+  d->ts_i = 0;
+  d->is_yielding = false;
+  WF_CUDA_OK(cudaMemsetAsync(d->d_status, 0, 8 * sizeof(int), d->stream));
+  launch_snapshot(d->n, d->F[d->cur], d->stream);               // x_h = x, :56
+  rc = rebuild(d, false);                                       // :109
+  if (rc) return rc;
+  k_setvel0<<<nblk(d->n), 256, 0, d->stream>>>(d->n, d->n_solid, d->F[d->cur]);   // :123
+  if (d->precision == 1) k_mixed_init<<<nblk(d->n), 256, 0, d->stream>>>(d->n, d->F[d->cur]);
+  WF_CUDA_OK(cudaGetLastError());
+  d->started = true;
+  return WF_OK;
+}
+
+static int solve_step(wf_domain* d) {
+  cudaStream_t s = d->stream;
+  if (d->ts_i == 0 && (d->is_yielding || !d->rebuild_after_yield)) {   // :166-182
+    int rc = rebuild(d, d->rebuild_current != 0);
+    if (rc) return rc;
+  }
+  StepParams P = make_params(d);
+  const Fields& F = d->F[d->cur];
+  NbBuffers N{d->nb, d->nbc};
+  const bool mixed = d->precision == 1;
+  if (!mixed) {
+    { KTimer t(d, KID_DENSITY); launch_fp64_density(P, F, d->vd2, N, s); }          // :193-202
+    { KTimer t(d, KID_STRESS); launch_fp64_stress(P, F, d->vd2, N, d->d_status, s); }  // :204-218
+    { KTimer t(d, KID_ACCEL); launch_fp64_accel(P, F, d->vd2, N, s); }               // :221
+  } else {
+    { KTimer t(d, KID_DENSITY); launch_fp32_density(P, F, d->vd2, d->v32b, N, s); }
+    { KTimer t(d, KID_STRESS);
+      launch_fp32_stress(P, F, d->v32b, d->sigr32, N, d->d_status, d->mlp_on ? d->mlp_w : nullptr, s); }
+    { KTimer t(d, KID_ACCEL); launch_fp32_accel(P, F, d->v32b, d->sigr32, N, s); }
+  }
+  { KTimer t(d, KID_INTEGRATE); launch_integrate(P, F, d->vd2, mixed ? 1 : 0, s); }   // :273-287
+  d->launches += 4;
+  if (d->thermal) {                                                                   // :285
+    KTimer t(d, KID_THERMAL);
+    launch_thermal(P, F, N, d->isfirst ? 1 : 0, d->chi > 0.0 ? 1 : 0, mixed ? 1 : 0, s);
+    d->launches += 2;
+  }
+  d->isfirst = false;
+  d->time += d->dt;
+  if (d->time >= d->t_out) {                                                          // :323-368
+    launch_snapshot(d->n, F, s);
+    d->launches += 1;
+    d->t_out += d->dt_out;
+  }
+  d->step++;
+  d->ts_i++;
+  if (d->ts_i > d->rebuild_every - 1) d->ts_i = 0;
+  // the yield flag matters only for the next rebuild decision
+  if (!d->is_yielding && d->ts_i == 0 && d->rebuild_after_yield) {
+    int rc = read_status(d);
+    if (rc) return rc;
+    if (d->h_status[1]) d->is_yielding = true;
+  }
+  return WF_OK;
+}
+
+static int finish(wf_domain* d) {
+  int rc = read_status(d);
+  if (rc) return rc;
+  WF_CUDA_OK(cudaGetLastError());
+  if (d->h_status[0] & WF_STATUS_NAN) return wf_fail(d, WF_ERR_NUMERIC, "non-finite stress detected");
+  return WF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char* wf_version(void) { return WF_VERSION; }
+
+const char* wf_last_error(const wf_domain* d) { return d ? d->err.c_str() : "null handle"; }
+
+int wf_create(wf_domain** out, int64_t n) {
+  if (!out || n <= 0 || n > (int64_t)INT32_MAX - 256) return WF_ERR_ARG;
+  *out = nullptr;
+  wf_domain* d = new wf_domain();
+  d->n = n;
+  d->n_solid = n;
+  d->npad = (n + 127) / 128 * 128;
+  int rc = WF_OK;
+  auto bail = [&](int code) { wf_destroy(d); return code; };
+  if (cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(WF_ERR_CUDA);
+  for (int k = 0; k < 2; k++) {
+    rc = alloc_fields(d, d->F[k]);
+    if (rc) return bail(rc);
+  }
+  if (dalloc(&d->vd2, d->npad) || dalloc(&d->v32b, d->npad) || dalloc(&d->sigr32, 8 * d->npad) ||
+      dalloc(&d->nb, (int64_t)WF_NB * d->npad) || dalloc(&d->nbc, d->npad) ||
+      dalloc(&d->inv, d->npad) || dalloc(&d->pf, d->npad) || dalloc(&d->pf2, d->npad) ||
+      dalloc(&d->cellid, d->npad) || dalloc(&d->s_src, d->npad) || dalloc(&d->s_orig, d->npad) ||
+      dalloc(&d->d_mm, 8) || dalloc(&d->d_status, 8) || dalloc(&d->d_stage, 6 * d->npad) ||
+      dalloc(&d->mlp_w, WF_MLP_NPARAM))
+    return bail(WF_ERR_ALLOC);
+  if (cudaMallocHost((void**)&d->h_status, 8 * sizeof(int)) != cudaSuccess) return bail(WF_ERR_ALLOC);
+  k_iota<<<nblk(n), 256, 0, d->stream>>>(n, d->F[0].perm, d->inv);
+  if (cudaStreamSynchronize(d->stream) != cudaSuccess) return bail(WF_ERR_CUDA);
+  *out = d;
+  return WF_OK;
+}
+
+int wf_destroy(wf_domain* d) {
+  if (!d) return WF_OK;
+  if (d->stream) cudaStreamSynchronize(d->stream);
+  for (int k = 0; k < 2; k++) free_fields(d->F[k]);
+  void* ptrs[] = {d->vd2, d->v32b, d->sigr32, d->mlp_w, d->nb, d->nbc, d->inv, d->pf, d->pf2,
+                  d->cellid, d->cell_count, d->cell_cursor, d->scan_tmp, d->s_src, d->s_orig,
+                  d->d_mm, d->d_status, d->d_stage};
+  for (void* p : ptrs) if (p) cudaFree(p);
+  if (d->h_status) cudaFreeHost(d->h_status);
+  for (cudaEvent_t e : d->ev_pool) cudaEventDestroy(e);
+  if (d->stream) cudaStreamDestroy(d->stream);
+  delete d;
+  return WF_OK;
+}
+
+}  // extern "C"
+
+// ---- scatter helpers ----------------------------------------------------
+static int upload_d(wf_domain* d, const double* src, int comps, double* dst, int stride, int off) {
+  WF_CUDA_OK(cudaMemcpyAsync(d->d_stage, src, sizeof(double) * comps * d->n, cudaMemcpyHostToDevice,
+                             d->stream));
+  k_scatter_d<<<nblk(d->n), 256, 0, d->stream>>>(d->n, d->inv, d->d_stage, comps, dst, stride, off);
+  WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+  return WF_OK;
+}
+template <class T>
+static int upload_t(wf_domain* d, const T* src, T* dst) {
+  WF_CUDA_OK(cudaMemcpyAsync(d->d_stage, src, sizeof(T) * d->n, cudaMemcpyHostToDevice, d->stream));
+  k_scatter_t<T><<<nblk(d->n), 256, 0, d->stream>>>(d->n, d->inv, (const T*)d->d_stage, dst);
+  WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+  return WF_OK;
+}
+static int fill_d(wf_domain* d, double v, double* dst, int stride, int off) {
+  k_fill_d<<<nblk(d->n), 256, 0, d->stream>>>(d->n, v, dst, stride, off);
+  WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+  return WF_OK;
+}
+static Fields& CF(wf_domain* d) { return d->F[d->cur]; }
+
+extern "C" {
+
+int wf_set_h(wf_domain* d, double h) {
+  if (!d || !(h > 0)) return WF_ERR_ARG;
+  d->h = h;
+  d->h_set = true;
+  return WF_OK;
+}
+int wf_set_density(wf_domain* d, double rho) {
+  if (!d || !(rho > 0)) return WF_ERR_ARG;
+  d->rho0 = rho;
+  d->rho_set = true;
+  return fill_d(d, rho, (double*)CF(d).vd, 4, 3);
+}
+int wf_set_shear_modulus(wf_domain* d, double G) {
+  if (!d) return WF_ERR_ARG;
+  d->G = G;
+  d->G_set = true;
+  return WF_OK;
+}
+int wf_set_sigma_y(wf_domain* d, double sy) {
+  if (!d) return WF_ERR_ARG;
+  return fill_d(d, sy, CF(d).sy, 1, 0);
+}
+int wf_set_conductivity(wf_domain* d, double k) {
+  if (!d) return WF_ERR_ARG;
+  return fill_d(d, k, CF(d).kT, 1, 0);
+}
+int wf_set_heat_cap(wf_domain* d, double cp) {
+  if (!d) return WF_ERR_ARG;
+  return fill_d(d, cp, CF(d).cpT, 1, 0);
+}
+int wf_set_cs(wf_domain* d, const double* cs) {
+  if (!d || !cs) return WF_ERR_ARG;
+  for (int64_t i = 1; i < d->n; i++)
+    if (cs[i] != cs[0]) return wf_fail(d, WF_ERR_ARG, "per-particle Cs must be uniform");
+  d->Cs = cs[0];
+  d->cs_set = true;
+  return WF_OK;
+}
+int wf_set_free(wf_domain* d, const uint8_t* f) {
+  if (!d || !f) return WF_ERR_ARG;
+  for (int64_t i = 0; i < d->n; i++)
+    if (!f[i]) return wf_fail(d, WF_ERR_ARG, "fixed (IsFree = false) particles are not supported");
+  return WF_OK;
+}
+int wf_set_id(wf_domain* d, const int32_t* id) {
+  if (!d || !id) return WF_ERR_ARG;
+  return upload_t<int32_t>(d, id, CF(d).id);
+}
+int wf_set_positions(wf_domain* d, const double* x) {
+  if (!d || !x) return WF_ERR_ARG;
+  for (int64_t i = 0; i < 3 * d->n; i++)
+    if (!std::isfinite(x[i])) return wf_fail(d, WF_ERR_ARG, "non-finite position");
+  d->x_set = true;
+  return upload_d(d, x, 3, (double*)CF(d).xm, 4, 0);
+}
+int wf_set_velocities(wf_domain* d, const double* v) {
+  if (!d || !v) return WF_ERR_ARG;
+  return upload_d(d, v, 3, (double*)CF(d).vd, 4, 0);
+}
+int wf_set_mass(wf_domain* d, const double* m) {
+  if (!d || !m) return WF_ERR_ARG;
+  d->m_set = true;
+  return upload_d(d, m, 1, (double*)CF(d).xm, 4, 3);
+}
+int wf_set_not_write_surf_id(wf_domain* d, const uint8_t* f) {
+  if (!d || !f) return WF_ERR_ARG;
+  return upload_t<uint8_t>(d, f, CF(d).nw);
+}
+int wf_set_solid_count(wf_domain* d, int64_t ns) {
+  if (!d || ns < 0 || ns > d->n) return WF_ERR_ARG;
+  d->n_solid = ns;
+  return WF_OK;
+}
+int wf_set_time_step(wf_domain* d, double dt) {
+  if (!d || !(dt > 0)) return WF_ERR_ARG;
+  d->dt = dt;
+  return WF_OK;
+}
+int wf_set_artificial_viscosity(wf_domain* d, double a, double b) {
+  if (!d) return WF_ERR_ARG;
+  d->alpha = a;
+  d->beta = b;
+  return WF_OK;
+}
+int wf_set_material(wf_domain* d, const wf_material* m) {
+  if (!d || !m) return WF_ERR_ARG;
+  if (m->model < WF_BILINEAR || m->model > WF_JOHNSON_COOK)
+    return wf_fail(d, WF_ERR_ARG, "unknown material model");
+  d->mat = *m;
+  d->mat_set = true;
+  return WF_OK;
+}
+int wf_add_velocity_bc(wf_domain* d, int32_t zone, double vx, double vy, double vz) {
+  if (!d) return WF_ERR_ARG;
+  if ((int)d->bc_zone.size() >= WF_MAX_BC) return wf_fail(d, WF_ERR_ARG, "too many boundary conditions");
+  d->bc_zone.push_back(zone);
+  d->bc_v.push_back({vx, vy, vz});
+  return WF_OK;
+}
+int wf_set_temperature(wf_domain* d, const double* T) {
+  if (!d || !T) return WF_ERR_ARG;
+  return upload_d(d, T, 1, CF(d).T, 1, 0);
+}
+int wf_set_thermal_bc(wf_domain* d, const int32_t* b) {
+  if (!d || !b) return WF_ERR_ARG;
+  return upload_t<int32_t>(d, b, CF(d).bct);
+}
+int wf_set_convection(wf_domain* d, double hc, double Tinf) {
+  if (!d) return WF_ERR_ARG;
+  d->h_conv = hc;
+  d->T_inf = Tinf;
+  return WF_OK;
+}
+
+int wf_set_option(wf_domain* d, const char* key, double v) {
+  if (!d || !key) return WF_ERR_ARG;
+  std::string k(key);
+  if (k == "precision") {
+    int p = (int)v;
+    if (p != 0 && p != 1) return wf_fail(d, WF_ERR_ARG, "precision must be 0 (fp64) or 1 (mixed)");
+    if (d->started && p != d->precision) {
+      if (p == 1) k_mixed_init<<<nblk(d->n), 256, 0, d->stream>>>(d->n, CF(d));
+      else k_mixed_to_fp64<<<nblk(d->n), 256, 0, d->stream>>>(d->n, CF(d));
+    }
+    d->precision = p;
+  } else if (k == "return_map") {
+    if (v != 0 && v != 1) return wf_fail(d, WF_ERR_ARG, "return_map must be 0 or 1");
+    d->return_map = (int)v;
+  } else if (k == "mlp") d->mlp_on = v != 0;
+  else if (k == "rebuild_every") {
+    if (v < 1) return WF_ERR_ARG;
+    d->rebuild_every = (int)v;
+  } else if (k == "rebuild_after_yield") d->rebuild_after_yield = v != 0;
+  else if (k == "rebuild_current_positions") d->rebuild_current = v != 0;
+  else if (k == "thermal") d->thermal = v != 0;
+  else if (k == "taylor_quinney") d->chi = v;
+  else if (k == "newton_rtol") d->newton_rtol = v;
+  else if (k == "newton_max_iter") d->newton_max_iter = (int)v;
+  else if (k == "energy_mode") d->energy_mode = (int)v;
+  else if (k == "output_interval") d->output_interval = v;
+  else if (k == "clamp_homologous") d->clamp_homologous = v != 0;
+  else if (k == "profile_kernel") d->profile_kernel = (int)v;
+  else if (k == "graph") { /* reserved */ }
+  else return wf_fail(d, WF_ERR_ARG, "unknown option: " + k);
+  return WF_OK;
+}
+
+int wf_find_neighbors(wf_domain* d) {
+  if (!d) return WF_ERR_ARG;
+  if (!d->h_set || !d->x_set) return wf_fail(d, WF_ERR_STATE, "h and positions required");
+  launch_snapshot(d->n, CF(d), d->stream);
+  int rc = rebuild(d, false);
+  if (rc) return rc;
+  return finish(d);
+}
+
+int wf_step(wf_domain* d, int64_t nsteps) {
+  if (!d || nsteps < 0) return WF_ERR_ARG;
+  if (!d->started) {
+    int rc = solve_begin(d, d->output_interval);
+    if (rc) return rc;
+  }
+  for (int64_t k = 0; k < nsteps; k++) {
+    int rc = solve_step(d);
+    if (rc) return rc;
+  }
+  return finish(d);
+}
+
+int wf_mech_fraser_solve(wf_domain* d, double tf, double dt_out) {
+  if (!d || !(dt_out > 0)) return WF_ERR_ARG;
+  int rc = solve_begin(d, dt_out);
+  if (rc) return rc;
+  while (d->time < tf) {
+    rc = solve_step(d);
+    if (rc) return rc;
+  }
+  return finish(d);
+}
+
+int wf_mech_solve(wf_domain* d, double tf, double dt_out) { return wf_mech_fraser_solve(d, tf, dt_out); }
+
+int wf_thermal_solve(wf_domain* d, double tf) {
+  if (!d) return WF_ERR_ARG;
+  if (!d->h_set || !d->x_set || !d->m_set || !d->rho_set || !(d->dt > 0))
+    return wf_fail(d, WF_ERR_STATE, "h, positions, masses, density and time step required");
+  d->time = 0.0;
+  d->isfirst = true;
+  WF_CUDA_OK(cudaMemsetAsync(d->d_status, 0, 8 * sizeof(int), d->stream));
+  int rc = rebuild(d, true);
+  if (rc) return rc;
+  if (d->precision == 1) k_mixed_init<<<nblk(d->n), 256, 0, d->stream>>>(d->n, CF(d));
+  StepParams P = make_params(d);
+  NbBuffers N{d->nb, d->nbc};
+  while (d->time < tf) {
+    {
+      KTimer t(d, KID_THERMAL);
+      launch_thermal(P, CF(d), N, d->isfirst ? 1 : 0, 0, d->precision == 1 ? 1 : 0, d->stream);
+    }
+    d->launches += 2;
+    d->isfirst = false;
+    d->time += d->dt;
+    d->step++;
+  }
+  return finish(d);
+}
+
+}  // extern "C"
+
+// ---- getters ---------------------------------------------------------------
+static int download(wf_domain* d, double* out, int64_t count) {
+  WF_CUDA_OK(cudaMemcpyAsync(out, d->d_stage, sizeof(double) * count, cudaMemcpyDeviceToHost, d->stream));
+  WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+  return WF_OK;
+}
+
+extern "C" {
+
+int wf_get_field(wf_domain* d, const char* name, double* out) {
+  if (!d || !name || !out) return WF_ERR_ARG;
+  const Fields& F = CF(d);
+  const int64_t n = d->n;
+  std::string s(name);
+  const bool mixed = d->precision == 1 && d->started;
+  double* st = d->d_stage;
+  auto g = [&](const double* src, int stride, int off, int comps) {
+    k_gather_d<<<nblk(n), 256, 0, d->stream>>>(n, d->inv, src, stride, off, comps, st);
+    return download(d, out, n * comps);
+  };
+  auto gf = [&](const float* src, int stride, int off, int comps) {
+    k_gather_f<<<nblk(n), 256, 0, d->stream>>>(n, d->inv, src, stride, off, comps, st);
+    return download(d, out, n * comps);
+  };
+  if (s == "x") return g((const double*)F.xm, 4, 0, 3);
+  if (s == "m") return g((const double*)F.xm, 4, 3, 1);
+  if (s == "v") return g((const double*)F.vd, 4, 0, 3);
+  if (s == "rho") return g((const double*)F.vd, 4, 3, 1);
+  if (s == "u") return g((const double*)F.u, 4, 0, 3);
+  if (s == "a") return g((const double*)F.a, 4, 0, 3);
+  if (s == "sigma") {
+    if (mixed) {
+      k_gather_sigma32<<<nblk(n), 256, 0, d->stream>>>(n, d->inv, F.ss32, F.p, st);
+      return download(d, out, 6 * n);
+    }
+    return g(F.sig6, 6, 0, 6);
+  }
+  if (s == "shearstress") return mixed ? gf(F.ss32, 6, 0, 6) : g(F.ss6, 6, 0, 6);
+  if (s == "strain") return g(F.eps6, 6, 0, 6);
+  if (s == "strrate") return g(F.sr6, 6, 0, 6);
+  if (s == "rotrate") return g(F.rr6, 6, 0, 6);
+  if (s == "p") return g(F.p, 1, 0, 1);
+  if (s == "sigma_eq") return g(F.seq, 1, 0, 1);
+  if (s == "pl_strain") return g(F.eps_p, 1, 0, 1);
+  if (s == "sigma_y") return g(F.sy, 1, 0, 1);
+  if (s == "eff_strain_rate") return g(F.eff, 1, 0, 1);
+  if (s == "dep") return g(F.dep, 1, 0, 1);
+  if (s == "drho") return g(F.drho, 1, 0, 1);
+  if (s == "int_energy") return g(F.eint, 1, 0, 1);
+  if (s == "T") return g(F.T, 1, 0, 1);
+  if (s == "Ta") return g(F.Ta, 1, 0, 1);
+  if (s == "Tb") return g(F.Tb, 1, 0, 1);
+  if (s == "dTdt") return g(F.dTdt, 1, 0, 1);
+  return wf_fail(d, WF_ERR_ARG, "unknown field: " + s);
+}
+
+int wf_get_field_i32(wf_domain* d, const char* name, int32_t* out) {
+  if (!d || !name || !out) return WF_ERR_ARG;
+  std::string s(name);
+  const Fields& F = CF(d);
+  const int32_t* src = nullptr;
+  if (s == "ID") src = F.id;
+  else if (s == "nb_count") src = d->nbc;
+  else if (s == "BC_T") src = F.bct;
+  else return wf_fail(d, WF_ERR_ARG, "unknown field: " + s);
+  k_gather_t<int32_t><<<nblk(d->n), 256, 0, d->stream>>>(d->n, d->inv, src, (int32_t*)d->d_stage);
+  WF_CUDA_OK(cudaMemcpyAsync(out, d->d_stage, sizeof(int32_t) * d->n, cudaMemcpyDeviceToHost, d->stream));
+  WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+  return WF_OK;
+}
+
+int wf_get_neighbors(wf_domain* d, int32_t* counts, int32_t* lists) {
+  if (!d || !counts || !lists) return WF_ERR_ARG;
+  if (!d->nb_built) return wf_fail(d, WF_ERR_STATE, "no neighbour list yet");
+  int32_t *dc = nullptr, *dl = nullptr;
+  WF_CUDA_OK(cudaMalloc((void**)&dc, sizeof(int32_t) * d->n));
+  cudaError_t e = cudaMalloc((void**)&dl, sizeof(int32_t) * d->n * WF_NB);
+  if (e != cudaSuccess) { cudaFree(dc); return wf_cuda_fail(d, e, "cudaMalloc"); }
+  k_gather_nb<<<nblk(d->n), 256, 0, d->stream>>>(d->n, d->npad, d->inv, CF(d).perm, d->nb, d->nbc, dc, dl);
+  cudaMemcpyAsync(counts, dc, sizeof(int32_t) * d->n, cudaMemcpyDeviceToHost, d->stream);
+  cudaMemcpyAsync(lists, dl, sizeof(int32_t) * d->n * WF_NB, cudaMemcpyDeviceToHost, d->stream);
+  e = cudaStreamSynchronize(d->stream);
+  cudaFree(dc);
+  cudaFree(dl);
+  if (e != cudaSuccess) return wf_cuda_fail(d, e, "get_neighbors");
+  return WF_OK;
+}
+
+int wf_get_scalar(wf_domain* d, const char* name, double* out) {
+  if (!d || !name || !out) return WF_ERR_ARG;
+  std::string s(name);
+  if (s == "time") { *out = d->time; return WF_OK; }
+  if (s == "step") { *out = (double)d->step; return WF_OK; }
+  if (s == "is_yielding") { *out = d->is_yielding; return WF_OK; }
+  if (s == "launches") { *out = (double)d->launches; return WF_OK; }
+  if (s == "newton_iters" || s == "newton_calls" || s == "status") {
+    int rc = read_status(d);
+    if (rc) return rc;
+    unsigned long long v;
+    if (s == "status") { *out = d->h_status[0]; return WF_OK; }
+    memcpy(&v, d->h_status + (s == "newton_iters" ? 2 : 4), sizeof v);
+    *out = (double)v;
+    return WF_OK;
+  }
+  if (s == "int_energy_sum") {
+    std::vector<double> e(d->n);
+    int rc = wf_get_field(d, "int_energy", e.data());
+    if (rc) return rc;
+    double sum = 0.0;
+    for (double v : e) sum += v;
+    *out = sum;
+    return WF_OK;
+  }
+  return wf_fail(d, WF_ERR_ARG, "unknown scalar: " + s);
+}
+
+// Domain_d::WriteCSV (src/cuda/Domain_d.cu:556-587): same header and format.
+int wf_write_csv(wf_domain* d, const char* path) {
+  if (!d || !path) return WF_ERR_ARG;
+  const int64_t n = d->n;
+  std::vector<double> x(3 * n), u(3 * n), v(3 * n), a(3 * n), rho(n), p(n), seq(n), ps(n);
+  std::vector<int32_t> id(n), nbc(n);
+  int rc = 0;
+  if ((rc = wf_get_field(d, "x", x.data())) || (rc = wf_get_field(d, "u", u.data())) ||
+      (rc = wf_get_field(d, "v", v.data())) || (rc = wf_get_field(d, "a", a.data())) ||
+      (rc = wf_get_field(d, "rho", rho.data())) || (rc = wf_get_field(d, "p", p.data())) ||
+      (rc = wf_get_field(d, "sigma_eq", seq.data())) || (rc = wf_get_field(d, "pl_strain", ps.data())) ||
+      (rc = wf_get_field_i32(d, "ID", id.data())) || (rc = wf_get_field_i32(d, "nb_count", nbc.data())))
+    return rc;
+  FILE* f = fopen(path, "w");
+  if (!f) return wf_fail(d, WF_ERR_IO, std::string("cannot open ") + path);
+  fprintf(f, "ID, X, Y, Z, posX,posY,posZ,Ux, Uy, Uz, Vx, Vy, Vz, Ax, Ay, Az, rho, p, SigmaEq, "
+             "Pl_Strain, Nb, ContNb, CFx, CFy, CFz, Nx, Ny, Nz, h\n");
+  for (int64_t i = 0; i < n; i++) {
+    fprintf(f,
+            "%d, %.6e, %.6e, %.6e, %.6e, %.6e, %.6e, %.6e, %.6e, %.6e, %.6e, %.6e, %.6e, %.6e, "
+            "%.6e, %.6e, %.6e, %.6e, %.6e, %.6e, %d, %d, %.6e, %.6e, %.6e, %.6e, %.6e, %.6e, %6e\n",
+            id[i], x[3 * i], x[3 * i + 1], x[3 * i + 2], x[3 * i], x[3 * i + 1], x[3 * i + 2],
+            u[3 * i], u[3 * i + 1], u[3 * i + 2], v[3 * i], v[3 * i + 1], v[3 * i + 2], a[3 * i],
+            a[3 * i + 1], a[3 * i + 2], rho[i], p[i], seq[i], ps[i], nbc[i], 0, 0.0, 0.0, 0.0,
+            0.0, 0.0, 0.0, d->h);
+  }
+  fclose(f);
+  return WF_OK;
+}
+
+int wf_time_steps(wf_domain* d, int64_t nsteps, double* elapsed_ms, double* kernel_ms,
+                  int64_t* kernel_launches, int64_t* total_launches) {
+  if (!d || nsteps < 0) return WF_ERR_ARG;
+  if (!d->started) {
+    int rc = solve_begin(d, d->output_interval);
+    if (rc) return rc;
+  }
+  cudaEvent_t e0, e1;
+  WF_CUDA_OK(cudaEventCreate(&e0));
+  WF_CUDA_OK(cudaEventCreate(&e1));
+  d->ev_used = 0;
+  const int64_t l0 = d->launches;
+  WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+  cudaEventRecord(e0, d->stream);
+  int rc = WF_OK;
+  d->timing = true;
+  for (int64_t k = 0; k < nsteps && rc == WF_OK; k++) rc = solve_step(d);
+  d->timing = false;
+  cudaEventRecord(e1, d->stream);
+  WF_CUDA_OK(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  if (elapsed_ms) *elapsed_ms = ms;
+  double kms = 0.0;
+  for (size_t k = 0; k + 1 < d->ev_used; k += 2) {
+    float t = 0.f;
+    cudaEventElapsedTime(&t, d->ev_pool[k], d->ev_pool[k + 1]);
+    kms += t;
+  }
+  if (kernel_ms) *kernel_ms = kms;
+  if (kernel_launches) *kernel_launches = (int64_t)(d->ev_used / 2);
+  if (total_launches) *total_launches = d->launches - l0;
+  d->ev_used = 0;
+  return finish(d);
+}
+
+}  // extern "C"

@@ -1,0 +1,154 @@
+// wf_common.cuh — shared definitions of the GB300 SPH step kernels.
+//
+// Per-particle state lives in "slots": particles are sorted by neighbour-search
+// cell (ties broken by original particle id) at every neighbour rebuild and
+// every per-particle array is physically reordered, so the pair loops gather
+// neighbours that sit close in memory.  perm[slot] = original id and
+// inv[original id] = slot translate at the ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/weldform_gb300.h"
+
+#define WF_NB WF_MAX_NEIGHBORS
+#define WF_MAX_BC 16
+#define WF_MAX_MESH 4
+#define WF_PI 3.14159265358979323846
+
+// Device status bits (d_status[0]), read by the host after a run.
+#define WF_STATUS_NAN       1   // a kernel produced NaN/Inf in the stress state
+#define WF_STATUS_NB_CAP    2   // some particle hit WF_MAX_NEIGHBORS (list truncated)
+#define WF_STATUS_GRID      4   // a particle fell outside the search grid
+
+// All per-slot arrays that move with the particles at a reorder.
+struct Fields {
+  double4* xm;      // position xyz, mass w
+  double4* vd;      // velocity xyz, density w (start of step)
+  double4* u;       // displacement xyz
+  double4* a;       // acceleration xyz
+  double* sig6;     // Cauchy stress, flat [xx yy zz xy yz xz]
+  double* ss6;      // deviatoric (shear) stress
+  double* eps6;     // accumulated strain
+  double* sr6;      // strain rate
+  double* rr6;      // rotation rate (upper triangle of the antisymmetric tensor)
+  double* p;        // pressure
+  double* seq;      // sigma_eq
+  double* eps_p;    // accumulated equivalent plastic strain
+  double* sy;       // yield stress
+  double* eff;      // effective strain rate
+  double* dep;      // plastic strain increment of the last step
+  double* drho;     // density rate of the last step
+  double* eint;     // internal energy
+  double* T;        // temperature
+  double* Ta;       // temperature leapfrog half steps
+  double* Tb;
+  double* dTdt;
+  double* kT;       // conductivity
+  double* cpT;      // heat capacity
+  int32_t* id;      // zone / surface id
+  int32_t* bct;     // thermal BC flag (1 = convection)
+  int32_t* perm;    // original particle id of the slot
+  uint8_t* nw;      // not_write_surf_ID
+  float4* xh;       // float positions the next neighbour rebuild reads (x_h)
+  // mixed-precision mirrors (written by the integration kernel)
+  float4* p32;      // position xyz, mass w
+  float4* v32;      // velocity xyz, density w
+  float* ss32;      // deviatoric stress FP32 state (mixed form), 6 per slot
+};
+
+// Johnson-Cook / bilinear / Hollomon constants as the kernels use them.
+struct MatParams {
+  int model;
+  double E, Et, Ep;               // bilinear
+  double K_hol, m_hol, eps0_hol, eps1_hol, sy0;
+  double A, B, n, C, eps0, m, Tm, Tt;
+};
+
+struct StepParams {
+  int64_t n;            // slots (all particles)
+  int64_t n_solid;      // original ids below this are solid (solid_part_count)
+  int64_t npad;         // column stride of the ELL neighbour list
+  double h, gkC;        // smoothing length (uniform) and 1/(h^4 pi)
+  double dt;
+  double Cs, G, rho0;   // uniform sound speed, shear modulus, reference density
+  double alpha, beta;   // Monaghan artificial viscosity
+  double chi;           // Taylor-Quinney coefficient (0: no plastic heat)
+  double h_conv, T_inf; // convection
+  int return_map;       // 0 reference radial return, 1 consistent Newton
+  int newton_max_iter;
+  double newton_rtol;
+  int clamp_homologous;
+  int energy_mode;      // 0 reference (particle 0's tensors), 1 per particle
+  const int32_t* inv;   // inv[original id] = slot (particle 0's slot for energy_mode 0)
+  int contact;          // contact pass filter active
+  int ncsid;
+  int32_t csid[WF_MAX_MESH];
+  int nbc;
+  int32_t bc_zone[WF_MAX_BC];
+  double bc_v[WF_MAX_BC][3];
+  int mlp_on;           // MLP warm start of the Newton return map
+  MatParams mat;
+};
+
+#define WF_CUDA_OK(call)                                   \
+  do {                                                     \
+    cudaError_t e_ = (call);                               \
+    if (e_ != cudaSuccess) return wf_cuda_fail(d, e_, #call); \
+  } while (0)
+
+// Cubic-spline kernel gradient (Dim 3) with C = 1/(h^4 pi) hoisted: the
+// reference recomputes C from h_ = (h_i + h_j)/2 = h for every pair
+// (src/cuda/Functions.cu:76-88); with a uniform h the value is identical.
+__device__ __forceinline__ double gradK64(double q, double h, double C) {
+  if (q == 0.0) return C / h * (-3.0 + (9.0 / 2.0) * q);
+  else if (q < 1.0) return C / (q * h) * (-3.0 * q + (9.0 / 4.0) * q * q);
+  else if (q < 2.0) return C / (q * h) * ((-3.0 / 4.0) * (2.0 - q) * (2.0 - q));
+  return 0.0;
+}
+
+__device__ __forceinline__ float gradK32(float q, float h, float C) {
+  if (q < 1.0f) return C / h * (-3.0f + 2.25f * q);
+  else if (q < 2.0f) return C / (q * h) * (-0.75f * (2.0f - q) * (2.0f - q));
+  return 0.0f;
+}
+
+__device__ __forceinline__ bool pass_ij(const StepParams& P, int32_t idi, int32_t idj) {
+  if (!P.contact) return true;
+  bool pass = false;
+  for (int mc = 0; mc < P.ncsid; mc++)
+    if (idj != P.csid[mc] && idi != P.csid[mc]) pass = true;
+  return pass;
+}
+__device__ __forceinline__ bool pass_j(const StepParams& P, int32_t idj) {
+  if (!P.contact) return true;
+  bool pass = false;
+  for (int mc = 0; mc < P.ncsid; mc++)
+    if (idj != P.csid[mc]) pass = true;
+  return pass;
+}
+
+// Kernel launchers (defined in the .cu files, called by wf_api.cu).
+struct NbBuffers {
+  int32_t* nb;      // [WF_NB * npad]
+  int32_t* cnt;     // [npad]
+};
+
+void launch_fp64_density(const StepParams& P, const Fields& F, double4* vd2, const NbBuffers& N,
+                         cudaStream_t s);
+void launch_fp64_stress(const StepParams& P, const Fields& F, const double4* vd2,
+                        const NbBuffers& N, int* status, cudaStream_t s);
+void launch_fp64_accel(const StepParams& P, const Fields& F, const double4* vd2,
+                       const NbBuffers& N, cudaStream_t s);
+void launch_integrate(const StepParams& P, const Fields& F, const double4* vd2, int mixed,
+                      cudaStream_t s);
+void launch_thermal(const StepParams& P, const Fields& F, const NbBuffers& N, int first,
+                    int plastic_heat, int mixed, cudaStream_t s);
+
+void launch_fp32_density(const StepParams& P, const Fields& F, double4* vd2, float4* v32b,
+                         const NbBuffers& N, cudaStream_t s);
+void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b,
+                        float* sigr32, const NbBuffers& N, int* status, const float* mlp_w,
+                        cudaStream_t s);
+void launch_fp32_accel(const StepParams& P, const Fields& F, const float4* v32b,
+                       const float* sigr32, const NbBuffers& N, cudaStream_t s);

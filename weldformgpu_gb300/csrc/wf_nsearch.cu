@@ -1,0 +1,320 @@
+// wf_nsearch.cu — neighbour search with cuNSearch's float32 rule, cell sort
+// and physical reorder of every per-particle array.
+//
+// Rule (src/cuNSearch/src/cuNSearchKernels.cu:41-234, cuNSearchDeviceData.cu:
+// 27-174): search radius r = float(2 h); cell = floor((p - GridMin) *
+// GridDelta) in float; candidates from the 27 cells in z, y, x order;
+// accept j when the float squared distance is < r*r and > 0; at most 70.
+// The distance is computed with round-to-nearest intrinsics, so no fused
+// multiply-add can change which pairs pass.
+//
+// Layout: particles are counting-sorted by linear cell index (z-major), ties
+// by original id, and all state is gathered into the new order.  The three
+// x-adjacent cells of a row are then one contiguous slot range, so a
+// particle's candidates are 9 ranges, visited in the reference's order.
+// Lists are stored column-major (nb[k * npad + slot]) so that consecutive
+// threads read consecutive words.
+#include "wf_common.cuh"
+#include "wf_nsearch.cuh"
+
+namespace {
+
+__device__ __forceinline__ int cell_coord(float p, float gmin, float gdelta) {
+  return (int)floorf(__fmul_rn(__fsub_rn(p, gmin), gdelta));
+}
+
+// float positions the search reads: x_h snapshot or the current positions
+__global__ void k_prep_positions(int64_t n, const Fields F, int use_current, float4* pf) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (use_current) {
+    double4 x = F.xm[i];
+    pf[i] = make_float4(__double2float_rn(x.x), __double2float_rn(x.y), __double2float_rn(x.z), 0.f);
+  } else {
+    pf[i] = F.xh[i];
+  }
+}
+
+// kComputeMinMax: integer cell bounds of floor(p / r), block-reduced first
+__global__ void k_minmax(int64_t n, const float4* __restrict__ pf, float r, int* mm) {
+  __shared__ int smn[3][32], smx[3][32];
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int mn[3] = {INT_MAX, INT_MAX, INT_MAX}, mx[3] = {INT_MIN, INT_MIN, INT_MIN};
+  if (i < n) {
+    float4 p = pf[i];
+    int c0 = (int)floorf(__fdiv_rn(p.x, r)), c1 = (int)floorf(__fdiv_rn(p.y, r)),
+        c2 = (int)floorf(__fdiv_rn(p.z, r));
+    mn[0] = mx[0] = c0; mn[1] = mx[1] = c1; mn[2] = mx[2] = c2;
+  }
+  for (int a = 0; a < 3; a++) {
+    for (int o = 16; o > 0; o >>= 1) {
+      mn[a] = min(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
+      mx[a] = max(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
+    }
+  }
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0)
+    for (int a = 0; a < 3; a++) { smn[a][w] = mn[a]; smx[a][w] = mx[a]; }
+  __syncthreads();
+  if (w == 0) {
+    int nw = blockDim.x >> 5;
+    for (int a = 0; a < 3; a++) {
+      int v = l < nw ? smn[a][l] : INT_MAX, u = l < nw ? smx[a][l] : INT_MIN;
+      for (int o = 16; o > 0; o >>= 1) {
+        v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+        u = max(u, __shfl_xor_sync(0xffffffffu, u, o));
+      }
+      if (l == 0) { atomicMin(mm + a, v); atomicMax(mm + 3 + a, u); }
+    }
+  }
+}
+
+__global__ void k_cell_count(int64_t n, const float4* __restrict__ pf, GridDev g,
+                             uint32_t* __restrict__ cellid, uint32_t* __restrict__ count,
+                             int* status) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 p = pf[i];
+  int cx = cell_coord(p.x, g.gmin[0], g.gdelta[0]);
+  int cy = cell_coord(p.y, g.gmin[1], g.gdelta[1]);
+  int cz = cell_coord(p.z, g.gmin[2], g.gdelta[2]);
+  if (cx < 0 || cy < 0 || cz < 0 || cx >= g.dim[0] || cy >= g.dim[1] || cz >= g.dim[2]) {
+    atomicOr(status, WF_STATUS_GRID);
+    cx = min(max(cx, 0), g.dim[0] - 1);
+    cy = min(max(cy, 0), g.dim[1] - 1);
+    cz = min(max(cz, 0), g.dim[2] - 1);
+  }
+  uint32_t c = ((uint32_t)cz * g.dim[1] + cy) * g.dim[0] + cx;
+  cellid[i] = c;
+  atomicAdd(count + c, 1u);
+}
+
+// exclusive scan, 1024 elements per block (256 threads x 4)
+__global__ void k_scan_block(uint32_t* data, int64_t n, uint32_t* block_sums) {
+  __shared__ uint32_t warp_tot[8];
+  int64_t base = (int64_t)blockIdx.x * 1024 + threadIdx.x * 4;
+  uint32_t v[4];
+  for (int k = 0; k < 4; k++) v[k] = (base + k < n) ? data[base + k] : 0u;
+  uint32_t t = v[0] + v[1] + v[2] + v[3];
+  uint32_t incl = t;
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) warp_tot[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    uint32_t x = lane < 8 ? warp_tot[lane] : 0u;
+    uint32_t xi = x;
+    for (int o = 1; o < 8; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, xi, o);
+      if (lane >= o) xi += y;
+    }
+    if (lane < 8) warp_tot[lane] = xi - x;
+    if (lane == 7 && block_sums) block_sums[blockIdx.x] = xi;
+  }
+  __syncthreads();
+  uint32_t run = warp_tot[w] + incl - t;
+  for (int k = 0; k < 4; k++) {
+    if (base + k < n) data[base + k] = run;
+    run += v[k];
+  }
+}
+
+__global__ void k_scan_add(uint32_t* data, int64_t n, const uint32_t* block_sums) {
+  int64_t base = (int64_t)blockIdx.x * 1024 + threadIdx.x * 4;
+  uint32_t add = block_sums[blockIdx.x];
+  for (int k = 0; k < 4; k++)
+    if (base + k < n) data[base + k] += add;
+}
+
+__global__ void k_cell_scatter(int64_t n, const uint32_t* __restrict__ cellid,
+                               const uint32_t* __restrict__ start, uint32_t* __restrict__ cursor,
+                               const int32_t* __restrict__ perm, int32_t* __restrict__ s_src,
+                               int32_t* __restrict__ s_orig) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint32_t c = cellid[i];
+  uint32_t pos = start[c] + atomicAdd(cursor + c, 1u);
+  s_src[pos] = (int32_t)i;
+  s_orig[pos] = perm[i];
+}
+
+// order each cell's slots by original id (insertion sort; cells hold ~14)
+__global__ void k_cell_sort(int64_t ncell, const uint32_t* __restrict__ start,
+                            int32_t* __restrict__ s_src, int32_t* __restrict__ s_orig) {
+  int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= ncell) return;
+  uint32_t b = start[c], e = start[c + 1];
+  for (uint32_t k = b + 1; k < e; k++) {
+    int32_t ko = s_orig[k], ks = s_src[k];
+    uint32_t m = k;
+    while (m > b && s_orig[m - 1] > ko) {
+      s_orig[m] = s_orig[m - 1];
+      s_src[m] = s_src[m - 1];
+      m--;
+    }
+    s_orig[m] = ko;
+    s_src[m] = ks;
+  }
+}
+
+template <class T>
+__device__ __forceinline__ void g1(T* dst, const T* src, int64_t k, int64_t s) {
+  if (dst) dst[k] = src[s];
+}
+__device__ __forceinline__ void g6(double* dst, const double* src, int64_t k, int64_t s) {
+  if (!dst) return;
+  const double2* a = reinterpret_cast<const double2*>(src + 6 * s);
+  double2* b = reinterpret_cast<double2*>(dst + 6 * k);
+  b[0] = a[0]; b[1] = a[1]; b[2] = a[2];
+}
+__device__ __forceinline__ void g6f(float* dst, const float* src, int64_t k, int64_t s) {
+  if (!dst) return;
+  const float2* a = reinterpret_cast<const float2*>(src + 6 * s);
+  float2* b = reinterpret_cast<float2*>(dst + 6 * k);
+  b[0] = a[0]; b[1] = a[1]; b[2] = a[2];
+}
+
+// gather every per-slot array into the new order; inv[orig] = new slot
+__global__ void k_reorder(int64_t n, const int32_t* __restrict__ s_src, const Fields A, Fields B,
+                          const float4* __restrict__ pf, float4* __restrict__ pf2,
+                          int32_t* __restrict__ inv) {
+  int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  int64_t s = s_src[k];
+  g1(B.xm, A.xm, k, s); g1(B.vd, A.vd, k, s); g1(B.u, A.u, k, s); g1(B.a, A.a, k, s);
+  g6(B.sig6, A.sig6, k, s); g6(B.ss6, A.ss6, k, s); g6(B.eps6, A.eps6, k, s);
+  g6(B.sr6, A.sr6, k, s); g6(B.rr6, A.rr6, k, s);
+  g1(B.p, A.p, k, s); g1(B.seq, A.seq, k, s); g1(B.eps_p, A.eps_p, k, s); g1(B.sy, A.sy, k, s);
+  g1(B.eff, A.eff, k, s); g1(B.dep, A.dep, k, s); g1(B.drho, A.drho, k, s);
+  g1(B.eint, A.eint, k, s);
+  g1(B.T, A.T, k, s); g1(B.Ta, A.Ta, k, s); g1(B.Tb, A.Tb, k, s); g1(B.dTdt, A.dTdt, k, s);
+  g1(B.kT, A.kT, k, s); g1(B.cpT, A.cpT, k, s);
+  g1(B.id, A.id, k, s); g1(B.bct, A.bct, k, s); g1(B.nw, A.nw, k, s); g1(B.xh, A.xh, k, s);
+  g1(B.p32, A.p32, k, s); g1(B.v32, A.v32, k, s); g6f(B.ss32, A.ss32, k, s);
+  int32_t o = A.perm[s];
+  B.perm[k] = o;
+  inv[o] = (int32_t)k;
+  pf2[k] = pf[s];
+}
+
+// kComputeCounts + kNeighborhoodQueryWithCounts in one pass (ELL output)
+__global__ void __launch_bounds__(128) k_nblist(int64_t n, int64_t npad, const float4* __restrict__ pf,
+                                                GridDev g, const uint32_t* __restrict__ start,
+                                                int32_t* __restrict__ nb, int32_t* __restrict__ cnt,
+                                                int* status) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 p = pf[i];
+  const int cx = cell_coord(p.x, g.gmin[0], g.gdelta[0]);
+  const int cy = cell_coord(p.y, g.gmin[1], g.gdelta[1]);
+  const int cz = cell_coord(p.z, g.gmin[2], g.gdelta[2]);
+  const float r2 = g.r2;
+  int count = 0;
+  const int x0 = max(cx - 1, 0), x1 = min(cx + 1, g.dim[0] - 1);
+  for (int z = -1; z < 2; z++) {
+    const int fz = cz + z;
+    if (fz < 0 || fz >= g.dim[2]) continue;
+    for (int y = -1; y < 2; y++) {
+      const int fy = cy + y;
+      if (fy < 0 || fy >= g.dim[1]) continue;
+      if (x0 > x1) continue;
+      const uint32_t rowc = ((uint32_t)fz * g.dim[1] + fy) * g.dim[0];
+      const uint32_t b = __ldg(start + rowc + x0), e = __ldg(start + rowc + x1 + 1);
+      for (uint32_t s = b; s < e; s++) {
+        const float4 q = pf[s];
+        const float dx = __fsub_rn(q.x, p.x), dy = __fsub_rn(q.y, p.y), dz = __fsub_rn(q.z, p.z);
+        const float sq = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+        if (sq < r2 && sq > 0.0f) {
+          nb[(int64_t)count * npad + i] = (int32_t)s;
+          count++;
+          if (count == WF_NB) {
+            cnt[i] = count;
+            atomicOr(status, WF_STATUS_NB_CAP);
+            return;
+          }
+        }
+      }
+    }
+  }
+  cnt[i] = count;
+}
+
+__global__ void k_snapshot(int64_t n, Fields F) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double4 x = F.xm[i];
+  F.xh[i] = make_float4(__double2float_rn(x.x), __double2float_rn(x.y), __double2float_rn(x.z), 0.f);
+}
+
+inline int nblocks(int64_t n, int t) { return (int)((n + t - 1) / t); }
+
+}  // namespace
+
+// host-side grid set-up, computeCellInformation (cuNSearchDeviceData.cu:80-123)
+void grid_from_minmax(const int mm[6], float r, GridDev* g) {
+  for (int a = 0; a < 3; a++) {
+    float Min = (float)mm[a] * r, Max = (float)mm[3 + a] * r;
+    float gridSize = Max - Min;
+    g->dim[a] = (int)((unsigned)ceilf(gridSize / r) + 4u);
+    g->gmin[a] = Min - r * 2.0f;
+    float gs2 = (float)(unsigned)g->dim[a] * r;
+    g->gdelta[a] = (float)(unsigned)g->dim[a] / gs2;
+  }
+  g->r2 = r * r;
+}
+
+void device_exclusive_scan(uint32_t* data, int64_t n, uint32_t* tmp, cudaStream_t s) {
+  int64_t nb = (n + 1023) / 1024;
+  if (nb <= 1) {
+    k_scan_block<<<1, 256, 0, s>>>(data, n, nullptr);
+    return;
+  }
+  k_scan_block<<<(int)nb, 256, 0, s>>>(data, n, tmp);
+  device_exclusive_scan(tmp, nb, tmp + nb, s);
+  k_scan_add<<<(int)nb, 256, 0, s>>>(data, n, tmp);
+}
+
+int64_t scan_tmp_words(int64_t n) {
+  int64_t w = 0;
+  while (n > 1024) {
+    n = (n + 1023) / 1024;
+    w += n;
+  }
+  return w + 1;
+}
+
+void launch_prep_positions(int64_t n, const Fields& F, int use_current, float4* pf,
+                           cudaStream_t s) {
+  k_prep_positions<<<nblocks(n, 256), 256, 0, s>>>(n, F, use_current, pf);
+}
+void launch_minmax(int64_t n, const float4* pf, float r, int* mm, cudaStream_t s) {
+  k_minmax<<<nblocks(n, 256), 256, 0, s>>>(n, pf, r, mm);
+}
+void launch_cell_count(int64_t n, const float4* pf, const GridDev& g, uint32_t* cellid,
+                       uint32_t* count, int* status, cudaStream_t s) {
+  k_cell_count<<<nblocks(n, 256), 256, 0, s>>>(n, pf, g, cellid, count, status);
+}
+void launch_cell_scatter(int64_t n, const uint32_t* cellid, const uint32_t* start,
+                         uint32_t* cursor, const int32_t* perm, int32_t* s_src, int32_t* s_orig,
+                         cudaStream_t s) {
+  k_cell_scatter<<<nblocks(n, 256), 256, 0, s>>>(n, cellid, start, cursor, perm, s_src, s_orig);
+}
+void launch_cell_sort(int64_t ncell, const uint32_t* start, int32_t* s_src, int32_t* s_orig,
+                      cudaStream_t s) {
+  k_cell_sort<<<nblocks(ncell, 256), 256, 0, s>>>(ncell, start, s_src, s_orig);
+}
+void launch_reorder(int64_t n, const int32_t* s_src, const Fields& A, const Fields& B,
+                    const float4* pf, float4* pf2, int32_t* inv, cudaStream_t s) {
+  k_reorder<<<nblocks(n, 256), 256, 0, s>>>(n, s_src, A, B, pf, pf2, inv);
+}
+void launch_nblist(int64_t n, int64_t npad, const float4* pf, const GridDev& g,
+                   const uint32_t* start, int32_t* nb, int32_t* cnt, int* status,
+                   cudaStream_t s) {
+  k_nblist<<<nblocks(n, 128), 128, 0, s>>>(n, npad, pf, g, start, nb, cnt, status);
+}
+void launch_snapshot(int64_t n, const Fields& F, cudaStream_t s) {
+  k_snapshot<<<nblocks(n, 256), 256, 0, s>>>(n, F);
+}

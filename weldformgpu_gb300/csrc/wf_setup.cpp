@@ -1,0 +1,154 @@
+// wf_setup.cpp — host domain set-up: the reference's particle generators and
+// zone assignment (src/Domain.cpp), used by the JSON driver and the C ABI.
+//
+// The generators reproduce the reference's floating-point sequence (running
+// sums, not products) so that particle positions are bit-identical.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+#include "../../include/weldform_gb300.h"
+#include "wf_setup.h"
+
+namespace {
+constexpr double kPi = 3.14159265358979323846;
+
+// calcHalfPartCount (src/Domain.cpp:473-488): particles on one quadrant row
+int half_count(double r, double R, int xinc) {
+  int cnt = -1;
+  if (xinc > 0) {
+    cnt = 1;
+    double yp = r;
+    double xp = r + (double)(xinc - 1) * 2. * r;
+    double rad = std::sqrt(yp * yp + xp * xp);
+    while (rad <= R - r) {
+      yp += 2. * r;
+      rad = std::sqrt(yp * yp + xp * xp);
+      cnt++;
+    }
+    cnt -= 1;
+  }
+  return cnt;
+}
+
+uint64_t splitmix64(uint64_t* s) {
+  uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+double uniform01(uint64_t* s) { return (double)(splitmix64(s) >> 11) * (1.0 / 9007199254740992.0); }
+}  // namespace
+
+extern "C" {
+
+// Domain::AddCylinderLength (src/Domain.cpp:490-573): layers of 2r pitch,
+// each layer built row by row from the quadrant counts; mass = pi R^2 L rho / N.
+int64_t wf_gen_cylinder(double x0, double y0, double z0, double Rxy, double Lz, double r,
+                        double density, double* x, double* mass) {
+  int64_t cnt = 0;
+  const int nxy = half_count(r, Rxy, 1);
+  double zp = z0 + r;
+  while (zp <= (z0 + Lz - r)) {
+    double yp = y0 - r - (2. * r * (nxy - 1));
+    const int nyp = 2 * nxy;
+    int yinc = nxy, sign = -1;
+    for (int j = 0; j < nyp; j++) {
+      const int nxp = half_count(r, Rxy, yinc);
+      double xp = x0 - r - (2. * r * (nxp - 1));
+      for (int i = 0; i < 2 * nxp; i++) {
+        if (x) { x[3 * cnt] = xp; x[3 * cnt + 1] = yp; x[3 * cnt + 2] = zp; }
+        cnt++;
+        xp += 2. * r;
+      }
+      yp += 2. * r;
+      yinc += sign;
+      if (yinc < 1) { yinc = 1; sign = 1; }
+    }
+    zp += 2. * r;
+  }
+  const double vol = kPi * Rxy * Rxy * Lz;
+  if (mass && cnt > 0) *mass = vol * density / (double)cnt;
+  return cnt;
+}
+
+// Domain::AddBoxLength, cubic packing (src/Domain.cpp:296-338): mass from
+// the bounding box of the generated centres grown by r.
+int64_t wf_gen_box(double x0, double y0, double z0, double Lx, double Ly, double Lz, double r,
+                   double density, double* x, double* mass) {
+  int64_t cnt = 0;
+  double mx[3] = {x0, y0, z0};
+  size_t k = 0;
+  double zp = z0;
+  while (zp <= (z0 + Lz - r)) {
+    size_t j = 0;
+    double yp = y0;
+    while (yp <= (y0 + Ly - r)) {
+      size_t i = 0;
+      double xp = x0;
+      while (xp <= (x0 + Lx - r)) {
+        const double px = x0 + (2.0 * i + 1) * r, py = y0 + (2.0 * j + 1) * r,
+                     pz = z0 + (2.0 * k + 1) * r;
+        if (x) { x[3 * cnt] = px; x[3 * cnt + 1] = py; x[3 * cnt + 2] = pz; }
+        if (px > mx[0]) mx[0] = px;
+        if (py > mx[1]) mx[1] = py;
+        if (pz > mx[2]) mx[2] = pz;
+        cnt++;
+        i++;
+        xp = x0 + (2 * i + 1) * r;
+      }
+      j++;
+      yp = y0 + (2.0 * j + 1) * r;
+    }
+    k++;
+    zp = z0 + (2.0 * k + 1) * r;
+  }
+  const double t0 = (mx[0] + r) - x0, t1 = (mx[1] + r) - y0, t2 = (mx[2] + r) - z0;
+  if (mass && cnt > 0) *mass = t0 * t1 * t2 * density / (double)cnt;
+  return cnt;
+}
+
+// Cubic lattice (spacing dx) clipped to a cylinder of radius R and height H
+// (axis z, base z = 0), each coordinate jittered by U[-jitter, jitter]*dx
+// from a splitmix64 stream seeded with `seed`.  The synthetic workload of
+// the compression benchmarks.
+int64_t wf_gen_cylinder_lattice(double R, double H, double dx, double jitter, uint64_t seed,
+                                double* x) {
+  int64_t cnt = 0;
+  const int nxy = (int)std::floor(2.0 * R / dx + 0.5);
+  const int nz = (int)std::floor(H / dx + 0.5);
+  uint64_t st = seed;
+  for (int k = 0; k < nz; k++)
+    for (int j = 0; j < nxy; j++)
+      for (int i = 0; i < nxy; i++) {
+        const double px = (i + 0.5) * dx - R, py = (j + 0.5) * dx - R, pz = (k + 0.5) * dx;
+        if (px * px + py * py > R * R) continue;
+        if (x) {
+          const double jx = (2.0 * uniform01(&st) - 1.0) * jitter * dx;
+          const double jy = (2.0 * uniform01(&st) - 1.0) * jitter * dx;
+          const double jz = (2.0 * uniform01(&st) - 1.0) * jitter * dx;
+          x[3 * cnt] = px + jx; x[3 * cnt + 1] = py + jy; x[3 * cnt + 2] = pz + jz;
+        }
+        cnt++;
+      }
+  return cnt;
+}
+
+// Domain::AssignZone (src/Domain.cpp:989-1005): inclusive box test.
+int64_t wf_assign_zone(const double* x, int64_t n, const double* start, const double* end,
+                       int32_t zone_id, int32_t* id, uint8_t* not_write) {
+  int64_t cnt = 0;
+  for (int64_t a = 0; a < n; a++) {
+    bool inc = true;
+    for (int c = 0; c < 3; c++)
+      if (x[3 * a + c] < start[c] || x[3 * a + c] > end[c]) inc = false;
+    if (inc) {
+      id[a] = zone_id;
+      if (not_write) not_write[a] = 1;
+      cnt++;
+    }
+  }
+  return cnt;
+}
+
+}  // extern "C"

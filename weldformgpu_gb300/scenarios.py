@@ -1,0 +1,128 @@
+"""Synthetic scenarios with the shapes of the benchmark configurations.
+
+A scenario is a plain dict (positions, masses, ids, scalars, material, BCs)
+that `load()` applies through the Domain_d setters.  The generators are the
+reference's (src/Domain.cpp) as implemented by the library, plus the seeded
+jittered lattice the benchmark configurations use.
+"""
+import math
+
+import numpy as np
+
+from . import _abi
+from . import setup as S
+
+
+def compression_cylinder(R=0.0025, H=0.005, dx=0.0005, generator="reference", vz_top=-1.0,
+                         material="bilinear", jitter=0.01, seed=1, layers=2, dt_rule="reference"):
+    """Elastoplastic cylinder compression (the reference's Compression example
+    shape; BASELINE config 1 at R=5 mm, H=10 mm).  Bottom `layers` layers are
+    fixed (zone 2), top `layers` layers move at vz_top (zone 3)."""
+    r = dx / 2.0
+    rho = 2700.0
+    if generator == "reference":
+        x, mass = S.gen_cylinder_ref((0.0, 0.0, 0.0), R, H, r, rho)
+        m = np.full(len(x), mass)
+    else:
+        x = S.gen_cylinder_lattice(R, H, dx, jitter, seed)
+        m = np.full(len(x), rho * dx ** 3)
+    n = len(x)
+    if material == "bilinear":
+        E, nu = 70e9, 0.33
+        mat = _abi.WfMaterial(model=_abi.WF_BILINEAR, E=E, nu=nu, sy0=300e6, Et=700e6)
+        sy = 300e6
+        T0 = 20.0
+    else:  # Johnson-Cook, BASELINE config 3 constants (aluminium)
+        E, nu = 70e9, 0.33
+        mat = _abi.WfMaterial(model=_abi.WF_JOHNSON_COOK, E=E, nu=nu, sy0=324e6, A=324e6,
+                              B=114e6, n=0.42, C=0.002, eps0=1.0, m=1.34, Tm=582.0, Tt=20.0)
+        sy = 324e6
+        T0 = 20.0
+    K = E / (3.0 * (1.0 - 2.0 * nu))
+    G = E / (2.0 * (1.0 + nu))
+    Cs = math.sqrt(K / rho)
+    h = 1.2 * dx
+    if dt_rule == "reference":       # src/WeldFormGPU.cu:906, VMAX = 10
+        dt = 0.4 * h / (Cs + 10.0)
+    else:                            # BASELINE config 1: 0.4 h / c
+        dt = 0.4 * h / Cs
+    ids = np.zeros(n, np.int32)
+    nw = np.zeros(n, np.uint8)
+    zmin, zmax = x[:, 2].min(), x[:, 2].max()
+    S.assign_zone(x, (-1, -1, -1), (1, 1, zmin + (layers - 0.5) * dx), 2, ids, nw)
+    S.assign_zone(x, (-1, -1, zmax - (layers - 0.5) * dx), (1, 1, 1), 3, ids, nw)
+    return dict(n=n, x=x, m=m, ids=ids, not_write=nw, h=h, rho=rho, G=G, sy=sy, Cs=Cs, dt=dt,
+                alpha=1.0, beta=0.0, mat=mat, T=np.full(n, T0),
+                bcs=[(2, (0.0, 0.0, 0.0)), (3, (0.0, 0.0, vz_top))], K=K, dx=dx)
+
+
+def load(dom, sc, options=None):
+    """Applies a scenario through the Domain_d setters (product or oracle)."""
+    n = sc["n"]
+    dom.set_h(sc["h"])
+    dom.set_density(sc["rho"])
+    dom.set_shear_modulus(sc["G"])
+    dom.set_sigma_y(sc["sy"])
+    dom.set_cs(np.full(n, sc["Cs"]))
+    dom.set_positions(np.ascontiguousarray(sc["x"]).ravel())
+    dom.set_mass(sc["m"])
+    dom.set_id(sc["ids"])
+    dom.set_not_write_surf_id(sc["not_write"])
+    dom.set_time_step(sc["dt"])
+    dom.set_artificial_viscosity(sc["alpha"], sc["beta"])
+    dom.set_material(sc["mat"])
+    dom.set_temperature(sc["T"])
+    for zone, v in sc["bcs"]:
+        dom.add_velocity_bc(zone, float(v[0]), float(v[1]), float(v[2]))
+    if "k" in sc:
+        dom.set_conductivity(sc["k"])
+        dom.set_heat_cap(sc["cp"])
+    for k, v in (options or {}).items():
+        dom.set_option(k, float(v))
+    return dom
+
+
+def heat_box(n_side=20, dx=1.0e-4, hot=500.0, T0=20.0, sigma=1.0e-3):
+    """Heat conduction only (BASELINE config 2 shape at n_side^3 particles):
+    steel cube, Gaussian hot spot at the centre, convection on the outer layer."""
+    rho, cp, k = 7850.0, 460.0, 50.0
+    L = n_side * dx
+    x, mass = S.gen_box_cubic((0.0, 0.0, 0.0), (L, L, L), dx / 2.0, rho)
+    n = len(x)
+    c = 0.5 * L
+    r2 = np.sum((x - c) ** 2, axis=1)
+    T = T0 + (hot - T0) * np.exp(-r2 / (2.0 * sigma * sigma))
+    lo, hi = x.min(axis=0), x.max(axis=0)
+    outer = np.any((x <= lo + 0.5 * dx) | (x >= hi - 0.5 * dx), axis=1)
+    bc_t = outer.astype(np.int32)
+    dt = 0.1 * dx * dx * rho * cp / k
+    return dict(n=n, x=x, m=np.full(n, mass), h=1.2 * dx, rho=rho, cp=cp, k=k, T=T, bc_t=bc_t,
+                dt=dt, h_conv=100.0, T_inf=T0, dx=dx)
+
+
+def load_heat(dom, sc):
+    n = sc["n"]
+    dom.set_h(sc["h"])
+    dom.set_density(sc["rho"])
+    dom.set_positions(np.ascontiguousarray(sc["x"]).ravel())
+    dom.set_mass(sc["m"])
+    dom.set_conductivity(sc["k"])
+    dom.set_heat_cap(sc["cp"])
+    dom.set_temperature(sc["T"])
+    dom.set_thermal_bc(sc["bc_t"])
+    dom.set_convection(sc["h_conv"], sc["T_inf"])
+    dom.set_time_step(sc["dt"])
+    return dom
+
+
+def jc_compression(R=0.025, H=0.050, dx=0.0005, jitter=0.01, seed=1, vz_top=-10.0, layers=2):
+    """Coupled thermo-mechanical Johnson-Cook compression (BASELINE configs 3/4):
+    R = 25 mm, H = 50 mm, dx = 0.5 mm (~0.79M particles), jitter +-0.01 dx,
+    JC A=324 MPa, B=114 MPa, n=0.42, C=0.002, m=1.34, eps0=1/s, Tref=20 C,
+    Tmelt=582 C; k=167 W/mK, cp=896 J/kgK, Taylor-Quinney 0.9 (set as an
+    option by the caller); top `layers` layers at vz_top, bottom ones fixed;
+    dt = 0.4 h / c."""
+    sc = compression_cylinder(R=R, H=H, dx=dx, generator="lattice", jitter=jitter, seed=seed,
+                              vz_top=vz_top, material="jc", layers=layers, dt_rule="baseline")
+    sc["k"], sc["cp"] = 167.0, 896.0
+    return sc

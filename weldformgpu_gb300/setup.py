@@ -1,0 +1,70 @@
+"""Host domain set-up: the reference's particle generators and zone
+assignment (src/Domain.cpp), implemented in the C++ library (csrc/wf_setup.cpp)."""
+import ctypes as C
+
+import numpy as np
+
+from .domain import lib
+
+_bound = False
+
+
+def _L():
+    global _bound
+    L = lib()
+    if not _bound:
+        L.wf_gen_cylinder.restype = C.c_int64
+        L.wf_gen_cylinder.argtypes = [C.c_double] * 7 + [C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.wf_gen_box.restype = C.c_int64
+        L.wf_gen_box.argtypes = [C.c_double] * 8 + [C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.wf_gen_cylinder_lattice.restype = C.c_int64
+        L.wf_gen_cylinder_lattice.argtypes = [C.c_double] * 4 + [C.c_uint64, C.POINTER(C.c_double)]
+        L.wf_assign_zone.restype = C.c_int64
+        L.wf_assign_zone.argtypes = [C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double), C.c_int32, C.POINTER(C.c_int32),
+                                     C.POINTER(C.c_uint8)]
+        _bound = True
+    return L
+
+
+def _p(a, ct=C.c_double):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+def gen_cylinder_ref(start, R, L, r, density):
+    """Domain::AddCylinderLength (src/Domain.cpp:490-573): (x[n,3], mass)."""
+    lib_ = _L()
+    m = C.c_double()
+    n = lib_.wf_gen_cylinder(start[0], start[1], start[2], R, L, r, density, None, C.byref(m))
+    x = np.empty(3 * n, dtype=np.float64)
+    lib_.wf_gen_cylinder(start[0], start[1], start[2], R, L, r, density, _p(x), C.byref(m))
+    return x.reshape(n, 3), m.value
+
+
+def gen_box_cubic(start, dims, r, density):
+    """Domain::AddBoxLength, cubic packing (src/Domain.cpp:296-338): (x[n,3], mass)."""
+    lib_ = _L()
+    m = C.c_double()
+    args = [float(v) for v in list(start) + list(dims)] + [r, density]
+    n = lib_.wf_gen_box(*args, None, C.byref(m))
+    x = np.empty(3 * n, dtype=np.float64)
+    lib_.wf_gen_box(*args, _p(x), C.byref(m))
+    return x.reshape(n, 3), m.value
+
+
+def gen_cylinder_lattice(R, H, dx, jitter, seed):
+    """Jittered cubic lattice inside a cylinder (the compression benchmarks' workload)."""
+    lib_ = _L()
+    n = lib_.wf_gen_cylinder_lattice(R, H, dx, jitter, seed, None)
+    x = np.empty(3 * n, dtype=np.float64)
+    lib_.wf_gen_cylinder_lattice(R, H, dx, jitter, seed, _p(x))
+    return x.reshape(n, 3)
+
+
+def assign_zone(x, start, end, zone, ids, not_write):
+    """Domain::AssignZone (src/Domain.cpp:989-1005); modifies ids / not_write in place."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    s = np.asarray(start, dtype=np.float64)
+    e = np.asarray(end, dtype=np.float64)
+    return _L().wf_assign_zone(_p(x), len(x), _p(s), _p(e), int(zone), _p(ids, C.c_int32),
+                               _p(not_write, C.c_uint8))
