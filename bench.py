@@ -133,10 +133,24 @@ def per_kernel_ms(d, kernels, reps=1):
     return out
 
 
-def run_form(sc, form, steps, warmup, mlp_params=None):
+def preload(sc, steps):
+    """Runs the mixed form from rest for `steps` steps and returns a checkpoint
+    (host arrays): the timed runs start from this plastic state."""
+    opts = base_options()
+    opts["precision"] = 1
+    d = build_domain(sc, opts)
+    d.step(steps)
+    st = d.checkpoint()
+    st["_plastic_fraction"] = float(np.mean(st["pl_strain"] > 0))
+    d.close()
+    return st
+
+
+def run_form(sc, form, steps, warmup, state, mlp_params=None):
     opts = base_options()
     opts["precision"] = 1 if form == "mixed" else 0
     d = build_domain(sc, opts)
+    d.restore(state)
     if mlp_params is not None:
         d.set_mlp_weights(mlp_params)
         d.set_option("mlp", 1)
@@ -154,12 +168,13 @@ def run_form(sc, form, steps, warmup, mlp_params=None):
     d.close()
     return dict(elapsed_ms=elapsed, kernel_ms=kernel_ms, kernel_launches=kernel_launches,
                 launches=launches, dominant=dominant, per_kernel_ms=kms, clocks=clk.summary(),
-                newton_iters_per_call=(it1 - it0) / max(c1 - c0, 1.0), fields=fields,
-                steps_done=warmup + len(kernels) + steps)
+                newton_iters_per_call=(it1 - it0) / max(c1 - c0, 1.0),
+                plastic_per_step=(c1 - c0) / max(steps, 1), fields=fields)
 
 
-def run_e2e(sc, form, steps, mlp_params=None):
-    """The drop-in call from host buffers, host wall clock around everything."""
+def run_e2e(sc, form, steps, state, mlp_params=None):
+    """The drop-in call from host buffers, host wall clock around everything:
+    create, setters, restart from the checkpoint, solve, read-back."""
     from weldformgpu_gb300 import Domain_d
     from weldformgpu_gb300 import scenarios as S
     opts = base_options()
@@ -167,6 +182,7 @@ def run_e2e(sc, form, steps, mlp_params=None):
     n = sc["n"]
     t0 = time.perf_counter()
     d = S.load(Domain_d(n), sc, opts)
+    d.restore(state)
     if mlp_params is not None:
         d.set_mlp_weights(mlp_params)
         d.set_option("mlp", 1)
@@ -174,7 +190,8 @@ def run_e2e(sc, form, steps, mlp_params=None):
     out = [d.get_field(f) for f in ("u", "pl_strain", "sigma_eq", "T")]
     d.close()
     t1 = time.perf_counter()
-    h2d = n * (3 * 8 + 8 + 4 + 1 + 8 + 8)           # x, m, id, not_write, Cs, T
+    h2d = n * (3 * 8 + 8 + 4 + 1 + 8 + 8)           # scenario: x, m, id, not_write, Cs, T
+    h2d += sum(v.nbytes for k, v in state.items() if not k.startswith("_"))
     d2h = sum(a.nbytes for a in out)
     return n * steps / (t1 - t0), h2d / steps, d2h / steps
 
@@ -230,10 +247,18 @@ def reduce_max(dist, v):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="small workload (quick check)")
+    ap.add_argument("--size", default="full", choices=["full", "medium", "small"],
+                    help="full: R=25 mm H=50 mm (0.79M); medium: R=15 mm H=30 mm (0.17M, > L2); "
+                         "small: R=6 mm H=12 mm")
+    ap.add_argument("--forms", default="fp64,mixed", help="forms to time (profiling runs)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-oracle baseline")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end arm")
+    ap.add_argument("--preload", type=int, default=4000,
+                    help="steps run (mixed form) before the timed runs, to reach plasticity")
     args = ap.parse_args()
     warmup = max(args.warmup, 3)
     rank, ws, dist = dist_setup(args.gpus)
@@ -241,13 +266,16 @@ def main():
     from weldformgpu_gb300 import build as B
     B.build()
     from weldformgpu_gb300 import scenarios as S
-    sc = S.jc_compression(R=0.006, H=0.012) if args.small else S.jc_compression()
+    size = "small" if args.small else args.size
+    sc = {"full": lambda: S.jc_compression(), "medium": lambda: S.jc_compression(R=0.015, H=0.030),
+          "small": lambda: S.jc_compression(R=0.006, H=0.012)}[size]()
     n = sc["n"]
-    config = {"workload": WORKLOAD if not args.small else WORKLOAD + "_small", "particles": n,
+    config = {"workload": WORKLOAD if size == "full" else WORKLOAD + "_" + size, "particles": n,
               "dx_m": sc["dx"], "dt_s": sc["dt"], "nnb": 56, "rebuild_every": 5,
               "return_map": "jc_newton_rtol1e-10", "thermal": "coupled, Taylor-Quinney 0.9",
               "l2": "inputs larger than L2 (state %.0f MB > 129 MB)" % (n * 1100 / 1e6),
-              "parallelism": "replicas" if ws > 1 else "single"}
+              "parallelism": "replicas" if ws > 1 else "single",
+              "preload_steps": args.preload}
 
     if args.impl == "reference":
         if rank != 0:
@@ -268,8 +296,14 @@ def main():
     mlp_path = os.path.join(ROOT, "weldformgpu_gb300", "mlp_jc_weights.npy")
     if os.path.exists(mlp_path):
         mlp = np.load(mlp_path)
-    plain = run_form(sc, "fp64", args.steps, warmup)
-    mixed = run_form(sc, "mixed", args.steps, warmup, mlp)
+    state = preload(sc, args.preload)
+    forms = args.forms.split(",")
+    mixed = run_form(sc, "mixed", args.steps, warmup, state, mlp)
+    if "fp64" not in forms:
+        print(json.dumps({"profiling_run": True, "ms_per_step": mixed["elapsed_ms"] / args.steps,
+                          "per_kernel_ms": mixed["per_kernel_ms"], "particles": n}))
+        return
+    plain = run_form(sc, "fp64", args.steps, warmup, state)
     t_mixed = reduce_max(dist, mixed["elapsed_ms"])
     t_plain = reduce_max(dist, plain["elapsed_ms"])
     value = ws * n * args.steps / (t_mixed / 1e3)
@@ -278,7 +312,7 @@ def main():
                       plain["fields"][f] - (20.0 if f == "T" else 0.0))
             for f in ("u", "pl_strain", "sigma_eq", "T")}
     e2e_steps = max(args.steps, 100)
-    e2e_v, h2d, d2h = run_e2e(sc, "mixed", e2e_steps, mlp)
+    e2e_v, h2d, d2h = (0.0, 0, 0) if args.no_e2e else run_e2e(sc, "mixed", e2e_steps, state, mlp)
     e2e_v = reduce_max(dist, e2e_v) * ws if dist else e2e_v
 
     peak, peak_kind = measured_peaks()
@@ -311,6 +345,8 @@ def main():
         "rel_l2_vs_fp64": errs,
         "mlp_warm_start": mlp is not None,
         "newton_iters_per_plastic_particle": mixed["newton_iters_per_call"],
+        "plastic_particles_per_step": mixed["plastic_per_step"],
+        "plastic_fraction_at_start": state["_plastic_fraction"],
         "per_kernel_ms": mixed["per_kernel_ms"],
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
@@ -325,7 +361,7 @@ def main():
         "clocks": mixed["clocks"],
     }
     if rank == 0:
-        line["cpu_baseline"] = cpu_baseline(sc)
+        line["cpu_baseline"] = None if args.no_cpu else cpu_baseline(sc)
         print(json.dumps(line))
 
 

@@ -118,6 +118,13 @@ int wf_get_field_i32(wf_domain* d, const char* name, int32_t* out);
 /* counts[n]; lists[n*WF_MAX_NEIGHBORS], neighbour ids in search order. */
 int wf_get_neighbors(wf_domain* d, int32_t* counts, int32_t* lists);
 int wf_get_scalar(wf_domain* d, const char* name, double* out);
+/* Checkpoint / restart (no reference counterpart: the reference's CSV
+ * snapshots are not restartable).  wf_set_field writes a state field in the
+ * caller's order (names as wf_get_field); wf_set_scalar sets "time",
+ * "step", "isfirst" or "is_yielding"; with wf_set_option("resume", 1) the
+ * next solve keeps time and velocities instead of restarting from rest. */
+int wf_set_field(wf_domain* d, const char* name, const double* in);
+int wf_set_scalar(wf_domain* d, const char* name, double value);
 /* Domain_d::WriteCSV (src/cuda/Domain_d.cu:556-587), same columns. */
 int wf_write_csv(wf_domain* d, const char* path);
 

@@ -95,6 +95,7 @@ SIGNATURES = {
     "get_field_i32": (C.c_int, [_vp, _cs, _pi32]),
     "get_neighbors": (C.c_int, [_vp, _pi32, _pi32]),
     "get_scalar": (C.c_int, [_vp, _cs, _pd]),
+    "set_field": (C.c_int, [_vp, _cs, _pd]),
 }
 
 # entry points only the product exports
@@ -102,6 +103,7 @@ PRODUCT_ONLY = {
     "version": (C.c_char_p, []),
     "mech_solve": (C.c_int, [_vp, _d, _d]),
     "write_csv": (C.c_int, [_vp, _cs]),
+    "set_scalar": (C.c_int, [_vp, _cs, _d]),
     "time_steps": (C.c_int, [_vp, _i64, _pd, _pd, C.POINTER(_i64), C.POINTER(_i64)]),
 }
 

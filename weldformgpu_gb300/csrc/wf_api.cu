@@ -40,7 +40,7 @@ struct wf_domain {
   // options
   int precision = 0, return_map = 0, mlp_on = 0, rebuild_every = 5, rebuild_after_yield = 1;
   int rebuild_current = 0, thermal = 0, energy_mode = 0, newton_max_iter = 50;
-  int clamp_homologous = 1, profile_kernel = KID_NONE;
+  int clamp_homologous = 1, profile_kernel = KID_NONE, resume = 0;
   double chi = 0.0, newton_rtol = 1.0e-10, output_interval = 1.0e300;
   // device arena
   Fields F[2]{};
@@ -174,28 +174,31 @@ inline int nblk(int64_t n, int t = 256) { return (int)((n + t - 1) / t); }
 // ---------------------------------------------------------------------------
 // allocation
 // ---------------------------------------------------------------------------
+// Zero-filled on the domain's own stream: that stream is non-blocking, so a
+// cudaMemset on the legacy default stream would not be ordered before it.
 template <class T>
-static cudaError_t dalloc(T** p, int64_t count) {
-  cudaError_t e = cudaMalloc((void**)p, sizeof(T) * (size_t)std::max<int64_t>(count, 1));
-  if (e == cudaSuccess) e = cudaMemset(*p, 0, sizeof(T) * (size_t)std::max<int64_t>(count, 1));
+static cudaError_t dalloc(T** p, int64_t count, cudaStream_t s) {
+  const size_t bytes = sizeof(T) * (size_t)std::max<int64_t>(count, 1);
+  cudaError_t e = cudaMalloc((void**)p, bytes);
+  if (e == cudaSuccess) e = cudaMemsetAsync(*p, 0, bytes, s);
   return e;
 }
 
 static int alloc_fields(wf_domain* d, Fields& F) {
   const int64_t n = d->npad;
-  WF_CUDA_OK(dalloc(&F.xm, n)); WF_CUDA_OK(dalloc(&F.vd, n));
-  WF_CUDA_OK(dalloc(&F.u, n)); WF_CUDA_OK(dalloc(&F.a, n));
-  WF_CUDA_OK(dalloc(&F.sig6, 6 * n)); WF_CUDA_OK(dalloc(&F.ss6, 6 * n));
-  WF_CUDA_OK(dalloc(&F.eps6, 6 * n)); WF_CUDA_OK(dalloc(&F.sr6, 6 * n));
-  WF_CUDA_OK(dalloc(&F.rr6, 6 * n));
-  WF_CUDA_OK(dalloc(&F.p, n)); WF_CUDA_OK(dalloc(&F.seq, n)); WF_CUDA_OK(dalloc(&F.eps_p, n));
-  WF_CUDA_OK(dalloc(&F.sy, n)); WF_CUDA_OK(dalloc(&F.eff, n)); WF_CUDA_OK(dalloc(&F.dep, n));
-  WF_CUDA_OK(dalloc(&F.drho, n)); WF_CUDA_OK(dalloc(&F.eint, n));
-  WF_CUDA_OK(dalloc(&F.T, n)); WF_CUDA_OK(dalloc(&F.Ta, n)); WF_CUDA_OK(dalloc(&F.Tb, n));
-  WF_CUDA_OK(dalloc(&F.dTdt, n)); WF_CUDA_OK(dalloc(&F.kT, n)); WF_CUDA_OK(dalloc(&F.cpT, n));
-  WF_CUDA_OK(dalloc(&F.id, n)); WF_CUDA_OK(dalloc(&F.bct, n)); WF_CUDA_OK(dalloc(&F.perm, n));
-  WF_CUDA_OK(dalloc(&F.nw, n)); WF_CUDA_OK(dalloc(&F.xh, n));
-  WF_CUDA_OK(dalloc(&F.p32, n)); WF_CUDA_OK(dalloc(&F.v32, n)); WF_CUDA_OK(dalloc(&F.ss32, 6 * n));
+  WF_CUDA_OK(dalloc(&F.xm, n, d->stream)); WF_CUDA_OK(dalloc(&F.vd, n, d->stream));
+  WF_CUDA_OK(dalloc(&F.u, n, d->stream)); WF_CUDA_OK(dalloc(&F.a, n, d->stream));
+  WF_CUDA_OK(dalloc(&F.sig6, 6 * n, d->stream)); WF_CUDA_OK(dalloc(&F.ss6, 6 * n, d->stream));
+  WF_CUDA_OK(dalloc(&F.eps6, 6 * n, d->stream)); WF_CUDA_OK(dalloc(&F.sr6, 6 * n, d->stream));
+  WF_CUDA_OK(dalloc(&F.rr6, 6 * n, d->stream));
+  WF_CUDA_OK(dalloc(&F.p, n, d->stream)); WF_CUDA_OK(dalloc(&F.seq, n, d->stream)); WF_CUDA_OK(dalloc(&F.eps_p, n, d->stream));
+  WF_CUDA_OK(dalloc(&F.sy, n, d->stream)); WF_CUDA_OK(dalloc(&F.eff, n, d->stream)); WF_CUDA_OK(dalloc(&F.dep, n, d->stream));
+  WF_CUDA_OK(dalloc(&F.drho, n, d->stream)); WF_CUDA_OK(dalloc(&F.eint, n, d->stream));
+  WF_CUDA_OK(dalloc(&F.T, n, d->stream)); WF_CUDA_OK(dalloc(&F.Ta, n, d->stream)); WF_CUDA_OK(dalloc(&F.Tb, n, d->stream));
+  WF_CUDA_OK(dalloc(&F.dTdt, n, d->stream)); WF_CUDA_OK(dalloc(&F.kT, n, d->stream)); WF_CUDA_OK(dalloc(&F.cpT, n, d->stream));
+  WF_CUDA_OK(dalloc(&F.id, n, d->stream)); WF_CUDA_OK(dalloc(&F.bct, n, d->stream)); WF_CUDA_OK(dalloc(&F.perm, n, d->stream));
+  WF_CUDA_OK(dalloc(&F.nw, n, d->stream)); WF_CUDA_OK(dalloc(&F.xh, n, d->stream));
+  WF_CUDA_OK(dalloc(&F.p32, n, d->stream)); WF_CUDA_OK(dalloc(&F.v32, n, d->stream)); WF_CUDA_OK(dalloc(&F.ss32, 6 * n, d->stream));
   return WF_OK;
 }
 
@@ -293,10 +296,10 @@ static int ensure_cells(wf_domain* d, int64_t ncell) {
   if (ncell + 1 <= d->cell_cap) return WF_OK;
   if (d->cell_count) { cudaFree(d->cell_count); cudaFree(d->cell_cursor); cudaFree(d->scan_tmp); }
   int64_t cap = (ncell + 1) + (ncell + 1) / 4 + 1024;
-  WF_CUDA_OK(dalloc(&d->cell_count, cap));
-  WF_CUDA_OK(dalloc(&d->cell_cursor, cap));
+  WF_CUDA_OK(dalloc(&d->cell_count, cap, d->stream));
+  WF_CUDA_OK(dalloc(&d->cell_cursor, cap, d->stream));
   d->scan_cap = scan_tmp_words(cap) + 16;
-  WF_CUDA_OK(dalloc(&d->scan_tmp, d->scan_cap));
+  WF_CUDA_OK(dalloc(&d->scan_tmp, d->scan_cap, d->stream));
   d->cell_cap = cap;
   return WF_OK;
 }
@@ -360,10 +363,13 @@ static int read_status(wf_domain* d) {
 static int solve_begin(wf_domain* d, double dt_out) {
   int rc = check_ready(d);
   if (rc) return rc;
-  d->time = 0.0;
-  d->isfirst = true;
-  d->step = 0;
-  d->t_out = dt_out;
+  const bool resume = d->resume != 0;
+  if (!resume) {
+    d->time = 0.0;
+    d->isfirst = true;
+    d->step = 0;
+  }
+  d->t_out = d->time + dt_out;
   d->dt_out = dt_out;
   d->ts_i = 0;
   d->is_yielding = false;
@@ -371,7 +377,7 @@ static int solve_begin(wf_domain* d, double dt_out) {
   launch_snapshot(d->n, d->F[d->cur], d->stream);               // x_h = x, :56
   rc = rebuild(d, false);                                       // :109
   if (rc) return rc;
-  k_setvel0<<<nblk(d->n), 256, 0, d->stream>>>(d->n, d->n_solid, d->F[d->cur]);   // :123
+  if (!resume) k_setvel0<<<nblk(d->n), 256, 0, d->stream>>>(d->n, d->n_solid, d->F[d->cur]);   // :123
   if (d->precision == 1) k_mixed_init<<<nblk(d->n), 256, 0, d->stream>>>(d->n, d->F[d->cur]);
   WF_CUDA_OK(cudaGetLastError());
   d->started = true;
@@ -456,12 +462,12 @@ int wf_create(wf_domain** out, int64_t n) {
     rc = alloc_fields(d, d->F[k]);
     if (rc) return bail(rc);
   }
-  if (dalloc(&d->vd2, d->npad) || dalloc(&d->v32b, d->npad) || dalloc(&d->sigr32, 8 * d->npad) ||
-      dalloc(&d->nb, (int64_t)WF_NB * d->npad) || dalloc(&d->nbc, d->npad) ||
-      dalloc(&d->inv, d->npad) || dalloc(&d->pf, d->npad) || dalloc(&d->pf2, d->npad) ||
-      dalloc(&d->cellid, d->npad) || dalloc(&d->s_src, d->npad) || dalloc(&d->s_orig, d->npad) ||
-      dalloc(&d->d_mm, 8) || dalloc(&d->d_status, 8) || dalloc(&d->d_stage, 6 * d->npad) ||
-      dalloc(&d->mlp_w, WF_MLP_NPARAM))
+  if (dalloc(&d->vd2, d->npad, d->stream) || dalloc(&d->v32b, d->npad, d->stream) || dalloc(&d->sigr32, 8 * d->npad, d->stream) ||
+      dalloc(&d->nb, (int64_t)WF_NB * d->npad, d->stream) || dalloc(&d->nbc, d->npad, d->stream) ||
+      dalloc(&d->inv, d->npad, d->stream) || dalloc(&d->pf, d->npad, d->stream) || dalloc(&d->pf2, d->npad, d->stream) ||
+      dalloc(&d->cellid, d->npad, d->stream) || dalloc(&d->s_src, d->npad, d->stream) || dalloc(&d->s_orig, d->npad, d->stream) ||
+      dalloc(&d->d_mm, 8, d->stream) || dalloc(&d->d_status, 8, d->stream) || dalloc(&d->d_stage, 6 * d->npad, d->stream) ||
+      dalloc(&d->mlp_w, WF_MLP_NPARAM, d->stream))
     return bail(WF_ERR_ALLOC);
   if (cudaMallocHost((void**)&d->h_status, 8 * sizeof(int)) != cudaSuccess) return bail(WF_ERR_ALLOC);
   k_iota<<<nblk(n), 256, 0, d->stream>>>(n, d->F[0].perm, d->inv);
@@ -653,6 +659,7 @@ int wf_set_option(wf_domain* d, const char* key, double v) {
   else if (k == "output_interval") d->output_interval = v;
   else if (k == "clamp_homologous") d->clamp_homologous = v != 0;
   else if (k == "profile_kernel") d->profile_kernel = (int)v;
+  else if (k == "resume") d->resume = v != 0;
   else if (k == "graph") { /* reserved */ }
   else return wf_fail(d, WF_ERR_ARG, "unknown option: " + k);
   return WF_OK;
@@ -728,6 +735,54 @@ static int download(wf_domain* d, double* out, int64_t count) {
 }
 
 extern "C" {
+
+// ---- state transfer (checkpoint / restart) ---------------------------------
+int wf_set_field(wf_domain* d, const char* name, const double* in) {
+  if (!d || !name || !in) return WF_ERR_ARG;
+  Fields& F = CF(d);
+  std::string s(name);
+  int rc;
+  if (s == "x") { d->x_set = true; rc = upload_d(d, in, 3, (double*)F.xm, 4, 0); }
+  else if (s == "m") { d->m_set = true; rc = upload_d(d, in, 1, (double*)F.xm, 4, 3); }
+  else if (s == "v") rc = upload_d(d, in, 3, (double*)F.vd, 4, 0);
+  else if (s == "rho") rc = upload_d(d, in, 1, (double*)F.vd, 4, 3);
+  else if (s == "u") rc = upload_d(d, in, 3, (double*)F.u, 4, 0);
+  else if (s == "a") rc = upload_d(d, in, 3, (double*)F.a, 4, 0);
+  else if (s == "sigma") rc = upload_d(d, in, 6, F.sig6, 6, 0);
+  else if (s == "shearstress") rc = upload_d(d, in, 6, F.ss6, 6, 0);
+  else if (s == "strain") rc = upload_d(d, in, 6, F.eps6, 6, 0);
+  else if (s == "strrate") rc = upload_d(d, in, 6, F.sr6, 6, 0);
+  else if (s == "rotrate") rc = upload_d(d, in, 6, F.rr6, 6, 0);
+  else if (s == "p") rc = upload_d(d, in, 1, F.p, 1, 0);
+  else if (s == "sigma_eq") rc = upload_d(d, in, 1, F.seq, 1, 0);
+  else if (s == "pl_strain") rc = upload_d(d, in, 1, F.eps_p, 1, 0);
+  else if (s == "sigma_y") rc = upload_d(d, in, 1, F.sy, 1, 0);
+  else if (s == "eff_strain_rate") rc = upload_d(d, in, 1, F.eff, 1, 0);
+  else if (s == "dep") rc = upload_d(d, in, 1, F.dep, 1, 0);
+  else if (s == "int_energy") rc = upload_d(d, in, 1, F.eint, 1, 0);
+  else if (s == "T") rc = upload_d(d, in, 1, F.T, 1, 0);
+  else if (s == "Ta") rc = upload_d(d, in, 1, F.Ta, 1, 0);
+  else if (s == "Tb") rc = upload_d(d, in, 1, F.Tb, 1, 0);
+  else if (s == "dTdt") rc = upload_d(d, in, 1, F.dTdt, 1, 0);
+  else return wf_fail(d, WF_ERR_ARG, "unknown or read-only field: " + s);
+  if (rc) return rc;
+  if (d->started && d->precision == 1) {
+    k_mixed_init<<<nblk(d->n), 256, 0, d->stream>>>(d->n, F);
+    WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+  }
+  return WF_OK;
+}
+
+int wf_set_scalar(wf_domain* d, const char* name, double v) {
+  if (!d || !name) return WF_ERR_ARG;
+  std::string s(name);
+  if (s == "time") d->time = v;
+  else if (s == "step") d->step = (int64_t)v;
+  else if (s == "isfirst") d->isfirst = v != 0;
+  else if (s == "is_yielding") d->is_yielding = v != 0;
+  else return wf_fail(d, WF_ERR_ARG, "unknown scalar: " + s);
+  return WF_OK;
+}
 
 int wf_get_field(wf_domain* d, const char* name, double* out) {
   if (!d || !name || !out) return WF_ERR_ARG;
@@ -814,6 +869,7 @@ int wf_get_scalar(wf_domain* d, const char* name, double* out) {
   if (s == "time") { *out = d->time; return WF_OK; }
   if (s == "step") { *out = (double)d->step; return WF_OK; }
   if (s == "is_yielding") { *out = d->is_yielding; return WF_OK; }
+  if (s == "isfirst") { *out = d->isfirst; return WF_OK; }
   if (s == "launches") { *out = (double)d->launches; return WF_OK; }
   if (s == "newton_iters" || s == "newton_calls" || s == "status") {
     int rc = read_status(d);

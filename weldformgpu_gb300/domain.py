@@ -161,6 +161,41 @@ class Domain_d:
                  "wf_get_field(%s)" % name)
         return out.reshape(self.n, c) if c > 1 else out
 
+    def set_field(self, name, values):
+        """Writes a state field (caller's order); see wf_set_field."""
+        c = _abi.FIELD_COMPONENTS.get(name, 1)
+        self._d_named("set_field", name, values, c)
+
+    def _d_named(self, fn, name, a, comps):
+        a = np.ascontiguousarray(a, dtype=np.float64).ravel()
+        if a.size != comps * self.n:
+            raise ValueError("%s: expected %d values, got %d" % (name, comps * self.n, a.size))
+        self._ck(getattr(self.L, "wf_" + fn)(self.h, name.encode(), _ptr(a, C.c_double)),
+                 "wf_%s(%s)" % (fn, name))
+
+    def set_scalar(self, name, value):
+        self._ck(self.L.wf_set_scalar(self.h, name.encode(), float(value)), "wf_set_scalar(%s)" % name)
+
+    CHECKPOINT_FIELDS = ("x", "m", "v", "rho", "u", "a", "sigma", "shearstress", "strain",
+                         "pl_strain", "sigma_y", "int_energy", "T", "Ta", "Tb", "dep")
+
+    def checkpoint(self):
+        """All state needed to continue a run, as host arrays."""
+        st = {f: self.get_field(f) for f in self.CHECKPOINT_FIELDS}
+        st["ID"] = self.get_field_i32("ID")
+        for s in ("time", "step", "isfirst", "is_yielding"):
+            st["_" + s] = self.get_scalar(s)
+        return st
+
+    def restore(self, st):
+        """Loads a checkpoint() into this domain; the next solve resumes from it."""
+        for f in self.CHECKPOINT_FIELDS:
+            self.set_field(f, st[f])
+        self.set_id(st["ID"])
+        for s in ("time", "step", "isfirst", "is_yielding"):
+            self.set_scalar(s, st["_" + s])
+        self.set_option("resume", 1)
+
     def get_field_i32(self, name):
         out = np.empty(self.n, dtype=np.int32)
         self._ck(self.L.wf_get_field_i32(self.h, name.encode(), _ptr(out, C.c_int32)),
