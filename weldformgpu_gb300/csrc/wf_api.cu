@@ -47,6 +47,7 @@ struct wf_domain {
   int cur = 0;
   double4* vd2 = nullptr;
   float4* v32b = nullptr;
+  float4* a32 = nullptr;       // mixed-form acceleration
   float* sigr32 = nullptr;
   float* mlp_w = nullptr;      // device MLP parameters (FP32 master copy, see wf_mlp.cu)
   int32_t *nb = nullptr, *nbc = nullptr, *inv = nullptr;
@@ -161,6 +162,9 @@ __global__ void k_mixed_init(int64_t n, Fields F) {
   F.p32[s] = make_float4((float)x.x, (float)x.y, (float)x.z, (float)x.w);
   F.v32[s] = make_float4((float)v.x, (float)v.y, (float)v.z, (float)v.w);
   for (int c = 0; c < 6; c++) F.ss32[s * 6 + c] = (float)F.ss6[s * 6 + c];
+  const double T = F.T[s];
+  const float thi = (float)T;
+  F.th32[s] = make_float4(thi, (float)(T - (double)thi), (float)F.kT[s], (float)v.w);
 }
 // FP64 copy of the FP32 deviatoric state (mixed -> plain switch)
 __global__ void k_mixed_to_fp64(int64_t n, Fields F) {
@@ -199,13 +203,14 @@ static int alloc_fields(wf_domain* d, Fields& F) {
   WF_CUDA_OK(dalloc(&F.id, n, d->stream)); WF_CUDA_OK(dalloc(&F.bct, n, d->stream)); WF_CUDA_OK(dalloc(&F.perm, n, d->stream));
   WF_CUDA_OK(dalloc(&F.nw, n, d->stream)); WF_CUDA_OK(dalloc(&F.xh, n, d->stream));
   WF_CUDA_OK(dalloc(&F.p32, n, d->stream)); WF_CUDA_OK(dalloc(&F.v32, n, d->stream)); WF_CUDA_OK(dalloc(&F.ss32, 6 * n, d->stream));
+  WF_CUDA_OK(dalloc(&F.th32, n, d->stream)); WF_CUDA_OK(dalloc(&F.pwn, n, d->stream));
   return WF_OK;
 }
 
 static void free_fields(Fields& F) {
   void* ptrs[] = {F.xm, F.vd, F.u, F.a, F.sig6, F.ss6, F.eps6, F.sr6, F.rr6, F.p, F.seq, F.eps_p,
                   F.sy, F.eff, F.dep, F.drho, F.eint, F.T, F.Ta, F.Tb, F.dTdt, F.kT, F.cpT,
-                  F.id, F.bct, F.perm, F.nw, F.xh, F.p32, F.v32, F.ss32};
+                  F.id, F.bct, F.perm, F.nw, F.xh, F.p32, F.v32, F.ss32, F.th32, F.pwn};
   for (void* p : ptrs) if (p) cudaFree(p);
   F = Fields{};
 }
@@ -258,6 +263,24 @@ static StepParams make_params(const wf_domain* d) {
     M.eps1_hol = std::pow(m.sy0 / m.K_hol, 1. / m.m_hol);
   }
   M.A = m.A; M.B = m.B; M.n = m.n; M.C = m.C; M.eps0 = m.eps0; M.m = m.m; M.Tm = m.Tm; M.Tt = m.Tt;
+  {  // C(n, k) for (1 + u)^n, k = 1..5
+    double c = 1.0;
+    for (int k = 1; k <= 5; k++) {
+      c = c * (m.n - (k - 1)) / k;
+      M.bin[k - 1] = c;
+    }
+  }
+  P.refresh_pow = (d->step % 64) == 0;   // bounds the drift of the cached eps_p^n
+  P.hf = (float)P.h;
+  P.invhf = (float)(1.0 / P.h);
+  P.Cf = (float)P.gkC;
+  P.Chf = (float)(P.gkC / P.h);
+  P.Csf = (float)P.Cs;
+  P.alphaf = (float)P.alpha;
+  P.betaf = (float)P.beta;
+  P.epsf = (float)(0.01 * P.h * P.h);
+  P.dtf = (float)P.dt;
+  P.G2f = (float)(2.0 * P.G);
   return P;
 }
 
@@ -402,9 +425,9 @@ static int solve_step(wf_domain* d) {
     { KTimer t(d, KID_DENSITY); launch_fp32_density(P, F, d->vd2, d->v32b, N, s); }
     { KTimer t(d, KID_STRESS);
       launch_fp32_stress(P, F, d->v32b, d->sigr32, N, d->d_status, d->mlp_on ? d->mlp_w : nullptr, s); }
-    { KTimer t(d, KID_ACCEL); launch_fp32_accel(P, F, d->v32b, d->sigr32, N, s); }
+    { KTimer t(d, KID_ACCEL); launch_fp32_accel(P, F, d->v32b, d->sigr32, d->a32, N, s); }
   }
-  { KTimer t(d, KID_INTEGRATE); launch_integrate(P, F, d->vd2, mixed ? 1 : 0, s); }   // :273-287
+  { KTimer t(d, KID_INTEGRATE); launch_integrate(P, F, d->vd2, mixed ? d->a32 : nullptr, s); }   // :273-287
   d->launches += 4;
   if (d->thermal) {                                                                   // :285
     KTimer t(d, KID_THERMAL);
@@ -462,7 +485,7 @@ int wf_create(wf_domain** out, int64_t n) {
     rc = alloc_fields(d, d->F[k]);
     if (rc) return bail(rc);
   }
-  if (dalloc(&d->vd2, d->npad, d->stream) || dalloc(&d->v32b, d->npad, d->stream) || dalloc(&d->sigr32, 8 * d->npad, d->stream) ||
+  if (dalloc(&d->vd2, d->npad, d->stream) || dalloc(&d->v32b, d->npad, d->stream) || dalloc(&d->a32, d->npad, d->stream) || dalloc(&d->sigr32, 8 * d->npad, d->stream) ||
       dalloc(&d->nb, (int64_t)WF_NB * d->npad, d->stream) || dalloc(&d->nbc, d->npad, d->stream) ||
       dalloc(&d->inv, d->npad, d->stream) || dalloc(&d->pf, d->npad, d->stream) || dalloc(&d->pf2, d->npad, d->stream) ||
       dalloc(&d->cellid, d->npad, d->stream) || dalloc(&d->s_src, d->npad, d->stream) || dalloc(&d->s_orig, d->npad, d->stream) ||
@@ -471,6 +494,7 @@ int wf_create(wf_domain** out, int64_t n) {
     return bail(WF_ERR_ALLOC);
   if (cudaMallocHost((void**)&d->h_status, 8 * sizeof(int)) != cudaSuccess) return bail(WF_ERR_ALLOC);
   k_iota<<<nblk(n), 256, 0, d->stream>>>(n, d->F[0].perm, d->inv);
+  k_fill_d<<<nblk(n), 256, 0, d->stream>>>(n, -1.0, d->F[0].pwn, 1, 0);
   if (cudaStreamSynchronize(d->stream) != cudaSuccess) return bail(WF_ERR_CUDA);
   *out = d;
   return WF_OK;
@@ -480,7 +504,7 @@ int wf_destroy(wf_domain* d) {
   if (!d) return WF_OK;
   if (d->stream) cudaStreamSynchronize(d->stream);
   for (int k = 0; k < 2; k++) free_fields(d->F[k]);
-  void* ptrs[] = {d->vd2, d->v32b, d->sigr32, d->mlp_w, d->nb, d->nbc, d->inv, d->pf, d->pf2,
+  void* ptrs[] = {d->vd2, d->v32b, d->a32, d->sigr32, d->mlp_w, d->nb, d->nbc, d->inv, d->pf, d->pf2,
                   d->cellid, d->cell_count, d->cell_cursor, d->scan_tmp, d->s_src, d->s_orig,
                   d->d_mm, d->d_status, d->d_stage};
   for (void* p : ptrs) if (p) cudaFree(p);
@@ -755,7 +779,10 @@ int wf_set_field(wf_domain* d, const char* name, const double* in) {
   else if (s == "rotrate") rc = upload_d(d, in, 6, F.rr6, 6, 0);
   else if (s == "p") rc = upload_d(d, in, 1, F.p, 1, 0);
   else if (s == "sigma_eq") rc = upload_d(d, in, 1, F.seq, 1, 0);
-  else if (s == "pl_strain") rc = upload_d(d, in, 1, F.eps_p, 1, 0);
+  else if (s == "pl_strain") {
+    rc = upload_d(d, in, 1, F.eps_p, 1, 0);
+    if (!rc) rc = fill_d(d, -1.0, F.pwn, 1, 0);    // cached eps_p^n no longer valid
+  }
   else if (s == "sigma_y") rc = upload_d(d, in, 1, F.sy, 1, 0);
   else if (s == "eff_strain_rate") rc = upload_d(d, in, 1, F.eff, 1, 0);
   else if (s == "dep") rc = upload_d(d, in, 1, F.dep, 1, 0);
@@ -871,12 +898,12 @@ int wf_get_scalar(wf_domain* d, const char* name, double* out) {
   if (s == "is_yielding") { *out = d->is_yielding; return WF_OK; }
   if (s == "isfirst") { *out = d->isfirst; return WF_OK; }
   if (s == "launches") { *out = (double)d->launches; return WF_OK; }
-  if (s == "newton_iters" || s == "newton_calls" || s == "status") {
+  if (s == "newton_iters" || s == "newton_calls" || s == "mlp_used" || s == "status") {
     int rc = read_status(d);
     if (rc) return rc;
     unsigned long long v;
     if (s == "status") { *out = d->h_status[0]; return WF_OK; }
-    memcpy(&v, d->h_status + (s == "newton_iters" ? 2 : 4), sizeof v);
+    memcpy(&v, d->h_status + (s == "newton_iters" ? 2 : (s == "newton_calls" ? 4 : 6)), sizeof v);
     *out = (double)v;
     return WF_OK;
   }

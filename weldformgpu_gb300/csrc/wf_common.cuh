@@ -55,6 +55,8 @@ struct Fields {
   float4* p32;      // position xyz, mass w
   float4* v32;      // velocity xyz, density w
   float* ss32;      // deviatoric stress FP32 state (mixed form), 6 per slot
+  float4* th32;     // heat-flux mirror (mixed form): T as a float pair (hi, lo), k, rho
+  double* pwn;      // cached eps_p^n of the Johnson-Cook law (< 0: not cached yet)
 };
 
 // Johnson-Cook / bilinear / Hollomon constants as the kernels use them.
@@ -63,6 +65,7 @@ struct MatParams {
   double E, Et, Ep;               // bilinear
   double K_hol, m_hol, eps0_hol, eps1_hol, sy0;
   double A, B, n, C, eps0, m, Tm, Tt;
+  double bin[5];                  // binomial coefficients C(n, k), k = 1..5
 };
 
 struct StepParams {
@@ -88,7 +91,11 @@ struct StepParams {
   int32_t bc_zone[WF_MAX_BC];
   double bc_v[WF_MAX_BC][3];
   int mlp_on;           // MLP warm start of the Newton return map
+  int refresh_pow;      // recompute eps_p^n with pow() this step (bounds series drift)
   MatParams mat;
+  // FP32 constants for the mixed form, computed once on the host: on GB300 a
+  // per-thread FP64 division or conversion costs as much as an FP32 pair loop
+  float hf, invhf, Cf, Chf, Csf, alphaf, betaf, epsf, dtf, G2f, mlp_scale;
 };
 
 #define WF_CUDA_OK(call)                                   \
@@ -140,8 +147,8 @@ void launch_fp64_stress(const StepParams& P, const Fields& F, const double4* vd2
                         const NbBuffers& N, int* status, cudaStream_t s);
 void launch_fp64_accel(const StepParams& P, const Fields& F, const double4* vd2,
                        const NbBuffers& N, cudaStream_t s);
-void launch_integrate(const StepParams& P, const Fields& F, const double4* vd2, int mixed,
-                      cudaStream_t s);
+void launch_integrate(const StepParams& P, const Fields& F, const double4* vd2,
+                      const float4* a32, cudaStream_t s);
 void launch_thermal(const StepParams& P, const Fields& F, const NbBuffers& N, int first,
                     int plastic_heat, int mixed, cudaStream_t s);
 
@@ -151,4 +158,4 @@ void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b
                         float* sigr32, const NbBuffers& N, int* status, const float* mlp_w,
                         cudaStream_t s);
 void launch_fp32_accel(const StepParams& P, const Fields& F, const float4* v32b,
-                       const float* sigr32, const NbBuffers& N, cudaStream_t s);
+                       const float* sigr32, float4* a32, const NbBuffers& N, cudaStream_t s);

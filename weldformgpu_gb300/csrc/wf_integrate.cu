@@ -20,12 +20,21 @@ __device__ __forceinline__ void apply_bc(const StepParams& P, int32_t id, double
 // UpdatePosFraser (:179-187), UpdateVel (:142-148), CalcIntEnergy
 // (src/cuda/Energy.cu:5-19), in SolverFraser.cu:273-287 order.
 __global__ void __launch_bounds__(256) k_integrate(StepParams P, Fields F,
-                                                   const double4* __restrict__ vd2, int mixed) {
+                                                   const double4* __restrict__ vd2,
+                                                   const float4* __restrict__ a32) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= P.n) return;
+  const bool mixed = a32 != nullptr;
   double4 xm = F.xm[i];
   const double4 v4 = vd2[i];
-  const double4 a4 = F.a[i];
+  double4 a4;
+  if (mixed) {
+    // rigid (non-solid) slots keep the acceleration the BCs left (zero)
+    const float4 af = F.perm[i] < P.n_solid ? a32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    a4 = make_double4(af.x, af.y, af.z, 0.0);
+  } else {
+    a4 = F.a[i];
+  }
   const int32_t id = F.id[i];
   double vx = v4.x, vy = v4.y, vz = v4.z, ax = a4.x, ay = a4.y, az = a4.z;
   apply_bc(P, id, vx, vy, vz, ax, ay, az);
@@ -58,6 +67,9 @@ __global__ void __launch_bounds__(256) k_integrate(StepParams P, Fields F,
   if (mixed) {
     F.p32[i] = make_float4((float)xm.x, (float)xm.y, (float)xm.z, (float)xm.w);
     F.v32[i] = make_float4((float)vx, (float)vy, (float)vz, (float)v4.w);
+    const double T = F.T[i];
+    const float thi = (float)T;
+    F.th32[i] = make_float4(thi, (float)(T - (double)thi), (float)F.kT[i], (float)v4.w);
   }
 }
 
@@ -89,22 +101,23 @@ __global__ void __launch_bounds__(128) k_heat_rate(StepParams P, Fields F,
            (xx * (xx * GK) + xy * (xy * GK) + xz * (xz * GK)) / (nxij * nxij);
     }
   } else {
+    // temperature differences from the (hi, lo) float pair: exact to ~1e-14 of T
     const float4 pi = F.p32[i];
-    const float h = (float)P.h, C = (float)P.gkC;
-    const float kif = (float)ki;
+    const float4 ti = F.th32[i];
+    const float invh = P.invhf, C = P.Cf, Ch = P.Chf;
     float sf = 0.0f;
     for (int k = 0; k < c; k++) {
       const int j = __ldg(nb + (int64_t)k * P.npad + i);
       const float4 pj = F.p32[j];
-      const float rhoj = F.v32[j].w;
-      const float kj = (float)F.kT[j];
-      const float dT = (float)(Ti - F.T[j]);
+      const float4 tj = F.th32[j];
+      const float dT = (ti.x - tj.x) + (ti.y - tj.y);
       const float xx = pi.x - pj.x, xy = pi.y - pj.y, xz = pi.z - pj.z;
-      const float r2 = xx * xx + xy * xy + xz * xz;
-      const float q = sqrtf(r2) / h;
-      // x.(GK x)/r^2 = GK for the cubic spline gradient magnitude form
-      const float GK = gradK32(q, h, C);
-      sf += pj.w / rhoj * (4.0f * kif * kj / (kif + kj) * dT) * GK;
+      const float r = sqrtf(xx * xx + xy * xy + xz * xz);
+      const float q = r * invh;
+      // x.(GK x) / r^2 = GK
+      const float GK = q < 1.0f ? Ch * (-3.0f + 2.25f * q)
+                     : (q < 2.0f ? __fdividef(C, r) * (-0.75f * (2.0f - q) * (2.0f - q)) : 0.0f);
+      sf += __fdividef(pj.w, tj.w) * __fdividef(4.0f * ti.z * tj.z, ti.z + tj.z) * dT * GK;
     }
     s = (double)sf;
   }
@@ -122,7 +135,8 @@ __global__ void __launch_bounds__(128) k_heat_rate(StepParams P, Fields F,
 }
 
 // TempCalcLeapfrogFirst / TempCalcLeapfrog (src/cuda/Thermal.cu:16-31)
-__global__ void __launch_bounds__(256) k_heat_leapfrog(StepParams P, Fields F, int first) {
+__global__ void __launch_bounds__(256) k_heat_leapfrog(StepParams P, Fields F, int first,
+                                                       int mixed) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= P.n) return;
   const double dt = P.dt;
@@ -133,7 +147,15 @@ __global__ void __launch_bounds__(256) k_heat_leapfrog(StepParams P, Fields F, i
     F.Tb[i] = ta;
     const double ta2 = ta + F.dTdt[i] * dt;
     F.Ta[i] = ta2;
-    F.T[i] = (ta2 + ta) / 2.;
+    const double T = (ta2 + ta) / 2.;
+    F.T[i] = T;
+    if (mixed) {
+      const float thi = (float)T;
+      float4 t = F.th32[i];
+      t.x = thi;
+      t.y = (float)(T - (double)thi);
+      F.th32[i] = t;
+    }
   }
 }
 
@@ -141,13 +163,13 @@ __global__ void __launch_bounds__(256) k_heat_leapfrog(StepParams P, Fields F, i
 
 static inline int blocks_for(int64_t n, int t) { return (int)((n + t - 1) / t); }
 
-void launch_integrate(const StepParams& P, const Fields& F, const double4* vd2, int mixed,
-                      cudaStream_t s) {
-  k_integrate<<<blocks_for(P.n, 256), 256, 0, s>>>(P, F, vd2, mixed);
+void launch_integrate(const StepParams& P, const Fields& F, const double4* vd2,
+                      const float4* a32, cudaStream_t s) {
+  k_integrate<<<blocks_for(P.n, 256), 256, 0, s>>>(P, F, vd2, a32);
 }
 
 void launch_thermal(const StepParams& P, const Fields& F, const NbBuffers& N, int first,
                     int plastic_heat, int mixed, cudaStream_t s) {
   k_heat_rate<<<blocks_for(P.n, 128), 128, 0, s>>>(P, F, N.nb, N.cnt, plastic_heat, mixed);
-  k_heat_leapfrog<<<blocks_for(P.n, 256), 256, 0, s>>>(P, F, first);
+  k_heat_leapfrog<<<blocks_for(P.n, 256), 256, 0, s>>>(P, F, first, mixed);
 }

@@ -4,9 +4,11 @@
 // FP32 accumulation in the fixed neighbour order.  Kept in FP64 (they sum
 // ~1e-7 s increments over long runs): positions, displacements, velocities
 // and their update, density accumulation, equivalent plastic strain, yield
-// stress, the Newton return map, and every reduction.  The gathered
+// stress and the Newton residual, and every reduction.  The gathered
 // neighbour data are FP32 mirrors written by the integration kernel:
 // p32 = (x, m), v32 = (v, rho), and (after the density pass) v32b = (v, rho_new).
+// All FP32 constants arrive precomputed in StepParams: on GB300 a per-thread
+// FP64 division or conversion costs as much as the whole FP32 pair loop.
 #include "wf_common.cuh"
 #include "wf_mlp.cuh"
 #include "wf_tensor.cuh"
@@ -54,7 +56,7 @@ __global__ void __launch_bounds__(128) k_density32(StepParams P, Fields F,
   const double4 vdi = F.vd[i];
   double rho_new = vdi.w;
   if (F.perm[i] < P.n_solid) {
-    const float invh = (float)(1.0 / P.h), C = (float)P.gkC, Ch = (float)(P.gkC / P.h);
+    const float invh = P.invhf, C = P.Cf, Ch = P.Chf;
     const int32_t idi = F.id[i];
     float drho = 0.0f;
     const int c = cnt[i];
@@ -115,10 +117,10 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
   const float4 pi = F.p32[i];
   const float4 vi = v32b[i];
   const double rho_new = F.vd[i].w + P.dt * F.drho[i];
-  const double p = 0.0 + (P.Cs * P.Cs) * (rho_new - P.rho0);
+  const double p = 0.0 + (P.Cs * P.Cs) * (rho_new - P.rho0);   // FP64: small density change
   F.p[i] = p;
   if (F.perm[i] >= P.n_solid) return;
-  const float invh = (float)(1.0 / P.h), C = (float)P.gkC, Ch = (float)(P.gkC / P.h);
+  const float invh = P.invhf, C = P.Cf, Ch = P.Chf;
   float Dxx = 0.f, Dyy = 0.f, Dzz = 0.f, Dxy = 0.f, Dyz = 0.f, Dxz = 0.f;
   float Wxy = 0.f, Wyz = 0.f, Wxz = 0.f;
   const int c = cnt[i];
@@ -154,7 +156,7 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
   WT.xy = W.yx; WT.xz = W.zx; WT.yx = W.xy; WT.yz = W.zy; WT.zx = W.xz; WT.zy = W.yz;
   const T3f SRT = mul_ref_f(S, WT);
   const T3f RS = mul_ref_f(W, S);
-  const float G2 = (float)(2.0 * P.G), dt = (float)P.dt;
+  const float G2 = P.G2f, dt = P.dtf;
   const float tr3 = (1.0f / 3.0f) * (Dxx + Dyy + Dzz);
   T3f Sn;
   Sn.xx = dt * (G2 * (Dxx - tr3) + SRT.xx + RS.xx) + S.xx;
@@ -176,43 +178,60 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
   double dep = 0.0, seq = st;
   float scale = 1.0f;
   const MatParams& M = P.mat;
-  const double Ti = F.T[i];
   if (P.return_map == 0) {
     // reference one-shot radial return (Mechanical.cu:503-536)
     if (sy < (double)st) scale = (float)(sy / (double)st);
     if (M.model == WF_HOLLOMON) sy = hollomon_yield(M, eps_p);
-    else if (M.model == WF_JOHNSON_COOK) sy = jc_yield_ref(M, eps_p, (double)eff, Ti);
+    else if (M.model == WF_JOHNSON_COOK) sy = jc_yield_ref(M, eps_p, (double)eff, F.T[i]);
     if ((double)st > sy) {
       dep = ((double)st - sy) / (3.0 * P.G);
       eps_p += dep;
       seq = sy;
       if (M.model == WF_BILINEAR) sy += dep * M.Ep;
     }
+  } else if (M.model == WF_JOHNSON_COOK) {
+    // consistent return map: rate and thermal factors in FP32, the yield
+    // function and its Newton residual in FP64 with the cached power
+    float Th = (float)(F.T[i] - M.Tt) * (float)(1.0 / (M.Tm - M.Tt));
+    if (P.clamp_homologous) Th = fminf(fmaxf(Th, 0.0f), 0.999f);
+    const float sr = eff == 0.0f ? 1.0e-5f : eff;
+    const float RTf = (1.0f + (float)M.C * __logf(sr * (float)(1.0 / M.eps0))) *
+                      (1.0f - __powf(Th, (float)M.m));
+    double ratio = -1.0;
+    double pwn = F.pwn[i];
+    if (mlp_w) {
+      // sigma_y0 from the cached power (FP32 suffices for the network input)
+      const float sy0f = ((float)M.A + (float)M.B * (float)fmax(pwn, 0.0)) * RTf;
+      if (st > sy0f) {
+        float f[4];
+        mlp_features(st / sy0f, eps_p, eff, Th, f);
+        const float y = mlp_eval_smem(smlp, f);
+        if (y > 0.0f && y <= 1.0f) ratio = (double)y;
+      }
+    }
+    int it = 0;
+    double sy1;
+    jc_return_cached(P, (double)st, 3.0 * P.G, eps_p, pwn, (double)RTf, ratio, &dep, &sy1, &it);
+    F.pwn[i] = pwn;
+    if (dep > 0.0) {
+      scale = (float)(sy1 / (double)st);
+      eps_p += dep;
+      seq = sy1;
+      atomicAdd((unsigned long long*)(status + 2), (unsigned long long)it);
+      atomicAdd((unsigned long long*)(status + 4), 1ull);
+      if (ratio > 0.0) atomicAdd((unsigned long long*)(status + 6), 1ull);
+    }
+    sy = sy1;
   } else {
-    // consistent return map in FP64 (Newton to the same relative tolerance)
+    // bilinear / Hollomon consistent return map in FP64
     Hard H;
     H.model = M.model; H.R = 1.0; H.Th = 1.0; H.sy_cur = sy; H.Ep = M.Ep;
-    double Th = 0.0;
-    if (M.model == WF_JOHNSON_COOK) {
-      Th = (Ti - M.Tt) / (M.Tm - M.Tt);
-      if (P.clamp_homologous) Th = Th < 0.0 ? 0.0 : (Th > 0.999 ? 0.999 : Th);
-      const double sr = eff == 0.0f ? 1.e-5 : (double)eff;
-      H.R = 1.0 + M.C * log(sr / M.eps0);
-      H.Th = 1.0 - pow(Th, M.m);
-    }
     double sy0, dsy0;
     hard_eval(M, H, eps_p, 0.0, &sy0, &dsy0);
     if ((double)st > sy0) {
       const double G3 = 3.0 * P.G;
-      double dl0 = ((double)st - sy0) / G3;
-      if (mlp_w && M.model == WF_JOHNSON_COOK) {
-        float f[4];
-        mlp_features((float)((double)st / sy0), eps_p, eff, (float)Th, f);
-        const float y = mlp_eval_smem(smlp, f);
-        if (y > 0.0f && y <= 1.0f) dl0 = (double)y * dl0;
-      }
       int it = 0;
-      dep = newton_return(P, H, (double)st, G3, eps_p, sy0, dl0, &it);
+      dep = newton_return(P, H, (double)st, G3, eps_p, sy0, ((double)st - sy0) / G3, &it);
       double sy1, dsy1;
       hard_eval(M, H, eps_p, dep, &sy1, &dsy1);
       scale = (float)(sy1 / (double)st);
@@ -230,7 +249,8 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
   ssp[0] = Sn.xx; ssp[1] = Sn.yy; ssp[2] = Sn.zz; ssp[3] = Sn.xy; ssp[4] = Sn.yz; ssp[5] = Sn.xz;
   // stress / rho^2 for the acceleration pass: two float4 per particle
   const float pf = (float)p;
-  const float ir2 = (float)(1.0 / (rho_new * rho_new));
+  const float rf = vi.w;
+  const float ir2 = 1.0f / (rf * rf);
   float4* sg = reinterpret_cast<float4*>(sigr32 + 8 * i);
   sg[0] = make_float4((Sn.xx - pf) * ir2, (Sn.yy - pf) * ir2, (Sn.zz - pf) * ir2, Sn.xy * ir2);
   sg[1] = make_float4(Sn.yz * ir2, Sn.xz * ir2, 0.f, 0.f);
@@ -239,11 +259,11 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
   F.seq[i] = seq;
   F.dep[i] = dep;
   F.eff[i] = (double)eff;
-  // CalcIntEnergy with the particle's own tensors (FP64 accumulation)
-  const double de = (double)pi.w / rho_new *
-                    (double)(Sn.xx * Dxx + Sn.yy * Dyy + Sn.zz * Dzz +
-                             2.0f * (Sn.xy * Dxy + Sn.yz * Dyz + Sn.xz * Dxz));
-  F.eint[i] += de * P.dt;
+  // CalcIntEnergy with the particle's own tensors, accumulated in FP64
+  const float def = __fdividef(pi.w, rf) *
+                    (Sn.xx * Dxx + Sn.yy * Dyy + Sn.zz * Dzz +
+                     2.0f * (Sn.xy * Dxy + Sn.yz * Dyz + Sn.xz * Dxz));
+  F.eint[i] += (double)def * P.dt;
   if (eps_p > 1.e-6) status[1] = 1;
   if (!isfinite(st)) atomicOr(status, WF_STATUS_NAN);
 }
@@ -252,6 +272,7 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
 __global__ void __launch_bounds__(128) k_accel32(StepParams P, Fields F,
                                                  const float4* __restrict__ v32b,
                                                  const float* __restrict__ sigr32,
+                                                 float4* __restrict__ a32,
                                                  const int32_t* __restrict__ nb,
                                                  const int32_t* __restrict__ cnt) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -262,10 +283,9 @@ __global__ void __launch_bounds__(128) k_accel32(StepParams P, Fields F,
   const int32_t idi = F.id[i];
   const float4* si = reinterpret_cast<const float4*>(sigr32 + 8 * i);
   const float4 s0 = si[0], s1 = si[1];
-  const float invh = (float)(1.0 / P.h), C = (float)P.gkC, Ch = (float)(P.gkC / P.h);
-  const float h = (float)P.h, Cs = (float)P.Cs, alpha = (float)P.alpha, beta = (float)P.beta;
-  const float eps = 0.01f * h * h;
-  const bool av = P.alpha != 0.0 || P.beta != 0.0;
+  const float invh = P.invhf, C = P.Cf, Ch = P.Chf;
+  const float h = P.hf, Cs = P.Csf, alpha = P.alphaf, beta = P.betaf, eps = P.epsf;
+  const bool av = alpha != 0.0f || beta != 0.0f;
   float ax = 0.f, ay = 0.f, az = 0.f;
   const int c = cnt[i];
   for (int k = 0; k < c; k++) {
@@ -294,7 +314,7 @@ __global__ void __launch_bounds__(128) k_accel32(StepParams P, Fields F,
     ay += Txy * gx + Tyy * gy + Tyz * gz;
     az += Txz * gx + Tyz * gy + Tzz * gz;
   }
-  F.a[i] = make_double4((double)ax, (double)ay, (double)az, 0.0);
+  a32[i] = make_float4(ax, ay, az, 0.f);
 }
 
 }  // namespace
@@ -311,6 +331,6 @@ void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b
   k_stress32<<<blocks_for(P.n, 128), 128, smem, s>>>(P, F, v32b, sigr32, N.nb, N.cnt, status, mlp_w);
 }
 void launch_fp32_accel(const StepParams& P, const Fields& F, const float4* v32b,
-                       const float* sigr32, const NbBuffers& N, cudaStream_t s) {
-  k_accel32<<<blocks_for(P.n, 128), 128, 0, s>>>(P, F, v32b, sigr32, N.nb, N.cnt);
+                       const float* sigr32, float4* a32, const NbBuffers& N, cudaStream_t s) {
+  k_accel32<<<blocks_for(P.n, 128), 128, 0, s>>>(P, F, v32b, sigr32, a32, N.nb, N.cnt);
 }

@@ -111,8 +111,10 @@ __global__ void __launch_bounds__(128) k_stress64(StepParams P, Fields F,
   StressState st;
   st.eps_p = F.eps_p[i];
   st.sy = F.sy[i];
+  st.pwn = F.pwn[i];
   StressOut out;
   stress_update_fp64(P, in, st, out);
+  F.pwn[i] = st.pwn;
   F.eff[i] = out.eff;
   F.seq[i] = out.seq;
   F.eps_p[i] = st.eps_p;

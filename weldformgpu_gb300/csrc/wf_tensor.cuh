@@ -91,6 +91,7 @@ struct StressIn {
 };
 struct StressState {
   double eps_p, sy;
+  double pwn;   // cached eps_p^n (Johnson-Cook), < 0 when not cached
 };
 struct StressOut {
   T3 S, Sig;
@@ -167,6 +168,65 @@ __device__ __forceinline__ double newton_return(const StepParams& P, const Hard&
   return dl;
 }
 
+// (ep + dl)^n from the cached ep^n.  Plastic increments per step are ~1e-4 of
+// the accumulated strain, so (1 + u)^n with u = dl / ep is summed as a
+// binomial series to u^5 (truncation below 1e-18 relative for |u| < 1e-3);
+// larger steps, and ep = 0, fall back to pow().  This keeps the yield
+// function FP64-exact without an FP64 transcendental per Newton iterate.
+__device__ __forceinline__ double pow_inc(const MatParams& M, double ep, double inv_ep, double pwn,
+                                          double dl) {
+  if (ep > 0.0 && fabs(dl) < 1.0e-3 * ep) {
+    const double u = dl * inv_ep;
+    const double s =
+        1.0 + u * (M.bin[0] + u * (M.bin[1] + u * (M.bin[2] + u * (M.bin[3] + u * M.bin[4]))));
+    return pwn * s;
+  }
+  const double e = ep + dl;
+  return e > 0.0 ? pow(e, M.n) : 0.0;
+}
+
+// Johnson-Cook consistent return map: Newton on
+//   f(dl) = st - 3G dl - (A + B (ep + dl)^n) * RT = 0,  RT = rate * thermal factor,
+// bracketed on [0, (st - sy0)/3G], stopping at |f| <= rtol * st.  `pwn` is the
+// cached ep^n (refreshed with pow() when < 0); on return it is (ep + dl)^n.
+// dl_ratio in (0, 1] scales the radial start (the MLP warm start).
+__device__ __forceinline__ void jc_return_cached(const StepParams& P, double st, double G3,
+                                                 double ep, double& pwn, double RT,
+                                                 double dl_ratio, double* dl_out, double* sy_out,
+                                                 int* iters) {
+  const MatParams& M = P.mat;
+  if (!(pwn >= 0.0) || P.refresh_pow) pwn = ep > 0.0 ? pow(ep, M.n) : 0.0;
+  const double inv_ep = ep > 0.0 ? 1.0 / ep : 0.0;
+  const double sy0 = (M.A + M.B * pwn) * RT;
+  *iters = 0;
+  if (!(st > sy0)) {
+    *dl_out = 0.0;
+    *sy_out = sy0;
+    return;
+  }
+  double hi = (st - sy0) / G3, lo = 0.0;
+  double dl = (dl_ratio > 0.0 && dl_ratio <= 1.0) ? dl_ratio * hi : hi;
+  double pw = pwn, sy = sy0;
+  int it = 0;
+  for (; it < P.newton_max_iter; it++) {
+    pw = pow_inc(M, ep, inv_ep, pwn, dl);
+    sy = (M.A + M.B * pw) * RT;
+    const double f = st - G3 * dl - sy;
+    if (fabs(f) <= P.newton_rtol * st) break;
+    if (f > 0.0) lo = dl; else hi = dl;
+    // the step needs the slope only to FP32 accuracy
+    const float e = (float)(ep + dl);
+    const float dsy = e > 0.0f ? (float)M.n * (float)M.B * (float)pw / e * (float)RT : 1.0e30f;
+    double dn = dl + (double)((float)f / ((float)G3 + dsy));
+    if (!(dn > lo && dn < hi)) dn = 0.5 * (lo + hi);
+    dl = dn;
+  }
+  *iters = it;
+  *dl_out = dl;
+  *sy_out = sy;
+  pwn = pw;
+}
+
 // Domain_d::StressStrainOne (src/cuda/Mechanical.cu:458-554): Jaumann update
 // of the shear stress, J2 trial, then the reference radial return
 // (return_map 0) or the consistent Newton return map (return_map 1).
@@ -214,8 +274,24 @@ __device__ __forceinline__ void stress_update_fp64(const StepParams& P, const St
       double Th = (in.T - M.Tt) / (M.Tm - M.Tt);
       if (P.clamp_homologous) Th = Th < 0.0 ? 0.0 : (Th > 0.999 ? 0.999 : Th);
       double sr = eff == 0.0 ? 1.e-5 : eff;
-      H.R = 1.0 + M.C * log(sr / M.eps0);
-      H.Th = 1.0 - pow(Th, M.m);
+      const double RT = (1.0 + M.C * log(sr / M.eps0)) * (1.0 - pow(Th, M.m));
+      out.seq = sig_trial;
+      double sy1;
+      int it = 0;
+      jc_return_cached(P, sig_trial, 3.0 * in.G, st.eps_p, st.pwn, RT, dl_start_ratio, &dep,
+                       &sy1, &it);
+      out.newton_iters = it;
+      if (dep > 0.0) {
+        S = t3_scale(S, sy1 / sig_trial);
+        st.eps_p += dep;
+        out.seq = sy1;
+      }
+      st.sy = sy1;
+      out.dep = dep;
+      out.eff = eff;
+      out.S = S;
+      out.Sig = t3_add(t3_ident(-in.p), S);
+      return;
     }
     double sy0, dsy0;
     hard_eval(M, H, st.eps_p, 0.0, &sy0, &dsy0);
