@@ -147,6 +147,39 @@ int64_t wf_gen_cylinder_lattice(double R, double H, double dx, double jitter, ui
 int64_t wf_assign_zone(const double* x, int64_t n, const double* start, const double* end,
                        int32_t zone_id, int32_t* id, uint8_t* not_write);
 
+/* ---- learned warm start of the Johnson-Cook return map ------------------
+ * No reference counterpart (the reference's return map is a one-shot radial
+ * return, src/cuda/Mechanical.cu:503-536).  A 4 -> 64 -> 64 -> 1 SiLU MLP
+ * proposes dlambda / dlambda_radial; Newton still converges to the same
+ * tolerance.  Parameters: float[4481] = W1[64*4], b1[64], W2[64*64], b2[64],
+ * W3[64], b3 (row-major, out x in); features: float4 per sample. */
+#define WF_MLP_NPARAMS 4481
+/* loads trained parameters into the domain; enable with option "mlp" = 1 */
+int wf_set_mlp_weights(wf_domain* d, const float* params);
+/* (features, dlambda/dlambda_radial) pairs logged by the plain FP64 solver
+ * while option "log_return_map" (capacity) is set: copies up to cap pairs */
+int wf_get_return_map_log(wf_domain* d, float* X, float* Y, int64_t cap, int64_t* count);
+/* Y = network(X) for n samples, BF16 tensor cores (FP32 accumulate) or FP32 */
+int wf_mlp_infer(const float* params, const float* X, int64_t n, int use_tensor_cores, float* Y);
+/* mean-squared-error loss and its gradient over n samples (training kernels) */
+int wf_mlp_grad(const float* params, const float* X, const float* Y, int64_t n, float* grad,
+                float* loss);
+/* Adam with cosine decay over `steps` mini-batches; params updated in place */
+int wf_mlp_train(float* params, const float* X, const float* Y, int64_t n, int64_t steps,
+                 int64_t batch, float lr, float* final_loss);
+/* synthetic states (ratio U[1,3], eps_p log-U[1e-4,2], rate log-U[1e-2,1e5],
+ * T U[20,550]) with their converged increments: features X, targets Y,
+ * raw states (ratio, eps_p, rate, T) and the Newton iterations from the
+ * radial start */
+int wf_mlp_synth(const wf_material* mat, double G, int64_t n, uint64_t seed, double rtol,
+                 float* X, float* Y, float* states, int32_t* iters_radial);
+/* Newton iterations on given raw states from the network's start
+ * (params != NULL, BF16 tensor cores) or the radial start; used[i] = 1 when
+ * the network's prediction was taken; dl = converged increment */
+int wf_mlp_newton_iters(const wf_material* mat, double G, const float* params,
+                        const float* states, int64_t n, double rtol, int32_t* iters,
+                        int32_t* used, float* dl);
+
 /* ---- measurement -------------------------------------------------------- */
 /* Runs `nsteps` steps on the handle's stream between CUDA events and
  * returns the elapsed device time; per-kernel event pairs are recorded

@@ -1,0 +1,90 @@
+"""The learned warm start: training kernels checked against the FP64 oracle,
+tensor-core inference against FP32/FP64, the gain over the radial start, and
+its use inside the solver (which must not change the converged answer)."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests import scenarios as S
+
+pytestmark = pytest.mark.gpu
+
+
+def jc_mat():
+    sc = S.compression_cylinder(material="jc")
+    return sc["mat"], sc["G"]
+
+
+def test_training_gradient_matches_fp64_oracle():
+    from weldformgpu_gb300 import mlp
+    rng = np.random.default_rng(5)
+    P = mlp.init_params(3)
+    X = rng.uniform(-1, 1, (1000, 4)).astype(np.float32)
+    Y = rng.uniform(0, 1, 1000).astype(np.float32)
+    loss, g = mlp.grad(P, X, Y)
+    lo, go = O.mlp_loss_grad(P.astype(np.float64), X.astype(np.float64), Y.astype(np.float64))
+    assert abs(loss - lo) <= 1e-5 * abs(lo)
+    # FP32 accumulation over 1000 samples: relative L2 error of the whole gradient
+    err = np.linalg.norm(g - go) / np.linalg.norm(go)
+    assert err < 1e-4, err
+
+
+def test_tensor_core_inference_close_to_fp64():
+    from weldformgpu_gb300 import mlp
+    rng = np.random.default_rng(6)
+    P = mlp.init_params(4)
+    X = rng.uniform(-1, 1, (5000, 4)).astype(np.float32)
+    y64 = O.mlp_forward(P.astype(np.float64), X.astype(np.float64))
+    y32 = mlp.infer(P, X, tensor_cores=False)
+    ytc = mlp.infer(P, X, tensor_cores=True)
+    np.testing.assert_allclose(y32, y64, rtol=1e-5, atol=1e-5)
+    # BF16 operands (8-bit mantissa), FP32 accumulation
+    assert np.max(np.abs(ytc - y64)) < 0.05 * np.max(np.abs(y64)) + 0.02
+    assert np.corrcoef(ytc, y64)[0, 1] > 0.999
+
+
+def test_trained_network_cuts_newton_iterations_on_large_increments():
+    from weldformgpu_gb300 import mlp
+    mat, G = jc_mat()
+    P, loss = mlp.train_jc_warm_start(mat, G, n_synth=131072, steps=2500)
+    assert loss < 2e-3, loss
+    _, Yt, St, it_plain = mlp.synth(mat, G, 20000, seed=11)
+    it_r, used_r, dl_r = mlp.newton_iters(mat, G, None, St)
+    it_m, used_m, dl_m = mlp.newton_iters(mat, G, P, St)
+    assert np.array_equal(it_r, it_plain)
+    assert used_m.mean() > 0.95                  # predictions inside (0, 1]
+    # same converged increment, fewer iterations
+    np.testing.assert_allclose(dl_m, dl_r, rtol=1e-6)
+    assert it_m.mean() < 0.75 * it_r.mean(), (it_m.mean(), it_r.mean())
+
+
+def test_plain_solver_logs_training_pairs():
+    from weldformgpu_gb300 import Domain_d
+    sc = S.compression_cylinder(material="jc", vz_top=-10.0)
+    d = S.load(Domain_d(sc["n"]), sc, {"return_map": 1, "log_return_map": 20000})
+    d.step(300)
+    X, Y = d.get_return_map_log(20000)
+    assert len(X) > 1000
+    assert np.all(Y > 0) and np.all(Y <= 1.0 + 1e-6)
+    assert np.all(X[:, 0] >= 0)                  # trial ratio - 1
+
+
+def test_mlp_in_solver_same_answer():
+    from weldformgpu_gb300 import Domain_d, mlp
+    mat, G = jc_mat()
+    P, _ = mlp.train_jc_warm_start(mat, G, n_synth=65536, steps=1500)
+    sc = S.compression_cylinder(R=0.004, H=0.008, material="jc", vz_top=-10.0,
+                                generator="lattice", dt_rule="baseline")
+    opts = {"return_map": 1, "precision": 1}
+    a = S.load(Domain_d(sc["n"]), sc, opts)
+    b = S.load(Domain_d(sc["n"]), sc, opts)
+    b.set_mlp_weights(P)
+    b.set_option("mlp", 1)
+    a.step(500)
+    b.step(500)
+    assert a.get_field("pl_strain").max() > 0.005
+    assert b.get_scalar("mlp_used") > 0
+    # both starts converge to the same residual tolerance
+    for f in ("pl_strain", "sigma_eq", "u"):
+        ref = a.get_field(f)
+        np.testing.assert_allclose(b.get_field(f), ref, rtol=1e-6, atol=1e-6 * np.abs(ref).max())

@@ -20,6 +20,10 @@
 #include "wf_mlp.cuh"
 #include "wf_nsearch.cuh"
 
+// wf_mlp.cu
+int wf_mlp_pack_device(const float* dparams, void* dpacked, cudaStream_t s);
+size_t wf_mlp_packed_bytes();
+
 #define WF_VERSION "weldform-gb300 0.1 (sm_103a)"
 
 // kernel ids for wf_set_option("profile_kernel", id)
@@ -49,7 +53,14 @@ struct wf_domain {
   float4* v32b = nullptr;
   float4* a32 = nullptr;       // mixed-form acceleration
   float* sigr32 = nullptr;
-  float* mlp_w = nullptr;      // device MLP parameters (FP32 master copy, see wf_mlp.cu)
+  float* mlp_w = nullptr;      // device MLP parameters (FP32, packed layout of wf_mlp.cuh)
+  void* mlp_packed = nullptr;  // BF16 tensor-core fragment image of mlp_w
+  bool mlp_loaded = false;
+  // return-map log: (features, converged increment) pairs from the plain form
+  int64_t log_cap = 0;
+  unsigned long long* log_count = nullptr;
+  float4* log_x = nullptr;
+  float* log_y = nullptr;
   int32_t *nb = nullptr, *nbc = nullptr, *inv = nullptr;
   float4 *pf = nullptr, *pf2 = nullptr;
   uint32_t *cellid = nullptr, *cell_count = nullptr, *cell_cursor = nullptr, *scan_tmp = nullptr;
@@ -271,6 +282,10 @@ static StepParams make_params(const wf_domain* d) {
     }
   }
   P.refresh_pow = (d->step % 64) == 0;   // bounds the drift of the cached eps_p^n
+  P.log_cap = d->log_cap;
+  P.log_count = d->log_count;
+  P.log_x = d->log_x;
+  P.log_y = d->log_y;
   P.hf = (float)P.h;
   P.invhf = (float)(1.0 / P.h);
   P.Cf = (float)P.gkC;
@@ -424,7 +439,8 @@ static int solve_step(wf_domain* d) {
   } else {
     { KTimer t(d, KID_DENSITY); launch_fp32_density(P, F, d->vd2, d->v32b, N, s); }
     { KTimer t(d, KID_STRESS);
-      launch_fp32_stress(P, F, d->v32b, d->sigr32, N, d->d_status, d->mlp_on ? d->mlp_w : nullptr, s); }
+      launch_fp32_stress(P, F, d->v32b, d->sigr32, N, d->d_status,
+                         (d->mlp_on && d->mlp_loaded) ? d->mlp_packed : nullptr, s); }
     { KTimer t(d, KID_ACCEL); launch_fp32_accel(P, F, d->v32b, d->sigr32, d->a32, N, s); }
   }
   { KTimer t(d, KID_INTEGRATE); launch_integrate(P, F, d->vd2, mixed ? d->a32 : nullptr, s); }   // :273-287
@@ -490,7 +506,8 @@ int wf_create(wf_domain** out, int64_t n) {
       dalloc(&d->inv, d->npad, d->stream) || dalloc(&d->pf, d->npad, d->stream) || dalloc(&d->pf2, d->npad, d->stream) ||
       dalloc(&d->cellid, d->npad, d->stream) || dalloc(&d->s_src, d->npad, d->stream) || dalloc(&d->s_orig, d->npad, d->stream) ||
       dalloc(&d->d_mm, 8, d->stream) || dalloc(&d->d_status, 8, d->stream) || dalloc(&d->d_stage, 6 * d->npad, d->stream) ||
-      dalloc(&d->mlp_w, WF_MLP_NPARAM, d->stream))
+      dalloc(&d->mlp_w, WF_MLP_NPARAM, d->stream) ||
+      dalloc(&d->mlp_packed, (int64_t)wf_mlp_packed_bytes(), d->stream))
     return bail(WF_ERR_ALLOC);
   if (cudaMallocHost((void**)&d->h_status, 8 * sizeof(int)) != cudaSuccess) return bail(WF_ERR_ALLOC);
   k_iota<<<nblk(n), 256, 0, d->stream>>>(n, d->F[0].perm, d->inv);
@@ -504,7 +521,8 @@ int wf_destroy(wf_domain* d) {
   if (!d) return WF_OK;
   if (d->stream) cudaStreamSynchronize(d->stream);
   for (int k = 0; k < 2; k++) free_fields(d->F[k]);
-  void* ptrs[] = {d->vd2, d->v32b, d->a32, d->sigr32, d->mlp_w, d->nb, d->nbc, d->inv, d->pf, d->pf2,
+  void* ptrs[] = {d->vd2, d->v32b, d->a32, d->sigr32, d->mlp_w, d->mlp_packed, d->log_x,
+                  d->log_y, d->log_count, d->nb, d->nbc, d->inv, d->pf, d->pf2,
                   d->cellid, d->cell_count, d->cell_cursor, d->scan_tmp, d->s_src, d->s_orig,
                   d->d_mm, d->d_status, d->d_stage};
   for (void* p : ptrs) if (p) cudaFree(p);
@@ -648,6 +666,28 @@ int wf_set_thermal_bc(wf_domain* d, const int32_t* b) {
   if (!d || !b) return WF_ERR_ARG;
   return upload_t<int32_t>(d, b, CF(d).bct);
 }
+int wf_get_return_map_log(wf_domain* d, float* X, float* Y, int64_t cap, int64_t* count) {
+  if (!d || !X || !Y || !count) return WF_ERR_ARG;
+  if (!d->log_cap) return wf_fail(d, WF_ERR_STATE, "option log_return_map not set");
+  unsigned long long c = 0;
+  WF_CUDA_OK(cudaMemcpyAsync(&c, d->log_count, sizeof c, cudaMemcpyDeviceToHost, d->stream));
+  WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+  int64_t m = std::min<int64_t>((int64_t)std::min<unsigned long long>(c, (unsigned long long)d->log_cap), cap);
+  WF_CUDA_OK(cudaMemcpy(X, d->log_x, sizeof(float4) * m, cudaMemcpyDeviceToHost));
+  WF_CUDA_OK(cudaMemcpy(Y, d->log_y, sizeof(float) * m, cudaMemcpyDeviceToHost));
+  *count = m;
+  return WF_OK;
+}
+
+int wf_set_mlp_weights(wf_domain* d, const float* params) {
+  if (!d || !params) return WF_ERR_ARG;
+  WF_CUDA_OK(cudaMemcpyAsync(d->mlp_w, params, sizeof(float) * WF_MLP_NPARAM,
+                             cudaMemcpyHostToDevice, d->stream));
+  if (wf_mlp_pack_device(d->mlp_w, d->mlp_packed, d->stream)) return wf_fail(d, WF_ERR_CUDA, "mlp pack");
+  WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+  d->mlp_loaded = true;
+  return WF_OK;
+}
 int wf_set_convection(wf_domain* d, double hc, double Tinf) {
   if (!d) return WF_ERR_ARG;
   d->h_conv = hc;
@@ -684,6 +724,18 @@ int wf_set_option(wf_domain* d, const char* key, double v) {
   else if (k == "clamp_homologous") d->clamp_homologous = v != 0;
   else if (k == "profile_kernel") d->profile_kernel = (int)v;
   else if (k == "resume") d->resume = v != 0;
+  else if (k == "log_return_map") {
+    // capacity of the (state, converged increment) log kept by the plain form
+    if (v < 0) return WF_ERR_ARG;
+    if (d->log_x) { cudaFree(d->log_x); cudaFree(d->log_y); cudaFree(d->log_count); }
+    d->log_x = nullptr; d->log_y = nullptr; d->log_count = nullptr;
+    d->log_cap = (int64_t)v;
+    if (d->log_cap > 0) {
+      WF_CUDA_OK(dalloc(&d->log_x, d->log_cap, d->stream));
+      WF_CUDA_OK(dalloc(&d->log_y, d->log_cap, d->stream));
+      WF_CUDA_OK(dalloc(&d->log_count, 1, d->stream));
+    }
+  }
   else if (k == "graph") { /* reserved */ }
   else return wf_fail(d, WF_ERR_ARG, "unknown option: " + k);
   return WF_OK;

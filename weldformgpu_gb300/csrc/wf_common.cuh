@@ -92,6 +92,10 @@ struct StepParams {
   double bc_v[WF_MAX_BC][3];
   int mlp_on;           // MLP warm start of the Newton return map
   int refresh_pow;      // recompute eps_p^n with pow() this step (bounds series drift)
+  int64_t log_cap;      // return-map log (training pairs for the MLP): capacity
+  unsigned long long* log_count;
+  float4* log_x;
+  float* log_y;
   MatParams mat;
   // FP32 constants for the mixed form, computed once on the host: on GB300 a
   // per-thread FP64 division or conversion costs as much as an FP32 pair loop
@@ -155,7 +159,7 @@ void launch_thermal(const StepParams& P, const Fields& F, const NbBuffers& N, in
 void launch_fp32_density(const StepParams& P, const Fields& F, double4* vd2, float4* v32b,
                          const NbBuffers& N, cudaStream_t s);
 void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b,
-                        float* sigr32, const NbBuffers& N, int* status, const float* mlp_w,
+                        float* sigr32, const NbBuffers& N, int* status, const void* mlp_packed,
                         cudaStream_t s);
 void launch_fp32_accel(const StepParams& P, const Fields& F, const float4* v32b,
                        const float* sigr32, float4* a32, const NbBuffers& N, cudaStream_t s);

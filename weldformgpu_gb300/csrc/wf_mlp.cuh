@@ -23,7 +23,109 @@
 #define WF_MLP_OFF_W3 (WF_MLP_OFF_B2 + WF_MLP_H)
 #define WF_MLP_OFF_B3 (WF_MLP_OFF_W3 + WF_MLP_H)
 
+#include <cuda_bf16.h>
+#include <stdint.h>
+
 __device__ __forceinline__ float mlp_silu(float z) { return z / (1.0f + __expf(-z)); }
+
+// ---------------------------------------------------------------------------
+// BF16 tensor-core inference (mma.sync m16n8k16, FP32 accumulation).
+//
+// One warp evaluates the network for its 32 particles: rows of the A operand
+// are particles (two m-tiles of 16), columns are input features.  Layer 1 has
+// K = 16 (4 features, a constant 1 that carries the bias b1, zeros); layer 2
+// has K = 64 in 4 k-steps; both have N = 64 in 8 n-tiles.  The FP32 layer-1
+// accumulator fragments become the BF16 A fragments of layer 2 without data
+// movement (for m16n8k16 the C layout of n-tiles 2k, 2k+1 is the A layout of
+// k-step k).  Layer 3 (N = 1) is a dot product reduced across each quad.
+//
+// Fragment layouts (PTX ISA, mma.m16n8k16 with .bf16): lane = 4 g + t;
+//   A regs: {A[g][2t..2t+1]}, {A[g+8][2t..]}, {A[g][2t+8..]}, {A[g+8][2t+8..]}
+//   B regs: {B[2t..2t+1][g]}, {B[2t+8..2t+9][g]}
+//   C/D:    C[g][2t], C[g][2t+1], C[g+8][2t], C[g+8][2t+1]
+// ---------------------------------------------------------------------------
+struct MlpPacked {
+  uint2 b1[8][32];       // layer-1 B fragments per n-tile and lane (W1 | b1)
+  uint2 b2[4][8][32];    // layer-2 B fragments per k-step, n-tile and lane
+  float bias2[WF_MLP_H];
+  float w3[WF_MLP_H];
+  float b3;
+  float pad[3];
+};
+#define WF_MLP_PACKED_WORDS ((int)(sizeof(MlpPacked) / 4))
+
+__device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t*>(&v);
+}
+
+__device__ __forceinline__ void mma_bf16_16816(float c[4], const uint32_t a[4], uint2 b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+      "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y));
+}
+
+// Warp-collective: every lane of the warp must call it, convergent.  Lanes
+// with want == false pass dummy features; returns the network output for the
+// calling lane's particle, or -1 when no lane of the warp wants a prediction.
+__device__ __forceinline__ float mlp_tc_warp(const MlpPacked& W, const float f[4], bool want) {
+  const unsigned full = 0xffffffffu;
+  if (__ballot_sync(full, want) == 0u) return -1.0f;
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  float out = 0.0f;
+#pragma unroll
+  for (int mt = 0; mt < 2; mt++) {
+    // layer-1 A fragment: feature columns 2t, 2t+1 of particles mt*16+g and mt*16+g+8
+    uint32_t a1[4];
+#pragma unroll
+    for (int half = 0; half < 2; half++) {
+      const int src = mt * 16 + g + half * 8;
+      const float f0 = __shfl_sync(full, f[0], src), f1 = __shfl_sync(full, f[1], src);
+      const float f2 = __shfl_sync(full, f[2], src), f3 = __shfl_sync(full, f[3], src);
+      const float c0 = t == 0 ? f0 : (t == 1 ? f2 : (t == 2 ? 1.0f : 0.0f));
+      const float c1 = t == 0 ? f1 : (t == 1 ? f3 : 0.0f);
+      a1[half] = bf16x2(c0, c1);
+    }
+    a1[2] = 0u;
+    a1[3] = 0u;
+    float acc1[8][4];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      acc1[j][0] = acc1[j][1] = acc1[j][2] = acc1[j][3] = 0.0f;
+      mma_bf16_16816(acc1[j], a1, W.b1[j][lane]);
+    }
+    // SiLU, then the accumulators of n-tiles 2k, 2k+1 are the A fragment of k-step k
+    uint32_t a2[4][4];
+#pragma unroll
+    for (int kk = 0; kk < 4; kk++) {
+      a2[kk][0] = bf16x2(mlp_silu(acc1[2 * kk][0]), mlp_silu(acc1[2 * kk][1]));
+      a2[kk][1] = bf16x2(mlp_silu(acc1[2 * kk][2]), mlp_silu(acc1[2 * kk][3]));
+      a2[kk][2] = bf16x2(mlp_silu(acc1[2 * kk + 1][0]), mlp_silu(acc1[2 * kk + 1][1]));
+      a2[kk][3] = bf16x2(mlp_silu(acc1[2 * kk + 1][2]), mlp_silu(acc1[2 * kk + 1][3]));
+    }
+    float y0 = 0.0f, y1 = 0.0f;   // rows g and g+8 of this m-tile
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const int col = 8 * j + 2 * t;
+      float acc2[4] = {W.bias2[col], W.bias2[col + 1], W.bias2[col], W.bias2[col + 1]};
+#pragma unroll
+      for (int kk = 0; kk < 4; kk++) mma_bf16_16816(acc2, a2[kk], W.b2[kk][j][lane]);
+      y0 += W.w3[col] * mlp_silu(acc2[0]) + W.w3[col + 1] * mlp_silu(acc2[1]);
+      y1 += W.w3[col] * mlp_silu(acc2[2]) + W.w3[col + 1] * mlp_silu(acc2[3]);
+    }
+    y0 += __shfl_xor_sync(full, y0, 1);
+    y0 += __shfl_xor_sync(full, y0, 2);
+    y1 += __shfl_xor_sync(full, y1, 1);
+    y1 += __shfl_xor_sync(full, y1, 2);
+    // particle p = mt*16 + half*8 + r sits in row r (+8 for half 1) of quad r
+    const float v0 = __shfl_sync(full, y0, 4 * (lane & 7));
+    const float v1 = __shfl_sync(full, y1, 4 * (lane & 7));
+    if ((lane >> 4) == mt) out = ((lane >> 3) & 1) ? v1 : v0;
+  }
+  return out + W.b3;
+}
 
 __device__ __forceinline__ void mlp_features(float ratio, double eps_p, float eff, float Th,
                                              float f[4]) {

@@ -78,26 +78,6 @@ __global__ void __launch_bounds__(128) k_density32(StepParams P, Fields F,
   v32b[i] = make_float4(vi.x, vi.y, vi.z, (float)rho_new);
 }
 
-// MLP forward in FP32 SIMT, weights staged in shared memory
-__device__ __forceinline__ float mlp_eval_smem(const float* W, const float f[4]) {
-  float h1[WF_MLP_H];
-#pragma unroll 8
-  for (int o = 0; o < WF_MLP_H; o++) {
-    float z = W[WF_MLP_OFF_B1 + o];
-#pragma unroll
-    for (int k = 0; k < 4; k++) z += W[WF_MLP_OFF_W1 + o * 4 + k] * f[k];
-    h1[o] = mlp_silu(z);
-  }
-  float y = W[WF_MLP_OFF_B3];
-  for (int o = 0; o < WF_MLP_H; o++) {
-    float z = W[WF_MLP_OFF_B2 + o];
-#pragma unroll 16
-    for (int k = 0; k < WF_MLP_H; k++) z += W[WF_MLP_OFF_W2 + o * WF_MLP_H + k] * h1[k];
-    y += W[WF_MLP_OFF_W3 + o] * mlp_silu(z);
-  }
-  return y;
-}
-
 // ---- B32: rate tensors + EOS + stress (InteractionAlt.cu:262-383,
 //      Mechanical.cu:289-298, :458-554), energy (Energy.cu:5-19, own tensors)
 __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
@@ -106,24 +86,31 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
                                                   const int32_t* __restrict__ nb,
                                                   const int32_t* __restrict__ cnt,
                                                   int* __restrict__ status,
-                                                  const float* __restrict__ mlp_w) {
-  extern __shared__ float smlp[];
-  if (mlp_w) {
-    for (int k = threadIdx.x; k < WF_MLP_NPARAM; k += blockDim.x) smlp[k] = mlp_w[k];
+                                                  const MlpPacked* __restrict__ mlp) {
+  // The MLP runs on tensor cores with warp-collective mma.sync: every lane of
+  // a warp must reach it, so out-of-range and non-solid lanes are predicated
+  // rather than returned before that point.
+  extern __shared__ uint32_t smlp[];
+  const MlpPacked& Wm = *reinterpret_cast<const MlpPacked*>(smlp);
+  if (mlp) {
+    for (int k = threadIdx.x; k < WF_MLP_PACKED_WORDS; k += blockDim.x)
+      smlp[k] = reinterpret_cast<const uint32_t*>(mlp)[k];
     __syncthreads();
   }
-  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= P.n) return;
+  const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool valid = i0 < P.n;
+  const int64_t i = valid ? i0 : 0;
   const float4 pi = F.p32[i];
   const float4 vi = v32b[i];
   const double rho_new = F.vd[i].w + P.dt * F.drho[i];
   const double p = 0.0 + (P.Cs * P.Cs) * (rho_new - P.rho0);   // FP64: small density change
-  F.p[i] = p;
-  if (F.perm[i] >= P.n_solid) return;
+  if (valid) F.p[i] = p;
+  const bool solid = valid && F.perm[i] < P.n_solid;
+  if (!mlp && !solid) return;
   const float invh = P.invhf, C = P.Cf, Ch = P.Chf;
   float Dxx = 0.f, Dyy = 0.f, Dzz = 0.f, Dxy = 0.f, Dyz = 0.f, Dxz = 0.f;
   float Wxy = 0.f, Wyz = 0.f, Wxz = 0.f;
-  const int c = cnt[i];
+  const int c = solid ? cnt[i] : 0;
   for (int k = 0; k < c; k++) {
     const int j = __ldg(nb + (int64_t)k * P.npad + i);
     if (P.contact && !pass_j(P, F.id[j])) continue;
@@ -178,6 +165,29 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
   double dep = 0.0, seq = st;
   float scale = 1.0f;
   const MatParams& M = P.mat;
+  // rate and thermal factors of the JC law in FP32 (mixed form)
+  float Th = 0.0f, RTf = 1.0f;
+  double pwn = F.pwn[i];
+  const bool jc_newton = P.return_map == 1 && M.model == WF_JOHNSON_COOK;
+  if (jc_newton) {
+    Th = (float)(F.T[i] - M.Tt) * (float)(1.0 / (M.Tm - M.Tt));
+    if (P.clamp_homologous) Th = fminf(fmaxf(Th, 0.0f), 0.999f);
+    const float sr = eff == 0.0f ? 1.0e-5f : eff;
+    RTf = (1.0f + (float)M.C * __logf(sr * (float)(1.0 / M.eps0))) *
+          (1.0f - __powf(Th, (float)M.m));
+  }
+  double ratio = -1.0;
+  if (mlp) {
+    // warm start: sigma_y0 from the cached power (FP32 suffices for the features)
+    const float sy0f = ((float)M.A + (float)M.B * (float)fmax(pwn, 0.0)) * RTf;
+    const bool want = solid && jc_newton && st > sy0f;
+    float f[4] = {0.f, 0.f, 0.f, 0.f};
+    if (want) mlp_features(st / sy0f, eps_p, eff, Th, f);
+    __syncwarp();
+    const float y = mlp_tc_warp(Wm, f, want);
+    if (want && y > 0.0f && y <= 1.0f) ratio = (double)y;
+    if (!solid) return;
+  }
   if (P.return_map == 0) {
     // reference one-shot radial return (Mechanical.cu:503-536)
     if (sy < (double)st) scale = (float)(sy / (double)st);
@@ -189,26 +199,9 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
       seq = sy;
       if (M.model == WF_BILINEAR) sy += dep * M.Ep;
     }
-  } else if (M.model == WF_JOHNSON_COOK) {
-    // consistent return map: rate and thermal factors in FP32, the yield
-    // function and its Newton residual in FP64 with the cached power
-    float Th = (float)(F.T[i] - M.Tt) * (float)(1.0 / (M.Tm - M.Tt));
-    if (P.clamp_homologous) Th = fminf(fmaxf(Th, 0.0f), 0.999f);
-    const float sr = eff == 0.0f ? 1.0e-5f : eff;
-    const float RTf = (1.0f + (float)M.C * __logf(sr * (float)(1.0 / M.eps0))) *
-                      (1.0f - __powf(Th, (float)M.m));
-    double ratio = -1.0;
-    double pwn = F.pwn[i];
-    if (mlp_w) {
-      // sigma_y0 from the cached power (FP32 suffices for the network input)
-      const float sy0f = ((float)M.A + (float)M.B * (float)fmax(pwn, 0.0)) * RTf;
-      if (st > sy0f) {
-        float f[4];
-        mlp_features(st / sy0f, eps_p, eff, Th, f);
-        const float y = mlp_eval_smem(smlp, f);
-        if (y > 0.0f && y <= 1.0f) ratio = (double)y;
-      }
-    }
+  } else if (jc_newton) {
+    // consistent return map: the yield function and its Newton residual in
+    // FP64 with the cached power
     int it = 0;
     double sy1;
     jc_return_cached(P, (double)st, 3.0 * P.G, eps_p, pwn, (double)RTf, ratio, &dep, &sy1, &it);
@@ -326,9 +319,10 @@ void launch_fp32_density(const StepParams& P, const Fields& F, double4* vd2, flo
   k_density32<<<blocks_for(P.n, 128), 128, 0, s>>>(P, F, vd2, v32b, N.nb, N.cnt);
 }
 void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b, float* sigr32,
-                        const NbBuffers& N, int* status, const float* mlp_w, cudaStream_t s) {
-  size_t smem = mlp_w ? sizeof(float) * WF_MLP_NPARAM : 0;
-  k_stress32<<<blocks_for(P.n, 128), 128, smem, s>>>(P, F, v32b, sigr32, N.nb, N.cnt, status, mlp_w);
+                        const NbBuffers& N, int* status, const void* mlp_packed, cudaStream_t s) {
+  const MlpPacked* W = reinterpret_cast<const MlpPacked*>(mlp_packed);
+  size_t smem = W ? sizeof(MlpPacked) : 0;
+  k_stress32<<<blocks_for(P.n, 128), 128, smem, s>>>(P, F, v32b, sigr32, N.nb, N.cnt, status, W);
 }
 void launch_fp32_accel(const StepParams& P, const Fields& F, const float4* v32b,
                        const float* sigr32, float4* a32, const NbBuffers& N, cudaStream_t s) {

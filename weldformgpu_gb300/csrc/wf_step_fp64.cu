@@ -6,6 +6,7 @@
 // the same neighbour order the sums are bit-identical to the CPU oracle.
 // Each kernel states the reference kernel(s) it replaces.
 #include "wf_common.cuh"
+#include "wf_mlp.cuh"
 #include "wf_tensor.cuh"
 
 namespace {
@@ -128,6 +129,16 @@ __global__ void __launch_bounds__(128) k_stress64(StepParams P, Fields F,
   // strain += dt * D (the reference accumulates into an uninitialised local)
   ep[0] += SRS.xx * P.dt; ep[1] += SRS.yy * P.dt; ep[2] += SRS.zz * P.dt;
   ep[3] += SRS.xy * P.dt; ep[4] += SRS.yz * P.dt; ep[5] += SRS.xz * P.dt;
+  if (P.log_cap > 0 && out.dep > 0.0 && P.mat.model == WF_JOHNSON_COOK && P.return_map == 1) {
+    // (state, converged increment) pairs for training the warm-start MLP
+    const unsigned long long slot = atomicAdd((unsigned long long*)P.log_count, 1ull);
+    if (slot < (unsigned long long)P.log_cap) {
+      float f[4];
+      mlp_features((float)(out.st / out.sy0), st.eps_p - out.dep, (float)out.eff, (float)out.Th, f);
+      P.log_x[slot] = make_float4(f[0], f[1], f[2], f[3]);
+      P.log_y[slot] = (float)(out.dep / ((out.st - out.sy0) / (3.0 * P.G)));
+    }
+  }
   if (st.eps_p > 1.e-6) status[1] = 1;                        // is_yielding flag
   if (!isfinite(out.seq)) atomicOr(status, WF_STATUS_NAN);
   if (out.newton_iters > 0) {

@@ -97,6 +97,7 @@ struct StressOut {
   T3 S, Sig;
   double seq, eff, dep;
   int newton_iters;
+  double sy0, Th, st;   // JC return map: yield stress at the start, homologous T, trial stress
 };
 
 // ---- hardening laws (src/cuda/Material.cuh:257-307) ----------------------
@@ -276,6 +277,10 @@ __device__ __forceinline__ void stress_update_fp64(const StepParams& P, const St
       double sr = eff == 0.0 ? 1.e-5 : eff;
       const double RT = (1.0 + M.C * log(sr / M.eps0)) * (1.0 - pow(Th, M.m));
       out.seq = sig_trial;
+      if (!(st.pwn >= 0.0) || P.refresh_pow) st.pwn = st.eps_p > 0.0 ? pow(st.eps_p, M.n) : 0.0;
+      out.sy0 = (M.A + M.B * st.pwn) * RT;
+      out.Th = Th;
+      out.st = sig_trial;
       double sy1;
       int it = 0;
       jc_return_cached(P, sig_trial, 3.0 * in.G, st.eps_p, st.pwn, RT, dl_start_ratio, &dep,

@@ -173,6 +173,16 @@ class Domain_d:
         self._ck(getattr(self.L, "wf_" + fn)(self.h, name.encode(), _ptr(a, C.c_double)),
                  "wf_%s(%s)" % (fn, name))
 
+    def set_mlp_weights(self, params):
+        """Loads warm-start MLP parameters (enable with set_option("mlp", 1))."""
+        from . import mlp
+        mlp.set_domain_weights(self, params)
+
+    def get_return_map_log(self, cap):
+        """(features, targets) logged by the plain form under option log_return_map."""
+        from . import mlp
+        return mlp.get_return_map_log(self, cap)
+
     def set_scalar(self, name, value):
         self._ck(self.L.wf_set_scalar(self.h, name.encode(), float(value)), "wf_set_scalar(%s)" % name)
 
