@@ -146,6 +146,26 @@ def preload(sc, steps):
     return st
 
 
+def train_mlp(sc, state, log_steps=5, cap=1 << 20):
+    """Warm-start network for this material: pairs logged by the plain FP64
+    form from the checkpoint plus synthetic states, trained on the GPU."""
+    from weldformgpu_gb300 import mlp
+    t0 = time.perf_counter()
+    opts = base_options()
+    opts["precision"] = 0
+    d = build_domain(sc, opts)
+    d.restore(state)
+    d.set_option("log_return_map", cap)
+    d.step(log_steps)
+    logged = d.get_return_map_log(cap)
+    d.close()
+    params, loss = mlp.train_jc_warm_start(sc["mat"], sc["G"], n_synth=262144, logged=logged,
+                                           steps=4000, batch=4096)
+    info = {"train_loss_mse": loss, "logged_pairs": int(len(logged[0])), "synthetic_pairs": 262144,
+            "train_steps": 4000, "batch": 4096, "train_s": time.perf_counter() - t0}
+    return params, info
+
+
 def run_form(sc, form, steps, warmup, state, mlp_params=None):
     opts = base_options()
     opts["precision"] = 1 if form == "mixed" else 0
@@ -160,16 +180,19 @@ def run_form(sc, form, steps, warmup, state, mlp_params=None):
     dominant = max(kms, key=kms.get)
     d.set_option("profile_kernel", KERNEL_IDS[dominant])
     it0, c0 = d.get_scalar("newton_iters"), d.get_scalar("newton_calls")
+    u0 = d.get_scalar("mlp_used")
     with ClockSampler() as clk:
         elapsed, kernel_ms, kernel_launches, launches = d.time_steps(steps)
     d.set_option("profile_kernel", 0)
     it1, c1 = d.get_scalar("newton_iters"), d.get_scalar("newton_calls")
+    u1 = d.get_scalar("mlp_used")
     fields = {f: d.get_field(f) for f in ("u", "pl_strain", "sigma_eq", "T")}
     d.close()
     return dict(elapsed_ms=elapsed, kernel_ms=kernel_ms, kernel_launches=kernel_launches,
                 launches=launches, dominant=dominant, per_kernel_ms=kms, clocks=clk.summary(),
                 newton_iters_per_call=(it1 - it0) / max(c1 - c0, 1.0),
-                plastic_per_step=(c1 - c0) / max(steps, 1), fields=fields)
+                plastic_per_step=(c1 - c0) / max(steps, 1),
+                mlp_used_per_step=(u1 - u0) / max(steps, 1), fields=fields)
 
 
 def run_e2e(sc, form, steps, state, mlp_params=None):
@@ -257,6 +280,7 @@ def main():
     ap.add_argument("--forms", default="fp64,mixed", help="forms to time (profiling runs)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-oracle baseline")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end arm")
+    ap.add_argument("--no-mlp", action="store_true", help="time the mixed form without the MLP")
     ap.add_argument("--preload", type=int, default=4000,
                     help="steps run (mixed form) before the timed runs, to reach plasticity")
     args = ap.parse_args()
@@ -292,17 +316,15 @@ def main():
         print(json.dumps(line))
         return
 
-    mlp = None
-    mlp_path = os.path.join(ROOT, "weldformgpu_gb300", "mlp_jc_weights.npy")
-    if os.path.exists(mlp_path):
-        mlp = np.load(mlp_path)
     state = preload(sc, args.preload)
     forms = args.forms.split(",")
+    mlp, mlp_info = (None, None) if args.no_mlp else train_mlp(sc, state)
     mixed = run_form(sc, "mixed", args.steps, warmup, state, mlp)
     if "fp64" not in forms:
         print(json.dumps({"profiling_run": True, "ms_per_step": mixed["elapsed_ms"] / args.steps,
                           "per_kernel_ms": mixed["per_kernel_ms"], "particles": n}))
         return
+    mixed_nomlp = run_form(sc, "mixed", args.steps, warmup, state) if mlp is not None else None
     plain = run_form(sc, "fp64", args.steps, warmup, state)
     t_mixed = reduce_max(dist, mixed["elapsed_ms"])
     t_plain = reduce_max(dist, plain["elapsed_ms"])
@@ -344,6 +366,12 @@ def main():
         "speedup_vs_plain_fp64": value / plain_value,
         "rel_l2_vs_fp64": errs,
         "mlp_warm_start": mlp is not None,
+        "mlp": None if mlp is None else dict(
+            mlp_info,
+            used_per_step=mixed["mlp_used_per_step"],
+            newton_iters_with_mlp=mixed["newton_iters_per_call"],
+            newton_iters_without_mlp=mixed_nomlp["newton_iters_per_call"],
+            mixed_without_mlp_ms_per_step=mixed_nomlp["elapsed_ms"] / args.steps),
         "newton_iters_per_plastic_particle": mixed["newton_iters_per_call"],
         "plastic_particles_per_step": mixed["plastic_per_step"],
         "plastic_fraction_at_start": state["_plastic_fraction"],

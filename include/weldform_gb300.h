@@ -151,9 +151,9 @@ int64_t wf_assign_zone(const double* x, int64_t n, const double* start, const do
  * No reference counterpart (the reference's return map is a one-shot radial
  * return, src/cuda/Mechanical.cu:503-536).  A 4 -> 64 -> 64 -> 1 SiLU MLP
  * proposes dlambda / dlambda_radial; Newton still converges to the same
- * tolerance.  Parameters: float[4481] = W1[64*4], b1[64], W2[64*64], b2[64],
+ * tolerance.  Parameters: float[4545] = W1[64*4], b1[64], W2[64*64], b2[64],
  * W3[64], b3 (row-major, out x in); features: float4 per sample. */
-#define WF_MLP_NPARAMS 4481
+#define WF_MLP_NPARAMS 4545
 /* loads trained parameters into the domain; enable with option "mlp" = 1 */
 int wf_set_mlp_weights(wf_domain* d, const float* params);
 /* (features, dlambda/dlambda_radial) pairs logged by the plain FP64 solver

@@ -579,6 +579,7 @@ static void stage_stress(wfo_domain* d) {
           double f[4];
           mlp_features(st / sy0, d->pl_strain[i], eff, Th, f);
           double y = mlp_eval1(d->mlp, f);
+          if (y > 1.0 && y <= 1.1) y = 1.0;           /* the GPU's mlp_accept() */
           if (y > 0.0 && y <= 1.0) { dl0 = y * dl0; used++; }
         }
         int it = 0;

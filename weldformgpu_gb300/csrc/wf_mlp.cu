@@ -157,7 +157,8 @@ __global__ void k_mlp_newton_iters(StepParams P, double G, const MlpPacked* __re
     mlp_features(s.x, (double)s.y, s.z, (float)Th, f);
     __syncwarp();
     const float y = mlp_tc_warp(W, f, valid);
-    if (y > 0.0f && y <= 1.0f) { ratio = (double)y; use = 1; }
+    const float yc = mlp_accept(y);
+    if (yc > 0.0f) { ratio = (double)yc; use = 1; }
   }
   if (!valid) return;
   double dl, sy1;
@@ -475,3 +476,5 @@ int wf_mlp_newton_iters(const wf_material* mat, double G, const float* params, c
 }
 
 }  // extern "C"
+
+static_assert(WF_MLP_NPARAM == WF_MLP_NPARAMS, "MLP parameter count mismatch between header and kernels");

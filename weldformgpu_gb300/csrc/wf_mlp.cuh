@@ -28,6 +28,15 @@
 
 __device__ __forceinline__ float mlp_silu(float z) { return z / (1.0f + __expf(-z)); }
 
+// The fallback rule: a prediction in (0, 1] is the start; one slightly above
+// 1 (up to 1.1) means "at the radial value" and is clamped to 1; anything
+// else is rejected (returns 0) and Newton starts from the radial value.
+__device__ __forceinline__ float mlp_accept(float y) {
+  if (y > 0.0f && y <= 1.0f) return y;
+  if (y > 1.0f && y <= 1.1f) return 1.0f;
+  return 0.0f;
+}
+
 // ---------------------------------------------------------------------------
 // BF16 tensor-core inference (mma.sync m16n8k16, FP32 accumulation).
 //

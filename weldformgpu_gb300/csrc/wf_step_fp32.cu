@@ -185,7 +185,8 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
     if (want) mlp_features(st / sy0f, eps_p, eff, Th, f);
     __syncwarp();
     const float y = mlp_tc_warp(Wm, f, want);
-    if (want && y > 0.0f && y <= 1.0f) ratio = (double)y;
+    const float yc = mlp_accept(y);
+    if (want && yc > 0.0f) ratio = (double)yc;
     if (!solid) return;
   }
   if (P.return_map == 0) {

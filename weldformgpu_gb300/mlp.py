@@ -17,8 +17,8 @@ import numpy as np
 from . import _abi
 from .domain import lib
 
-NPARAM = 4481
 H = 64
+NPARAM = H * 4 + H + H * H + H + H + 1     # 4545, WF_MLP_NPARAMS
 _bound = False
 
 
