@@ -112,6 +112,39 @@ int wf_step(wf_domain* d, int64_t nsteps);
 /* Rebuild the neighbour list now (cuNSearch find_neighbors, cuNSearch.cu:111). */
 int wf_find_neighbors(wf_domain* d);
 
+/* Neighbour search that allocates no device memory.  No counterpart in the
+ * reference.  For callers that cannot call cudaMalloc: hosts whose framework
+ * owns every device allocation (its own pool or allocator), hosts held to a
+ * device-memory budget reserved up front, and code that must not allocate
+ * while other work runs on the GPU.  Gives the lists of wf_find_neighbors +
+ * wf_get_neighbors for the same positions and h: radius 2h, cuNSearch's
+ * float32 rule, candidates in the z, y, x cell order, ascending index inside a
+ * cell, at most WF_MAX_NEIGHBORS per particle (a count of 70 may mean the list
+ * was cut, as in the reference).
+ *   x       device, 3*n doubles, interleaved xyz (read only)
+ *   counts  device, n int32 (written)
+ *   lists   device, n*WF_MAX_NEIGHBORS int32, row-major; row i holds particle
+ *           i's neighbour indices, entries past counts[i] are left untouched
+ *   stream  cudaStream_t to run on (NULL: the legacy default stream); the call
+ *           returns once the lists are written (it waits for the stream twice)
+ *   err     optional buffer of err_len bytes for a one-line message
+ * Temporaries live in one fixed device array inside the library,
+ * WF_STATIC_SCRATCH_BYTES (about 4.5 MiB), which every GPU that loads the
+ * library holds until the process exits.  Limits: n <= WF_STATIC_MAX_PARTICLES
+ * and a search grid (bounding box in cells of size 2h, plus a margin of two
+ * cells a side) of at most WF_STATIC_MAX_CELLS cells; larger inputs fail with
+ * WF_ERR_ARG and a message naming the limit.  The first call on each device
+ * looks up the array's device address (cudaGetSymbolAddress) for the device
+ * current at the call and caches it: make that first call before any stream
+ * capture.  All calls share the array and each call overwrites what the last
+ * one left there: calls whose GPU work overlaps on one device (two streams or
+ * two host threads at once) race and give wrong lists, so serialise them. */
+#define WF_STATIC_MAX_PARTICLES 65536
+#define WF_STATIC_MAX_CELLS     262144
+#define WF_STATIC_SCRATCH_BYTES 4723200
+int wf_find_neighbors_static(const double* x, int64_t n, double h, int32_t* counts,
+                             int32_t* lists, void* stream, char* err, int64_t err_len);
+
 /* ---- outputs (caller's particle order) --------------------------------- */
 int wf_get_field(wf_domain* d, const char* name, double* out);
 int wf_get_field_i32(wf_domain* d, const char* name, int32_t* out);

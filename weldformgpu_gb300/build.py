@@ -22,7 +22,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=o
 # units whose FP64 arithmetic must round like the reference / the CPU oracle
 NO_FMA = {"wf_step_fp64.cu", "wf_integrate.cu"}
 SOURCES = ["wf_api.cu", "wf_nsearch.cu", "wf_step_fp64.cu", "wf_step_fp32.cu", "wf_integrate.cu",
-           "wf_mlp.cu", "wf_setup.cpp"]
+           "wf_mlp.cu", "wf_setup.cpp", "wf_noalloc.cu"]
 
 
 def nvcc():
