@@ -111,6 +111,26 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+class ProfilerRange:
+    """cuProfilerStart/Stop around a timed region, so that `ncu
+    --profile-from-start off` captures only the timed steps; without a
+    profiler attached both calls do nothing."""
+
+    def __enter__(self):
+        self.lib = None
+        try:
+            import ctypes
+            self.lib = ctypes.CDLL("libcuda.so.1")
+            self.lib.cuProfilerStart()
+        except OSError:
+            self.lib = None
+        return self
+
+    def __exit__(self, *a):
+        if self.lib is not None:
+            self.lib.cuProfilerStop()
+
+
 def build_domain(sc, opts):
     from weldformgpu_gb300 import Domain_d
     from weldformgpu_gb300 import scenarios as S
@@ -181,7 +201,7 @@ def run_form(sc, form, steps, warmup, state, mlp_params=None):
     d.set_option("profile_kernel", KERNEL_IDS[dominant])
     it0, c0 = d.get_scalar("newton_iters"), d.get_scalar("newton_calls")
     u0 = d.get_scalar("mlp_used")
-    with ClockSampler() as clk:
+    with ClockSampler() as clk, ProfilerRange():
         elapsed, kernel_ms, kernel_launches, launches = d.time_steps(steps)
     d.set_option("profile_kernel", 0)
     it1, c1 = d.get_scalar("newton_iters"), d.get_scalar("newton_calls")
