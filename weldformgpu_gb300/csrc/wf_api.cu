@@ -146,7 +146,7 @@ __global__ void k_iota(int64_t n, int32_t* a, int32_t* b) {
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s < n) { a[s] = (int32_t)s; b[s] = (int32_t)s; }
 }
-// neighbour lists in caller ids: lists[o*70+k] = perm[nb[k*npad + inv[o]]]
+// neighbour lists in caller ids: lists[o*70+k] = perm[entry k of slot inv[o]]
 __global__ void k_gather_nb(int64_t n, int64_t npad, const int32_t* inv, const int32_t* perm,
                             const int32_t* nb, const int32_t* cnt, int32_t* ocnt, int32_t* olst) {
   int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -154,7 +154,7 @@ __global__ void k_gather_nb(int64_t n, int64_t npad, const int32_t* inv, const i
   int64_t s = inv[o];
   int c = cnt[s];
   ocnt[o] = c;
-  for (int k = 0; k < WF_NB; k++) olst[o * WF_NB + k] = k < c ? perm[nb[(int64_t)k * npad + s]] : -1;
+  for (int k = 0; k < WF_NB; k++) olst[o * WF_NB + k] = k < c ? perm[nb[nb_at(npad, s, k)]] : -1;
 }
 // SetVelKernel (src/cuda/Mechanical.cu:154-163): v = 0 for solid particles
 __global__ void k_setvel0(int64_t n, int64_t n_solid, Fields F) {
@@ -296,6 +296,19 @@ static StepParams make_params(const wf_domain* d) {
   P.epsf = (float)(0.01 * P.h * P.h);
   P.dtf = (float)P.dt;
   P.G2f = (float)(2.0 * P.G);
+  P.G3f = (float)(3.0 * P.G);
+  P.jcAf = (float)M.A;
+  P.jcBf = (float)M.B;
+  P.jcnf = (float)M.n;
+  for (int k = 0; k < 5; k++) P.binf[k] = (float)M.bin[k];
+  P.jcTtf = (float)M.Tt;
+  P.jcinvdTf = (float)(1.0 / (M.Tm - M.Tt));
+  P.jcCf = (float)M.C;
+  P.jcinveps0f = (float)(1.0 / M.eps0);
+  P.jcmf = (float)M.m;
+  P.chif = (float)P.chi;
+  P.h_convf = (float)P.h_conv;
+  P.T_inff = (float)P.T_inf;
   return P;
 }
 
@@ -502,7 +515,7 @@ int wf_create(wf_domain** out, int64_t n) {
     if (rc) return bail(rc);
   }
   if (dalloc(&d->vd2, d->npad, d->stream) || dalloc(&d->v32b, d->npad, d->stream) || dalloc(&d->a32, d->npad, d->stream) || dalloc(&d->sigr32, 8 * d->npad, d->stream) ||
-      dalloc(&d->nb, (int64_t)WF_NB * d->npad, d->stream) || dalloc(&d->nbc, d->npad, d->stream) ||
+      dalloc(&d->nb, (int64_t)WF_NB_ALLOC * d->npad, d->stream) || dalloc(&d->nbc, d->npad, d->stream) ||
       dalloc(&d->inv, d->npad, d->stream) || dalloc(&d->pf, d->npad, d->stream) || dalloc(&d->pf2, d->npad, d->stream) ||
       dalloc(&d->cellid, d->npad, d->stream) || dalloc(&d->s_src, d->npad, d->stream) || dalloc(&d->s_orig, d->npad, d->stream) ||
       dalloc(&d->d_mm, 8, d->stream) || dalloc(&d->d_status, 8, d->stream) || dalloc(&d->d_stage, 6 * d->npad, d->stream) ||

@@ -12,6 +12,29 @@
 #include "../../include/weldform_gb300.h"
 
 #define WF_NB WF_MAX_NEIGHBORS
+
+// Neighbour lists are stored in blocks of 8 entries, block-major:
+//   entry k of slot i is nb[((k / 8) * npad + i) * 8 + k % 8].
+// A thread reads the 8 entries of one block as two int4 loads (32 contiguous
+// bytes) and the 32 threads of a warp read one contiguous kilobyte, so a pair
+// loop meets the latency of a list load once per 8 neighbours, and the next
+// block can be fetched while the current one is processed.  Entries between a
+// particle's count and the end of its last block hold the particle's own slot,
+// so that whole blocks may be gathered without bounds checks.
+#define WF_NB_BLK 8
+#define WF_NB_BLOCKS ((WF_NB + WF_NB_BLK - 1) / WF_NB_BLK)
+#define WF_NB_ALLOC (WF_NB_BLOCKS * WF_NB_BLK)   // entries allocated per slot
+__host__ __device__ __forceinline__ int64_t nb_at(int64_t npad, int64_t i, int k) {
+  return ((int64_t)(k >> 3) * npad + i) * WF_NB_BLK + (k & 7);
+}
+// block b of slot i as two int4 (entries 8b .. 8b+7)
+__device__ __forceinline__ void nb_block(const int32_t* __restrict__ nb, int64_t npad, int64_t i,
+                                         int b, int4& lo, int4& hi) {
+  const int4* q = reinterpret_cast<const int4*>(nb + ((int64_t)b * npad + i) * WF_NB_BLK);
+  lo = __ldg(q);
+  hi = __ldg(q + 1);
+}
+
 #define WF_MAX_BC 16
 #define WF_MAX_MESH 4
 #define WF_PI 3.14159265358979323846
@@ -71,7 +94,7 @@ struct MatParams {
 struct StepParams {
   int64_t n;            // slots (all particles)
   int64_t n_solid;      // original ids below this are solid (solid_part_count)
-  int64_t npad;         // column stride of the ELL neighbour list
+  int64_t npad;         // slot stride of the neighbour-list blocks (nb_at)
   double h, gkC;        // smoothing length (uniform) and 1/(h^4 pi)
   double dt;
   double Cs, G, rho0;   // uniform sound speed, shear modulus, reference density
@@ -100,6 +123,10 @@ struct StepParams {
   // FP32 constants for the mixed form, computed once on the host: on GB300 a
   // per-thread FP64 division or conversion costs as much as an FP32 pair loop
   float hf, invhf, Cf, Chf, Csf, alphaf, betaf, epsf, dtf, G2f, mlp_scale;
+  // Johnson-Cook constants of the FP32 increment form of the Newton return map
+  float G3f, jcAf, jcBf, jcnf, binf[5];
+  float jcTtf, jcinvdTf, jcCf, jcinveps0f, jcmf;   // T_t, 1/(T_m - T_t), C, 1/eps_0, m
+  float chif, h_convf, T_inff;                      // heat: Taylor-Quinney, convection
 };
 
 #define WF_CUDA_OK(call)                                   \
@@ -124,6 +151,19 @@ __device__ __forceinline__ float gradK32(float q, float h, float C) {
   return 0.0f;
 }
 
+// The mixed form's cubic-spline gradient factor GK (Functions.cu:82-88) from
+// r^2 > 0 (invh = 1/h, Ch = C/h; the q < 1 branch is C/(q h) q (-3 + 9/4 q)
+// without the division): r and C/r from one reciprocal square root, the two
+// branches of the spline selected without a branch.
+__device__ __forceinline__ float gk32_r2(float r2, float invh, float Ch, float C) {
+  const float ri = rsqrtf(r2);
+  const float q = r2 * ri * invh;
+  const float t = 2.0f - q;
+  const float inner = Ch * (-3.0f + 2.25f * q);
+  const float outer = C * ri * (-0.75f * t * t);
+  return q < 1.0f ? inner : (q < 2.0f ? outer : 0.0f);
+}
+
 __device__ __forceinline__ bool pass_ij(const StepParams& P, int32_t idi, int32_t idj) {
   if (!P.contact) return true;
   bool pass = false;
@@ -141,7 +181,7 @@ __device__ __forceinline__ bool pass_j(const StepParams& P, int32_t idj) {
 
 // Kernel launchers (defined in the .cu files, called by wf_api.cu).
 struct NbBuffers {
-  int32_t* nb;      // [WF_NB * npad]
+  int32_t* nb;      // [WF_NB_ALLOC * npad], blocks of 8 (nb_at)
   int32_t* cnt;     // [npad]
 };
 

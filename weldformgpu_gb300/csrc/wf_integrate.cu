@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(128) k_heat_rate(StepParams P, Fields F,
   double s = 0.0;
   if (!mixed) {
     for (int k = 0; k < c; k++) {
-      const int j = __ldg(nb + (int64_t)k * P.npad + i);
+      const int j = __ldg(nb + nb_at(P.npad, i, k));
       const double4 xj = F.xm[j];
       const double rhoj = F.vd[j].w;
       const double kj = F.kT[j];
@@ -106,20 +106,47 @@ __global__ void __launch_bounds__(128) k_heat_rate(StepParams P, Fields F,
     const float4 ti = F.th32[i];
     const float invh = P.invhf, C = P.Cf, Ch = P.Chf;
     float sf = 0.0f;
-    for (int k = 0; k < c; k++) {
-      const int j = __ldg(nb + (int64_t)k * P.npad + i);
-      const float4 pj = F.p32[j];
-      const float4 tj = F.th32[j];
-      const float dT = (ti.x - tj.x) + (ti.y - tj.y);
-      const float xx = pi.x - pj.x, xy = pi.y - pj.y, xz = pi.z - pj.z;
-      const float r = sqrtf(xx * xx + xy * xy + xz * xz);
-      const float q = r * invh;
-      // x.(GK x) / r^2 = GK
-      const float GK = q < 1.0f ? Ch * (-3.0f + 2.25f * q)
-                     : (q < 2.0f ? __fdividef(C, r) * (-0.75f * (2.0f - q) * (2.0f - q)) : 0.0f);
-      sf += __fdividef(pj.w, tj.w) * __fdividef(4.0f * ti.z * tj.z, ti.z + tj.z) * dT * GK;
+    int4 lo = make_int4(0, 0, 0, 0), hi = lo;
+    if (c > 0) nb_block(nb, P.npad, i, 0, lo, hi);
+    for (int b = 0; WF_NB_BLK * b < c; b++) {
+      const int js[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+      const int m = c - WF_NB_BLK * b;
+      if (m > WF_NB_BLK) nb_block(nb, P.npad, i, b + 1, lo, hi);
+#pragma unroll
+      for (int h = 0; h < WF_NB_BLK; h += 4) {
+        float4 pj[4], tj[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          pj[u] = F.p32[js[h + u]];
+          tj[u] = F.th32[js[h + u]];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          if (h + u >= m) continue;
+          const float dT = (ti.x - tj[u].x) + (ti.y - tj[u].y);
+          const float xx = pi.x - pj[u].x, xy = pi.y - pj[u].y, xz = pi.z - pj[u].z;
+          // x.(GK x) / r^2 = GK
+          const float GK = gk32_r2(xx * xx + xy * xy + xz * xz, invh, Ch, C);
+          sf += __fdividef(pj[u].w, tj[u].w) * __fdividef(4.0f * ti.z * tj[u].z, ti.z + tj[u].z) *
+                dT * GK;
+        }
+      }
     }
-    s = (double)sf;
+    // the rate needs FP32 accuracy only (T integrates in FP64): no FP64
+    // division or pow per particle
+    const float rf = (float)rhoi, cpf = (float)F.cpT[i];
+    float sm = sf / (rf * cpf);
+    if (plastic_heat && F.perm[i] < P.n_solid) {
+      const double dep = F.dep[i];
+      if (dep > 0.0) sm += P.chif * (float)F.sy[i] * (float)dep / (rf * cpf * P.dtf);
+    }
+    if (F.bct[i] == 1) {
+      const float mf = (float)xi.w;
+      const float dS2 = powf(mf / rf, 0.666666666f);
+      sm += P.h_convf * dS2 * (P.T_inff - (float)Ti) / (mf * cpf);
+    }
+    F.dTdt[i] = (double)sm;
+    return;
   }
   s *= 1. / (rhoi * F.cpT[i]);
   if (plastic_heat && F.perm[i] < P.n_solid) {

@@ -26,7 +26,9 @@
 #include <cuda_bf16.h>
 #include <stdint.h>
 
-__device__ __forceinline__ float mlp_silu(float z) { return z / (1.0f + __expf(-z)); }
+// SiLU with the fast reciprocal: for z << 0, 1 + exp(-z) overflows to +inf
+// and the quotient is 0 (the limit of z sigmoid(z)); z is finite here.
+__device__ __forceinline__ float mlp_silu(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
 
 // The fallback rule: a prediction in (0, 1] is the start; one slightly above
 // 1 (up to 1.1) means "at the radial value" and is clamped to 1; anything

@@ -12,8 +12,8 @@
 // by original id, and all state is gathered into the new order.  The three
 // x-adjacent cells of a row are then one contiguous slot range, so a
 // particle's candidates are 9 ranges, visited in the reference's order.
-// Lists are stored column-major (nb[k * npad + slot]) so that consecutive
-// threads read consecutive words.
+// Lists are stored in blocks of 8 entries (nb_at in wf_common.cuh): a thread
+// reads 8 entries with two 16-byte loads and a warp reads contiguous memory.
 #include "wf_common.cuh"
 #include "wf_nsearch.cuh"
 
@@ -229,18 +229,21 @@ __global__ void __launch_bounds__(128) k_nblist(int64_t n, int64_t npad, const f
         const float dx = __fsub_rn(q.x, p.x), dy = __fsub_rn(q.y, p.y), dz = __fsub_rn(q.z, p.z);
         const float sq = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
         if (sq < r2 && sq > 0.0f) {
-          nb[(int64_t)count * npad + i] = (int32_t)s;
+          nb[nb_at(npad, i, count)] = (int32_t)s;
           count++;
           if (count == WF_NB) {
-            cnt[i] = count;
             atomicOr(status, WF_STATUS_NB_CAP);
-            return;
+            goto done;
           }
         }
       }
     }
   }
+done:
   cnt[i] = count;
+  // pad the last block with the particle's own slot (see nb_at)
+  for (int k = count; k < ((count + WF_NB_BLK - 1) & ~(WF_NB_BLK - 1)); k++)
+    nb[nb_at(npad, i, k)] = (int32_t)i;
 }
 
 __global__ void k_snapshot(int64_t n, Fields F) {

@@ -34,15 +34,6 @@ __device__ __forceinline__ T3f mul_ref_f(const T3f& a, const T3f& b) {
   return r;
 }
 
-// cubic-spline gradient factor GK (Functions.cu:82-88) with invh = 1/h,
-// Ch = C/h; the q < 1 branch is C/(q h) * q (-3 + 9/4 q) without the division.
-__device__ __forceinline__ float gk32(float r, float invh, float Ch, float C) {
-  const float q = r * invh;
-  if (q < 1.0f) return Ch * (-3.0f + 2.25f * q);
-  if (q < 2.0f) return __fdividef(C, r) * (-0.75f * (2.0f - q) * (2.0f - q));
-  return 0.0f;
-}
-
 // ---- A32: density rate + update (InteractionAlt.cu:166-246, Mechanical.cu:198) --
 __global__ void __launch_bounds__(128) k_density32(StepParams P, Fields F,
                                                    double4* __restrict__ vd2,
@@ -60,22 +51,90 @@ __global__ void __launch_bounds__(128) k_density32(StepParams P, Fields F,
     const int32_t idi = F.id[i];
     float drho = 0.0f;
     const int c = cnt[i];
-    for (int k = 0; k < c; k++) {
-      const int j = __ldg(nb + (int64_t)k * P.npad + i);
-      if (P.contact && !pass_ij(P, idi, F.id[j])) continue;
-      const float4 pj = F.p32[j];
-      const float4 vj = F.v32[j];
-      const float xx = pi.x - pj.x, xy = pi.y - pj.y, xz = pi.z - pj.z;
-      const float r = sqrtf(xx * xx + xy * xy + xz * xz);
-      const float GK = gk32(r, invh, Ch, C);
-      const float vx = vi.x - vj.x, vy = vi.y - vj.y, vz = vi.z - vj.z;
-      drho += pj.w * __fdividef(vi.w, vj.w) * ((vx * xx + vy * xy + vz * xz) * GK);
+    int4 lo = make_int4(0, 0, 0, 0), hi = lo;
+    if (c > 0) nb_block(nb, P.npad, i, 0, lo, hi);
+    for (int b = 0; WF_NB_BLK * b < c; b++) {
+      const int js[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+      const int m = c - WF_NB_BLK * b;   // valid entries of this block (capped at 8)
+      if (m > WF_NB_BLK) nb_block(nb, P.npad, i, b + 1, lo, hi);
+#pragma unroll
+      for (int h = 0; h < WF_NB_BLK; h += 4) {
+        float4 pj[4], vj[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          pj[q] = F.p32[js[h + q]];
+          vj[q] = F.v32[js[h + q]];
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          if (h + q >= m || (P.contact && !pass_ij(P, idi, F.id[js[h + q]]))) continue;
+          const float xx = pi.x - pj[q].x, xy = pi.y - pj[q].y, xz = pi.z - pj[q].z;
+          const float GK = gk32_r2(xx * xx + xy * xy + xz * xz, invh, Ch, C);
+          const float vx = vi.x - vj[q].x, vy = vi.y - vj[q].y, vz = vi.z - vj[q].z;
+          drho += pj[q].w * __fdividef(vi.w, vj[q].w) * ((vx * xx + vy * xy + vz * xz) * GK);
+        }
+      }
     }
     F.drho[i] = (double)drho;
     rho_new = vdi.w + P.dt * (double)drho;
   }
   vd2[i] = make_double4(vdi.x, vdi.y, vdi.z, rho_new);
   v32b[i] = make_float4(vi.x, vi.y, vi.z, (float)rho_new);
+}
+
+// Johnson-Cook consistent return map of the mixed form, solved for the
+// increment.  With the cached power pwn = ep^n and u = dl / ep,
+//   f(dl) = d0 - 3G dl - B RT pwn ((1 + u)^n - 1),   d0 = st - (A + B pwn) RT,
+// is the same residual as st - 3G dl - (A + B (ep + dl)^n) RT, but every term
+// is of the size of the overshoot d0, so FP32 resolves the root to ~1e-7 of dl
+// (st itself is an FP32 value).  The written form subtracts numbers ~1e3 times
+// larger than d0 and needs FP64, which GB300 issues at 1/64 of the FP32 rate.
+// Valid while the bracket [0, d0 / 3G] keeps |u| < 1e-3, where the 5-term
+// binomial series of (1 + u)^n is exact to FP32 rounding; returns false
+// otherwise (first yield, large increments, a power refresh step) and the
+// caller takes the FP64 form.  On success pwn is advanced to (ep + dl)^n in FP64.
+__device__ __forceinline__ bool jc_return_inc32(const StepParams& P, float st, float RT,
+                                                double ep, double& pwn, float dl_ratio,
+                                                float* dl_out, float* sy_out, int* iters) {
+  if (!(pwn >= 0.0) || P.refresh_pow || !(ep > 0.0)) return false;
+  const float pw = (float)pwn;
+  const float BRp = P.jcBf * RT * pw;
+  const float sy0 = P.jcAf * RT + BRp;
+  const float d0 = st - sy0;
+  *iters = 0;
+  if (!(d0 > 0.0f)) {
+    *dl_out = 0.0f;
+    *sy_out = sy0;
+    return true;
+  }
+  const float epf = (float)ep;
+  float hi = d0 / P.G3f, lo = 0.0f;
+  if (!(hi < 1.0e-3f * epf)) return false;
+  const float inv_ep = 1.0f / epf;
+  const float b0 = P.binf[0], b1 = P.binf[1], b2 = P.binf[2], b3 = P.binf[3], b4 = P.binf[4];
+  const float tol = fmaxf((float)P.newton_rtol * st, 16.0f * 1.1920929e-7f * d0);
+  float dl = (dl_ratio > 0.0f && dl_ratio <= 1.0f) ? dl_ratio * hi : hi;
+  int it = 0;
+  for (; it < P.newton_max_iter; it++) {
+    const float u = dl * inv_ep;
+    const float ser = u * (b0 + u * (b1 + u * (b2 + u * (b3 + u * b4))));
+    const float f = d0 - P.G3f * dl - BRp * ser;
+    if (fabsf(f) <= tol) break;
+    if (f > 0.0f) lo = dl; else hi = dl;
+    // f'(dl) = -3G - B RT pwn n (1 + u)^(n - 1) / ep
+    const float dser =
+        inv_ep * (b0 + u * (2.0f * b1 + u * (3.0f * b2 + u * (4.0f * b3 + u * 5.0f * b4))));
+    float dn = dl + f / (P.G3f + BRp * dser);
+    if (!(dn > lo && dn < hi)) dn = 0.5f * (lo + hi);
+    dl = dn;
+  }
+  const float u = dl * inv_ep;
+  const float ser = u * (b0 + u * (b1 + u * (b2 + u * (b3 + u * b4))));
+  *iters = it;
+  *dl_out = dl;
+  *sy_out = sy0 + BRp * ser;
+  pwn += pwn * (double)ser;
+  return true;
 }
 
 // ---- B32: rate tensors + EOS + stress (InteractionAlt.cu:262-383,
@@ -111,30 +170,55 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
   float Dxx = 0.f, Dyy = 0.f, Dzz = 0.f, Dxy = 0.f, Dyz = 0.f, Dxz = 0.f;
   float Wxy = 0.f, Wyz = 0.f, Wxz = 0.f;
   const int c = solid ? cnt[i] : 0;
-  for (int k = 0; k < c; k++) {
-    const int j = __ldg(nb + (int64_t)k * P.npad + i);
-    if (P.contact && !pass_j(P, F.id[j])) continue;
-    const float4 pj = F.p32[j];
-    const float4 vj = v32b[j];
-    const float xx = pi.x - pj.x, xy = pi.y - pj.y, xz = pi.z - pj.z;
-    const float r = sqrtf(xx * xx + xy * xy + xz * xz);
-    const float s = -0.5f * gk32(r, invh, Ch, C) * __fdividef(pj.w, vj.w);
-    const float ax = vi.x - vj.x, ay = vi.y - vj.y, az = vi.z - vj.z;
-    Dxx += 2.0f * ax * xx * s;
-    Dyy += 2.0f * ay * xy * s;
-    Dzz += 2.0f * az * xz * s;
-    Dxy += (ax * xy + ay * xx) * s;
-    Dxz += (ax * xz + az * xx) * s;
-    Dyz += (ay * xz + az * xy) * s;
-    Wxy += (ax * xy - ay * xx) * s;
-    Wxz -= (ax * xz - az * xx) * s;
-    Wyz += (ay * xz - az * xy) * s;
+  int4 lo = make_int4(0, 0, 0, 0), hi = lo;
+  if (c > 0) nb_block(nb, P.npad, i, 0, lo, hi);
+  for (int b = 0; WF_NB_BLK * b < c; b++) {
+    const int js[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+    const int m = c - WF_NB_BLK * b;
+    if (m > WF_NB_BLK) nb_block(nb, P.npad, i, b + 1, lo, hi);
+#pragma unroll
+    for (int h = 0; h < WF_NB_BLK; h += 4) {
+      float4 pj[4], vj[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        pj[q] = F.p32[js[h + q]];
+        vj[q] = v32b[js[h + q]];
+      }
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        if (h + q >= m || (P.contact && !pass_j(P, F.id[js[h + q]]))) continue;
+        const float xx = pi.x - pj[q].x, xy = pi.y - pj[q].y, xz = pi.z - pj[q].z;
+        // w = 2 s of the reference's s = -GK m_j / (2 rho_j); the off-diagonal
+        // sums carry the factor 2 and are halved after the loop
+        const float w = -gk32_r2(xx * xx + xy * xy + xz * xz, invh, Ch, C) *
+                        __fdividef(pj[q].w, vj[q].w);
+        const float sa = (vi.x - vj[q].x) * w, sb = (vi.y - vj[q].y) * w,
+                    sc = (vi.z - vj[q].z) * w;
+        Dxx += sa * xx;
+        Dyy += sb * xy;
+        Dzz += sc * xz;
+        float t = sa * xy, u = sb * xx;
+        Dxy += t + u;
+        Wxy += t - u;
+        t = sa * xz;
+        u = sc * xx;
+        Dxz += t + u;
+        Wxz += u - t;
+        t = sb * xz;
+        u = sc * xy;
+        Dyz += t + u;
+        Wyz += t - u;
+      }
+    }
   }
+  Dxy *= 0.5f; Dxz *= 0.5f; Dyz *= 0.5f;
+  Wxy *= 0.5f; Wxz *= 0.5f; Wyz *= 0.5f;
   // Jaumann update with the reference's product
-  float* ssp = F.ss32 + 6 * i;
+  float2* ssp = reinterpret_cast<float2*>(F.ss32 + 6 * i);
+  const float2 s01 = ssp[0], s23 = ssp[1], s45 = ssp[2];
   T3f S;
-  S.xx = ssp[0]; S.yy = ssp[1]; S.zz = ssp[2];
-  S.xy = S.yx = ssp[3]; S.yz = S.zy = ssp[4]; S.xz = S.zx = ssp[5];
+  S.xx = s01.x; S.yy = s01.y; S.zz = s23.x;
+  S.xy = S.yx = s23.y; S.yz = S.zy = s45.x; S.xz = S.zx = s45.y;
   T3f W;
   W.xx = W.yy = W.zz = 0.f;
   W.xy = Wxy; W.yz = Wyz; W.xz = Wxz; W.yx = -Wxy; W.zy = -Wyz; W.zx = -Wxz;
@@ -170,11 +254,10 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
   double pwn = F.pwn[i];
   const bool jc_newton = P.return_map == 1 && M.model == WF_JOHNSON_COOK;
   if (jc_newton) {
-    Th = (float)(F.T[i] - M.Tt) * (float)(1.0 / (M.Tm - M.Tt));
+    Th = ((float)F.T[i] - P.jcTtf) * P.jcinvdTf;
     if (P.clamp_homologous) Th = fminf(fmaxf(Th, 0.0f), 0.999f);
     const float sr = eff == 0.0f ? 1.0e-5f : eff;
-    RTf = (1.0f + (float)M.C * __logf(sr * (float)(1.0 / M.eps0))) *
-          (1.0f - __powf(Th, (float)M.m));
+    RTf = (1.0f + P.jcCf * __logf(sr * P.jcinveps0f)) * (1.0f - __powf(Th, P.jcmf));
   }
   double ratio = -1.0;
   if (mlp) {
@@ -201,14 +284,22 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
       if (M.model == WF_BILINEAR) sy += dep * M.Ep;
     }
   } else if (jc_newton) {
-    // consistent return map: the yield function and its Newton residual in
-    // FP64 with the cached power
+    // consistent return map: FP32 Newton on the increment where the series
+    // form holds, else the FP64 residual with the cached power
     int it = 0;
     double sy1;
-    jc_return_cached(P, (double)st, 3.0 * P.G, eps_p, pwn, (double)RTf, ratio, &dep, &sy1, &it);
+    float dlf, sy1f;
+    const bool inc32 = jc_return_inc32(P, st, RTf, eps_p, pwn, (float)ratio, &dlf, &sy1f, &it);
+    if (inc32) {
+      dep = (double)dlf;
+      sy1 = (double)sy1f;
+    } else {
+      jc_return_cached(P, (double)st, 3.0 * P.G, eps_p, pwn, (double)RTf, ratio, &dep, &sy1,
+                       &it);
+    }
     F.pwn[i] = pwn;
     if (dep > 0.0) {
-      scale = (float)(sy1 / (double)st);
+      scale = inc32 ? sy1f / st : (float)(sy1 / (double)st);
       eps_p += dep;
       seq = sy1;
       atomicAdd((unsigned long long*)(status + 2), (unsigned long long)it);
@@ -240,7 +331,9 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
   }
   Sn.xx *= scale; Sn.yy *= scale; Sn.zz *= scale;
   Sn.xy *= scale; Sn.yz *= scale; Sn.xz *= scale;
-  ssp[0] = Sn.xx; ssp[1] = Sn.yy; ssp[2] = Sn.zz; ssp[3] = Sn.xy; ssp[4] = Sn.yz; ssp[5] = Sn.xz;
+  ssp[0] = make_float2(Sn.xx, Sn.yy);
+  ssp[1] = make_float2(Sn.zz, Sn.xy);
+  ssp[2] = make_float2(Sn.yz, Sn.xz);
   // stress / rho^2 for the acceleration pass: two float4 per particle
   const float pf = (float)p;
   const float rf = vi.w;
@@ -263,6 +356,10 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
 }
 
 // ---- C32: acceleration + Monaghan viscosity (InteractionAlt.cu:18-150) ----
+// Neighbours gathered per batch: each carries 64 bytes (position, velocity,
+// stress/rho^2), so two at a time keep the kernel near 64 registers; the pass
+// is bound by L1 throughput rather than by gather latency.
+constexpr int kAccelBatch = 2;
 __global__ void __launch_bounds__(128) k_accel32(StepParams P, Fields F,
                                                  const float4* __restrict__ v32b,
                                                  const float* __restrict__ sigr32,
@@ -282,31 +379,48 @@ __global__ void __launch_bounds__(128) k_accel32(StepParams P, Fields F,
   const bool av = alpha != 0.0f || beta != 0.0f;
   float ax = 0.f, ay = 0.f, az = 0.f;
   const int c = cnt[i];
-  for (int k = 0; k < c; k++) {
-    const int j = __ldg(nb + (int64_t)k * P.npad + i);
-    if (P.contact && !pass_ij(P, idi, F.id[j])) continue;
-    const float4 pj = F.p32[j];
-    const float4 vj = v32b[j];
-    const float4* sjp = reinterpret_cast<const float4*>(sigr32 + 8 * (int64_t)j);
-    const float4 t0 = sjp[0], t1 = sjp[1];
-    const float xx = pi.x - pj.x, xy = pi.y - pj.y, xz = pi.z - pj.z;
-    const float r2 = xx * xx + xy * xy + xz * xz;
-    const float r = sqrtf(r2);
-    const float GK = gk32(r, invh, Ch, C) * pj.w;
-    float PI = 0.f;
-    if (av) {
-      const float vdx = (vi.x - vj.x) * xx + (vi.y - vj.y) * xy + (vi.z - vj.z) * xz;
-      if (vdx < 0.f) {
-        const float MU = h * vdx / (r2 + eps);
-        PI = (alpha * Cs * MU + beta * MU * MU) / (0.5f * (vi.w + vj.w));
+  int4 lo = make_int4(0, 0, 0, 0), hi = lo;
+  if (c > 0) nb_block(nb, P.npad, i, 0, lo, hi);
+  for (int b = 0; WF_NB_BLK * b < c; b++) {
+    const int js[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+    const int m = c - WF_NB_BLK * b;
+    if (m > WF_NB_BLK) nb_block(nb, P.npad, i, b + 1, lo, hi);
+#pragma unroll
+    for (int hh = 0; hh < WF_NB_BLK; hh += kAccelBatch) {
+      float4 pj[kAccelBatch], vj[kAccelBatch], t0[kAccelBatch], t1[kAccelBatch];
+#pragma unroll
+      for (int q = 0; q < kAccelBatch; q++) {
+        const int j = js[hh + q];
+        pj[q] = F.p32[j];
+        vj[q] = v32b[j];
+        const float4* sjp = reinterpret_cast<const float4*>(sigr32 + 8 * (int64_t)j);
+        t0[q] = sjp[0];
+        t1[q] = sjp[1];
+      }
+#pragma unroll
+      for (int q = 0; q < kAccelBatch; q++) {
+        if (hh + q >= m || (P.contact && !pass_ij(P, idi, F.id[js[hh + q]]))) continue;
+        const float xx = pi.x - pj[q].x, xy = pi.y - pj[q].y, xz = pi.z - pj[q].z;
+        const float r2 = xx * xx + xy * xy + xz * xz;
+        const float GK = gk32_r2(r2, invh, Ch, C) * pj[q].w;
+        float PI = 0.f;
+        if (av) {
+          const float vdx =
+              (vi.x - vj[q].x) * xx + (vi.y - vj[q].y) * xy + (vi.z - vj[q].z) * xz;
+          if (vdx < 0.f) {
+            const float MU = __fdividef(h * vdx, r2 + eps);
+            PI = __fdividef(alpha * Cs * MU + beta * MU * MU, 0.5f * (vi.w + vj[q].w));
+          }
+        }
+        const float Txx = s0.x + t0[q].x + PI, Tyy = s0.y + t0[q].y + PI,
+                    Tzz = s0.z + t0[q].z + PI;
+        const float Txy = s0.w + t0[q].w, Tyz = s1.x + t1[q].x, Txz = s1.y + t1[q].y;
+        const float gx = xx * GK, gy = xy * GK, gz = xz * GK;
+        ax += Txx * gx + Txy * gy + Txz * gz;
+        ay += Txy * gx + Tyy * gy + Tyz * gz;
+        az += Txz * gx + Tyz * gy + Tzz * gz;
       }
     }
-    const float Txx = s0.x + t0.x + PI, Tyy = s0.y + t0.y + PI, Tzz = s0.z + t0.z + PI;
-    const float Txy = s0.w + t0.w, Tyz = s1.x + t1.x, Txz = s1.y + t1.y;
-    const float gx = xx * GK, gy = xy * GK, gz = xz * GK;
-    ax += Txx * gx + Txy * gy + Txz * gz;
-    ay += Txy * gx + Tyy * gy + Tyz * gz;
-    az += Txz * gx + Tyz * gy + Tzz * gz;
   }
   a32[i] = make_float4(ax, ay, az, 0.f);
 }

@@ -29,7 +29,7 @@ __global__ void __launch_bounds__(128) k_density64(StepParams P, Fields F,
     double drho = 0.0;
     const int c = cnt[i];
     for (int k = 0; k < c; k++) {
-      const int j = __ldg(nb + (int64_t)k * P.npad + i);
+      const int j = __ldg(nb + nb_at(P.npad, i, k));
       if (P.contact && !pass_ij(P, idi, F.id[j])) continue;
       const double4 xj = F.xm[j];
       const double4 vj = F.vd[j];
@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(128) k_stress64(StepParams P, Fields F,
   T3 SRS = t3_zero(), RRS = t3_zero();
   const int c = cnt[i];
   for (int k = 0; k < c; k++) {
-    const int j = __ldg(nb + (int64_t)k * P.npad + i);
+    const int j = __ldg(nb + nb_at(P.npad, i, k));
     if (P.contact && !pass_j(P, F.id[j])) continue;
     const double4 xj = F.xm[j];
     const double4 vj = vd2[j];
@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(128) k_accel64(StepParams P, Fields F,
   double ax = 0.0, ay = 0.0, az = 0.0;
   const int c = cnt[i];
   for (int k = 0; k < c; k++) {
-    const int j = __ldg(nb + (int64_t)k * P.npad + i);
+    const int j = __ldg(nb + nb_at(P.npad, i, k));
     if (P.contact && !pass_ij(P, idi, F.id[j])) continue;
     const double4 xj = F.xm[j];
     const double4 vj = vd2[j];
