@@ -173,6 +173,26 @@ def test_coupled_thermomechanical_jc_vs_oracle():
                                atol=1e-12)
 
 
+def test_mixed_fused_heat_matches_separate_heat_pass():
+    """Mixed form: the heat pass fused into the next step's density pass gives
+    the temperatures of the separate heat pass (to FP32 rounding), including
+    across neighbour rebuilds, calls that end mid-run (the pending heat pass is
+    run before results are read) and the first-step leapfrog."""
+    sc = S.compression_cylinder(material="jc", vz_top=-10.0)
+    sc["k"], sc["cp"] = 167.0, 896.0
+    opts = {"return_map": 1, "thermal": 1, "taylor_quinney": 0.9, "precision": 1,
+            "rebuild_every": 5, "rebuild_current_positions": 1, "rebuild_after_yield": 0}
+    fused = gpu(sc, dict(opts, fuse_heat=1))
+    sep = gpu(sc, dict(opts, fuse_heat=0))
+    for n in (1, 7, 92):                       # uneven calls: flushes at odd places
+        fused.step(n)
+        sep.step(n)
+        Tf, Ts = fused.get_field("T"), sep.get_field("T")
+        assert rel_l2(Tf - 20.0, Ts - 20.0) < 1e-5
+        assert rel_l2(fused.get_field("u"), sep.get_field("u")) < 1e-6
+    assert Ts.max() > 20.5
+
+
 def test_reference_api_mech_fraser_solve_bit_exact():
     """MechFraserSolve(tf, dt_out) through the reference's method names: stale
     (last-output) positions for the rebuilds, outputs every dt_out."""

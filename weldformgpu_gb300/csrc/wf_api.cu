@@ -72,6 +72,9 @@ struct wf_domain {
   double* d_stage = nullptr;   // staging for ABI copies (6 doubles per particle)
   // solver state
   bool started = false, nb_built = false, is_yielding = false, isfirst = true;
+  // mixed form: the heat pass of the last step runs inside the next step's
+  // density pass, or in finish() when the call ends first
+  bool fuse_heat = true, heat_pending = false, heat_pending_first = false;
   double time = 0, t_out = 0, dt_out = 0;
   int64_t step = 0;
   int ts_i = 0;
@@ -450,7 +453,15 @@ static int solve_step(wf_domain* d) {
     { KTimer t(d, KID_STRESS); launch_fp64_stress(P, F, d->vd2, N, d->d_status, s); }  // :204-218
     { KTimer t(d, KID_ACCEL); launch_fp64_accel(P, F, d->vd2, N, s); }               // :221
   } else {
-    { KTimer t(d, KID_DENSITY); launch_fp32_density(P, F, d->vd2, d->v32b, N, s); }
+    {
+      KTimer t(d, KID_DENSITY);
+      if (d->heat_pending)
+        launch_fp32_density_heat(P, F, d->vd2, d->v32b, N, d->heat_pending_first ? 1 : 0,
+                                 d->chi > 0.0 ? 1 : 0, s);
+      else
+        launch_fp32_density(P, F, d->vd2, d->v32b, N, s);
+      d->heat_pending = false;
+    }
     { KTimer t(d, KID_STRESS);
       launch_fp32_stress(P, F, d->v32b, d->sigr32, N, d->d_status,
                          (d->mlp_on && d->mlp_loaded) ? d->mlp_packed : nullptr, s); }
@@ -459,9 +470,14 @@ static int solve_step(wf_domain* d) {
   { KTimer t(d, KID_INTEGRATE); launch_integrate(P, F, d->vd2, mixed ? d->a32 : nullptr, s); }   // :273-287
   d->launches += 4;
   if (d->thermal) {                                                                   // :285
-    KTimer t(d, KID_THERMAL);
-    launch_thermal(P, F, N, d->isfirst ? 1 : 0, d->chi > 0.0 ? 1 : 0, mixed ? 1 : 0, s);
-    d->launches += 2;
+    if (mixed && d->fuse_heat) {
+      d->heat_pending = true;
+      d->heat_pending_first = d->isfirst;
+    } else {
+      KTimer t(d, KID_THERMAL);
+      launch_thermal(P, F, N, d->isfirst ? 1 : 0, d->chi > 0.0 ? 1 : 0, mixed ? 1 : 0, s);
+      d->launches += 2;
+    }
   }
   d->isfirst = false;
   d->time += d->dt;
@@ -482,7 +498,20 @@ static int solve_step(wf_domain* d) {
   return WF_OK;
 }
 
+// the last step's heat pass (mixed form), before any result leaves a call
+static void flush_heat(wf_domain* d) {
+  if (!d->heat_pending) return;
+  StepParams P = make_params(d);
+  NbBuffers N{d->nb, d->nbc};
+  KTimer t(d, KID_THERMAL);
+  launch_thermal(P, d->F[d->cur], N, d->heat_pending_first ? 1 : 0, d->chi > 0.0 ? 1 : 0, 1,
+                 d->stream);
+  d->launches += 2;
+  d->heat_pending = false;
+}
+
 static int finish(wf_domain* d) {
+  flush_heat(d);
   int rc = read_status(d);
   if (rc) return rc;
   WF_CUDA_OK(cudaGetLastError());
@@ -729,6 +758,7 @@ int wf_set_option(wf_domain* d, const char* key, double v) {
   } else if (k == "rebuild_after_yield") d->rebuild_after_yield = v != 0;
   else if (k == "rebuild_current_positions") d->rebuild_current = v != 0;
   else if (k == "thermal") d->thermal = v != 0;
+  else if (k == "fuse_heat") d->fuse_heat = v != 0;
   else if (k == "taylor_quinney") d->chi = v;
   else if (k == "newton_rtol") d->newton_rtol = v;
   else if (k == "newton_max_iter") d->newton_max_iter = (int)v;
@@ -1031,6 +1061,7 @@ int wf_time_steps(wf_domain* d, int64_t nsteps, double* elapsed_ms, double* kern
   int rc = WF_OK;
   d->timing = true;
   for (int64_t k = 0; k < nsteps && rc == WF_OK; k++) rc = solve_step(d);
+  flush_heat(d);   // the timed steps include their whole heat work
   d->timing = false;
   cudaEventRecord(e1, d->stream);
   WF_CUDA_OK(cudaEventSynchronize(e1));

@@ -164,6 +164,25 @@ __device__ __forceinline__ float gk32_r2(float r2, float invh, float Ch, float C
   return q < 1.0f ? inner : (q < 2.0f ? outer : 0.0f);
 }
 
+// Return-map counters (64-bit status words at 2, 4, 6: Newton iterations,
+// plastic calls, MLP starts taken) and the yielding flag (word 1), summed over
+// the warp's active lanes first: one atomic per warp instead of one per
+// particle, which would serialise on one L2 address.
+__device__ __forceinline__ void warp_count(int* status, unsigned iters, unsigned calls,
+                                           unsigned mlp_used, bool yielding) {
+  const unsigned mask = __activemask();
+  const unsigned si = __reduce_add_sync(mask, iters);
+  const unsigned sc = __reduce_add_sync(mask, calls);
+  const unsigned sm = __reduce_add_sync(mask, mlp_used);
+  const bool y = __any_sync(mask, yielding);
+  if ((int)(threadIdx.x & 31) == __ffs(mask) - 1) {
+    if (si) atomicAdd((unsigned long long*)(status + 2), (unsigned long long)si);
+    if (sc) atomicAdd((unsigned long long*)(status + 4), (unsigned long long)sc);
+    if (sm) atomicAdd((unsigned long long*)(status + 6), (unsigned long long)sm);
+    if (y) status[1] = 1;
+  }
+}
+
 __device__ __forceinline__ bool pass_ij(const StepParams& P, int32_t idi, int32_t idj) {
   if (!P.contact) return true;
   bool pass = false;
@@ -198,6 +217,9 @@ void launch_thermal(const StepParams& P, const Fields& F, const NbBuffers& N, in
 
 void launch_fp32_density(const StepParams& P, const Fields& F, double4* vd2, float4* v32b,
                          const NbBuffers& N, cudaStream_t s);
+// density pass of this step with the previous step's heat pass (mixed form)
+void launch_fp32_density_heat(const StepParams& P, const Fields& F, double4* vd2, float4* v32b,
+                              const NbBuffers& N, int first, int plastic_heat, cudaStream_t s);
 void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b,
                         float* sigr32, const NbBuffers& N, int* status, const void* mlp_packed,
                         cudaStream_t s);

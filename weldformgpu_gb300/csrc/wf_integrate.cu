@@ -3,6 +3,7 @@
 // Compiled with -fmad=false: the FP64 leapfrog, position and temperature
 // updates round exactly like the reference (--fmad=false).
 #include "wf_common.cuh"
+#include "wf_heat.cuh"
 
 namespace {
 
@@ -132,20 +133,7 @@ __global__ void __launch_bounds__(128) k_heat_rate(StepParams P, Fields F,
         }
       }
     }
-    // the rate needs FP32 accuracy only (T integrates in FP64): no FP64
-    // division or pow per particle
-    const float rf = (float)rhoi, cpf = (float)F.cpT[i];
-    float sm = sf / (rf * cpf);
-    if (plastic_heat && F.perm[i] < P.n_solid) {
-      const double dep = F.dep[i];
-      if (dep > 0.0) sm += P.chif * (float)F.sy[i] * (float)dep / (rf * cpf * P.dtf);
-    }
-    if (F.bct[i] == 1) {
-      const float mf = (float)xi.w;
-      const float dS2 = powf(mf / rf, 0.666666666f);
-      sm += P.h_convf * dS2 * (P.T_inff - (float)Ti) / (mf * cpf);
-    }
-    F.dTdt[i] = (double)sm;
+    F.dTdt[i] = heat_rate_mixed(P, F, i, sf, rhoi, xi.w, Ti, plastic_heat);
     return;
   }
   s *= 1. / (rhoi * F.cpT[i]);
@@ -166,23 +154,13 @@ __global__ void __launch_bounds__(256) k_heat_leapfrog(StepParams P, Fields F, i
                                                        int mixed) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= P.n) return;
-  const double dt = P.dt;
-  if (first) {
-    F.Ta[i] = F.T[i] - dt / 2.0 * F.dTdt[i];
-  } else {
-    const double ta = F.Ta[i];
-    F.Tb[i] = ta;
-    const double ta2 = ta + F.dTdt[i] * dt;
-    F.Ta[i] = ta2;
-    const double T = (ta2 + ta) / 2.;
-    F.T[i] = T;
-    if (mixed) {
-      const float thi = (float)T;
-      float4 t = F.th32[i];
-      t.x = thi;
-      t.y = (float)(T - (double)thi);
-      F.th32[i] = t;
-    }
+  const double T = heat_leapfrog_one(P, F, i, F.dTdt[i], first);
+  if (mixed && !first) {
+    const float thi = (float)T;
+    float4 t = F.th32[i];
+    t.x = thi;
+    t.y = (float)(T - (double)thi);
+    F.th32[i] = t;
   }
 }
 

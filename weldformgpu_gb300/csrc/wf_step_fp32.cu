@@ -10,6 +10,7 @@
 // All FP32 constants arrive precomputed in StepParams: on GB300 a per-thread
 // FP64 division or conversion costs as much as the whole FP32 pair loop.
 #include "wf_common.cuh"
+#include "wf_heat.cuh"
 #include "wf_mlp.cuh"
 #include "wf_tensor.cuh"
 
@@ -75,6 +76,77 @@ __global__ void __launch_bounds__(128) k_density32(StepParams P, Fields F,
         }
       }
     }
+    F.drho[i] = (double)drho;
+    rho_new = vdi.w + P.dt * (double)drho;
+  }
+  vd2[i] = make_double4(vdi.x, vdi.y, vdi.z, rho_new);
+  v32b[i] = make_float4(vi.x, vi.y, vi.z, (float)rho_new);
+}
+
+// ---- A32 + heat: the previous step's heat pass fused into this density pass.
+// Heat at the end of step n (ThermalSolveKernel + plastic heat + convection +
+// leapfrog, src/cuda/Thermal.cu:16-142) and the density pass of step n+1 read
+// the same positions x^{n+1}, velocities and densities, so one walk over the
+// neighbour list serves both.  Neighbour temperatures come from the th32
+// mirror (T^n, written by the integration kernel), so each thread may update
+// its own FP64 temperature in place.  After a rebuild at the start of step
+// n+1 the heat flux of step n uses the new list (built for these positions).
+__global__ void __launch_bounds__(128) k_density_heat32(StepParams P, Fields F,
+                                                        double4* __restrict__ vd2,
+                                                        float4* __restrict__ v32b,
+                                                        const int32_t* __restrict__ nb,
+                                                        const int32_t* __restrict__ cnt,
+                                                        int first, int plastic_heat) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  const float4 pi = F.p32[i];
+  const float4 vi = F.v32[i];
+  const float4 ti = F.th32[i];
+  const double4 vdi = F.vd[i];
+  const bool solid = F.perm[i] < P.n_solid;
+  const float invh = P.invhf, C = P.Cf, Ch = P.Chf;
+  const int32_t idi = F.id[i];
+  float drho = 0.0f, sf = 0.0f;
+  const int c = cnt[i];
+  int4 lo = make_int4(0, 0, 0, 0), hi = lo;
+  if (c > 0) nb_block(nb, P.npad, i, 0, lo, hi);
+  for (int b = 0; WF_NB_BLK * b < c; b++) {
+    const int js[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+    const int m = c - WF_NB_BLK * b;
+    if (m > WF_NB_BLK) nb_block(nb, P.npad, i, b + 1, lo, hi);
+#pragma unroll
+    for (int h = 0; h < WF_NB_BLK; h += 4) {
+      float4 pj[4], vj[4], tj[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        pj[q] = F.p32[js[h + q]];
+        vj[q] = F.v32[js[h + q]];
+        tj[q] = F.th32[js[h + q]];
+      }
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        if (h + q >= m) continue;
+        const float xx = pi.x - pj[q].x, xy = pi.y - pj[q].y, xz = pi.z - pj[q].z;
+        const float GK = gk32_r2(xx * xx + xy * xy + xz * xz, invh, Ch, C);
+        const float mr = __fdividef(pj[q].w, vj[q].w);   // m_j / rho_j
+        // heat flux (every particle, no contact filter)
+        const float dT = (ti.x - tj[q].x) + (ti.y - tj[q].y);
+        sf += mr * __fdividef(4.0f * ti.z * tj[q].z, ti.z + tj[q].z) * dT * GK;
+        // density rate (solid particles, contact filter)
+        if (solid && !(P.contact && !pass_ij(P, idi, F.id[js[h + q]]))) {
+          const float vx = vi.x - vj[q].x, vy = vi.y - vj[q].y, vz = vi.z - vj[q].z;
+          drho += mr * vi.w * ((vx * xx + vy * xy + vz * xz) * GK);
+        }
+      }
+    }
+  }
+  // heat of the previous step: rate and leapfrog, own particle only
+  const double dTdt = heat_rate_mixed(P, F, i, sf, vdi.w, (double)pi.w, F.T[i], plastic_heat);
+  F.dTdt[i] = dTdt;
+  heat_leapfrog_one(P, F, i, dTdt, first);
+  // density of this step
+  double rho_new = vdi.w;
+  if (solid) {
     F.drho[i] = (double)drho;
     rho_new = vdi.w + P.dt * (double)drho;
   }
@@ -272,6 +344,7 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
     if (want && yc > 0.0f) ratio = (double)yc;
     if (!solid) return;
   }
+  unsigned n_it = 0u, n_call = 0u, n_mlp = 0u;   // this particle's return-map counters
   if (P.return_map == 0) {
     // reference one-shot radial return (Mechanical.cu:503-536)
     if (sy < (double)st) scale = (float)(sy / (double)st);
@@ -302,9 +375,9 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
       scale = inc32 ? sy1f / st : (float)(sy1 / (double)st);
       eps_p += dep;
       seq = sy1;
-      atomicAdd((unsigned long long*)(status + 2), (unsigned long long)it);
-      atomicAdd((unsigned long long*)(status + 4), 1ull);
-      if (ratio > 0.0) atomicAdd((unsigned long long*)(status + 6), 1ull);
+      n_it = (unsigned)it;
+      n_call = 1u;
+      n_mlp = ratio > 0.0 ? 1u : 0u;
     }
     sy = sy1;
   } else {
@@ -323,8 +396,8 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
       eps_p += dep;
       sy = sy1;
       seq = sy1;
-      atomicAdd((unsigned long long*)(status + 2), (unsigned long long)it);
-      atomicAdd((unsigned long long*)(status + 4), 1ull);
+      n_it = (unsigned)it;
+      n_call = 1u;
     } else {
       sy = sy0;
     }
@@ -351,7 +424,7 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
                     (Sn.xx * Dxx + Sn.yy * Dyy + Sn.zz * Dzz +
                      2.0f * (Sn.xy * Dxy + Sn.yz * Dyz + Sn.xz * Dxz));
   F.eint[i] += (double)def * P.dt;
-  if (eps_p > 1.e-6) status[1] = 1;
+  warp_count(status, n_it, n_call, n_mlp, eps_p > 1.e-6);
   if (!isfinite(st)) atomicOr(status, WF_STATUS_NAN);
 }
 
@@ -432,6 +505,11 @@ static inline int blocks_for(int64_t n, int t) { return (int)((n + t - 1) / t); 
 void launch_fp32_density(const StepParams& P, const Fields& F, double4* vd2, float4* v32b,
                          const NbBuffers& N, cudaStream_t s) {
   k_density32<<<blocks_for(P.n, 128), 128, 0, s>>>(P, F, vd2, v32b, N.nb, N.cnt);
+}
+void launch_fp32_density_heat(const StepParams& P, const Fields& F, double4* vd2, float4* v32b,
+                              const NbBuffers& N, int first, int plastic_heat, cudaStream_t s) {
+  k_density_heat32<<<blocks_for(P.n, 128), 128, 0, s>>>(P, F, vd2, v32b, N.nb, N.cnt, first,
+                                                        plastic_heat);
 }
 void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b, float* sigr32,
                         const NbBuffers& N, int* status, const void* mlp_packed, cudaStream_t s) {

@@ -139,12 +139,10 @@ __global__ void __launch_bounds__(128) k_stress64(StepParams P, Fields F,
       P.log_y[slot] = (float)(out.dep / ((out.st - out.sy0) / (3.0 * P.G)));
     }
   }
-  if (st.eps_p > 1.e-6) status[1] = 1;                        // is_yielding flag
   if (!isfinite(out.seq)) atomicOr(status, WF_STATUS_NAN);
-  if (out.newton_iters > 0) {
-    atomicAdd((unsigned long long*)(status + 2), (unsigned long long)out.newton_iters);
-    atomicAdd((unsigned long long*)(status + 4), 1ull);
-  }
+  // Newton counters and the is_yielding flag (eps_p > 1e-6), one atomic per warp
+  warp_count(status, (unsigned)out.newton_iters, out.newton_iters > 0 ? 1u : 0u, 0u,
+             st.eps_p > 1.e-6);
 }
 
 // ---- C: Domain_d::CalcAccel (src/cuda/InteractionAlt.cu:18-150) ---------
