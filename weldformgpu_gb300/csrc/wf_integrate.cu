@@ -39,6 +39,30 @@ __global__ void __launch_bounds__(256) k_integrate(StepParams P, Fields F,
   const int32_t id = F.id[i];
   double vx = v4.x, vy = v4.y, vz = v4.z, ax = a4.x, ay = a4.y, az = a4.z;
   apply_bc(P, id, vx, vy, vz, ax, ay, az);
+  if (mixed) {
+    // the increments in FP32 (relative error ~1e-7 of the increment), added
+    // to the FP64 positions, displacements and velocities
+    const float dtf = P.dtf, hdt2 = 0.5f * P.dtf * P.dtf;
+    const float fax = (float)ax, fay = (float)ay, faz = (float)az;
+    const double ux = (double)((float)vx * dtf + fax * hdt2);
+    const double uy = (double)((float)vy * dtf + fay * hdt2);
+    const double uz = (double)((float)vz * dtf + faz * hdt2);
+    xm.x += ux; xm.y += uy; xm.z += uz;
+    double4 u = F.u[i];
+    u.x += ux; u.y += uy; u.z += uz;
+    vx += (double)(fax * dtf); vy += (double)(fay * dtf); vz += (double)(faz * dtf);
+    apply_bc(P, id, vx, vy, vz, ax, ay, az);
+    F.xm[i] = xm;
+    F.vd[i] = make_double4(vx, vy, vz, v4.w);
+    F.u[i] = u;
+    F.a[i] = make_double4(ax, ay, az, 0.0);
+    F.p32[i] = make_float4((float)xm.x, (float)xm.y, (float)xm.z, (float)xm.w);
+    F.v32[i] = make_float4((float)vx, (float)vy, (float)vz, (float)v4.w);
+    const double T = F.T[i];
+    const float thi = (float)T;
+    F.th32[i] = make_float4(thi, (float)(T - (double)thi), (float)F.kT[i], (float)v4.w);
+    return;
+  }
   const double dt = P.dt;
   const double ux = vx * dt + ((ax * 0.5) * dt) * dt;
   const double uy = vy * dt + ((ay * 0.5) * dt) * dt;
@@ -48,30 +72,21 @@ __global__ void __launch_bounds__(256) k_integrate(StepParams P, Fields F,
   u.x = u.x + ux; u.y = u.y + uy; u.z = u.z + uz;
   vx = vx + ax * dt; vy = vy + ay * dt; vz = vz + az * dt;
   apply_bc(P, id, vx, vy, vz, ax, ay, az);
-  if (!mixed) {
-    // energy_mode 0 reads particle 0's tensors for every particle, like the
-    // reference; mode 1 uses each particle's own.
-    const bool own = P.energy_mode != 0;
-    if (!own || F.perm[i] < P.n_solid) {
-      const double* ss = F.ss6 + 6 * (own ? i : (int64_t)P.inv[0]);
-      const double* sr = F.sr6 + 6 * (own ? i : (int64_t)P.inv[0]);
-      const double de = xm.w / v4.w *
-                        (ss[0] * sr[0] + ss[1] * sr[1] + ss[2] * sr[2] +
-                         2.0 * (ss[3] * sr[3] + ss[4] * sr[4] + ss[5] * sr[5]));
-      F.eint[i] += de * dt;
-    }
+  // energy_mode 0 reads particle 0's tensors for every particle, like the
+  // reference; mode 1 uses each particle's own.
+  const bool own = P.energy_mode != 0;
+  if (!own || F.perm[i] < P.n_solid) {
+    const double* ss = F.ss6 + 6 * (own ? i : (int64_t)P.inv[0]);
+    const double* sr = F.sr6 + 6 * (own ? i : (int64_t)P.inv[0]);
+    const double de = xm.w / v4.w *
+                      (ss[0] * sr[0] + ss[1] * sr[1] + ss[2] * sr[2] +
+                       2.0 * (ss[3] * sr[3] + ss[4] * sr[4] + ss[5] * sr[5]));
+    F.eint[i] += de * dt;
   }
   F.xm[i] = xm;
   F.vd[i] = make_double4(vx, vy, vz, v4.w);
   F.u[i] = u;
   F.a[i] = make_double4(ax, ay, az, 0.0);
-  if (mixed) {
-    F.p32[i] = make_float4((float)xm.x, (float)xm.y, (float)xm.z, (float)xm.w);
-    F.v32[i] = make_float4((float)vx, (float)vy, (float)vz, (float)v4.w);
-    const double T = F.T[i];
-    const float thi = (float)T;
-    F.th32[i] = make_float4(thi, (float)(T - (double)thi), (float)F.kT[i], (float)v4.w);
-  }
 }
 
 // ---- heat: ThermalSolveKernel + plastic heat + CalcConvHeatKernel -------

@@ -70,6 +70,27 @@ __device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
   return *reinterpret_cast<uint32_t*>(&v);
 }
 
+// SiLU(z) = z sigmoid(z) = h (1 + tanh(h)), h = z / 2, with the hardware tanh
+// approximation: one MUFU operation per value instead of an exponential and a
+// reciprocal (the tensor-core inference is MUFU-bound otherwise).
+__device__ __forceinline__ float silu_tanh(float z) {
+  const float h = 0.5f * z;
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(h));
+  return fmaf(h, t, h);
+}
+
+// Two SiLUs in BF16 for a pair of layer-1 outputs that become one BF16x2 A
+// operand of layer 2 anyway: tanh.approx.bf16x2 handles both values in one
+// MUFU operation.
+__device__ __forceinline__ uint32_t silu_bf16x2(float z0, float z1) {
+  const uint32_t h = bf16x2(0.5f * z0, 0.5f * z1);
+  uint32_t t, r;
+  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(h));
+  asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(r) : "r"(h), "r"(t), "r"(h));
+  return r;
+}
+
 __device__ __forceinline__ void mma_bf16_16816(float c[4], const uint32_t a[4], uint2 b) {
   asm volatile(
       "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
@@ -111,10 +132,10 @@ __device__ __forceinline__ float mlp_tc_warp(const MlpPacked& W, const float f[4
     uint32_t a2[4][4];
 #pragma unroll
     for (int kk = 0; kk < 4; kk++) {
-      a2[kk][0] = bf16x2(mlp_silu(acc1[2 * kk][0]), mlp_silu(acc1[2 * kk][1]));
-      a2[kk][1] = bf16x2(mlp_silu(acc1[2 * kk][2]), mlp_silu(acc1[2 * kk][3]));
-      a2[kk][2] = bf16x2(mlp_silu(acc1[2 * kk + 1][0]), mlp_silu(acc1[2 * kk + 1][1]));
-      a2[kk][3] = bf16x2(mlp_silu(acc1[2 * kk + 1][2]), mlp_silu(acc1[2 * kk + 1][3]));
+      a2[kk][0] = silu_bf16x2(acc1[2 * kk][0], acc1[2 * kk][1]);
+      a2[kk][1] = silu_bf16x2(acc1[2 * kk][2], acc1[2 * kk][3]);
+      a2[kk][2] = silu_bf16x2(acc1[2 * kk + 1][0], acc1[2 * kk + 1][1]);
+      a2[kk][3] = silu_bf16x2(acc1[2 * kk + 1][2], acc1[2 * kk + 1][3]);
     }
     float y0 = 0.0f, y1 = 0.0f;   // rows g and g+8 of this m-tile
 #pragma unroll
@@ -123,8 +144,8 @@ __device__ __forceinline__ float mlp_tc_warp(const MlpPacked& W, const float f[4
       float acc2[4] = {W.bias2[col], W.bias2[col + 1], W.bias2[col], W.bias2[col + 1]};
 #pragma unroll
       for (int kk = 0; kk < 4; kk++) mma_bf16_16816(acc2, a2[kk], W.b2[kk][j][lane]);
-      y0 += W.w3[col] * mlp_silu(acc2[0]) + W.w3[col + 1] * mlp_silu(acc2[1]);
-      y1 += W.w3[col] * mlp_silu(acc2[2]) + W.w3[col + 1] * mlp_silu(acc2[3]);
+      y0 += W.w3[col] * silu_tanh(acc2[0]) + W.w3[col + 1] * silu_tanh(acc2[1]);
+      y1 += W.w3[col] * silu_tanh(acc2[2]) + W.w3[col + 1] * silu_tanh(acc2[3]);
     }
     y0 += __shfl_xor_sync(full, y0, 1);
     y0 += __shfl_xor_sync(full, y0, 2);
