@@ -95,6 +95,25 @@ int wf_set_temperature(wf_domain* d, const double* T);   /* T (Domain_d::CopyDat
 int wf_set_thermal_bc(wf_domain* d, const int32_t* bc_t); /* BC_T: 0 none, 1 convection */
 int wf_set_convection(wf_domain* d, double h_conv, double T_inf); /* h_conv_double, T_inf */
 
+/* ---- contact with rigid triangle meshes ---------------------------------
+ * friction_sta / friction_dyn (src/WeldFormGPU.cu:631-641, Domain_d.cuh:260)
+ * and the contact law: 0 = the reference's penalty law
+ * (CalcContactForcesWang, src/cuda/Contact.cu:134-321). */
+int wf_set_contact(wf_domain* d, double mu_static, double mu_dynamic, int law);
+/* A rigid triangle mesh (TriMesh_d, src/cuda/Mesh.cuh:19-54) as main adds it
+ * (AddTrimeshParticles + AssignTrimeshAddress + SetMeshVel,
+ * src/WeldFormGPU.cu:545-610): particles first .. first+ne-1, which must
+ * follow the solid ones (wf_set_solid_count), become the element centroids
+ * with mass 0 and the mesh's zone id; the mesh moves with velocity `vel`
+ * and angular velocity `angvel` (m_v, m_w).  nodes: 3*nn doubles; tris:
+ * 3*ne node indices; normals: 3*ne doubles or NULL (computed as
+ * TriMesh_d::CalcNormals).  Call after wf_set_positions and wf_set_mass;
+ * turns contact on (surface tagging, contact list, penalty forces, mesh
+ * motion in MechFraserSolve order).  Zone id 1 is the free-surface id. */
+int wf_add_trimesh(wf_domain* d, const double* nodes, int32_t nn, const int32_t* tris,
+                   int32_t ne, const double* normals, int32_t zone_id, int64_t first,
+                   const double* vel, const double* angvel);
+
 /* Options with no reference field (precision, return map, rebuild cadence…).
  * Keys are listed in the library documentation; unknown keys fail. */
 int wf_set_option(wf_domain* d, const char* key, double value);
@@ -175,6 +194,15 @@ int64_t wf_gen_box(double x0, double y0, double z0, double Lx, double Ly, double
  * no reference counterpart (synthetic benchmark workload). */
 int64_t wf_gen_cylinder_lattice(double R, double H, double dx, double jitter, uint64_t seed,
                                 double* x);
+/* TriMesh_d::AxisPlaneMesh (src/cuda/Mesh.cu:48-194) as main builds a
+ * "Plane" rigid body (src/WeldFormGPU.cu:545-552): (dens+1)^2 nodes stepped
+ * by (p2[0] - p1[0])/dens in x and y from p1 at z = p1[2], 2 dens^2
+ * triangles ordered for a normal along +axis when `positive` (main passes
+ * axis 2, positive 0).  Returns the triangle count; nodes (3 (dens+1)^2),
+ * tris (3 per triangle) and normals (3 per triangle) are written when not
+ * NULL. */
+int64_t wf_gen_plane_mesh(int axis, int positive, const double* p1, const double* p2, int dens,
+                          double* nodes, int32_t* tris, double* normals);
 /* Domain::AssignZone (src/Domain.cpp:989-1005): tags particles inside the
  * inclusive box [start, end]; returns how many. */
 int64_t wf_assign_zone(const double* x, int64_t n, const double* start, const double* end,

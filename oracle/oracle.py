@@ -134,6 +134,20 @@ class OracleDomain:
         p = np.ascontiguousarray(params, dtype=np.float64)
         self._ck(self.L.wfo_set_mlp_params(self.h, _p(p)), "set_mlp_params")
 
+    def set_contact(self, mu_static, mu_dynamic, law=0):
+        self._ck(self.L.wfo_set_contact(self.h, float(mu_static), float(mu_dynamic), int(law)),
+                 "set_contact")
+
+    def add_trimesh(self, nodes, tris, zone_id, first, vel, angvel=(0.0, 0.0, 0.0), normals=None):
+        nd = np.ascontiguousarray(nodes, dtype=np.float64).reshape(-1, 3)
+        tr = np.ascontiguousarray(tris, dtype=np.int32).reshape(-1, 3)
+        na = None if normals is None else np.ascontiguousarray(normals, dtype=np.float64)
+        v = np.ascontiguousarray(vel, dtype=np.float64)
+        w = np.ascontiguousarray(angvel, dtype=np.float64)
+        self._ck(self.L.wfo_add_trimesh(self.h, _p(nd), len(nd), _p(tr, C.c_int32), len(tr),
+                                        None if na is None else _p(na), int(zone_id), int(first),
+                                        _p(v), _p(w)), "add_trimesh")
+
     def get_field(self, name):
         c = _abi.FIELD_COMPONENTS.get(name, 1)
         out = np.empty(self.n * c, dtype=np.float64)
@@ -194,6 +208,19 @@ def gen_cylinder_lattice(R, H, dx, jitter, seed):
     return x.reshape(n, 3)
 
 
+def gen_plane_mesh(axis, positive, p1, p2, dens):
+    """AxisPlaneMesh restated: (nodes[nn,3], tris[ne,3], normals[ne,3])."""
+    L = lib()
+    a, b = np.asarray(p1, dtype=np.float64), np.asarray(p2, dtype=np.float64)
+    ne = L.wfo_gen_plane_mesh(int(axis), int(positive), _p(a), _p(b), int(dens), None, None, None)
+    nodes = np.empty(3 * (dens + 1) ** 2)
+    tris = np.empty(3 * ne, dtype=np.int32)
+    normals = np.empty(3 * ne)
+    L.wfo_gen_plane_mesh(int(axis), int(positive), _p(a), _p(b), int(dens), _p(nodes),
+                         _p(tris, C.c_int32), _p(normals))
+    return nodes.reshape(-1, 3), tris.reshape(-1, 3), normals.reshape(-1, 3)
+
+
 def assign_zone(x, start, end, zone, ids, not_write):
     x = np.ascontiguousarray(x, dtype=np.float64)
     s = np.asarray(start, dtype=np.float64)
@@ -247,6 +274,13 @@ def ref_lib():
         L.wfr_step.argtypes = [C.c_void_p, C.c_int64]
         L.wfr_get.restype = C.c_int
         L.wfr_get.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_double)]
+        L.wfr_get_id.restype = C.c_int
+        L.wfr_get_id.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
+        L.wfr_set_not_write.argtypes = [C.c_void_p, C.POINTER(C.c_uint8)]
+        L.wfr_set_contact.argtypes = [C.c_void_p, C.c_double, C.c_double]
+        pd = C.POINTER(C.c_double)
+        L.wfr_add_trimesh.argtypes = [C.c_void_p, pd, C.c_int, C.POINTER(C.c_int32), C.c_int, pd,
+                                      C.c_int, C.c_int64, pd, pd]
         _ref = L
     return _ref
 
@@ -286,6 +320,28 @@ class RefDomain:
 
     def add_bc(self, zone, v):
         self.L.wfr_add_bc(self.h, int(zone), float(v[0]), float(v[1]), float(v[2]))
+
+    def set_not_write(self, flags):
+        f = np.ascontiguousarray(flags, dtype=np.uint8)
+        self.L.wfr_set_not_write(self.h, _p(f, C.c_uint8))
+
+    def set_contact(self, mu_static, mu_dynamic):
+        self.L.wfr_set_contact(self.h, float(mu_static), float(mu_dynamic))
+
+    def add_trimesh(self, nodes, tris, zone_id, first, vel, angvel=(0.0, 0.0, 0.0), normals=None):
+        nd = np.ascontiguousarray(nodes, dtype=np.float64).reshape(-1, 3)
+        tr = np.ascontiguousarray(tris, dtype=np.int32).reshape(-1, 3)
+        na = None if normals is None else np.ascontiguousarray(normals, dtype=np.float64)
+        v = np.ascontiguousarray(vel, dtype=np.float64)
+        w = np.ascontiguousarray(angvel, dtype=np.float64)
+        self.L.wfr_add_trimesh(self.h, _p(nd), len(nd), _p(tr, C.c_int32), len(tr),
+                               None if na is None else _p(na), int(zone_id), int(first), _p(v),
+                               _p(w))
+
+    def get_id(self):
+        out = np.empty(self.n, dtype=np.int32)
+        self.L.wfr_get_id(self.h, _p(out, C.c_int32))
+        return out
 
     def begin(self):
         self.L.wfr_begin(self.h)

@@ -32,7 +32,7 @@
 #include "Functions.cuh"
 #include "Mechanical.cu"
 #include "InteractionAlt.cu"
-#include "Energy.cu"
+#include "Energy.cu"   /* Mechanical.cu brings Geometry.cu, Contact.cu and Mesh.cu */
 
 using namespace SPH;
 
@@ -130,6 +130,12 @@ void* wfr_create(int64_t n) {
   d->eff_strain_rate = alloc<double>(n); d->int_energy = alloc<double>(n);
   d->T = alloc<double>(n);
   d->IsFree = alloc<bool>(n); d->NoSlip = alloc<bool>(n); d->ID = alloc<int>(n);
+  /* contact arrays (WeldFormGPU.cu:503-511, Domain_d.cu:160-170) */
+  d->not_write_surf_ID = alloc<bool>(n);
+  d->contneib_count = alloc<int>(n); d->contneib_part = alloc<int>(20 * n + 20);
+  d->mesh_id = alloc<int>(n);
+  d->contact_surf_id = alloc<int>(8); d->first_fem_particle_idx = alloc<int>(8);
+  d->trimesh = alloc<TriMesh_d*>(8);
   d->mat = alloc<Material_*>(n);
   for (int64_t i = 0; i < n; i++) { d->IsFree[i] = true; d->FPMassC[i] = 1.0; }
   d->Alpha = 1.0;    /* SetDimension, Domain_d.cu:191-192 */
@@ -155,8 +161,17 @@ void wfr_destroy(void* h) {
                   d->h, d->m, d->rho, d->rho_0, d->p, d->PresEq, d->Cs, d->P0, d->FPMassC,
                   d->G, d->drho, d->sigma, d->strrate, d->rotrate, d->shearstress, d->strain,
                   d->sigma_eq, d->pl_strain, d->sigma_y, d->eff_strain_rate, d->int_energy, d->T,
-                  d->IsFree, d->NoSlip, d->ID, d->mat, r->x_h};
+                  d->IsFree, d->NoSlip, d->ID, d->mat, r->x_h, d->not_write_surf_ID,
+                  d->contneib_count, d->contneib_part, d->mesh_id, d->contact_surf_id,
+                  d->first_fem_particle_idx};
   for (void* p : ptrs) free(p);
+  for (int mi = 0; mi < d->trimesh_count; mi++) {
+    TriMesh_d* t = d->trimesh[mi];
+    void* mp[] = {t->node, t->node_v, t->elnode, t->pplane, t->centroid, t->normal, t->nfar};
+    for (void* p : mp) free(p);
+    delete t;
+  }
+  free(d->trimesh);
   free(d);
   delete r->mat;
   delete r;
@@ -207,6 +222,61 @@ void wfr_add_bc(void* h, int zone, double vx, double vy, double vz) {
 
 void wfr_set_rebuild_every(void* h, int k) { ((RefDom*)h)->rebuild_every = k; }
 
+void wfr_set_not_write(void* h, const uint8_t* f) {
+  RefDom* r = (RefDom*)h;
+  for (int64_t i = 0; i < r->n; i++) r->dom->not_write_surf_ID[i] = f[i] != 0;
+}
+
+void wfr_set_contact(void* h, double mu_s, double mu_d) {
+  Domain_d* d = ((RefDom*)h)->dom;
+  d->friction_sta = mu_s;
+  d->friction_dyn = mu_d;
+}
+
+/* a rigid mesh as main sets it up (WeldFormGPU.cu:545-610): the device mesh
+ * (nodes, connectivity, centroids by CalcCentroids, normals given or by
+ * CalcNormals), AddTrimeshParticles' bookkeeping, mesh_id and the centroid
+ * particles (mass 0, the zone id) of the host domain (Domain.cpp:969-990) */
+void wfr_add_trimesh(void* h, const double* nodes, int nn, const int32_t* tris, int ne,
+                     const double* normals, int zone, int64_t first, const double* vel,
+                     const double* angvel) {
+  RefDom* r = (RefDom*)h;
+  Domain_d* d = r->dom;
+  TriMesh_d* t = new TriMesh_d();
+  t->nodecount = nn;
+  t->elemcount = ne;
+  t->node = alloc<double3>(nn); t->node_v = alloc<double3>(nn);
+  t->elnode = alloc<int>(3 * ne); t->pplane = alloc<double>(ne);
+  t->centroid = alloc<double3>(ne); t->normal = alloc<double3>(ne); t->nfar = alloc<int>(ne);
+  for (int q = 0; q < nn; q++) t->node[q] = make_double3(nodes[3 * q], nodes[3 * q + 1], nodes[3 * q + 2]);
+  for (int k = 0; k < 3 * ne; k++) t->elnode[k] = tris[k];
+  launch_seq(ne, [&] { t->CalcCentroids(); });
+  if (normals) {
+    for (int e = 0; e < ne; e++) t->normal[e] = make_double3(normals[3 * e], normals[3 * e + 1], normals[3 * e + 2]);
+  } else {
+    launch_seq(ne, [&] { t->CalcNormals(); });
+  }
+  t->m_v = make_double3(vel[0], vel[1], vel[2]);
+  t->m_w = make_double3(angvel[0], angvel[1], angvel[2]);
+  t->id = zone;
+  const int m = d->trimesh_count;
+  d->first_fem_particle_idx[m] = (int)first;       /* AddTrimeshParticles, Domain_d.cu:644-655 */
+  d->contact_surf_id[m] = zone;
+  d->trimesh[m] = t;
+  d->trimesh_count++;
+  for (int e = 0; e < ne; e++) {
+    const int64_t p = first + e;
+    d->x[p] = t->centroid[e];
+    d->m[p] = 0.0;
+    d->ID[p] = zone;
+    d->mesh_id[p] = m;
+    d->normal[p] = t->normal[e];
+  }
+  d->contact = true;
+  d->solid_part_count = (int)d->first_fem_particle_idx[0];
+  r->n_solid = d->solid_part_count;
+}
+
 /* MechFraserSolve prologue (SolverFraser.cu:56-123) */
 void wfr_begin(void* h) {
   RefDom* r = (RefDom*)h;
@@ -216,6 +286,18 @@ void wfr_begin(void* h) {
   launch_seq(r->n, [&] { d->SetVel(make_double3(0., 0., 0.)); });
   r->ts_i = 0; r->is_yielding = 0; r->max_pl_strain = 0.0; r->time = 0.0;
   d->isfirst_step = true;
+  d->id_free_surf = 1;                               /* SolverFraser.cu:118 */
+  d->totmass = 0.0;                                  /* WeldFormGPU.cu:808-820 */
+  for (int64_t i = 0; i < r->n; i++) d->totmass += d->m[i];
+  if (d->contact)
+    for (int m = 0; m < d->trimesh_count; m++) {
+      /* CalcSpheresKernel (SolverFraser.cu:129-141): its radius loop reads
+       * node[3e + n], past the node array for most elements, and only leaves
+       * nfar = 2; that value is set here and the plane coefficients computed */
+      TriMesh_d* t = d->trimesh[m];
+      for (int e = 0; e < t->elemcount; e++) t->nfar[e] = 2;
+      launch_seq(t->elemcount, [&] { t->UpdatePlaneCoeff(); });
+    }
 }
 
 /* one iteration of the Fraser loop body (SolverFraser.cu:164-398), no
@@ -234,6 +316,11 @@ void wfr_step(void* h, int64_t nsteps) {
     launch_seq(N, [&] { PressureKernelExt(d->p, d->PresEq, d->Cs, d->P0, d->rho, d->rho_0, d->particle_count); });
     launch_seq(N, [&] { d->StressStrainOne((int)threadIdx.x); });
     launch_seq(N, [&] { d->CalcAccel(c, o, l, 0, 0.0); });
+    if (d->contact) {                                 /* SolverFraser.cu:233-257 */
+      launch_seq(N, [&] { d->CalculateSurface(c, o, l, d->totmass); });
+      if (r->ts_i == 0) launch_seq(N, [&] { d->CalcContactNb(c, o, l); });
+      launch_seq(N, [&] { d->CalcContactForcesWang(c, o, l); });
+    }
     if (!r->is_yielding) {
       for (int64_t i = 0; i < N; i++)
         if (d->pl_strain[i] > r->max_pl_strain) r->max_pl_strain = d->pl_strain[i];
@@ -246,6 +333,19 @@ void wfr_step(void* h, int64_t nsteps) {
     for (size_t b = 0; b < r->bc_zone.size(); b++)
       launch_seq(N, [&] { d->ApplyBCVel(r->bc_zone[b], r->bc_v[b]); });
     launch_seq(N, [&] { d->CalcIntEnergy(); });
+    if (d->contact) {                                 /* SolverFraser.cu:290-316 */
+      /* MeshUpdateKernel's four stages, each over the whole mesh before the
+       * next (the kernel runs them without a grid barrier) */
+      for (int m = 0; m < d->trimesh_count; m++) {
+        TriMesh_d* t = d->trimesh[m];
+        launch_seq(t->nodecount, [&] { t->Move(d->deltat); });
+        launch_seq(t->elemcount, [&] { t->CalcCentroids(); });
+        launch_seq(t->elemcount, [&] { t->CalcNormals(); });
+        launch_seq(t->elemcount, [&] { t->UpdatePlaneCoeff(); });
+      }
+      for (int m = 0; m < d->trimesh_count; m++)
+        launch_seq(d->trimesh[m]->elemcount, [&] { d->UpdateContactParticles(m); });
+    }
     d->isfirst_step = false;
     r->time += d->deltat;
     r->ts_i++;
@@ -279,7 +379,15 @@ int wfr_get(void* h, const char* name, double* out) {
   else if (s == "sigma_y") cp(d->sigma_y, 1);
   else if (s == "eff_strain_rate") cp(d->eff_strain_rate, 1);
   else if (s == "int_energy") cp(d->int_energy, 1);
+  else if (s == "normal") cp3(d->normal);
+  else if (s == "contforce") cp3(d->contforce);
   else return -1;
+  return 0;
+}
+
+int wfr_get_id(void* h, int32_t* out) {
+  RefDom* r = (RefDom*)h;
+  for (int64_t i = 0; i < r->n; i++) out[i] = r->dom->ID[i];
   return 0;
 }
 

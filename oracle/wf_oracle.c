@@ -73,9 +73,19 @@ struct wfo_domain {
   int newton_max_iter, mlp_on, clamp_homologous;
   double chi, newton_rtol, output_interval;
   double mlp[WFO_MLP_NPARAM];
-  /* contact (one mesh id list; the reference allows several) */
-  int contact, trimesh_count;
-  int32_t csid[WFO_MAX_MESH];
+  /* contact with rigid triangle meshes (TriMesh_d, src/cuda/Mesh.cuh:19-54) */
+  int contact, trimesh_count, contact_law;
+  int32_t csid[WFO_MAX_MESH];      /* contact_surf_id: the zone id of each mesh */
+  struct {
+    int32_t nn, ne, first;         /* nodes, elements, first rigid particle */
+    d3 *node, *node_v, *centroid, *normal;
+    int32_t* elnode;
+    double* pplane;
+    d3 m_v, m_w;
+  } mesh[WFO_MAX_MESH];
+  int32_t *cont_cnt, *cont_nb;     /* contneib_count / contneib_part (20 per particle) */
+  double mu_s, mu_d;               /* friction_sta / friction_dyn */
+  int32_t id_free_surf;            /* 1, set by MechFraserSolve (SolverFraser.cu:118) */
   /* solver state */
   int started, ts_i, is_yielding, isfirst_step, nb_built;
   double time, t_out, dt_out, max_pl_strain, int_energy_sum;
@@ -738,6 +748,162 @@ static void stage_energy(wfo_domain* d) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* contact with rigid triangle meshes (src/cuda/Geometry.cu, Contact.cu,    */
+/* Mesh.cu), in SolverFraser.cu:233-257 and :289-316 order                  */
+/* ------------------------------------------------------------------------ */
+/* mesh_id[j]: the mesh whose element centroids include particle j */
+static inline int mesh_of(const wfo_domain* d, int64_t j) {
+  for (int mi = 0; mi < d->trimesh_count; mi++)
+    if (j >= d->mesh[mi].first && j < (int64_t)d->mesh[mi].first + d->mesh[mi].ne) return mi;
+  return -1;
+}
+
+/* Domain_d::CalculateSurface (Geometry.cu:26-88): normal of every solid
+ * particle from its neighbours that are not rigid particles of the first
+ * mesh (the reference loops mc < 1); |n| >= 0.25 h with at most 46 such
+ * neighbours makes it a free-surface particle unless its zone is protected.
+ * A particle without such neighbours gets 0 * inf = NaN components, as in the
+ * reference, and is never tagged. */
+static void stage_surface(wfo_domain* d) {
+  const double np = (double)d->n;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < d->n_solid; i++) {
+    d3 nrm = v3(0., 0., 0.);
+    int corr = 0;
+    const int32_t* L = d->nb + (size_t)i * NBMAX;
+    for (int k = 0; k < d->nb_count[i]; k++) {
+      const int64_t j = L[k];
+      const d3 xij = d3_sub(d->x[i], d->x[j]);
+      if (d->ID[j] != d->csid[0]) {
+        nrm = d3_add(nrm, d3_scale(xij, d->m[j]));
+        corr++;
+      }
+    }
+    nrm = d3_scale(nrm, np / (d->totmass * (double)corr));
+    d->normal[i] = nrm;
+    if (d3_len(nrm) >= 0.25 * d->h[i] && corr <= 46 && !d->not_write[i])
+      d->ID[i] = d->id_free_surf;
+  }
+}
+
+/* Domain_d::CalcContactNb (Contact.cu:29-62), every rebuild_every steps: the
+ * rigid neighbours within 2h of each free-surface particle, in neighbour
+ * order, once per mesh whose zone id matches.  The reference has no bound
+ * on the 20 slots; here a full list stops growing. */
+static void stage_contact_nb(wfo_domain* d) {
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < d->n_solid; i++) {
+    int cnt = 0;
+    const int32_t* L = d->nb + (size_t)i * NBMAX;
+    for (int k = 0; k < d->nb_count[i]; k++) {
+      const int64_t j = L[k];
+      const d3 xij = d3_sub(d->x[i], d->x[j]);
+      for (int mc = 0; mc < d->trimesh_count; mc++)
+        if (d->ID[i] == d->id_free_surf && d->ID[j] == d->csid[mc] &&
+            d3_len(xij) < 2. * d->h[i] && cnt < CONT_MAX_NB)
+          d->cont_nb[i * CONT_MAX_NB + cnt++] = (int32_t)j;
+    }
+    d->cont_cnt[i] = cnt;
+  }
+}
+
+/* Domain_d::CalcContactForcesWang (Contact.cu:134-321): penalty force of the
+ * rigid triangle of each contact neighbour on the predicted position, with
+ * static / dynamic friction.  The force of the last contact is kept in
+ * contforce; the acceleration accumulates every contact, and the predicted
+ * position of a later contact sees the earlier ones. */
+static void stage_contact_forces(wfo_domain* d) {
+  const double dt = d->dt;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < d->n_solid; i++) {
+    d->contforce[i] = v3(0., 0., 0.);
+    for (int k = 0; k < d->cont_cnt[i]; k++) {
+      const int64_t j = d->cont_nb[i * CONT_MAX_NB + k];
+      const int mid = mesh_of(d, j);
+      const int e = (int)(j - d->mesh[mid].first);
+      const d3 x_pred = d3_add(d3_add(d->x[i], d3_scale(d->v[i], dt)),
+                               d3_div(d3_scale(d3_scale(d->a[i], dt), dt), 2.));
+      const d3 n = d->mesh[mid].normal[e];
+      const double dist = d3_dot(n, x_pred) - d->mesh[mid].pplane[e];
+      if (!(dist < d->h[i])) continue;
+      const d3 Qj = d3_sub(d->x[i], d3_scale(n, dist));
+      int inside = 1;
+      const int32_t* en = d->mesh[mid].elnode + 3 * e;
+      const d3* node = d->mesh[mid].node;
+      for (int l = 0; l < 3 && inside; l++) {
+        const int nx = l + 1 > 2 ? 0 : l + 1;
+        const double crit = d3_dot(d3_cross(d3_sub(node[en[nx]], node[en[l]]),
+                                            d3_sub(Qj, node[en[l]])), n);
+        if (crit < 0.0) inside = 0;
+      }
+      if (!inside) continue;
+      const double delta = d->h[i] - dist;
+      const double kij = 2.0 * d->m[i] / (dt * dt);
+      d->contforce[i] = d3_scale(n, 0.4 * kij * delta);
+      d->a[i] = d3_add(d->a[i], d3_div(d->contforce[i], d->m[i]));
+      if (d->mu_s > 0.) {
+        const d3 du = d3_sub(d3_sub(x_pred, d->x[i]), d3_scale(d->v[j], dt));
+        const d3 dtg = d3_sub(du, d3_scale(n, d3_dot(du, n)));
+        const d3 ft = d3_scale(dtg, kij);
+        if (d3_len(ft) < d->mu_s * d3_len(d->contforce[i])) {
+          d->a[i] = d3_sub(d->a[i], d3_div(ft, d->m[i]));
+        } else {
+          const d3 fd = d3_div(d3_scale(ft, d->mu_d * d3_len(d->contforce[i])), d3_len(ft));
+          d->contforce[i] = d3_sub(d->contforce[i], fd);
+          d->a[i] = d3_sub(d->a[i], d3_div(fd, d->m[i]));
+        }
+      }
+    }
+  }
+}
+
+/* MeshUpdateKernel (Mesh.cu:24-29): TriMesh_d::Move, CalcCentroids,
+ * CalcNormals, UpdatePlaneCoeff.  The reference runs the four in one kernel
+ * without a grid-wide barrier, so an element may read nodes before or after
+ * they move; here each runs over the whole mesh before the next (the
+ * sequential meaning).  UpdatePlaneCoeff reads node[elnode[3e] + nfar] with
+ * nfar = 2, the last index CalcSpheres assigns (Mesh.cu:205-231). */
+static void mesh_plane_coeff(wfo_domain* d, int mi) {
+  for (int e = 0; e < d->mesh[mi].ne; e++)
+    d->mesh[mi].pplane[e] = d3_dot(d->mesh[mi].node[d->mesh[mi].elnode[3 * e] + 2],
+                                   d->mesh[mi].normal[e]);
+}
+static void mesh_update(wfo_domain* d, int mi, double dt) {
+  d3* node = d->mesh[mi].node;
+  for (int q = 0; q < d->mesh[mi].nn; q++) {
+    const d3 vr = d3_cross(d->mesh[mi].m_w, node[q]);
+    d->mesh[mi].node_v[q] = d3_add(d->mesh[mi].m_v, vr);
+    node[q] = d3_add(node[q], d3_scale(d->mesh[mi].node_v[q], dt));
+  }
+  for (int e = 0; e < d->mesh[mi].ne; e++) {
+    const int32_t* en = d->mesh[mi].elnode + 3 * e;
+    d->mesh[mi].centroid[e] = d3_div(d3_add(d3_add(node[en[0]], node[en[1]]), node[en[2]]), 3.);
+  }
+  for (int e = 0; e < d->mesh[mi].ne; e++) {
+    const int32_t* en = d->mesh[mi].elnode + 3 * e;
+    const d3 u = d3_sub(node[en[1]], node[en[0]]);
+    const d3 v = d3_sub(node[en[2]], node[en[0]]);
+    const d3 w = d3_cross(u, v);
+    d->mesh[mi].normal[e] = d3_div(w, d3_len(w));
+  }
+  mesh_plane_coeff(d, mi);
+}
+
+/* Domain_d::UpdateContactParticles (Contact.cu:85-112): each element's rigid
+ * particle takes the mean node velocity, zero acceleration and the normal. */
+static void contact_particles_update(wfo_domain* d, int mi) {
+  for (int e = 0; e < d->mesh[mi].ne; e++) {
+    const int32_t* en = d->mesh[mi].elnode + 3 * e;
+    d3 vv = v3(0., 0., 0.);
+    for (int q = 0; q < 3; q++) vv = d3_add(vv, d->mesh[mi].node_v[en[q]]);
+    const int64_t p = d->mesh[mi].first + e;
+    d->v[p] = d3_div(vv, 3.);
+    d->a[p] = v3(0., 0., 0.);
+    d->normal[p] = d->mesh[mi].normal[e];
+  }
+}
+
+/* ------------------------------------------------------------------------ */
 /* solve loop (SolverFraser.cu:30-409)                                       */
 /* ------------------------------------------------------------------------ */
 static int check_ready(wfo_domain* d) {
@@ -759,6 +925,8 @@ static int solve_begin(wfo_domain* d, double dt_out) {
   rc = nb_search_from(d, d->x_h);                      /* :109 */
   if (rc) return rc;
   for (int64_t i = 0; i < d->n_solid; i++) d->v[i] = v3(0., 0., 0.);   /* SetVelKernel :123 */
+  if (d->contact)                                      /* CalcSpheresKernel :129-141 */
+    for (int mi = 0; mi < d->trimesh_count; mi++) mesh_plane_coeff(d, mi);
   d->ts_i = 0;
   d->is_yielding = 0;
   d->max_pl_strain = 0.0;
@@ -777,6 +945,11 @@ static int solve_step(wfo_domain* d) {
   stage_pressure(d);        /* :213 */
   stage_stress(d);          /* :217 */
   stage_accel(d);           /* :221 */
+  if (d->contact) {         /* :233-257 */
+    stage_surface(d);
+    if (d->ts_i == 0) stage_contact_nb(d);
+    stage_contact_forces(d);
+  }
   if (!d->is_yielding) {    /* :260-271 */
     for (int64_t i = 0; i < d->n; i++)
       if (d->pl_strain[i] > d->max_pl_strain) d->max_pl_strain = d->pl_strain[i];
@@ -791,6 +964,10 @@ static int solve_step(wfo_domain* d) {
     thermal_leapfrog(d);
   }
   stage_energy(d);          /* :287 */
+  if (d->contact) {         /* :290-316 */
+    for (int mi = 0; mi < d->trimesh_count; mi++) mesh_update(d, mi, d->dt);
+    for (int mi = 0; mi < d->trimesh_count; mi++) contact_particles_update(d, mi);
+  }
   d->isfirst_step = 0;      /* :320 */
   d->time += d->dt;
   if (d->time >= d->t_out) {                           /* :323-368 */
@@ -895,7 +1072,9 @@ int wfo_create(wfo_domain** out, int64_t n) {
   A(dep, n); A(ID, n); A(is_free, n); A(not_write, n);
   A(T, n); A(Ta, n); A(Tb, n); A(dTdt, n); A(k_T, n); A(cp_T, n); A(BC_T, n);
   A(nb_count, n); A(nb, (size_t)n * NBMAX);
+  A(cont_cnt, n); A(cont_nb, (size_t)n * CONT_MAX_NB);
 #undef A
+  d->id_free_surf = 1;
   for (int64_t i = 0; i < n; i++) d->is_free[i] = 1;
   /* SetDimension resets Alpha = 1, Beta = 0 (Domain_d.cu:191-192) */
   d->alpha = 1.0;
@@ -922,8 +1101,13 @@ int wfo_destroy(wfo_domain* d) {
                   d->rho0, d->p, d->drho, d->Cs, d->G, d->sigma, d->strrate, d->rotrate,
                   d->shearstress, d->strain, d->sigma_eq, d->pl_strain, d->sigma_y,
                   d->eff_strain_rate, d->int_energy, d->dep, d->ID, d->is_free, d->not_write,
-                  d->T, d->Ta, d->Tb, d->dTdt, d->k_T, d->cp_T, d->BC_T, d->nb_count, d->nb};
+                  d->T, d->Ta, d->Tb, d->dTdt, d->k_T, d->cp_T, d->BC_T, d->nb_count, d->nb,
+                  d->cont_cnt, d->cont_nb};
   for (size_t k = 0; k < sizeof ptrs / sizeof ptrs[0]; k++) free(ptrs[k]);
+  for (int mi = 0; mi < d->trimesh_count; mi++) {
+    free(d->mesh[mi].node); free(d->mesh[mi].node_v); free(d->mesh[mi].centroid);
+    free(d->mesh[mi].normal); free(d->mesh[mi].elnode); free(d->mesh[mi].pplane);
+  }
   free(d);
   return WF_OK;
 }
@@ -1037,10 +1221,116 @@ int wfo_set_option(wfo_domain* d, const char* key, double v) {
   else if (!strcmp(key, "output_interval")) d->output_interval = v;
   else if (!strcmp(key, "clamp_homologous")) d->clamp_homologous = v != 0.0;
   else if (!strcmp(key, "mlp")) d->mlp_on = v != 0.0;
-  else if (!strcmp(key, "precision") || !strcmp(key, "profile_kernel") || !strcmp(key, "graph")) {
+  else if (!strcmp(key, "precision") || !strcmp(key, "profile_kernel") || !strcmp(key, "graph") ||
+           !strcmp(key, "fuse_heat")) {
     /* GPU-only switches: accepted and ignored by the FP64 oracle */
   } else return fail(d, WF_ERR_ARG, "unknown option");
   return WF_OK;
+}
+
+/* friction_sta / friction_dyn (WeldFormGPU.cu:640-641) and the contact law
+ * (0: the reference's penalty law, CalcContactForcesWang) */
+int wfo_set_contact(wfo_domain* d, double mu_static, double mu_dynamic, int law) {
+  if (!d || law != 0 || !(mu_static >= 0.0) || !(mu_dynamic >= 0.0)) return WF_ERR_ARG;
+  d->mu_s = mu_static;
+  d->mu_d = mu_dynamic;
+  d->contact_law = law;
+  return WF_OK;
+}
+
+/* A rigid triangle mesh and its centroid particles (AddTrimeshParticles,
+ * WeldFormGPU.cu:545-610, Domain.cpp:969-990): particles first .. first+ne-1
+ * become the element centroids, with mass 0 and the mesh's zone id; the mesh
+ * moves with velocity v and angular velocity w (m_v, m_w).  normals == NULL:
+ * computed as in TriMesh_d::CalcNormals.  Turns contact on. */
+int wfo_add_trimesh(wfo_domain* d, const double* nodes, int32_t nn, const int32_t* tris,
+                    int32_t ne, const double* normals, int32_t zone_id, int64_t first,
+                    const double* vel, const double* angvel) {
+  if (!d || !nodes || !tris || nn <= 0 || ne <= 0 || !vel || !angvel) return WF_ERR_ARG;
+  if (d->trimesh_count >= WFO_MAX_MESH) return fail(d, WF_ERR_ARG, "too many meshes");
+  if (first < d->n_solid || first + ne > d->n) return fail(d, WF_ERR_ARG, "rigid particle range");
+  if (zone_id == d->id_free_surf) return fail(d, WF_ERR_ARG, "zone id 1 is the free-surface id");
+  for (int64_t k = 0; k < 3 * (int64_t)ne; k++)
+    if (tris[k] < 0 || tris[k] >= nn) return fail(d, WF_ERR_ARG, "triangle node out of range");
+  const int mi = d->trimesh_count;
+  d->mesh[mi].nn = nn;
+  d->mesh[mi].ne = ne;
+  d->mesh[mi].first = (int32_t)first;
+  d->mesh[mi].node = xcalloc(nn, sizeof(d3));
+  d->mesh[mi].node_v = xcalloc(nn, sizeof(d3));
+  d->mesh[mi].centroid = xcalloc(ne, sizeof(d3));
+  d->mesh[mi].normal = xcalloc(ne, sizeof(d3));
+  d->mesh[mi].elnode = xcalloc(3 * (size_t)ne, sizeof(int32_t));
+  d->mesh[mi].pplane = xcalloc(ne, sizeof(double));
+  for (int q = 0; q < nn; q++) d->mesh[mi].node[q] = v3(nodes[3 * q], nodes[3 * q + 1], nodes[3 * q + 2]);
+  memcpy(d->mesh[mi].elnode, tris, sizeof(int32_t) * 3 * (size_t)ne);
+  const d3* node = d->mesh[mi].node;
+  for (int e = 0; e < ne; e++) {
+    const int32_t* en = tris + 3 * e;
+    d->mesh[mi].centroid[e] = d3_div(d3_add(d3_add(node[en[0]], node[en[1]]), node[en[2]]), 3.);
+    if (normals) {
+      d->mesh[mi].normal[e] = v3(normals[3 * e], normals[3 * e + 1], normals[3 * e + 2]);
+    } else {
+      const d3 w = d3_cross(d3_sub(node[en[1]], node[en[0]]), d3_sub(node[en[2]], node[en[0]]));
+      d->mesh[mi].normal[e] = d3_div(w, d3_len(w));
+    }
+    const int64_t p = first + e;
+    d->x[p] = d->mesh[mi].centroid[e];
+    d->m[p] = 0.0;
+    d->ID[p] = zone_id;
+    d->normal[p] = d->mesh[mi].normal[e];
+  }
+  d->mesh[mi].m_v = v3(vel[0], vel[1], vel[2]);
+  d->mesh[mi].m_w = v3(angvel[0], angvel[1], angvel[2]);
+  d->csid[mi] = zone_id;
+  d->trimesh_count++;
+  d->contact = 1;
+  d->totmass = 0.0;                                   /* WeldFormGPU.cu:808-820 */
+  for (int64_t i = 0; i < d->n; i++) d->totmass += d->m[i];
+  return WF_OK;
+}
+
+/* TriMesh_d::AxisPlaneMesh (src/cuda/Mesh.cu:48-194) as main builds a
+ * "Plane" rigid body: (dens+1)^2 nodes stepped by dl = (p2.x - p1.x)/dens in
+ * x (inner) and y (outer) from p1, at z = p1.z whatever the axis; two
+ * triangles per cell, ordered for an outward normal +axis when positive;
+ * normals are set on the axis.  Returns the element count 2 dens^2; nodes
+ * (3 (dens+1)^2), tris (3 per element) and normals (3 per element) are
+ * written when not NULL. */
+int64_t wfo_gen_plane_mesh(int axis, int positive, const double* p1, const double* p2, int dens,
+                           double* nodes, int32_t* tris, double* normals) {
+  if (dens < 1 || axis < 0 || axis > 2 || !p1 || !p2) return -1;
+  const int64_t ne = 2 * (int64_t)dens * dens;
+  if (!nodes && !tris && !normals) return ne;
+  const double dl = (p2[0] - p1[0]) / dens;
+  const double x3 = p1[2];
+  double x2 = p1[1];
+  int64_t vi = 0;
+  for (int j = 0; j <= dens; j++) {
+    double x1 = p1[0];
+    for (int i = 0; i <= dens; i++) {
+      if (nodes) { nodes[3 * vi] = x1; nodes[3 * vi + 1] = x2; nodes[3 * vi + 2] = x3; }
+      vi++;
+      x1 += dl;
+    }
+    x2 += dl;
+  }
+  int64_t el = 0;
+  for (int j = 0; j < dens; j++)
+    for (int i = 0; i < dens; i++) {
+      const int32_t n0 = (dens + 1) * j + i, n1 = n0 + 1;
+      const int32_t n2 = (dens + 1) * (j + 1) + i, n3 = n2 + 1;
+      const int32_t c[2][3] = {{n0, positive ? n1 : n2, positive ? n2 : n1},
+                               {n1, positive ? n3 : n2, positive ? n2 : n3}};
+      for (int e = 0; e < 2; e++, el++)
+        if (tris) for (int q = 0; q < 3; q++) tris[3 * el + q] = c[e][q];
+    }
+  if (normals)
+    for (int64_t e = 0; e < ne; e++) {
+      normals[3 * e] = normals[3 * e + 1] = normals[3 * e + 2] = 0.0;
+      normals[3 * e + axis] = positive ? 1.0 : -1.0;
+    }
+  return ne;
 }
 
 int wfo_set_mlp_params(wfo_domain* d, const double* params) {
@@ -1109,6 +1399,7 @@ int wfo_get_field_i32(wfo_domain* d, const char* name, int32_t* out) {
   if (!strcmp(name, "ID")) memcpy(out, d->ID, sizeof(int32_t) * d->n);
   else if (!strcmp(name, "nb_count")) memcpy(out, d->nb_count, sizeof(int32_t) * d->n);
   else if (!strcmp(name, "BC_T")) memcpy(out, d->BC_T, sizeof(int32_t) * d->n);
+  else if (!strcmp(name, "cont_count")) memcpy(out, d->cont_cnt, sizeof(int32_t) * d->n);
   else return fail(d, WF_ERR_ARG, "unknown field");
   return WF_OK;
 }

@@ -54,6 +54,13 @@ int wfo_set_temperature(wfo_domain* d, const double* T);
 int wfo_set_thermal_bc(wfo_domain* d, const int32_t* bc_t);
 int wfo_set_convection(wfo_domain* d, double h_conv, double T_inf);
 int wfo_set_option(wfo_domain* d, const char* key, double value);
+/* contact with rigid triangle meshes (src/cuda/Contact.cu, Geometry.cu, Mesh.cu) */
+int wfo_set_contact(wfo_domain* d, double mu_static, double mu_dynamic, int law);
+int wfo_add_trimesh(wfo_domain* d, const double* nodes, int32_t nn, const int32_t* tris,
+                    int32_t ne, const double* normals, int32_t zone_id, int64_t first,
+                    const double* vel, const double* angvel);
+int64_t wfo_gen_plane_mesh(int axis, int positive, const double* p1, const double* p2, int dens,
+                           double* nodes, int32_t* tris, double* normals);
 int wfo_set_threads(int nthreads);
 
 int wfo_mech_fraser_solve(wfo_domain* d, double tf, double dt_out);

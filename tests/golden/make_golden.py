@@ -49,9 +49,14 @@ def run_fraser(sc, checkpoints):
     for k in checkpoints:
         R.step(k - done)
         done = k
-        for f in FIELDS:
+        for f in FIELDS + (CONTACT_FIELDS if "mesh" in sc else []):
             out["s%d_%s" % (k, f)] = R.get(f)
+        if "mesh" in sc:
+            out["s%d_ID" % k] = R.get_id()
     return out
+
+
+CONTACT_FIELDS = ["u", "normal", "contforce"]
 
 
 def main():
@@ -77,6 +82,11 @@ def main():
     # 4. Fraser loop, Johnson-Cook material (reference radial return), v_top = -10 m/s
     jc = S.compression_cylinder(material="jc", vz_top=-10.0)
     np.savez_compressed(os.path.join(HERE, "fraser_jc.npz"), **run_fraser(jc, [300]))
+    # 5. contact: the small cylinder compressed by a rigid plane at -10 m/s
+    #    (surface tagging, contact lists, penalty law with friction, mesh motion)
+    ct = S.contact_cylinder(R=0.0025, H=0.005, dens=6, mu=(0.3, 0.2))
+    np.savez_compressed(os.path.join(HERE, "fraser_contact.npz"),
+                        **run_fraser(ct, [1, 200, 600]))
     print("golden vectors written to", HERE)
     return 0
 

@@ -10,4 +10,10 @@ def load_ref(R, sc):
             sc["dt"], sc["alpha"], sc["beta"], sc["mat"], T=sc["T"])
     for zone, v in sc["bcs"]:
         R.add_bc(zone, v)
+    if "mesh" in sc:
+        ms = sc["mesh"]
+        R.set_not_write(sc["not_write"])
+        R.add_trimesh(ms["nodes"], ms["tris"], ms["zone"], ms["first"], ms["vel"], ms["angvel"],
+                      normals=ms["normals"])
+        R.set_contact(sc["mu"][0], sc["mu"][1])
     return R

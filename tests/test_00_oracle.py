@@ -93,6 +93,31 @@ def test_generators_match_between_oracle_and_library():
     c1 = P.assign_zone(l1, (-1, -1, -1), (1, 1, 0.001), 2, ids1, nw1)
     c2 = O.assign_zone(l2, (-1, -1, -1), (1, 1, 0.001), 2, ids2, nw2)
     assert c1 == c2 > 0 and np.array_equal(ids1, ids2) and np.array_equal(nw1, nw2)
+    for positive in (0, 1):
+        m1 = P.gen_plane_mesh(2, positive, (-0.003, -0.003, 0.006), (0.003, 0.003, 0.006), 7)
+        m2 = O.gen_plane_mesh(2, positive, (-0.003, -0.003, 0.006), (0.003, 0.003, 0.006), 7)
+        assert all(np.array_equal(a, b) for a, b in zip(m1, m2))
+        assert m1[0].shape == (64, 3) and m1[1].shape == (98, 3)
+
+
+def test_contact_matches_reference_bitwise():
+    """A rigid plane pressing the small cylinder (surface tagging, contact
+    lists, the penalty law with friction, mesh motion, rigid particles), against
+    the reference's own contact kernels: every field and the ids bit for bit."""
+    g = np.load(os.path.join(GOLDEN, "fraser_contact.npz"))
+    sc = S.contact_cylinder(R=0.0025, H=0.005, dens=6, mu=(0.3, 0.2))
+    d = _oracle(sc)
+    done = 0
+    for k in (1, 200, 600):
+        d.step(k - done)
+        done = k
+        for f in STATE_FIELDS + ["u", "normal", "contforce"]:
+            ref = g["s%d_%s" % (k, f)]
+            got = d.get_field(f)
+            assert np.array_equal(got, ref, equal_nan=True), "step %d field %s differs" % (k, f)
+        assert np.array_equal(d.get_field_i32("ID"), g["s%d_ID" % k])
+    assert (np.abs(d.get_field("contforce")).sum(axis=1) > 0).sum() > 20     # in contact
+    assert d.get_field("pl_strain").max() > 0.1
 
 
 def test_jc_yield_table_and_newton_residual():

@@ -173,6 +173,73 @@ def test_coupled_thermomechanical_jc_vs_oracle():
                                atol=1e-12)
 
 
+def test_contact_fp64_bit_exact_vs_reference_golden():
+    """Rigid plane pressing the small cylinder: surface tagging, contact lists,
+    penalty law with friction, mesh motion and rigid particles on the GPU,
+    against the reference's own contact kernels, bit for bit."""
+    g = np.load(os.path.join(GOLDEN, "fraser_contact.npz"))
+    sc = S.contact_cylinder(R=0.0025, H=0.005, dens=6, mu=(0.3, 0.2))
+    d = gpu(sc)
+    done = 0
+    for k in (1, 200, 600):
+        d.step(k - done)
+        done = k
+        for f in STATE_FIELDS + ["u", "normal", "contforce"]:
+            got, ref = d.get_field(f), g["s%d_%s" % (k, f)]
+            assert np.array_equal(got, ref, equal_nan=True), "step %d %s: max |d| %.3e" % (
+                k, f, np.nanmax(np.abs(got - ref)))
+        assert np.array_equal(d.get_field_i32("ID"), g["s%d_ID" % k])
+    assert (np.abs(d.get_field("contforce")).sum(axis=1) > 0).sum() > 20
+
+
+def test_contact_config1_fp64_bit_exact_vs_oracle():
+    """Config-1 cylinder (5,244 particles) under a 200-triangle plane at
+    -10 m/s with friction: plain FP64 bit for bit against the oracle."""
+    sc = S.contact_cylinder(mu=(0.3, 0.2))
+    o, g64 = ora(sc), gpu(sc)
+    for d in (o, g64):
+        d.step(300)
+    for f in ("x", "u", "v", "pl_strain", "sigma_eq", "normal", "contforce"):
+        assert np.array_equal(g64.get_field(f), o.get_field(f), equal_nan=True), f
+    for f in ("ID", "cont_count"):
+        assert np.array_equal(g64.get_field_i32(f), o.get_field_i32(f)), f
+    assert (g64.get_field_i32("cont_count") > 0).sum() > 100
+
+
+CONTACT_FIELDS = ("u", "pl_strain", "sigma_eq", "contforce")
+
+
+def test_contact_mixed_within_1e3_frictionless():
+    """Mixed form against plain FP64 under the frictionless plane: 1e-3."""
+    sc = S.contact_cylinder(mu=(0.0, 0.0))
+    g64, gm = gpu(sc), gpu(sc, {"precision": 1})
+    for d in (g64, gm):
+        d.step(300)
+    for f in CONTACT_FIELDS:
+        err = rel_l2(gm.get_field(f), g64.get_field(f))
+        assert err < 1e-3, (f, err)
+    Fz64, Fzm = g64.get_field("contforce")[:, 2].sum(), gm.get_field("contforce")[:, 2].sum()
+    assert abs(Fzm - Fz64) <= 1e-3 * abs(Fz64)
+
+
+def test_contact_mixed_with_friction_within_fp64_sensitivity():
+    """With friction the stick/slip switch makes the problem ill-conditioned:
+    two plain FP64 runs whose positions differ by 1e-12 (relative) already
+    differ by ~5e-4 in u and ~5e-2 in the contact forces after 300 steps.  The
+    mixed form must stay within three times that spread (and 1e-3)."""
+    sc = S.contact_cylinder(mu=(0.3, 0.2))
+    sp = dict(sc)
+    sp["x"] = sc["x"] * (1.0 + 1e-12 * np.random.default_rng(3).standard_normal(sc["x"].shape))
+    g64, gp, gm = gpu(sc), gpu(sp), gpu(sc, {"precision": 1})
+    for d in (g64, gp, gm):
+        d.step(300)
+    for f in CONTACT_FIELDS:
+        ref = g64.get_field(f)
+        spread = rel_l2(gp.get_field(f), ref)
+        err = rel_l2(gm.get_field(f), ref)
+        assert err < max(1e-3, 3.0 * spread), (f, err, spread)
+
+
 def test_mixed_fused_heat_matches_separate_heat_pass():
     """Mixed form: the heat pass fused into the next step's density pass gives
     the temperatures of the separate heat pass (to FP32 rounding), including

@@ -96,7 +96,14 @@ SIGNATURES = {
     "get_neighbors": (C.c_int, [_vp, _pi32, _pi32]),
     "get_scalar": (C.c_int, [_vp, _cs, _pd]),
     "set_field": (C.c_int, [_vp, _cs, _pd]),
+    # contact with rigid triangle meshes
+    "set_contact": (C.c_int, [_vp, _d, _d, C.c_int]),
+    "add_trimesh": (C.c_int, [_vp, _pd, _i32, _pi32, _i32, _pd, _i32, _i64, _pd, _pd]),
+    "gen_plane_mesh": (_i64, [C.c_int, C.c_int, _pd, _pd, C.c_int, _pd, _pi32, _pd]),
 }
+
+# entry points without a domain handle
+NO_HANDLE = {"gen_plane_mesh"}
 
 # entry points only the product exports
 PRODUCT_ONLY = {

@@ -28,7 +28,7 @@ size_t wf_mlp_packed_bytes();
 
 // kernel ids for wf_set_option("profile_kernel", id)
 enum { KID_NONE = 0, KID_DENSITY = 1, KID_STRESS = 2, KID_ACCEL = 3, KID_INTEGRATE = 4,
-       KID_THERMAL = 5, KID_REBUILD = 6 };
+       KID_THERMAL = 5, KID_REBUILD = 6, KID_CONTACT = 7 };
 
 struct wf_domain {
   int64_t n = 0, n_solid = 0, npad = 0;
@@ -75,6 +75,12 @@ struct wf_domain {
   // mixed form: the heat pass of the last step runs inside the next step's
   // density pass, or in finish() when the call ends first
   bool fuse_heat = true, heat_pending = false, heat_pending_first = false;
+  // contact with rigid triangle meshes
+  std::vector<MeshDev> meshes;
+  double mu_s = 0.0, mu_d = 0.0, totmass = 0.0;
+  int contact_law = 0;
+  std::vector<double> h_mass;      // masses in caller order (totmass, rigid particles)
+  int32_t *cnb = nullptr, *ccnt = nullptr;
   double time = 0, t_out = 0, dt_out = 0;
   int64_t step = 0;
   int ts_i = 0;
@@ -186,6 +192,19 @@ __global__ void k_mixed_to_fp64(int64_t n, Fields F) {
   if (s >= n) return;
   for (int c = 0; c < 6; c++) F.ss6[s * 6 + c] = (double)F.ss32[s * 6 + c];
 }
+// the rigid particles of a mesh (AddTrimeshParticles, Domain.cpp:969-990):
+// at the element centroids, mass 0, the mesh's zone id, the element normal
+__global__ void k_place_rigid(int32_t ne, int32_t first, const int32_t* inv,
+                              const double4* centroid, const double4* normal, int32_t zone,
+                              Fields F) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const int32_t s = inv[first + e];
+  const double4 c = centroid[e];
+  F.xm[s] = make_double4(c.x, c.y, c.z, 0.0);
+  F.id[s] = zone;
+  F.nrm[s] = normal[e];
+}
 inline int nblk(int64_t n, int t = 256) { return (int)((n + t - 1) / t); }
 }  // namespace
 
@@ -224,7 +243,8 @@ static int alloc_fields(wf_domain* d, Fields& F) {
 static void free_fields(Fields& F) {
   void* ptrs[] = {F.xm, F.vd, F.u, F.a, F.sig6, F.ss6, F.eps6, F.sr6, F.rr6, F.p, F.seq, F.eps_p,
                   F.sy, F.eff, F.dep, F.drho, F.eint, F.T, F.Ta, F.Tb, F.dTdt, F.kT, F.cpT,
-                  F.id, F.bct, F.perm, F.nw, F.xh, F.p32, F.v32, F.ss32, F.th32, F.pwn};
+                  F.id, F.bct, F.perm, F.nw, F.xh, F.p32, F.v32, F.ss32, F.th32, F.pwn,
+                  F.nrm, F.cf};
   for (void* p : ptrs) if (p) cudaFree(p);
   F = Fields{};
 }
@@ -255,8 +275,18 @@ static StepParams make_params(const wf_domain* d) {
   P.clamp_homologous = d->clamp_homologous;
   P.energy_mode = d->energy_mode;
   P.inv = d->inv;
-  P.contact = 0;
-  P.ncsid = 0;
+  P.contact = d->meshes.empty() ? 0 : 1;
+  P.ncsid = (int)d->meshes.size();
+  for (int m = 0; m < P.ncsid; m++) {
+    P.mesh[m] = d->meshes[m];
+    P.csid[m] = d->meshes[m].zone;
+  }
+  P.mu_s = d->mu_s;
+  P.mu_d = d->mu_d;
+  P.totmass = d->totmass;
+  P.id_free_surf = 1;              // MechFraserSolve, SolverFraser.cu:118
+  P.cnb = d->cnb;
+  P.ccnt = d->ccnt;
   P.nbc = (int)d->bc_zone.size();
   for (int b = 0; b < P.nbc; b++) {
     P.bc_zone[b] = d->bc_zone[b];
@@ -432,6 +462,11 @@ static int solve_begin(wf_domain* d, double dt_out) {
   rc = rebuild(d, false);                                       // :109
   if (rc) return rc;
   if (!resume) k_setvel0<<<nblk(d->n), 256, 0, d->stream>>>(d->n, d->n_solid, d->F[d->cur]);   // :123
+  if (!d->meshes.empty()) {
+    d->totmass = 0.0;                              // WeldFormGPU.cu:808-820, in index order
+    for (double mm : d->h_mass) d->totmass += mm;
+    launch_mesh_plane(make_params(d), d->stream);  // CalcSpheresKernel, :129-141
+  }
   if (d->precision == 1) k_mixed_init<<<nblk(d->n), 256, 0, d->stream>>>(d->n, d->F[d->cur]);
   WF_CUDA_OK(cudaGetLastError());
   d->started = true;
@@ -467,6 +502,11 @@ static int solve_step(wf_domain* d) {
                          (d->mlp_on && d->mlp_loaded) ? d->mlp_packed : nullptr, s); }
     { KTimer t(d, KID_ACCEL); launch_fp32_accel(P, F, d->v32b, d->sigr32, d->a32, N, s); }
   }
+  if (P.contact) {                                                                    // :233-257
+    KTimer t(d, KID_CONTACT);
+    launch_contact_stage(P, F, N, d->ts_i == 0, mixed ? d->a32 : nullptr, s);
+    d->launches += d->ts_i == 0 ? 3 : 2;
+  }
   { KTimer t(d, KID_INTEGRATE); launch_integrate(P, F, d->vd2, mixed ? d->a32 : nullptr, s); }   // :273-287
   d->launches += 4;
   if (d->thermal) {                                                                   // :285
@@ -478,6 +518,11 @@ static int solve_step(wf_domain* d) {
       launch_thermal(P, F, N, d->isfirst ? 1 : 0, d->chi > 0.0 ? 1 : 0, mixed ? 1 : 0, s);
       d->launches += 2;
     }
+  }
+  if (P.contact) {                                                                    // :289-316
+    KTimer t(d, KID_CONTACT);
+    launch_mesh_update(P, F, mixed ? 1 : 0, s);
+    d->launches += 3 * P.ncsid;
   }
   d->isfirst = false;
   d->time += d->dt;
@@ -563,6 +608,12 @@ int wf_destroy(wf_domain* d) {
   if (!d) return WF_OK;
   if (d->stream) cudaStreamSynchronize(d->stream);
   for (int k = 0; k < 2; k++) free_fields(d->F[k]);
+  for (MeshDev& M : d->meshes) {
+    void* mp[] = {M.node, M.node_v, M.centroid, M.normal, M.elnode, M.pplane};
+    for (void* p : mp) if (p) cudaFree(p);
+  }
+  if (d->cnb) cudaFree(d->cnb);
+  if (d->ccnt) cudaFree(d->ccnt);
   void* ptrs[] = {d->vd2, d->v32b, d->a32, d->sigr32, d->mlp_w, d->mlp_packed, d->log_x,
                   d->log_y, d->log_count, d->nb, d->nbc, d->inv, d->pf, d->pf2,
                   d->cellid, d->cell_count, d->cell_cursor, d->scan_tmp, d->s_src, d->s_orig,
@@ -663,6 +714,7 @@ int wf_set_velocities(wf_domain* d, const double* v) {
 int wf_set_mass(wf_domain* d, const double* m) {
   if (!d || !m) return WF_ERR_ARG;
   d->m_set = true;
+  d->h_mass.assign(m, m + d->n);
   return upload_d(d, m, 1, (double*)CF(d).xm, 4, 3);
 }
 int wf_set_not_write_surf_id(wf_domain* d, const uint8_t* f) {
@@ -700,6 +752,87 @@ int wf_add_velocity_bc(wf_domain* d, int32_t zone, double vx, double vy, double 
   d->bc_v.push_back({vx, vy, vz});
   return WF_OK;
 }
+int wf_set_contact(wf_domain* d, double mu_static, double mu_dynamic, int law) {
+  if (!d) return WF_ERR_ARG;
+  if (law != 0) return wf_fail(d, WF_ERR_ARG, "contact law must be 0 (the reference's penalty law)");
+  if (!(mu_static >= 0.0) || !(mu_dynamic >= 0.0))
+    return wf_fail(d, WF_ERR_ARG, "friction coefficients must be >= 0");
+  d->mu_s = mu_static;
+  d->mu_d = mu_dynamic;
+  d->contact_law = law;
+  return WF_OK;
+}
+
+int wf_add_trimesh(wf_domain* d, const double* nodes, int32_t nn, const int32_t* tris,
+                   int32_t ne, const double* normals, int32_t zone_id, int64_t first,
+                   const double* vel, const double* angvel) {
+  if (!d || !nodes || !tris || nn <= 0 || ne <= 0 || !vel || !angvel) return WF_ERR_ARG;
+  if ((int)d->meshes.size() >= WF_MAX_MESH) return wf_fail(d, WF_ERR_ARG, "at most 4 rigid meshes");
+  if (first < d->n_solid || first + ne > d->n)
+    return wf_fail(d, WF_ERR_ARG, "rigid particles first .. first+ne-1 must follow the solid ones");
+  for (const MeshDev& M : d->meshes)
+    if (first < M.first + M.ne && M.first < first + ne)
+      return wf_fail(d, WF_ERR_ARG, "rigid particle ranges of two meshes overlap");
+  if (zone_id == 1) return wf_fail(d, WF_ERR_ARG, "zone id 1 is the free-surface id");
+  if (!d->m_set || !d->x_set) return wf_fail(d, WF_ERR_STATE, "set positions and masses first");
+  if (d->started) return wf_fail(d, WF_ERR_STATE, "meshes are added before the first solve");
+  for (int64_t k = 0; k < 3 * (int64_t)ne; k++)
+    if (tris[k] < 0 || tris[k] >= nn) return wf_fail(d, WF_ERR_ARG, "triangle node out of range");
+  for (int64_t k = 0; k < 3 * (int64_t)nn; k++)
+    if (!std::isfinite(nodes[k])) return wf_fail(d, WF_ERR_ARG, "non-finite node");
+  // element centroids and normals in the reference's arithmetic (CalcCentroids,
+  // CalcNormals, Mesh.cu:233-257); normals given by the caller are kept
+  std::vector<double4> hn(nn), hc(ne), hnorm(ne), hv(nn);
+  for (int q = 0; q < nn; q++) {
+    hn[q] = make_double4(nodes[3 * q], nodes[3 * q + 1], nodes[3 * q + 2], 0.0);
+    hv[q] = make_double4(0.0, 0.0, 0.0, 0.0);
+  }
+  for (int e = 0; e < ne; e++) {
+    const double4 a = hn[tris[3 * e]], b = hn[tris[3 * e + 1]], c = hn[tris[3 * e + 2]];
+    const double third = 1.0 / 3.;
+    hc[e] = make_double4(((a.x + b.x) + c.x) * third, ((a.y + b.y) + c.y) * third,
+                         ((a.z + b.z) + c.z) * third, 0.0);
+    if (normals) {
+      hnorm[e] = make_double4(normals[3 * e], normals[3 * e + 1], normals[3 * e + 2], 0.0);
+    } else {
+      const double ux = b.x - a.x, uy = b.y - a.y, uz = b.z - a.z;
+      const double vx = c.x - a.x, vy = c.y - a.y, vz = c.z - a.z;
+      const double wx = uy * vz - uz * vy, wy = uz * vx - ux * vz, wz = ux * vy - uy * vx;
+      const double inv = 1.0 / std::sqrt(wx * wx + wy * wy + wz * wz);
+      hnorm[e] = make_double4(wx * inv, wy * inv, wz * inv, 0.0);
+    }
+  }
+  MeshDev M{};
+  M.nn = nn; M.ne = ne; M.first = (int32_t)first; M.zone = zone_id;
+  for (int k = 0; k < 3; k++) { M.mv[k] = vel[k]; M.mw[k] = angvel[k]; }
+  cudaStream_t s = d->stream;
+  if (dalloc(&M.node, nn, s) || dalloc(&M.node_v, nn, s) || dalloc(&M.centroid, ne, s) ||
+      dalloc(&M.normal, ne, s) || dalloc(&M.elnode, 3 * (int64_t)ne, s) || dalloc(&M.pplane, ne, s)) {
+    void* mp[] = {M.node, M.node_v, M.centroid, M.normal, M.elnode, M.pplane};
+    for (void* p : mp) if (p) cudaFree(p);
+    return wf_fail(d, WF_ERR_ALLOC, "mesh arrays");
+  }
+  d->meshes.push_back(M);      // freed with the domain from here on
+  WF_CUDA_OK(cudaMemcpyAsync(M.node, hn.data(), sizeof(double4) * nn, cudaMemcpyHostToDevice, s));
+  WF_CUDA_OK(cudaMemcpyAsync(M.node_v, hv.data(), sizeof(double4) * nn, cudaMemcpyHostToDevice, s));
+  WF_CUDA_OK(cudaMemcpyAsync(M.centroid, hc.data(), sizeof(double4) * ne, cudaMemcpyHostToDevice, s));
+  WF_CUDA_OK(cudaMemcpyAsync(M.normal, hnorm.data(), sizeof(double4) * ne, cudaMemcpyHostToDevice, s));
+  WF_CUDA_OK(cudaMemcpyAsync(M.elnode, tris, sizeof(int32_t) * 3 * ne, cudaMemcpyHostToDevice, s));
+  if (!d->cnb) {               // per-particle contact state, on the first mesh
+    for (int k = 0; k < 2; k++)
+      if (dalloc(&d->F[k].nrm, d->npad, s) || dalloc(&d->F[k].cf, d->npad, s))
+        return wf_fail(d, WF_ERR_ALLOC, "contact fields");
+    if (dalloc(&d->cnb, (int64_t)WF_CONT_NB * d->npad, s) || dalloc(&d->ccnt, d->npad, s))
+      return wf_fail(d, WF_ERR_ALLOC, "contact lists");
+  }
+  k_place_rigid<<<nblk(ne), 256, 0, s>>>(ne, (int32_t)first, d->inv, M.centroid, M.normal,
+                                          zone_id, CF(d));
+  WF_CUDA_OK(cudaStreamSynchronize(s));
+  WF_CUDA_OK(cudaGetLastError());
+  for (int64_t p = first; p < first + ne; p++) d->h_mass[p] = 0.0;
+  return WF_OK;
+}
+
 int wf_set_temperature(wf_domain* d, const double* T) {
   if (!d || !T) return WF_ERR_ARG;
   return upload_d(d, T, 1, CF(d).T, 1, 0);
@@ -950,6 +1083,14 @@ int wf_get_field(wf_domain* d, const char* name, double* out) {
   if (s == "Ta") return g(F.Ta, 1, 0, 1);
   if (s == "Tb") return g(F.Tb, 1, 0, 1);
   if (s == "dTdt") return g(F.dTdt, 1, 0, 1);
+  if (s == "normal" || s == "contforce") {         // zero until a rigid mesh is added
+    const double4* src = s == "normal" ? F.nrm : F.cf;
+    if (!src) {
+      std::fill(out, out + 3 * n, 0.0);
+      return WF_OK;
+    }
+    return g((const double*)src, 4, 0, 3);
+  }
   return wf_fail(d, WF_ERR_ARG, "unknown field: " + s);
 }
 
@@ -961,6 +1102,13 @@ int wf_get_field_i32(wf_domain* d, const char* name, int32_t* out) {
   if (s == "ID") src = F.id;
   else if (s == "nb_count") src = d->nbc;
   else if (s == "BC_T") src = F.bct;
+  else if (s == "cont_count") {          // zero until a rigid mesh is added
+    if (!d->ccnt) {
+      std::fill(out, out + d->n, 0);
+      return WF_OK;
+    }
+    src = d->ccnt;
+  }
   else return wf_fail(d, WF_ERR_ARG, "unknown field: " + s);
   k_gather_t<int32_t><<<nblk(d->n), 256, 0, d->stream>>>(d->n, d->inv, src, (int32_t*)d->d_stage);
   WF_CUDA_OK(cudaMemcpyAsync(out, d->d_stage, sizeof(int32_t) * d->n, cudaMemcpyDeviceToHost, d->stream));

@@ -80,7 +80,24 @@ struct Fields {
   float* ss32;      // deviatoric stress FP32 state (mixed form), 6 per slot
   float4* th32;     // heat-flux mirror (mixed form): T as a float pair (hi, lo), k, rho
   double* pwn;      // cached eps_p^n of the Johnson-Cook law (< 0: not cached yet)
+  // contact (allocated when a rigid mesh is added)
+  double4* nrm;     // surface normal (solid particles) / element normal (rigid particles)
+  double4* cf;      // contact force of the last contact (contforce)
 };
+
+// A rigid triangle mesh on the device (TriMesh_d, src/cuda/Mesh.cuh:19-54);
+// its element e is carried by the rigid particle of original id first + e.
+struct MeshDev {
+  double4* node;      // node positions
+  double4* node_v;    // node velocities
+  double4* centroid;  // element centroids
+  double4* normal;    // element normals
+  int32_t* elnode;    // 3 nodes per element
+  double* pplane;     // plane coefficient n . node
+  int32_t nn, ne, first, zone;
+  double mv[3], mw[3];  // translational and angular velocity (m_v, m_w)
+};
+#define WF_CONT_NB 20     // contact neighbours per particle (MAX_NB_COUNT, src/cuda/Contact.cu:7)
 
 // Johnson-Cook / bilinear / Hollomon constants as the kernels use them.
 struct MatParams {
@@ -110,6 +127,12 @@ struct StepParams {
   int contact;          // contact pass filter active
   int ncsid;
   int32_t csid[WF_MAX_MESH];
+  MeshDev mesh[WF_MAX_MESH];   // ncsid meshes, zone ids in csid
+  double mu_s, mu_d;    // static / dynamic friction coefficients
+  double totmass;       // sum of all particle masses (WeldFormGPU.cu:808-820)
+  int32_t id_free_surf; // 1, the id of free-surface particles
+  int32_t* cnb;         // contact neighbours [WF_CONT_NB * npad] (slot indices)
+  int32_t* ccnt;        // contact neighbour counts [npad]
   int nbc;
   int32_t bc_zone[WF_MAX_BC];
   double bc_v[WF_MAX_BC][3];
@@ -217,6 +240,13 @@ void launch_thermal(const StepParams& P, const Fields& F, const NbBuffers& N, in
 
 void launch_fp32_density(const StepParams& P, const Fields& F, double4* vd2, float4* v32b,
                          const NbBuffers& N, cudaStream_t s);
+// contact (wf_contact.cu): surface tagging, contact list (when `list`) and
+// penalty forces after the acceleration pass; mesh motion and rigid particles
+// after the integration; plane coefficients at solve start
+void launch_contact_stage(const StepParams& P, const Fields& F, const NbBuffers& N, bool list,
+                          float4* a32, cudaStream_t s);
+void launch_mesh_update(const StepParams& P, const Fields& F, int mixed, cudaStream_t s);
+void launch_mesh_plane(const StepParams& P, cudaStream_t s);
 // density pass of this step with the previous step's heat pass (mixed form)
 void launch_fp32_density_heat(const StepParams& P, const Fields& F, double4* vd2, float4* v32b,
                               const NbBuffers& N, int first, int plastic_heat, cudaStream_t s);

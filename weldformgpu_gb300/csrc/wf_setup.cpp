@@ -151,4 +151,41 @@ int64_t wf_assign_zone(const double* x, int64_t n, const double* start, const do
   return cnt;
 }
 
+// TriMesh_d::AxisPlaneMesh (src/cuda/Mesh.cu:48-194), the rigid plane main
+// builds for a "Plane" body (src/WeldFormGPU.cu:545-552).  The reference
+// steps both in-plane directions by dl = (p2.x - p1.x) / dens from p1 (x
+// inner, y outer, running sums) at z = p1.z whatever the axis; the two
+// triangles of a cell are ordered for an outward normal along +axis when
+// `positive`, and the normals are set on the axis.
+int64_t wf_gen_plane_mesh(int axis, int positive, const double* p1, const double* p2, int dens,
+                          double* nodes, int32_t* tris, double* normals) {
+  if (dens < 1 || axis < 0 || axis > 2 || !p1 || !p2) return -1;
+  const int64_t ne = 2 * (int64_t)dens * dens;
+  if (!nodes && !tris && !normals) return ne;
+  const double dl = (p2[0] - p1[0]) / dens;
+  const double z = p1[2];
+  double y = p1[1];
+  int64_t vi = 0;
+  for (int j = 0; j <= dens; j++, y += dl) {
+    double x = p1[0];
+    for (int i = 0; i <= dens; i++, vi++, x += dl)
+      if (nodes) { nodes[3 * vi] = x; nodes[3 * vi + 1] = y; nodes[3 * vi + 2] = z; }
+  }
+  int64_t el = 0;
+  for (int j = 0; j < dens; j++)
+    for (int i = 0; i < dens; i++) {
+      const int32_t a = (dens + 1) * j + i, b = a + 1, c = (dens + 1) * (j + 1) + i, e = c + 1;
+      const int32_t tri[2][3] = {{a, positive ? b : c, positive ? c : b},
+                                 {b, positive ? e : c, positive ? c : e}};
+      for (int t = 0; t < 2; t++, el++)
+        if (tris) for (int q = 0; q < 3; q++) tris[3 * el + q] = tri[t][q];
+    }
+  if (normals)
+    for (int64_t k = 0; k < ne; k++) {
+      normals[3 * k] = normals[3 * k + 1] = normals[3 * k + 2] = 0.0;
+      normals[3 * k + axis] = positive ? 1.0 : -1.0;
+    }
+  return ne;
+}
+
 }  // extern "C"

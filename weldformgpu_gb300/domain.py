@@ -93,6 +93,22 @@ class Domain_d:
         self._ck(self.L.wf_add_velocity_bc(self.h, int(zone), float(vx), float(vy), float(vz)),
                  "wf_add_velocity_bc")
 
+    def set_contact(self, mu_static, mu_dynamic, law=0):
+        self._ck(self.L.wf_set_contact(self.h, float(mu_static), float(mu_dynamic), int(law)),
+                 "wf_set_contact")
+
+    def add_trimesh(self, nodes, tris, zone_id, first, vel, angvel=(0.0, 0.0, 0.0), normals=None):
+        """Rigid triangle mesh; its element centroids become particles first.. (mass 0)."""
+        nd = np.ascontiguousarray(nodes, dtype=np.float64).reshape(-1, 3)
+        tr = np.ascontiguousarray(tris, dtype=np.int32).reshape(-1, 3)
+        na = None if normals is None else np.ascontiguousarray(normals, dtype=np.float64)
+        nr = None if na is None else _ptr(na, C.c_double)
+        v = np.ascontiguousarray(vel, dtype=np.float64)
+        w = np.ascontiguousarray(angvel, dtype=np.float64)
+        self._ck(self.L.wf_add_trimesh(self.h, _ptr(nd, C.c_double), len(nd), _ptr(tr, C.c_int32),
+                                       len(tr), nr, int(zone_id), int(first), _ptr(v, C.c_double),
+                                       _ptr(w, C.c_double)), "wf_add_trimesh")
+
     def set_convection(self, h_conv, T_inf):
         self._ck(self.L.wf_set_convection(self.h, float(h_conv), float(T_inf)), "wf_set_convection")
 

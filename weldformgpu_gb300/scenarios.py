@@ -56,9 +56,46 @@ def compression_cylinder(R=0.0025, H=0.005, dx=0.0005, generator="reference", vz
                 bcs=[(2, (0.0, 0.0, 0.0)), (3, (0.0, 0.0, vz_top))], K=K, dx=dx)
 
 
+def contact_cylinder(R=0.005, H=0.010, dx=0.0005, dens=10, v_plane=-10.0, gap=1.0e-7,
+                     mu=(0.0, 0.0), material="bilinear", zone=5):
+    """Cylinder (the reference generator) with its bottom two layers fixed,
+    compressed by a rigid plane from above, as main sets up a "Plane" rigid
+    body (src/WeldFormGPU.cu:498-610): AxisPlaneMesh(2, false, ...) with
+    `dens` cells a side, normal -z, starting `gap` beyond contact range (one
+    smoothing length above the top particles) and moving at v_plane; its
+    2 dens^2 element centroids are the last particles (zone `zone`)."""
+    sc = compression_cylinder(R=R, H=H, dx=dx, material=material)
+    x_s = sc["x"]
+    ns = len(x_s)
+    ids = np.zeros(ns, np.int32)
+    nw = np.zeros(ns, np.uint8)
+    zmin, zmax = x_s[:, 2].min(), x_s[:, 2].max()
+    S.assign_zone(x_s, (-1, -1, -1), (1, 1, zmin + 1.5 * dx), 2, ids, nw)
+    side = 2.0 * R + 2.0 * dx
+    p1 = (-R - dx, -R - dx, zmax + sc["h"] + gap)
+    p2 = (p1[0] + side, p1[1] + side, p1[2])
+    nodes, tris, normals = S.gen_plane_mesh(2, 0, p1, p2, dens)
+    ne = len(tris)
+    n = ns + ne
+    sc.update(
+        n=n, n_solid=ns,
+        x=np.vstack([x_s, np.zeros((ne, 3))]),
+        m=np.concatenate([sc["m"], np.zeros(ne)]),
+        ids=np.concatenate([ids, np.full(ne, zone, np.int32)]),
+        not_write=np.concatenate([nw, np.zeros(ne, np.uint8)]),
+        T=np.full(n, 20.0),
+        bcs=[(2, (0.0, 0.0, 0.0)), (zone, (0.0, 0.0, v_plane))],
+        mesh=dict(nodes=nodes, tris=tris, normals=normals, zone=zone, first=ns,
+                  vel=(0.0, 0.0, v_plane), angvel=(0.0, 0.0, 0.0)),
+        mu=mu)
+    return sc
+
+
 def load(dom, sc, options=None):
     """Applies a scenario through the Domain_d setters (product or oracle)."""
     n = sc["n"]
+    if "n_solid" in sc:
+        dom.set_solid_count(sc["n_solid"])
     dom.set_h(sc["h"])
     dom.set_density(sc["rho"])
     dom.set_shear_modulus(sc["G"])
@@ -77,6 +114,11 @@ def load(dom, sc, options=None):
     if "k" in sc:
         dom.set_conductivity(sc["k"])
         dom.set_heat_cap(sc["cp"])
+    if "mesh" in sc:
+        ms = sc["mesh"]
+        dom.add_trimesh(ms["nodes"], ms["tris"], ms["zone"], ms["first"], ms["vel"], ms["angvel"],
+                        normals=ms["normals"])
+        dom.set_contact(sc["mu"][0], sc["mu"][1])
     for k, v in (options or {}).items():
         dom.set_option(k, float(v))
     return dom

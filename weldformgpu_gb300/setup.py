@@ -61,6 +61,21 @@ def gen_cylinder_lattice(R, H, dx, jitter, seed):
     return x.reshape(n, 3)
 
 
+def gen_plane_mesh(axis, positive, p1, p2, dens):
+    """TriMesh_d::AxisPlaneMesh (src/cuda/Mesh.cu:48-194): (nodes[nn,3], tris[ne,3], normals[ne,3])."""
+    lib_ = _L()
+    a, b = np.asarray(p1, dtype=np.float64), np.asarray(p2, dtype=np.float64)
+    ne = lib_.wf_gen_plane_mesh(int(axis), int(positive), _p(a), _p(b), int(dens), None, None, None)
+    if ne < 0:
+        raise ValueError("bad plane mesh arguments")
+    nodes = np.empty(3 * (dens + 1) ** 2, dtype=np.float64)
+    tris = np.empty(3 * ne, dtype=np.int32)
+    normals = np.empty(3 * ne, dtype=np.float64)
+    lib_.wf_gen_plane_mesh(int(axis), int(positive), _p(a), _p(b), int(dens), _p(nodes),
+                           _p(tris, C.c_int32), _p(normals))
+    return nodes.reshape(-1, 3), tris.reshape(-1, 3), normals.reshape(-1, 3)
+
+
 def assign_zone(x, start, end, zone, ids, not_write):
     """Domain::AssignZone (src/Domain.cpp:989-1005); modifies ids / not_write in place."""
     x = np.ascontiguousarray(x, dtype=np.float64)
