@@ -179,6 +179,23 @@ int wf_set_field(wf_domain* d, const char* name, const double* in);
 int wf_set_scalar(wf_domain* d, const char* name, double value);
 /* Domain_d::WriteCSV (src/cuda/Domain_d.cu:556-587), same columns. */
 int wf_write_csv(wf_domain* d, const char* path);
+/* MechFraserSolve's snapshots (SolverFraser.cu:142-144, 357-360): with a
+ * non-NULL prefix, solves write <prefix>out_<time %.6f>.csv at their start
+ * and at every output time; NULL turns them off (the default). */
+int wf_set_csv_output(wf_domain* d, const char* prefix);
+
+/* ---- the reference's input-file driver ---------------------------------
+ * main of src/WeldFormGPU.cu:142-926: reads the reference's JSON keys
+ * (Configuration, Materials, DomainBlocks Box / Cylinder, DomainZones,
+ * RigidBodies Plane, Contact, BoundaryConditions), builds and sets up the
+ * domain as main does, runs MechFraserSolve(simTime, outTime) writing
+ * out_<time>.csv into out_dir and test.csv at the end.  err (optional,
+ * err_len bytes) receives a one-line message on failure.  Keys with no
+ * reference counterpart: Configuration.precision ("fp64" | "mixed"),
+ * returnMap ("radial" | "newton"), solver "Mech-Thermal" with
+ * Materials.thermalCond / thermalHeatCap and taylorQuinney,
+ * InitialConditions[0].Temp. */
+int wf_run_json(const char* path, const char* out_dir, char* err, int64_t err_len);
 
 /* ---- host domain set-up (src/Domain.cpp) --------------------------------- */
 /* Two-call protocol: pass x == NULL to get the particle count, then a buffer

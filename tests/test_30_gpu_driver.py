@@ -1,0 +1,120 @@
+"""The reference's input-file driver (wf_run_json and the `wf` executable).
+
+An input file in the reference's format (the keys of src/WeldFormGPU.cu's
+main) runs end to end; its CSV snapshots have the reference's columns and
+its final state equals the same set-up built through the Python API.
+"""
+import ctypes
+import json
+import math
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from weldformgpu_gb300 import _abi
+from weldformgpu_gb300 import setup as P
+
+pytestmark = pytest.mark.gpu
+
+HEADER = ("ID, X, Y, Z, posX,posY,posZ,Ux, Uy, Uz, Vx, Vy, Vz, Ax, Ay, Az, rho, p, SigmaEq, "
+          "Pl_Strain, Nb, ContNb, CFx, CFy, CFz, Nx, Ny, Nz, h")
+
+R, H, r = 0.0025, 0.005, 0.00025
+E, nu, rho, Fy, Et = 70e9, 0.33, 2700.0, 300e6, 7e8
+SIM, OUT = 2.0e-5, 5.0e-6
+
+
+def _inputs():
+    x, _ = P.gen_cylinder_ref((0.0, 0.0, 0.0), R, H, r, rho)
+    h = 1.2 * 2 * r
+    zp = float(x[:, 2].max()) + h + 1e-7
+    cfg = {
+        "Configuration": {"particleRadius": r, "hFactor": 1.2, "simTime": SIM, "outTime": OUT},
+        "Materials": [{"id": "Solid", "type": "Bilinear", "const": [Et], "density0": rho,
+                       "youngsModulus": E, "poissonsRatio": nu, "yieldStress0": Fy}],
+        "DomainBlocks": [{"type": "Cylinder", "zoneId": 0, "start": [0.0, 0.0, 0.0],
+                          "dim": [2 * R, 0.0, H]}],
+        "DomainZones": [{"id": 2, "start": [-1.0, -1.0, -1.0], "end": [1.0, 1.0, 0.0004]}],
+        "RigidBodies": [{"type": "Plane", "zoneId": 10, "start": [-0.003, -0.003, zp],
+                         "partSide": 6, "dim": [0.006, 0.006, 0.0]}],
+        "Contact": [{"fricCoeffStatic": 0.3, "fricCoeffDynamic": 0.2}],
+        "BoundaryConditions": [{"zoneId": 2, "value": [0.0, 0.0, 0.0], "free": True},
+                               {"zoneId": 10, "valuetype": 0, "value": [0.0, 0.0, -10.0],
+                                "free": True}],
+    }
+    return cfg, zp
+
+
+def _api_domain(zp):
+    """main's set-up (src/WeldFormGPU.cu:689-914) through the Python API."""
+    from weldformgpu_gb300 import Domain_d
+    x, mass = P.gen_cylinder_ref((0.0, 0.0, 0.0), R, H, r, rho)
+    ns = len(x)
+    ids = np.zeros(ns, np.int32)
+    P.assign_zone(x, (-1, -1, -1), (1, 1, 0.0004), 2, ids, np.zeros(ns, np.uint8))
+    nodes, tris, normals = P.gen_plane_mesh(2, 0, (-0.003, -0.003, zp), (0.003, 0.003, zp), 6)
+    n = ns + len(tris)
+    K, G = E / (3 * (1 - 2 * nu)), E / (2 * (1 + nu))
+    Cs, h = math.sqrt(K / rho), 1.2 * 2 * r
+    d = Domain_d(n)
+    d.set_solid_count(ns)
+    d.set_material(_abi.WfMaterial(model=_abi.WF_BILINEAR, E=E, nu=nu, sy0=Fy, Et=Et))
+    d.set_density(rho)
+    d.set_h(h)
+    d.set_positions(np.vstack([x, np.zeros((len(tris), 3))]))
+    d.set_mass(np.concatenate([np.full(ns, mass), np.zeros(len(tris))]))
+    d.set_shear_modulus(G)
+    d.set_free(np.ones(n, np.uint8))
+    d.set_id(np.concatenate([ids, np.full(len(tris), 10, np.int32)]))
+    d.set_cs(np.full(n, Cs))
+    d.set_sigma_y(Fy)
+    d.set_not_write_surf_id(np.concatenate([(ids != 0).astype(np.uint8), np.zeros(len(tris), np.uint8)]))
+    d.set_temperature(np.full(n, 20.0))
+    d.set_time_step(0.4 * h / (Cs + 10.0))
+    d.add_velocity_bc(2, 0.0, 0.0, 0.0)
+    d.add_velocity_bc(10, 0.0, 0.0, -10.0)
+    d.add_trimesh(nodes, tris, 10, ns, (0.0, 0.0, -10.0), normals=normals)
+    d.set_contact(0.3, 0.2)
+    d.mech_fraser_solve(SIM, OUT)
+    return d, n
+
+
+def _csv(path):
+    with open(path) as f:
+        head = f.readline().strip()
+        rows = np.loadtxt(f, delimiter=",")
+    return head, rows
+
+
+def test_json_driver_matches_api_and_writes_reference_csv(tmp_path):
+    from weldformgpu_gb300.domain import LIB_PATH, lib
+    lib()
+    L = ctypes.CDLL(LIB_PATH)
+    L.wf_run_json.restype = ctypes.c_int
+    L.wf_run_json.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int64]
+    cfg, zp = _inputs()
+    inp = tmp_path / "Contact_Compression_small.json"
+    inp.write_text(json.dumps(cfg, indent=1))
+    out = tmp_path / "run"
+    out.mkdir()
+    err = ctypes.create_string_buffer(512)
+    assert L.wf_run_json(str(inp).encode(), str(out).encode(), err, 512) == 0, err.value
+    snaps = sorted(f for f in os.listdir(out) if f.startswith("out_"))
+    assert snaps[0] == "out_0.000000.csv" and len(snaps) >= int(SIM / OUT)
+    head, rows = _csv(out / "test.csv")
+    assert head == HEADER
+    d, n = _api_domain(zp)
+    assert rows.shape == (n, 29)
+    np.testing.assert_allclose(rows[:, 1:4], d.get_field("x"), rtol=2e-6, atol=1e-12)
+    np.testing.assert_allclose(rows[:, 19], d.get_field("pl_strain"), rtol=2e-6, atol=1e-12)
+    assert np.array_equal(rows[:, 0].astype(np.int32), d.get_field_i32("ID"))
+    assert (rows[:, 21] > 0).sum() > 20                       # contact neighbours written
+    assert np.abs(rows[:, 22:25]).sum() > 0                   # contact forces written
+    # the command-line executable gives the same file
+    exe = os.path.join(os.path.dirname(LIB_PATH), "wf")
+    out2 = tmp_path / "cli"
+    out2.mkdir()
+    subprocess.run([exe, str(inp), str(out2)], check=True, capture_output=True)
+    assert (out2 / "test.csv").read_bytes() == (out / "test.csv").read_bytes()

@@ -16,13 +16,14 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libweldform_gb300.so")
+CLI = os.path.join(HERE, "wf")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
           "--expt-relaxed-constexpr"]
 # units whose FP64 arithmetic must round like the reference / the CPU oracle
 NO_FMA = {"wf_step_fp64.cu", "wf_integrate.cu", "wf_contact.cu"}
 SOURCES = ["wf_api.cu", "wf_nsearch.cu", "wf_step_fp64.cu", "wf_step_fp32.cu", "wf_integrate.cu",
-           "wf_mlp.cu", "wf_setup.cpp", "wf_noalloc.cu", "wf_contact.cu"]
+           "wf_mlp.cu", "wf_setup.cpp", "wf_noalloc.cu", "wf_contact.cu", "wf_json.cpp"]
 
 
 def nvcc():
@@ -38,7 +39,8 @@ def _deps():
 
 
 def up_to_date():
-    return os.path.exists(LIB) and os.path.getmtime(LIB) >= _deps()
+    return (os.path.exists(LIB) and os.path.exists(CLI)
+            and min(os.path.getmtime(LIB), os.path.getmtime(CLI)) >= _deps())
 
 
 def _compile(src, verbose):
@@ -69,6 +71,13 @@ def build(force=False, verbose=False):
         print(" ".join(cmd), flush=True)
     subprocess.run(cmd, check=True)
     os.replace(tmp, LIB)
+    # the command-line driver (wf <input.json> [out dir]), linked to the library
+    cli = [shutil.which("g++") or "g++", "-O2", "-std=c++17", "-o", CLI,
+           os.path.join(CSRC, "wf_cli.cpp"), "-L" + HERE, "-lweldform_gb300",
+           "-Wl,-rpath,$ORIGIN"]
+    if verbose:
+        print(" ".join(cli), flush=True)
+    subprocess.run(cli, check=True)
     return LIB
 
 

@@ -81,6 +81,9 @@ struct wf_domain {
   int contact_law = 0;
   std::vector<double> h_mass;      // masses in caller order (totmass, rigid particles)
   int32_t *cnb = nullptr, *ccnt = nullptr;
+  // MechFraserSolve's CSV snapshots (out_<time>.csv), when a prefix is set
+  bool csv_on = false;
+  std::string csv_prefix;
   double time = 0, t_out = 0, dt_out = 0;
   int64_t step = 0;
   int ts_i = 0;
@@ -444,6 +447,16 @@ static int read_status(wf_domain* d) {
   return WF_OK;
 }
 
+// out_<time>.csv as MechFraserSolve writes it (SolverFraser.cu:142-144, 357-360)
+extern "C" int wf_write_csv(wf_domain* d, const char* path);
+static void flush_heat(wf_domain* d);
+static int write_snapshot(wf_domain* d) {
+  flush_heat(d);
+  char name[64];
+  snprintf(name, sizeof name, "out_%.6f.csv", d->time);
+  return wf_write_csv(d, (d->csv_prefix + name).c_str());
+}
+
 static int solve_begin(wf_domain* d, double dt_out) {
   int rc = check_ready(d);
   if (rc) return rc;
@@ -470,6 +483,7 @@ static int solve_begin(wf_domain* d, double dt_out) {
   if (d->precision == 1) k_mixed_init<<<nblk(d->n), 256, 0, d->stream>>>(d->n, d->F[d->cur]);
   WF_CUDA_OK(cudaGetLastError());
   d->started = true;
+  if (d->csv_on) return write_snapshot(d);
   return WF_OK;
 }
 
@@ -530,6 +544,10 @@ static int solve_step(wf_domain* d) {
     launch_snapshot(d->n, F, s);
     d->launches += 1;
     d->t_out += d->dt_out;
+    if (d->csv_on) {
+      int rc = write_snapshot(d);
+      if (rc) return rc;
+    }
   }
   d->step++;
   d->ts_i++;
@@ -752,6 +770,13 @@ int wf_add_velocity_bc(wf_domain* d, int32_t zone, double vx, double vy, double 
   d->bc_v.push_back({vx, vy, vz});
   return WF_OK;
 }
+int wf_set_csv_output(wf_domain* d, const char* prefix) {
+  if (!d) return WF_ERR_ARG;
+  d->csv_on = prefix != nullptr;
+  d->csv_prefix = prefix ? prefix : "";
+  return WF_OK;
+}
+
 int wf_set_contact(wf_domain* d, double mu_static, double mu_dynamic, int law) {
   if (!d) return WF_ERR_ARG;
   if (law != 0) return wf_fail(d, WF_ERR_ARG, "contact law must be 0 (the reference's penalty law)");
@@ -1166,14 +1191,17 @@ int wf_get_scalar(wf_domain* d, const char* name, double* out) {
 int wf_write_csv(wf_domain* d, const char* path) {
   if (!d || !path) return WF_ERR_ARG;
   const int64_t n = d->n;
-  std::vector<double> x(3 * n), u(3 * n), v(3 * n), a(3 * n), rho(n), p(n), seq(n), ps(n);
-  std::vector<int32_t> id(n), nbc(n);
+  std::vector<double> x(3 * n), u(3 * n), v(3 * n), a(3 * n), rho(n), p(n), seq(n), ps(n),
+      cf(3 * n), nr(3 * n);
+  std::vector<int32_t> id(n), nbc(n), cnc(n);
   int rc = 0;
   if ((rc = wf_get_field(d, "x", x.data())) || (rc = wf_get_field(d, "u", u.data())) ||
       (rc = wf_get_field(d, "v", v.data())) || (rc = wf_get_field(d, "a", a.data())) ||
       (rc = wf_get_field(d, "rho", rho.data())) || (rc = wf_get_field(d, "p", p.data())) ||
       (rc = wf_get_field(d, "sigma_eq", seq.data())) || (rc = wf_get_field(d, "pl_strain", ps.data())) ||
-      (rc = wf_get_field_i32(d, "ID", id.data())) || (rc = wf_get_field_i32(d, "nb_count", nbc.data())))
+      (rc = wf_get_field(d, "contforce", cf.data())) || (rc = wf_get_field(d, "normal", nr.data())) ||
+      (rc = wf_get_field_i32(d, "ID", id.data())) || (rc = wf_get_field_i32(d, "nb_count", nbc.data())) ||
+      (rc = wf_get_field_i32(d, "cont_count", cnc.data())))
     return rc;
   FILE* f = fopen(path, "w");
   if (!f) return wf_fail(d, WF_ERR_IO, std::string("cannot open ") + path);
@@ -1185,8 +1213,8 @@ int wf_write_csv(wf_domain* d, const char* path) {
             "%.6e, %.6e, %.6e, %.6e, %.6e, %.6e, %d, %d, %.6e, %.6e, %.6e, %.6e, %.6e, %.6e, %6e\n",
             id[i], x[3 * i], x[3 * i + 1], x[3 * i + 2], x[3 * i], x[3 * i + 1], x[3 * i + 2],
             u[3 * i], u[3 * i + 1], u[3 * i + 2], v[3 * i], v[3 * i + 1], v[3 * i + 2], a[3 * i],
-            a[3 * i + 1], a[3 * i + 2], rho[i], p[i], seq[i], ps[i], nbc[i], 0, 0.0, 0.0, 0.0,
-            0.0, 0.0, 0.0, d->h);
+            a[3 * i + 1], a[3 * i + 2], rho[i], p[i], seq[i], ps[i], nbc[i], cnc[i], cf[3 * i],
+            cf[3 * i + 1], cf[3 * i + 2], nr[3 * i], nr[3 * i + 1], nr[3 * i + 2], d->h);
   }
   fclose(f);
   return WF_OK;
