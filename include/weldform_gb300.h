@@ -187,7 +187,7 @@ int wf_set_csv_output(wf_domain* d, const char* prefix);
 /* ---- the reference's input-file driver ---------------------------------
  * main of src/WeldFormGPU.cu:142-926: reads the reference's JSON keys
  * (Configuration, Materials, DomainBlocks Box / Cylinder, DomainZones,
- * RigidBodies Plane, Contact, BoundaryConditions), builds and sets up the
+ * RigidBodies Plane / File (Nastran), Contact, BoundaryConditions), builds and sets up the
  * domain as main does, runs MechFraserSolve(simTime, outTime) writing
  * out_<time>.csv into out_dir and test.csv at the end.  err (optional,
  * err_len bytes) receives a one-line message on failure.  Keys with no
@@ -220,6 +220,13 @@ int64_t wf_gen_cylinder_lattice(double R, double H, double dx, double jitter, ui
  * NULL. */
 int64_t wf_gen_plane_mesh(int axis, int positive, const double* p1, const double* p2, int dens,
                           double* nodes, int32_t* tris, double* normals);
+/* NastranReader::read (src/NastranReader.cpp:5-150) + TriMesh_d::
+ * ReadFromNastran (src/cuda/Mesh_reader.cu:5-100): fixed-field GRID / CTRIA
+ * cards with implicit exponents ("0.7354-03").  Returns the triangle count
+ * (negative WF_ERR_IO / WF_ERR_ARG on a missing file, beam elements or an
+ * unknown node id) and *n_nodes; with nodes (3 n_nodes) and tris (3 per
+ * triangle, node positions) not NULL, fills them. */
+int64_t wf_read_nastran(const char* path, double* nodes, int32_t* tris, int64_t* n_nodes);
 /* Domain::AssignZone (src/Domain.cpp:989-1005): tags particles inside the
  * inclusive box [start, end]; returns how many. */
 int64_t wf_assign_zone(const double* x, int64_t n, const double* start, const double* end,

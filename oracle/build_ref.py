@@ -43,7 +43,7 @@ def build(verbose=False):
              "-DTHRUST_DEVICE_SYSTEM=THRUST_DEVICE_SYSTEM_CPP", "-Wno-cpp"]
     os.makedirs(OUT_DIR, exist_ok=True)
     objs = []
-    for tu in ("ref_domain.cpp", "ref_nsearch.cpp"):
+    for tu in ("ref_domain.cpp", "ref_nsearch.cpp", "ref_nastran.cpp"):
         obj = os.path.join(OUT_DIR, tu.replace(".cpp", ".o"))
         cmd = ["g++"] + flags + inc + ["-c", os.path.join(HERE, tu), "-o", obj]
         if verbose:

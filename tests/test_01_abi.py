@@ -4,6 +4,7 @@ import ctypes
 import os
 import re
 
+import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -79,6 +80,75 @@ def test_json_driver_rejects_bad_inputs_before_any_gpu_work(tmp_path, has_gpu):
         good = tmp_path / "good.json"
         good.write_text(amp.read_text().replace('"valueType": 1', '"valueType": 0'))
         assert L.wf_run_json(str(good).encode(), str(tmp_path).encode(), err, 512) == -2
+
+
+def _nastran_deck(path):
+    """A fixed-field (8-character) deck: GRID id, cp, x, y, z with implicit
+    exponents, and CTRIA3 eid, pid, g1, g2, g3 referring to node ids."""
+    # negative values fill the 8 characters, as mesh generators write them; a
+    # right-justified "    -4.0" reads as 0 in the reference's parser (its
+    # first '-' is not the field's first character, so it is taken for an
+    # exponent sign) and here alike
+    coords = [("0.0", "0.0", "0.0"), ("1.25-03", "0.0", "0.0"), ("0.0", "-2.500-3", "0.5+2"),
+              ("-.750000", "3.0", "-1.0+1"), ("2.0-1", "-4.00000", "7.125"),
+              ("0.0", "-4.0", "1.0")]
+    expect = [(0.0, 0.0, 0.0), (1.25e-3, 0.0, 0.0), (0.0, -2.5e-3, 50.0),
+              (-0.75, 3.0, -10.0), (0.2, -4.0, 7.125), (0.0, 0.0, 1.0)]
+    ids = [11, 12, 20, 31, 40, 41]
+    lines = ["$ deck written by the test", "BEGIN BULK"]
+    for i, (x, y, z) in zip(ids, coords):
+        lines.append("GRID    %8d%8d%8s%8s%8s" % (i, 0, x, y, z))
+    tris = [(11, 12, 20), (12, 31, 20), (31, 40, 20)]
+    for e, (a, b, c) in enumerate(tris):
+        lines.append("CTRIA3  %8d%8d%8d%8d%8d" % (e + 1, 1, a, b, c))
+    lines.append("ENDDATA")
+    path.write_text("\n".join(lines) + "\n")
+    pos = {i: k for k, i in enumerate(ids)}
+    return np.array(expect), np.array([[pos[a], pos[b], pos[c]] for a, b, c in tris], np.int32)
+
+
+def _read_nastran(fn, path):
+    n = ctypes.c_int64()
+    ne = fn(str(path).encode(), None, None, ctypes.byref(n))
+    assert ne > 0
+    nodes = np.empty(3 * n.value)
+    tris = np.empty(3 * ne, np.int32)
+    fn(str(path).encode(), nodes.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+       tris.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), ctypes.byref(n))
+    return nodes.reshape(-1, 3), tris.reshape(-1, 3)
+
+
+def _bind_reader(L, name):
+    fn = getattr(L, name)
+    fn.restype = ctypes.c_int64
+    fn.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double),
+                   ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int64)]
+    return fn
+
+
+def test_nastran_reader_implicit_exponents_and_reference_parser(tmp_path):
+    from weldformgpu_gb300.domain import lib
+    from oracle import oracle as O
+    rd = _bind_reader(lib(), "wf_read_nastran")
+    deck = tmp_path / "tool.nas"
+    expect, etris = _nastran_deck(deck)
+    nodes, tris = _read_nastran(rd, deck)
+    assert np.array_equal(nodes, expect) and np.array_equal(tris, etris)
+    assert rd(str(tmp_path / "none.nas").encode(), None, None, None) == -6
+    ref = O.ref_lib()
+    if ref is None:
+        pytest.skip("reference tree absent: reference parser not built")
+    rr = _bind_reader(ref, "wfr_read_nastran")
+    import contextlib
+    import io
+    with contextlib.redirect_stdout(io.StringIO()):
+        rn, rt = _read_nastran(rr, deck)
+    assert np.array_equal(rn, nodes) and np.array_equal(rt, tris)
+    example = "/root/reference/examples/input/tool_metal_cut_mm.nas"
+    if os.path.exists(example):
+        a = _read_nastran(rd, example)
+        b = _read_nastran(rr, example)
+        assert all(np.array_equal(x, y) for x, y in zip(a, b)) and len(a[1]) == 1388
 
 
 def test_header_documents_reference_citations():

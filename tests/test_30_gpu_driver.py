@@ -47,14 +47,18 @@ def _inputs():
     return cfg, zp
 
 
-def _api_domain(zp):
-    """main's set-up (src/WeldFormGPU.cu:689-914) through the Python API."""
+def _api_domain(zp, mesh=None):
+    """main's set-up (src/WeldFormGPU.cu:689-914) through the Python API;
+    mesh = (nodes, tris) of a file rigid body, else main's plane."""
     from weldformgpu_gb300 import Domain_d
     x, mass = P.gen_cylinder_ref((0.0, 0.0, 0.0), R, H, r, rho)
     ns = len(x)
     ids = np.zeros(ns, np.int32)
     P.assign_zone(x, (-1, -1, -1), (1, 1, 0.0004), 2, ids, np.zeros(ns, np.uint8))
-    nodes, tris, normals = P.gen_plane_mesh(2, 0, (-0.003, -0.003, zp), (0.003, 0.003, zp), 6)
+    if mesh is None:
+        nodes, tris, normals = P.gen_plane_mesh(2, 0, (-0.003, -0.003, zp), (0.003, 0.003, zp), 6)
+    else:
+        (nodes, tris), normals = mesh, None
     n = ns + len(tris)
     K, G = E / (3 * (1 - 2 * nu)), E / (2 * (1 + nu))
     Cs, h = math.sqrt(K / rho), 1.2 * 2 * r
@@ -118,3 +122,52 @@ def test_json_driver_matches_api_and_writes_reference_csv(tmp_path):
     out2.mkdir()
     subprocess.run([exe, str(inp), str(out2)], check=True, capture_output=True)
     assert (out2 / "test.csv").read_bytes() == (out / "test.csv").read_bytes()
+
+
+def test_json_driver_nastran_rigid_body(tmp_path):
+    """RigidBodies type "File": a plane tool written as a fixed-field Nastran
+    deck (normal -z from its node order) gives the run the API gives with the
+    mesh read by wf_read_nastran."""
+    from weldformgpu_gb300.domain import LIB_PATH, lib
+    lib()
+    L = ctypes.CDLL(LIB_PATH)
+    L.wf_run_json.restype = ctypes.c_int
+    L.wf_run_json.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int64]
+    L.wf_read_nastran.restype = ctypes.c_int64
+    L.wf_read_nastran.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double),
+                                  ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int64)]
+    cfg, zp = _inputs()
+    # an 8-character field that is not below zp: mantissa and implicit exponent
+    zs = "%.4f-3" % (math.ceil(zp * 1e7) / 1e4)
+    grid = [-0.003, -0.002, -0.001, 0.0, 0.001, 0.002, 0.003]
+    lines = ["$ plane tool", "BEGIN BULK"]
+    for j, y in enumerate(grid):
+        for i, x in enumerate(grid):
+            lines.append("GRID    %8d%8d%8s%8s%8s" % (1 + 7 * j + i, 0, "%.5f" % x, "%.5f" % y, zs))
+    e = 1
+    for j in range(6):
+        for i in range(6):
+            a, b = 1 + 7 * j + i, 2 + 7 * j + i
+            c, d = a + 7, b + 7
+            for t in ((a, c, b), (b, c, d)):               # normal -z
+                lines.append("CTRIA3  %8d%8d%8d%8d%8d" % (e, 1, *t))
+                e += 1
+    deck = tmp_path / "tool.nas"
+    deck.write_text("\n".join(lines) + "\n")
+    cfg["RigidBodies"] = [{"type": "File", "zoneId": 10, "fileName": "tool.nas"}]
+    inp = tmp_path / "file_tool.json"
+    inp.write_text(json.dumps(cfg))
+    out = tmp_path / "run"
+    out.mkdir()
+    err = ctypes.create_string_buffer(512)
+    assert L.wf_run_json(str(inp).encode(), str(out).encode(), err, 512) == 0, err.value
+    nn = ctypes.c_int64()
+    ne = L.wf_read_nastran(str(deck).encode(), None, None, ctypes.byref(nn))
+    assert ne == 72 and nn.value == 49
+    nodes, tris = np.empty(3 * nn.value), np.empty(3 * ne, np.int32)
+    L.wf_read_nastran(str(deck).encode(), nodes.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                      tris.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), ctypes.byref(nn))
+    d, n = _api_domain(zp, (nodes.reshape(-1, 3), tris.reshape(-1, 3)))
+    head, rows = _csv(out / "test.csv")
+    np.testing.assert_allclose(rows[:, 1:4], d.get_field("x"), rtol=2e-6, atol=1e-12)
+    assert (rows[:, 21] > 0).sum() > 20                       # in contact with the tool

@@ -199,7 +199,8 @@ struct Bc {
   double v[3];
 };
 
-bool run_input(const Json& root, const std::string& out_dir, Run& run) {
+bool run_input(const Json& root, const std::string& out_dir, const std::string& json_dir,
+               Run& run) {
   const Json* config = root.get("Configuration");
   const Json* materials = root.get("Materials");
   const Json* domblock = root.get("DomainBlocks");
@@ -325,14 +326,35 @@ bool run_input(const Json& root, const std::string& out_dir, Run& run) {
     read_vec3(rb, "dim", rd);
     read_int(rb, "partSide", dens);
     read_int(rb, "zoneId", rzone);
-    if (rbtype != "Plane") return run.fail(WF_ERR_ARG, "rigid body type must be Plane");
-    const double p2[3] = {rs[0] + rd[0], rs[1] + rd[1], rs[2]};
-    ne = wf_gen_plane_mesh(2, 0, rs, p2, dens, nullptr, nullptr, nullptr);
-    if (ne <= 0) return run.fail(WF_ERR_ARG, "rigid plane partSide");
-    nodes.resize(3 * (size_t)(dens + 1) * (dens + 1));
-    tris.resize(3 * (size_t)ne);
-    normals.resize(3 * (size_t)ne);
-    wf_gen_plane_mesh(2, 0, rs, p2, dens, nodes.data(), tris.data(), normals.data());
+    if (rbtype == "Plane") {
+      const double p2[3] = {rs[0] + rd[0], rs[1] + rd[1], rs[2]};
+      ne = wf_gen_plane_mesh(2, 0, rs, p2, dens, nullptr, nullptr, nullptr);
+      if (ne <= 0) return run.fail(WF_ERR_ARG, "rigid plane partSide");
+      nodes.resize(3 * (size_t)(dens + 1) * (dens + 1));
+      tris.resize(3 * (size_t)ne);
+      normals.resize(3 * (size_t)ne);
+      wf_gen_plane_mesh(2, 0, rs, p2, dens, nodes.data(), tris.data(), normals.data());
+    } else if (rbtype == "File") {
+      // Nastran mesh (:553-566); the file is looked up as given, then beside
+      // the input file.  moveDir moves the mesh (the reference moves only its
+      // host copy, so its rigid particles and contact geometry disagree).
+      std::string fname;
+      read_str(rb, "fileName", fname);
+      std::string path = fname;
+      if (!std::ifstream(path) && !json_dir.empty()) path = json_dir + "/" + fname;
+      double md[3] = {0, 0, 0};
+      read_vec3(rb, "moveDir", md);
+      int64_t nn = 0;
+      ne = wf_read_nastran(path.c_str(), nullptr, nullptr, &nn);
+      if (ne <= 0) return run.fail(ne < 0 ? (int)ne : WF_ERR_ARG, "cannot read mesh " + fname);
+      nodes.resize(3 * (size_t)nn);
+      tris.resize(3 * (size_t)ne);
+      wf_read_nastran(path.c_str(), nodes.data(), tris.data(), &nn);
+      for (int64_t q = 0; q < nn; q++)
+        for (int k = 0; k < 3; k++) nodes[3 * q + k] += md[k];
+    } else {
+      return run.fail(WF_ERR_ARG, "rigid body type must be Plane or File");
+    }
     const Json* ct = contact ? contact->at(0) : nullptr;
     read_num(ct, "fricCoeffStatic", mu_s);
     read_num(ct, "fricCoeffDynamic", mu_d);
@@ -380,7 +402,8 @@ bool run_input(const Json& root, const std::string& out_dir, Run& run) {
   if (has_contact) {
     const double w[3] = {0, 0, 0};
     if (!ok(run, d, wf_add_trimesh(d, nodes.data(), (int32_t)(nodes.size() / 3), tris.data(),
-                                   (int32_t)ne, normals.data(), rzone, ns, mesh_v, w),
+                                   (int32_t)ne, normals.empty() ? nullptr : normals.data(),
+                                   rzone, ns, mesh_v, w),
             "rigid plane") ||
         !ok(run, d, wf_set_contact(d, mu_s, mu_d, 0), "contact"))
       return false;
@@ -426,7 +449,12 @@ extern "C" int wf_run_json(const char* path, const char* out_dir, char* err, int
     Parser p(text);
     std::string perr;
     if (!p.parse(root, perr)) run.fail(WF_ERR_IO, perr);
-    else run_input(root, out_dir ? out_dir : "", run);
+    else {
+      const std::string p(path);
+      const size_t slash = p.find_last_of('/');
+      run_input(root, out_dir ? out_dir : "", slash == std::string::npos ? "" : p.substr(0, slash),
+                run);
+    }
   }
   if (err && err_len > 0) snprintf(err, (size_t)err_len, "%s", run.err.c_str());
   return run.code;

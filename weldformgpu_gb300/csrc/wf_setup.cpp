@@ -5,7 +5,12 @@
 // sums, not products) so that particle positions are bit-identical.
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
+#include <fstream>
+#include <map>
+#include <string>
+#include <vector>
 
 #include "../../include/weldform_gb300.h"
 #include "wf_setup.h"
@@ -149,6 +154,72 @@ int64_t wf_assign_zone(const double* x, int64_t n, const double* start, const do
     }
   }
   return cnt;
+}
+
+// NastranReader::read (src/NastranReader.cpp:5-150): fixed-field (8-character)
+// GRID and CTRIA cards.  Nodes are the consecutive lines from the first GRID
+// card (id in field 2, x y z in fields 4-6, implicit exponents); elements are
+// the consecutive lines from the first CTRIA / CBEAM / CBAR card (node ids in
+// fields 4-6, mapped to node positions).  Two-call protocol: NULL buffers
+// return the element count and *n_nodes only.  Negative return: WF_ERR_IO
+// (file), WF_ERR_ARG (beam elements, unknown node id).
+int64_t wf_read_nastran(const char* path, double* nodes, int32_t* tris, int64_t* n_nodes) {
+  if (!path) return WF_ERR_ARG;
+  std::ifstream f(path);
+  if (!f) return WF_ERR_IO;
+  std::vector<std::string> lines;
+  for (std::string l; std::getline(f, l);) lines.push_back(l);
+  int64_t nn = 0, ne = 0, first_node = -1, first_elem = -1;
+  bool beams = false;
+  for (int64_t l = 0; l < (int64_t)lines.size(); l++) {
+    const std::string& s = lines[l];
+    if (s.compare(0, 4, "GRID") == 0) {
+      if (first_node < 0) first_node = l;
+      nn++;
+    } else if (s.compare(0, 5, "CTRIA") == 0 || s.compare(0, 5, "CBEAM") == 0 ||
+               s.compare(0, 4, "CBAR") == 0) {
+      if (first_elem < 0) first_elem = l;
+      if (s.compare(0, 5, "CTRIA") != 0) beams = true;
+      ne++;
+    }
+  }
+  if (beams) return WF_ERR_ARG;                       // dim = 2: not a triangle mesh
+  if (n_nodes) *n_nodes = nn;
+  if (!nodes && !tris) return ne;
+  auto field = [](const std::string& s, int k) {
+    const size_t p = 8 * (size_t)k;
+    return p < s.size() ? s.substr(p, 8) : std::string();
+  };
+  // "0.7354-03" is 0.7354E-03: an exponent sign is the first '+', or the
+  // first '-' that is not the field's leading sign
+  auto real = [](std::string t) {
+    size_t s = t.find('+');
+    if (s != std::string::npos) {
+      t.insert(s, "E");
+    } else if ((s = t.find('-')) != std::string::npos) {
+      if (s != 0) t.insert(s, "E");
+      else if ((s = t.find('-', 1)) != std::string::npos) t.insert(s, "E");
+    }
+    return strtod(t.c_str(), nullptr);
+  };
+  std::map<int, int32_t> pos;
+  for (int64_t q = 0; q < nn; q++) {
+    const std::string& s = lines[first_node + q];
+    pos[atoi(field(s, 1).c_str())] = (int32_t)q;
+    for (int i = 0; i < 3; i++) {
+      const double v = real(field(s, 3 + i));
+      if (nodes) nodes[3 * q + i] = v;
+    }
+  }
+  for (int64_t e = 0; e < ne; e++) {
+    const std::string& s = lines[first_elem + e];
+    for (int k = 0; k < 3; k++) {
+      auto it = pos.find(atoi(field(s, 3 + k).c_str()));
+      if (it == pos.end()) return WF_ERR_ARG;
+      if (tris) tris[3 * e + k] = it->second;
+    }
+  }
+  return ne;
 }
 
 // TriMesh_d::AxisPlaneMesh (src/cuda/Mesh.cu:48-194), the rigid plane main
