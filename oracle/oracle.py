@@ -274,6 +274,7 @@ def ref_lib():
         L.wfr_step.argtypes = [C.c_void_p, C.c_int64]
         L.wfr_get.restype = C.c_int
         L.wfr_get.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_double)]
+        L.wfr_set_hollomon.argtypes = [C.c_void_p] + [C.c_double] * 5
         L.wfr_get_id.restype = C.c_int
         L.wfr_get_id.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
         L.wfr_set_not_write.argtypes = [C.c_void_p, C.POINTER(C.c_uint8)]
@@ -314,8 +315,11 @@ class RefDomain:
         ids = np.ascontiguousarray(ids, dtype=np.int32)
         Tp = None if T is None else _p(np.ascontiguousarray(T, dtype=np.float64))
         self.L.wfr_set_scalars(self.h, h, rho, G, sy, Cs, dt, alpha, beta)
-        self.L.wfr_set_material(self.h, mat.model, mat.E, mat.nu, mat.Et, mat.A, mat.B, mat.n,
-                                mat.C, mat.eps0, mat.m, mat.Tm, mat.Tt)
+        if mat.model == _abi.WF_HOLLOMON:
+            self.L.wfr_set_hollomon(self.h, mat.E, mat.nu, mat.sy0, mat.K_hol, mat.m_hol)
+        else:
+            self.L.wfr_set_material(self.h, mat.model, mat.E, mat.nu, mat.Et, mat.A, mat.B, mat.n,
+                                    mat.C, mat.eps0, mat.m, mat.Tm, mat.Tt)
         self.L.wfr_set_arrays(self.h, _p(x), _p(m), _p(ids, C.c_int32), Tp)
 
     def add_bc(self, zone, v):

@@ -214,6 +214,14 @@ void wfr_set_arrays(void* h, const double* x, const double* m, const int32_t* id
   }
 }
 
+/* the Hollomon power law as the reference initialises it (Material.cuh:48-63) */
+void wfr_set_hollomon(void* h, double E, double nu, double sy0, double K, double m) {
+  RefDom* r = (RefDom*)h;
+  Quiet q;                                     /* InitHollomon printf()s */
+  *r->mat = Material_(Elastic_(E, nu));
+  r->mat->InitHollomon(Elastic_(E, nu), sy0, K, m);
+}
+
 void wfr_add_bc(void* h, int zone, double vx, double vy, double vz) {
   RefDom* r = (RefDom*)h;
   r->bc_zone.push_back(zone);

@@ -82,7 +82,10 @@ def main():
     # 4. Fraser loop, Johnson-Cook material (reference radial return), v_top = -10 m/s
     jc = S.compression_cylinder(material="jc", vz_top=-10.0)
     np.savez_compressed(os.path.join(HERE, "fraser_jc.npz"), **run_fraser(jc, [300]))
-    # 5. contact: the small cylinder compressed by a rigid plane at -10 m/s
+    # 5. Hollomon power law (reference radial return), v_top = -10 m/s
+    ho = S.compression_cylinder(material="hollomon", vz_top=-10.0)
+    np.savez_compressed(os.path.join(HERE, "fraser_hollomon.npz"), **run_fraser(ho, [300]))
+    # 6. contact: the small cylinder compressed by a rigid plane at -10 m/s
     #    (surface tagging, contact lists, penalty law with friction, mesh motion)
     ct = S.contact_cylinder(R=0.0025, H=0.005, dens=6, mu=(0.3, 0.2))
     np.savez_compressed(os.path.join(HERE, "fraser_contact.npz"),

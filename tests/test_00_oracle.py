@@ -53,11 +53,12 @@ def test_neighbors_config1_digest():
     assert cnt.max() == 56 and cnt.max() <= _abi.WF_MAX_NEIGHBORS
 
 
-@pytest.mark.parametrize("case,checkpoints", [("bilinear", [1, 600, 1500]), ("jc", [300])])
+@pytest.mark.parametrize("case,checkpoints", [("bilinear", [1, 600, 1500]), ("jc", [300]),
+                                              ("hollomon", [300])])
 def test_fraser_loop_matches_reference_bitwise(case, checkpoints):
     g = np.load(os.path.join(GOLDEN, "fraser_%s.npz" % case))
     sc = (S.compression_cylinder() if case == "bilinear"
-          else S.compression_cylinder(material="jc", vz_top=-10.0))
+          else S.compression_cylinder(material=case, vz_top=-10.0))
     d = _oracle(sc)
     done = 0
     for k in checkpoints:

@@ -32,6 +32,12 @@ def compression_cylinder(R=0.0025, H=0.005, dx=0.0005, generator="reference", vz
         mat = _abi.WfMaterial(model=_abi.WF_BILINEAR, E=E, nu=nu, sy0=300e6, Et=700e6)
         sy = 300e6
         T0 = 20.0
+    elif material == "hollomon":   # power law K (eps + eps0)^m with a plateau at sy0
+        E, nu = 70e9, 0.33
+        mat = _abi.WfMaterial(model=_abi.WF_HOLLOMON, E=E, nu=nu, sy0=300e6, K_hol=500e6,
+                              m_hol=0.2)
+        sy = 300e6
+        T0 = 20.0
     else:  # Johnson-Cook, BASELINE config 3 constants (aluminium)
         E, nu = 70e9, 0.33
         mat = _abi.WfMaterial(model=_abi.WF_JOHNSON_COOK, E=E, nu=nu, sy0=324e6, A=324e6,
