@@ -206,6 +206,14 @@ int64_t wf_gen_cylinder(double x0, double y0, double z0, double Rxy, double Lz, 
 /* Domain::AddBoxLength, cubic packing (src/Domain.cpp:296-338) */
 int64_t wf_gen_box(double x0, double y0, double z0, double Lx, double Ly, double Lz, double r,
                    double density, double* x, double* mass);
+/* Domain::AddCylUniformLength (src/Domain.cpp:1071-1192), the reference's
+ * "Cylindrical" grid: rings of ceil(ang ri / 2r) particles at radii r_i,
+ * r_i + 2r, ... < Rxy in rows z = r, 3r, ... (axis z, base z = 0); ids
+ * `tag`, 2 / 3 on the first / last `rows` of a slice (ang < 2 pi), 4 on the
+ * axis; *mass = pi Rxy^2 Lz density / count.  Two-call protocol. */
+int64_t wf_gen_cylinder_uniform(double Rxy, double Lz, double r, double density, double ang,
+                                int rows, double r_i, int32_t tag, double* x, int32_t* ids,
+                                double* mass);
 /* Cubic lattice of spacing dx clipped to a cylinder (axis z, base z = 0),
  * jittered by U[-jitter, jitter]*dx per coordinate from a splitmix64 stream;
  * no reference counterpart (synthetic benchmark workload). */

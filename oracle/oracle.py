@@ -200,6 +200,21 @@ def gen_box_cubic(start, dims, r, density):
     return x.reshape(n, 3), m.value
 
 
+def gen_cylinder_uniform(Rxy, Lz, r, density, ang=2.0 * np.pi, rows=1, r_i=0.0, tag=0):
+    """AddCylUniformLength restated: (x[n,3], ids[n], mass)."""
+    L = lib()
+    fn = L.wfo_gen_cylinder_uniform
+    fn.restype = C.c_int64
+    fn.argtypes = [C.c_double] * 5 + [C.c_int, C.c_double, C.c_int32, C.POINTER(C.c_double),
+                                      C.POINTER(C.c_int32), C.POINTER(C.c_double)]
+    m = C.c_double()
+    n = fn(Rxy, Lz, r, density, ang, rows, r_i, tag, None, None, C.byref(m))
+    x = np.empty(3 * n)
+    ids = np.empty(n, np.int32)
+    fn(Rxy, Lz, r, density, ang, rows, r_i, tag, _p(x), _p(ids, C.c_int32), C.byref(m))
+    return x.reshape(n, 3), ids, m.value
+
+
 def gen_cylinder_lattice(R, H, dx, jitter, seed):
     L_ = lib()
     n = L_.wfo_gen_cylinder_lattice(R, H, dx, jitter, seed, None)

@@ -1516,6 +1516,45 @@ static inline uint64_t splitmix64(uint64_t* s) {
 }
 static inline double u01(uint64_t* s) { return (double)(splitmix64(s) >> 11) * (1.0 / 9007199254740992.0); }
 
+/* Domain::AddCylUniformLength (Domain.cpp:1071-1192): rings of ceil(ang ri/2r)
+ * particles at radii r_i, r_i + 2r, ... < Rxy, rows z = r, 3r, ... <= Lz;
+ * mass pi Rxy^2 Lz density / count */
+int64_t wfo_gen_cylinder_uniform(double Rxy, double Lz, double r, double density, double ang,
+                                 int rows, double r_i, int32_t tag, double* x, int32_t* ids,
+                                 double* mass) {
+  if (!(r > 0.0) || !(Rxy > 0.0) || !(Lz > 0.0) || !(ang > 0.0)) return -1;
+  const double z0 = r;
+  int64_t cnt = 0;
+  double zp = z0;
+  while (zp <= (z0 + Lz - r)) {
+    for (double ri = r_i; ri < Rxy; ri += 2. * r) {
+      int tgcount;
+      double dalpha;
+      if (ri == 0.) { tgcount = 1; dalpha = 0.; }
+      else { tgcount = (int)ceil((ang * ri) / (2. * r)); dalpha = ang / (tgcount); }
+      for (int alphai = 0; alphai < tgcount; alphai++) {
+        int32_t id = tag;
+        if (ang < 2.0 * WFO_PI) {
+          if (alphai < rows) id = 2;
+          else if (alphai > tgcount - 1 - rows) id = 3;
+        }
+        double xp = ri * cos(alphai * dalpha);
+        double yp = ri * sin(alphai * dalpha);
+        if ((fabs(xp) < r / 10) && (fabs(yp) < r / 10)) id = 4;
+        if (x) { x[3 * cnt] = xp; x[3 * cnt + 1] = yp; x[3 * cnt + 2] = zp; }
+        if (ids) ids[cnt] = id;
+        cnt++;
+      }
+    }
+    zp += 2.0 * r;
+  }
+  if (mass && cnt > 0) {
+    double Vol = WFO_PI * Rxy * Rxy * Lz;
+    *mass = Vol * density / (double)cnt;
+  }
+  return cnt;
+}
+
 int64_t wfo_gen_cylinder_lattice(double R, double H, double dx, double jitter, uint64_t seed,
                                  double* x) {
   int64_t cnt = 0;

@@ -89,6 +89,9 @@ int64_t wfo_gen_box_cubic(double x0, double y0, double z0, double Lx, double Ly,
                           double r, double density, double* x, double* mass);
 /* Cubic lattice of spacing dx inside a cylinder (axis z, base at z0), with
  * seeded uniform jitter of +-jitter*dx per coordinate (splitmix64). */
+int64_t wfo_gen_cylinder_uniform(double Rxy, double Lz, double r, double density, double ang,
+                                 int rows, double r_i, int32_t tag, double* x, int32_t* ids,
+                                 double* mass);
 int64_t wfo_gen_cylinder_lattice(double R, double H, double dx, double jitter,
                                  uint64_t seed, double* x);
 /* Domain::AssignZone (src/Domain.cpp:989-1005): returns the count tagged. */

@@ -94,6 +94,18 @@ def test_generators_match_between_oracle_and_library():
     c1 = P.assign_zone(l1, (-1, -1, -1), (1, 1, 0.001), 2, ids1, nw1)
     c2 = O.assign_zone(l2, (-1, -1, -1), (1, 1, 0.001), 2, ids2, nw2)
     assert c1 == c2 > 0 and np.array_equal(ids1, ids2) and np.array_equal(nw1, nw2)
+    # the "Cylindrical" grid: full cylinder and a pi/16 slice with its side ids
+    for ang, rows, ri in ((2.0 * np.pi, 1, 0.0), (np.pi / 16.0, 1, 0.0025)):
+        u1 = P.gen_cylinder_uniform(0.005, 0.004, 0.00025, 2700.0, ang, rows, ri)
+        u2 = O.gen_cylinder_uniform(0.005, 0.004, 0.00025, 2700.0, ang, rows, ri)
+        assert np.array_equal(u1[0], u2[0]) and np.array_equal(u1[1], u2[1]) and u1[2] == u2[2]
+        n = len(u1[0])
+        assert u1[2] == np.pi * 0.005 * 0.005 * 0.004 * 2700.0 / n    # Domain.cpp:1171-1173
+        assert np.allclose(np.unique(np.round(u1[0][:, 2] / 0.00025)), np.arange(1, 16, 2))
+        if ang < 2.0 * np.pi:
+            assert {2, 3} <= set(u1[1].tolist())
+        else:
+            assert set(u1[1].tolist()) == {0, 4} and (u1[1] == 4).sum() == 8   # axis
     for positive in (0, 1):
         m1 = P.gen_plane_mesh(2, positive, (-0.003, -0.003, 0.006), (0.003, 0.003, 0.006), 7)
         m2 = O.gen_plane_mesh(2, positive, (-0.003, -0.003, 0.006), (0.003, 0.003, 0.006), 7)

@@ -76,6 +76,10 @@ def test_json_driver_rejects_bad_inputs_before_any_gpu_work(tmp_path, has_gpu):
                    ' "valueType": 1}]}')
     assert L.wf_run_json(str(amp).encode(), None, err, 512) == -1
     assert b"amplitude" in err.value
+    sl = tmp_path / "slice.json"        # main's default sliceAngle (2.0000001 pi): a slice
+    sl.write_text(amp.read_text().replace('"Box"', '"Cylinder", "gridCoordSys": "Cylindrical"'))
+    assert L.wf_run_json(str(sl).encode(), None, err, 512) == -1
+    assert b"axisymmetric" in err.value
     if not has_gpu:   # a complete input is parsed, then the domain needs the GPU
         good = tmp_path / "good.json"
         good.write_text(amp.read_text().replace('"valueType": 1', '"valueType": 0'))

@@ -124,6 +124,35 @@ def test_json_driver_matches_api_and_writes_reference_csv(tmp_path):
     assert (out2 / "test.csv").read_bytes() == (out / "test.csv").read_bytes()
 
 
+def test_json_driver_cylindrical_grid(tmp_path):
+    """DomainBlocks Cylinder on the "Cylindrical" grid (AddCylUniformLength)
+    with sliceAngle 2 pi: the particle set of the generator, axis ids kept."""
+    from weldformgpu_gb300.domain import LIB_PATH, lib
+    lib()
+    L = ctypes.CDLL(LIB_PATH)
+    L.wf_run_json.restype = ctypes.c_int
+    L.wf_run_json.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int64]
+    cfg, _ = _inputs()
+    cfg.pop("RigidBodies")
+    cfg.pop("Contact")
+    cfg["DomainBlocks"] = [{"type": "Cylinder", "gridCoordSys": "Cylindrical",
+                            "sliceAngle": 2.0 * math.pi, "start": [0.0, 0.0, 0.0],
+                            "dim": [2 * R, 0.0, H]}]
+    cfg["BoundaryConditions"] = [{"zoneId": 2, "value": [0.0, 0.0, 0.0]}]
+    cfg["Configuration"]["simTime"] = 2.0e-6
+    inp = tmp_path / "cyl.json"
+    inp.write_text(json.dumps(cfg))
+    err = ctypes.create_string_buffer(512)
+    assert L.wf_run_json(str(inp).encode(), str(tmp_path).encode(), err, 512) == 0, err.value
+    x, ids, _ = P.gen_cylinder_uniform(R, H, r, rho)
+    head, rows = _csv(tmp_path / "test.csv")
+    assert rows.shape[0] == len(x)
+    got = rows[:, 0].astype(np.int32)
+    # axis particles keep id 4 unless the bottom zone (z <= 0.4 mm) takes them
+    assert (got == 4).sum() == ((ids == 4) & (x[:, 2] > 0.0004)).sum() > 0
+    assert (got == 2).sum() > 0                                  # the bottom zone
+
+
 def test_json_driver_nastran_rigid_body(tmp_path):
     """RigidBodies type "File": a plane tool written as a fixed-field Nastran
     deck (normal -z from its node order) gives the run the API gives with the

@@ -270,10 +270,25 @@ bool run_input(const Json& root, const std::string& out_dir, const std::string& 
   read_vec3(db, "start", start);
   read_vec3(db, "dim", L);
   std::vector<double> x;
+  std::vector<int32_t> gen_ids;
   double mass = 0.0;
   int64_t ns = 0;
-  if (domtype == "Cylinder") {
-    if (grid != "Cartesian") return run.fail(WF_ERR_ARG, "only the Cartesian cylinder grid is supported");
+  double slice = 2.0000001 * 3.14159265358979323846;   // the reference's default (:307)
+  read_num(db, "sliceAngle", slice);
+  if (domtype == "Cylinder" && grid == "Cylindrical") {
+    // AddCylUniformLength (:336-349): the full cylinder when sliceAngle is
+    // exactly 2 pi; any other angle is main's axisymmetric slice, not built
+    if (slice != 2.0 * 3.14159265358979323846)
+      return run.fail(WF_ERR_ARG, "axisymmetric slices (sliceAngle != 2 pi) are not supported");
+    ns = wf_gen_cylinder_uniform(L[0] / 2.0, L[2], r, rho, slice, 1, 0.0, 0, nullptr, nullptr,
+                                 &mass);
+    if (ns <= 0) return run.fail(WF_ERR_ARG, "the domain block holds no particles");
+    x.resize(3 * (size_t)ns);
+    gen_ids.resize((size_t)ns);
+    wf_gen_cylinder_uniform(L[0] / 2.0, L[2], r, rho, slice, 1, 0.0, 0, x.data(), gen_ids.data(),
+                            &mass);
+  } else if (domtype == "Cylinder") {
+    if (grid != "Cartesian") return run.fail(WF_ERR_ARG, "gridCoordSys must be Cartesian or Cylindrical");
     ns = wf_gen_cylinder(start[0], start[1], start[2], L[0] / 2., L[2], r, rho, nullptr, &mass);
     x.resize(3 * (size_t)ns);
     wf_gen_cylinder(start[0], start[1], start[2], L[0] / 2., L[2], r, rho, x.data(), &mass);
@@ -286,7 +301,7 @@ bool run_input(const Json& root, const std::string& out_dir, const std::string& 
   }
   if (ns <= 0) return run.fail(WF_ERR_ARG, "the domain block holds no particles");
   // DomainZones (:396-412); main then protects every zoned particle (:851-858)
-  std::vector<int32_t> ids((size_t)ns, 0);
+  std::vector<int32_t> ids = gen_ids.empty() ? std::vector<int32_t>((size_t)ns, 0) : gen_ids;
   std::vector<uint8_t> nw((size_t)ns, 0);
   if (zones && zones->kind == Json::ARR)
     for (const Json& z : zones->arr) {

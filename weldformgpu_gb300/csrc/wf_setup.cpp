@@ -139,6 +139,47 @@ int64_t wf_gen_cylinder_lattice(double R, double H, double dx, double jitter, ui
   return cnt;
 }
 
+// Domain::AddCylUniformLength (src/Domain.cpp:1071-1192): rows at z = r,
+// 3r, ... up to Lz - r; in each row, rings at radius r_i, r_i + 2r, ... < Rxy
+// (running sums) of ceil(ang ri / 2r) particles ang / count apart (one at
+// ri = 0).  Ids: `tag`; 2 / 3 on the first / last `rows` of a partial slice
+// (ang < 2 pi); 4 within r/10 of the axis.  Every particle's mass is
+// pi Rxy^2 Lz density / count.  Two-call protocol as wf_gen_cylinder.
+int64_t wf_gen_cylinder_uniform(double Rxy, double Lz, double r, double density, double ang,
+                                int rows, double r_i, int32_t tag, double* x, int32_t* ids,
+                                double* mass) {
+  if (!(r > 0.0) || !(Rxy > 0.0) || !(Lz > 0.0) || !(ang > 0.0)) return -1;
+  const double z0 = r;
+  int64_t cnt = 0;
+  for (double zp = z0; zp <= z0 + Lz - r; zp += 2.0 * r) {
+    for (double ri = r_i; ri < Rxy; ri += 2. * r) {
+      int tg;
+      double dalpha;
+      if (ri == 0.) {
+        tg = 1;
+        dalpha = 0.;
+      } else {
+        tg = (int)ceil((ang * ri) / (2. * r));
+        dalpha = ang / tg;
+      }
+      for (int a = 0; a < tg; a++) {
+        int32_t id = tag;
+        if (ang < 2.0 * kPi) {
+          if (a < rows) id = 2;
+          else if (a > tg - 1 - rows) id = 3;
+        }
+        const double xp = ri * cos(a * dalpha), yp = ri * sin(a * dalpha);
+        if (std::fabs(xp) < r / 10 && std::fabs(yp) < r / 10) id = 4;
+        if (x) { x[3 * cnt] = xp; x[3 * cnt + 1] = yp; x[3 * cnt + 2] = zp; }
+        if (ids) ids[cnt] = id;
+        cnt++;
+      }
+    }
+  }
+  if (mass && cnt > 0) *mass = kPi * Rxy * Rxy * Lz * density / (double)cnt;
+  return cnt;
+}
+
 // Domain::AssignZone (src/Domain.cpp:989-1005): inclusive box test.
 int64_t wf_assign_zone(const double* x, int64_t n, const double* start, const double* end,
                        int32_t zone_id, int32_t* id, uint8_t* not_write) {
