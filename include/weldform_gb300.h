@@ -98,7 +98,17 @@ int wf_set_convection(wf_domain* d, double h_conv, double T_inf); /* h_conv_doub
 /* ---- contact with rigid triangle meshes ---------------------------------
  * friction_sta / friction_dyn (src/WeldFormGPU.cu:631-641, Domain_d.cuh:260)
  * and the contact law: 0 = the reference's penalty law
- * (CalcContactForcesWang, src/cuda/Contact.cu:134-321). */
+ * (CalcContactForcesWang, src/cuda/Contact.cu:134-321); 1 = a law with no
+ * reference counterpart, for tools of many triangles: each solid particle
+ * takes its nearest triangle within h (triangles binned in cells that move
+ * with the tool), the gap to the nearest surface point along the direction
+ * from that point (the face normal for a centre behind the face), penalty
+ * F_n = contact_stiffness * K * contact_dx * (contact_dx/2 - gap), Coulomb
+ * friction -mu_static F_n v_t / max(|v_t|, contact_vreg) and frictional heat
+ * contact_heat_fraction * mu_static F_n |v_t|^2 / max(|v_t|, contact_vreg)
+ * into the particle ("fric_heat", W).  Law 1 needs the option contact_dx and
+ * tools that translate only (angular velocity 0); the solve fails with
+ * WF_ERR_STATE otherwise. */
 int wf_set_contact(wf_domain* d, double mu_static, double mu_dynamic, int law);
 /* A rigid triangle mesh (TriMesh_d, src/cuda/Mesh.cuh:19-54) as main adds it
  * (AddTrimeshParticles + AssignTrimeshAddress + SetMeshVel,
@@ -169,6 +179,9 @@ int wf_get_field(wf_domain* d, const char* name, double* out);
 int wf_get_field_i32(wf_domain* d, const char* name, int32_t* out);
 /* counts[n]; lists[n*WF_MAX_NEIGHBORS], neighbour ids in search order. */
 int wf_get_neighbors(wf_domain* d, int32_t* counts, int32_t* lists);
+/* "time", "step", "is_yielding", "isfirst", "launches", "rebuilds" (neighbour
+ * rebuilds inside the step loop), "newton_iters", "newton_calls", "mlp_used",
+ * "status", "int_energy_sum". */
 int wf_get_scalar(wf_domain* d, const char* name, double* out);
 /* Checkpoint / restart (no reference counterpart: the reference's CSV
  * snapshots are not restartable).  wf_set_field writes a state field in the
@@ -228,6 +241,13 @@ int64_t wf_gen_cylinder_lattice(double R, double H, double dx, double jitter, ui
  * NULL. */
 int64_t wf_gen_plane_mesh(int axis, int positive, const double* p1, const double* p2, int dens,
                           double* nodes, int32_t* tris, double* normals);
+/* Icosphere tool (no reference counterpart: the rigid indenter of the
+ * 2M-particle contact workload): radius R about center[3], the icosahedron
+ * split `level` times (20 * 4^level faces), outward normals; lower_half keeps
+ * the faces at or below center[2].  Returns the face count and *n_nodes;
+ * fills nodes / tris when not NULL. */
+int64_t wf_gen_icosphere(double R, const double* center, int level, int lower_half,
+                         double* nodes, int32_t* tris, int64_t* n_nodes);
 /* NastranReader::read (src/NastranReader.cpp:5-150) + TriMesh_d::
  * ReadFromNastran (src/cuda/Mesh_reader.cu:5-100): fixed-field GRID / CTRIA
  * cards with implicit exponents ("0.7354-03").  Returns the triangle count

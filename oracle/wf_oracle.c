@@ -86,10 +86,17 @@ struct wfo_domain {
   int32_t *cont_cnt, *cont_nb;     /* contneib_count / contneib_part (20 per particle) */
   double mu_s, mu_d;               /* friction_sta / friction_dyn */
   int32_t id_free_surf;            /* 1, set by MechFraserSolve (SolverFraser.cu:118) */
+  /* contact law 1 (no reference counterpart): penalty kappa K dx delta, regularised
+   * Coulomb friction, frictional heat */
+  double c_kappa, c_dx, c_vreg, c_eta;
+  double* qf;                      /* frictional heat into each particle (W) */
+  /* adaptive rebuild: at a plastic-strain increment (0: off) */
+  double rb_dep;
+  double* eps_rb;                  /* plastic strain at the last rebuild */
   /* solver state */
   int started, ts_i, is_yielding, isfirst_step, nb_built;
   double time, t_out, dt_out, max_pl_strain, int_energy_sum;
-  int64_t step, newton_calls, newton_iters, mlp_used;
+  int64_t step, newton_calls, newton_iters, mlp_used, rebuilds;
   char err[256];
 };
 
@@ -703,6 +710,7 @@ static void thermal_rates(wfo_domain* d, double h_conv, int plastic_heat) {
     s *= 1. / (d->rho[i] * d->cp_T[i]);
     if (plastic_heat && i < d->n_solid && d->dep[i] > 0.0)
       s += d->chi * d->sigma_y[i] * d->dep[i] / (d->rho[i] * d->cp_T[i] * d->dt);
+    if (d->qf[i] > 0.0) s += d->qf[i] / (d->m[i] * d->cp_T[i]);   /* frictional heat, law 1 */
     if (d->BC_T[i] == 1) {
       double dS2 = pow(d->m[i] / d->rho[i], 0.666666666);
       double q_conv = h_conv * dS2 * (d->T_inf - d->T[i]) / d->m[i];
@@ -857,6 +865,89 @@ static void stage_contact_forces(wfo_domain* d) {
   }
 }
 
+/* Closest point of triangle abc to p (Ericson, Real-Time Collision
+ * Detection, 5.1.5: Voronoi regions of the vertices, edges and face). */
+static d3 closest_on_tri(d3 p, d3 a, d3 b, d3 c) {
+  const d3 ab = d3_sub(b, a), ac = d3_sub(c, a), ap = d3_sub(p, a);
+  const double d1 = d3_dot(ab, ap), d2 = d3_dot(ac, ap);
+  if (d1 <= 0.0 && d2 <= 0.0) return a;
+  const d3 bp = d3_sub(p, b);
+  const double d3v = d3_dot(ab, bp), d4 = d3_dot(ac, bp);
+  if (d3v >= 0.0 && d4 <= d3v) return b;
+  const double vc = d1 * d4 - d3v * d2;
+  if (vc <= 0.0 && d1 >= 0.0 && d3v <= 0.0) return d3_add(a, d3_scale(ab, d1 / (d1 - d3v)));
+  const d3 cp = d3_sub(p, c);
+  const double d5 = d3_dot(ab, cp), d6 = d3_dot(ac, cp);
+  if (d6 >= 0.0 && d5 <= d6) return c;
+  const double vb = d5 * d2 - d1 * d6;
+  if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) return d3_add(a, d3_scale(ac, d2 / (d2 - d6)));
+  const double va = d3v * d6 - d5 * d4;
+  if (va <= 0.0 && (d4 - d3v) >= 0.0 && (d5 - d6) >= 0.0)
+    return d3_add(b, d3_scale(d3_sub(c, b), (d4 - d3v) / ((d4 - d3v) + (d5 - d6))));
+  const double denom = 1.0 / (va + vb + vc);
+  return d3_add(d3_add(a, d3_scale(ab, vb * denom)), d3_scale(ac, vc * denom));
+}
+
+/* Contact law 1 (the 2M-particle contact workload; no reference
+ * counterpart).  Each solid particle takes the nearest tool triangle whose
+ * closest point lies within h (ties: the first mesh, then the lowest
+ * triangle index); with the gap g = (x - q).n along the face's outward normal
+ * and the penetration delta = dx/2 - g > 0, the normal force is
+ * kappa K dx delta (a pressure kappa K / dx on the particle's face dx^2).
+ * Friction is Coulomb, regularised below the sliding speed v_reg:
+ * F_t = -mu F_n v_t / max(|v_t|, v_reg), v_t the tangential velocity
+ * relative to the tool; eta of the frictional power F_t . v_t heats the
+ * particle. */
+static void stage_contact_law1(wfo_domain* d) {
+  const double K = d->mat.E / (3.0 * (1.0 - 2.0 * d->mat.nu));
+  const double hs = d->h_glob * d->h_glob;
+  const double rc = 0.5 * d->c_dx;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < d->n_solid; i++) {
+    d->contforce[i] = v3(0., 0., 0.);
+    d->qf[i] = 0.0;
+    d->cont_cnt[i] = 0;
+    double best = hs;
+    int bm = -1, be = -1;
+    d3 bq = v3(0., 0., 0.);
+    for (int mi = 0; mi < d->trimesh_count; mi++)
+      for (int e = 0; e < d->mesh[mi].ne; e++) {
+        const int32_t* en = d->mesh[mi].elnode + 3 * e;
+        const d3* nd = d->mesh[mi].node;
+        const d3 q = closest_on_tri(d->x[i], nd[en[0]], nd[en[1]], nd[en[2]]);
+        const d3 dv = d3_sub(d->x[i], q);
+        const double d2 = d3_dot(dv, dv);
+        if (d2 < best) { best = d2; bm = mi; be = e; bq = q; }
+      }
+    if (bm < 0) continue;
+    /* contact normal: from the nearest surface point to the particle (the
+     * face normal inside a face, continuous across edges and vertices); the
+     * face normal and its signed gap for a centre behind the face */
+    const d3 dv = d3_sub(d->x[i], bq);
+    const double dist = sqrt(best);
+    const double gf = d3_dot(dv, d->mesh[bm].normal[be]);
+    d3 n;
+    double g;
+    if (gf >= 0.0 && dist > 0.0) { n = d3_div(dv, dist); g = dist; }
+    else { n = d->mesh[bm].normal[be]; g = gf; }
+    const double delta = rc - g;
+    if (!(delta > 0.0)) continue;
+    const double fn = d->c_kappa * K * d->c_dx * delta;
+    d3 f = d3_scale(n, fn);
+    const d3 vrel = d3_sub(d->v[i], d->mesh[bm].m_v);
+    const d3 vt = d3_sub(vrel, d3_scale(n, d3_dot(vrel, n)));
+    const double vtl = d3_len(vt);
+    if (d->mu_s > 0.0) {
+      const double s = d->mu_s * fn / (vtl > d->c_vreg ? vtl : d->c_vreg);
+      f = d3_sub(f, d3_scale(vt, s));
+      d->qf[i] = d->c_eta * s * vtl * vtl;
+    }
+    d->a[i] = d3_add(d->a[i], d3_div(f, d->m[i]));
+    d->contforce[i] = f;
+    d->cont_cnt[i] = 1;
+  }
+}
+
 /* MeshUpdateKernel (Mesh.cu:24-29): TriMesh_d::Move, CalcCentroids,
  * CalcNormals, UpdatePlaneCoeff.  The reference runs the four in one kernel
  * without a grid-wide barrier, so an element may read nodes before or after
@@ -924,6 +1015,9 @@ static int solve_begin(wfo_domain* d, double dt_out) {
   memcpy(d->x_h, d->x, sizeof(d3) * d->n);             /* :56 */
   rc = nb_search_from(d, d->x_h);                      /* :109 */
   if (rc) return rc;
+  memcpy(d->eps_rb, d->pl_strain, sizeof(double) * d->n);
+  if (d->contact && d->contact_law == 1 && !(d->c_dx > 0.0))
+    return fail(d, WF_ERR_STATE, "contact law 1 needs the option contact_dx");
   for (int64_t i = 0; i < d->n_solid; i++) d->v[i] = v3(0., 0., 0.);   /* SetVelKernel :123 */
   if (d->contact)                                      /* CalcSpheresKernel :129-141 */
     for (int mi = 0; mi < d->trimesh_count; mi++) mesh_plane_coeff(d, mi);
@@ -935,9 +1029,20 @@ static int solve_begin(wfo_domain* d, double dt_out) {
 }
 
 static int solve_step(wfo_domain* d) {
-  if (d->ts_i == 0 && (d->is_yielding || !d->rebuild_after_yield)) {   /* :166 */
+  int rebuild;
+  if (d->rb_dep > 0.0) {    /* adaptive: a plastic-strain increment since the last rebuild */
+    double mx = 0.0;
+    for (int64_t i = 0; i < d->n; i++)
+      if (d->pl_strain[i] - d->eps_rb[i] > mx) mx = d->pl_strain[i] - d->eps_rb[i];
+    rebuild = mx > d->rb_dep;
+  } else {
+    rebuild = d->ts_i == 0 && (d->is_yielding || !d->rebuild_after_yield);   /* :166 */
+  }
+  if (rebuild) {
     int rc = nb_search_from(d, d->rebuild_current ? d->x : d->x_h);
     if (rc) return rc;
+    memcpy(d->eps_rb, d->pl_strain, sizeof(double) * d->n);
+    d->rebuilds++;
   }
   stage_density(d);         /* :193 */
   stage_update_density(d);  /* :201 */
@@ -945,7 +1050,9 @@ static int solve_step(wfo_domain* d) {
   stage_pressure(d);        /* :213 */
   stage_stress(d);          /* :217 */
   stage_accel(d);           /* :221 */
-  if (d->contact) {         /* :233-257 */
+  if (d->contact && d->contact_law == 1) {
+    stage_contact_law1(d);
+  } else if (d->contact) {  /* :233-257 */
     stage_surface(d);
     if (d->ts_i == 0) stage_contact_nb(d);
     stage_contact_forces(d);
@@ -1072,9 +1179,12 @@ int wfo_create(wfo_domain** out, int64_t n) {
   A(dep, n); A(ID, n); A(is_free, n); A(not_write, n);
   A(T, n); A(Ta, n); A(Tb, n); A(dTdt, n); A(k_T, n); A(cp_T, n); A(BC_T, n);
   A(nb_count, n); A(nb, (size_t)n * NBMAX);
-  A(cont_cnt, n); A(cont_nb, (size_t)n * CONT_MAX_NB);
+  A(cont_cnt, n); A(cont_nb, (size_t)n * CONT_MAX_NB); A(qf, n); A(eps_rb, n);
 #undef A
   d->id_free_surf = 1;
+  d->c_kappa = 0.1;
+  d->c_vreg = 1.0e-3;
+  d->c_eta = 1.0;
   for (int64_t i = 0; i < n; i++) d->is_free[i] = 1;
   /* SetDimension resets Alpha = 1, Beta = 0 (Domain_d.cu:191-192) */
   d->alpha = 1.0;
@@ -1102,7 +1212,7 @@ int wfo_destroy(wfo_domain* d) {
                   d->shearstress, d->strain, d->sigma_eq, d->pl_strain, d->sigma_y,
                   d->eff_strain_rate, d->int_energy, d->dep, d->ID, d->is_free, d->not_write,
                   d->T, d->Ta, d->Tb, d->dTdt, d->k_T, d->cp_T, d->BC_T, d->nb_count, d->nb,
-                  d->cont_cnt, d->cont_nb};
+                  d->cont_cnt, d->cont_nb, d->qf, d->eps_rb};
   for (size_t k = 0; k < sizeof ptrs / sizeof ptrs[0]; k++) free(ptrs[k]);
   for (int mi = 0; mi < d->trimesh_count; mi++) {
     free(d->mesh[mi].node); free(d->mesh[mi].node_v); free(d->mesh[mi].centroid);
@@ -1221,6 +1331,11 @@ int wfo_set_option(wfo_domain* d, const char* key, double v) {
   else if (!strcmp(key, "output_interval")) d->output_interval = v;
   else if (!strcmp(key, "clamp_homologous")) d->clamp_homologous = v != 0.0;
   else if (!strcmp(key, "mlp")) d->mlp_on = v != 0.0;
+  else if (!strcmp(key, "contact_stiffness")) d->c_kappa = v;
+  else if (!strcmp(key, "contact_dx")) d->c_dx = v;
+  else if (!strcmp(key, "contact_vreg")) d->c_vreg = v;
+  else if (!strcmp(key, "contact_heat_fraction")) d->c_eta = v;
+  else if (!strcmp(key, "rebuild_strain_increment")) d->rb_dep = v;
   else if (!strcmp(key, "precision") || !strcmp(key, "profile_kernel") || !strcmp(key, "graph") ||
            !strcmp(key, "fuse_heat")) {
     /* GPU-only switches: accepted and ignored by the FP64 oracle */
@@ -1231,7 +1346,11 @@ int wfo_set_option(wfo_domain* d, const char* key, double v) {
 /* friction_sta / friction_dyn (WeldFormGPU.cu:640-641) and the contact law
  * (0: the reference's penalty law, CalcContactForcesWang) */
 int wfo_set_contact(wfo_domain* d, double mu_static, double mu_dynamic, int law) {
-  if (!d || law != 0 || !(mu_static >= 0.0) || !(mu_dynamic >= 0.0)) return WF_ERR_ARG;
+  if (!d || law < 0 || law > 1 || !(mu_static >= 0.0) || !(mu_dynamic >= 0.0)) return WF_ERR_ARG;
+  if (law == 1)
+    for (int mi = 0; mi < d->trimesh_count; mi++)
+      if (d->mesh[mi].m_w.x != 0.0 || d->mesh[mi].m_w.y != 0.0 || d->mesh[mi].m_w.z != 0.0)
+        return fail(d, WF_ERR_ARG, "contact law 1 takes translating tools only");
   d->mu_s = mu_static;
   d->mu_d = mu_dynamic;
   d->contact_law = law;
@@ -1350,6 +1469,7 @@ static const double* field_ptr(wfo_domain* d, const char* name, int* comps) {
   if (!strcmp(name, "u")) { *comps = 3; return (double*)d->u; }
   if (!strcmp(name, "normal")) { *comps = 3; return (double*)d->normal; }
   if (!strcmp(name, "contforce")) { *comps = 3; return (double*)d->contforce; }
+  if (!strcmp(name, "fric_heat")) return d->qf;
   if (!strcmp(name, "sigma")) { *comps = 6; return d->sigma; }
   if (!strcmp(name, "strrate")) { *comps = 6; return d->strrate; }
   if (!strcmp(name, "rotrate")) { *comps = 6; return d->rotrate; }
@@ -1421,6 +1541,7 @@ int wfo_get_scalar(wfo_domain* d, const char* name, double* out) {
   else if (!strcmp(name, "newton_calls")) *out = (double)d->newton_calls;
   else if (!strcmp(name, "newton_iters")) *out = (double)d->newton_iters;
   else if (!strcmp(name, "mlp_used")) *out = (double)d->mlp_used;
+  else if (!strcmp(name, "rebuilds")) *out = (double)d->rebuilds;
   else if (!strcmp(name, "totmass")) *out = d->totmass;
   else return fail(d, WF_ERR_ARG, "unknown scalar");
   return WF_OK;

@@ -133,6 +133,55 @@ def test_contact_matches_reference_bitwise():
     assert d.get_field("pl_strain").max() > 0.1
 
 
+# Contact law 1 known answers: one particle and one triangle (normal -z at
+# z = 4e-4, dx = 1e-3, contact radius dx/2): x0, the tool velocity and the
+# nearest point on the triangle.
+TRI = [(-0.01, -0.01, 4e-4), (-0.01, 0.01, 4e-4), (0.01, -0.01, 4e-4)]
+LAW1_CASES = {
+    "face": ((-0.002, -0.002, 0.0), (-2.0, 0.0, -5.0), (-0.002, -0.002, 4e-4)),
+    "beyond_edge": ((-0.0102, 0.0, 1e-4), (-2.0, -1.0, -5.0), (-0.01, 0.0, 4e-4)),
+    "slow_slide": ((-0.002, -0.002, 0.0), (0.0, -4e-4, 0.0), (-0.002, -0.002, 4e-4)),
+    "behind_face": ((-0.002, -0.002, 5e-4), (-1.0, 0.0, -5.0), (-0.002, -0.002, 4e-4)),
+    "out_of_range": ((-0.002, -0.002, -2e-4), (-2.0, 0.0, -5.0), (-0.002, -0.002, 4e-4)),
+}
+
+
+def law1_one_step(make_domain, case):
+    x0, v_tool, q = LAW1_CASES[case]
+    sc, expected = S.one_particle_under_triangle(x0, TRI, v_tool)
+    d = S.load(make_domain(sc["n"]), sc)
+    d.step(1)
+    return d, sc, expected(q)
+
+
+def check_law1_closed_form(d, sc, exp):
+    f, qf, n = exp
+    m, dt = sc["m"][0], sc["dt"]
+    got = d.get_field("contforce")[0]
+    np.testing.assert_allclose(got, f, rtol=1e-12, atol=1e-12 * max(1.0, np.abs(f).max()))
+    np.testing.assert_allclose(d.get_field("fric_heat")[0], qf, rtol=1e-12, atol=1e-300)
+    assert d.get_field_i32("cont_count")[0] == (1 if np.abs(f).max() > 0 else 0)
+    np.testing.assert_allclose(d.get_field("v")[0], f / m * dt, rtol=1e-14, atol=1e-300)
+    np.testing.assert_allclose(d.get_field("dTdt")[0], qf / (m * 896.0), rtol=1e-12,
+                               atol=1e-300)
+
+
+@pytest.mark.parametrize("case", sorted(LAW1_CASES))
+def test_contact_law1_known_answers(case):
+    """Penalty 0.1 K dx delta along the nearest-point normal (the face normal
+    for a centre behind the face), regularised Coulomb friction and its heat,
+    against the closed form for one particle under one triangle."""
+    d, sc, exp = law1_one_step(O.OracleDomain, case)
+    check_law1_closed_form(d, sc, exp)
+    f, qf, n = exp
+    if case == "beyond_edge":
+        assert abs(n[2]) < 0.9 and abs(n[0]) > 0.5           # the edge normal, not the face's
+    if case == "out_of_range":
+        assert not f.any() and qf == 0.0
+    else:
+        assert np.abs(f).max() > 0.0 and qf > 0.0
+
+
 def test_jc_yield_table_and_newton_residual():
     """KATs: JC sigma_y from the formula; Newton converges to 1e-10 relative."""
     sc = S.compression_cylinder(material="jc", vz_top=-10.0)

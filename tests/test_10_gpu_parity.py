@@ -241,6 +241,60 @@ def test_contact_mixed_with_friction_within_fp64_sensitivity():
         assert err < max(1e-3, 3.0 * spread), (f, err, spread)
 
 
+@pytest.mark.parametrize("case", ["beyond_edge", "behind_face", "face", "out_of_range",
+                                  "slow_slide"])
+def test_contact_law1_known_answers_gpu(case):
+    """Contact law 1 for one particle under one triangle: the closed form, and
+    the oracle bit for bit."""
+    from weldformgpu_gb300 import Domain_d
+    from tests.test_00_oracle import check_law1_closed_form, law1_one_step
+    g, sc, exp = law1_one_step(Domain_d, case)
+    check_law1_closed_form(g, sc, exp)
+    o = law1_one_step(O.OracleDomain, case)[0]
+    for f in ("x", "v", "contforce", "fric_heat", "dTdt"):
+        assert np.array_equal(g.get_field(f), o.get_field(f)), f
+    assert np.array_equal(g.get_field_i32("cont_count"), o.get_field_i32("cont_count"))
+
+
+LAW1_FIELDS = ("x", "u", "v", "pl_strain", "sigma_eq", "contforce", "fric_heat")
+
+
+def test_contact_law1_fp64_vs_oracle_with_adaptive_rebuild():
+    """Block (12,288 particles) indented by a lower-half icosphere (656
+    triangles) at -5 m/s: contact law 1 with friction and frictional heat, JC
+    Newton, heat conduction, neighbour rebuild at a plastic-strain increment of
+    0.002 (11 rebuilds in 600 steps).  Plain FP64 against the oracle: 1e-9
+    (pow/log of JC and the heat terms may differ in the last bit), the same
+    rebuild steps and the same contact set."""
+    sc = S.indent_block(rebuild_increment=0.002)
+    o, g = ora(sc), gpu(sc)
+    for d in (o, g):
+        d.step(600)
+    nrb = g.get_scalar("rebuilds")
+    assert nrb == o.get_scalar("rebuilds") and nrb >= 5
+    for f in LAW1_FIELDS:
+        err = rel_l2(g.get_field(f), o.get_field(f))
+        assert err < 1e-9, (f, err)
+    assert rel_l2(g.get_field("T") - 20.0, o.get_field("T") - 20.0) < 1e-9
+    assert np.array_equal(g.get_field_i32("cont_count"), o.get_field_i32("cont_count"))
+    assert (g.get_field_i32("cont_count") > 0).sum() >= 10
+    assert g.get_field("T").max() > 30.0                 # frictional and plastic heating
+
+
+def test_contact_law1_mixed_within_1e3():
+    """Mixed form against plain FP64 on the icosphere indentation (law 1 is
+    well conditioned: a 1e-12 relative change of the positions moves the
+    contact forces by ~4e-9 after 300 steps): 1e-3 per field."""
+    sc = S.indent_block(rebuild_increment=0.002)
+    g64, gm = gpu(sc), gpu(sc, {"precision": 1})
+    for d in (g64, gm):
+        d.step(600)
+    for f in ("u", "pl_strain", "sigma_eq", "contforce", "fric_heat"):
+        err = rel_l2(gm.get_field(f), g64.get_field(f))
+        assert err < 1e-3, (f, err)
+    assert rel_l2(gm.get_field("T") - 20.0, g64.get_field("T") - 20.0) < 1e-3
+
+
 def test_mixed_fused_heat_matches_separate_heat_pass():
     """Mixed form: the heat pass fused into the next step's density pass gives
     the temperatures of the separate heat pass (to FP32 rounding), including

@@ -81,6 +81,14 @@ struct wf_domain {
   int contact_law = 0;
   std::vector<double> h_mass;      // masses in caller order (totmass, rigid particles)
   int32_t *cnb = nullptr, *ccnt = nullptr;
+  // contact law 1 constants; tool bins built at the first solve
+  double c_kappa = 0.1, c_dx = 0.0, c_vreg = 1.0e-3, c_eta = 1.0;
+  bool bins_built = false;
+  // adaptive rebuild at a plastic-strain increment (0: the reference's cadence)
+  double rb_dep = 0.0;
+  int64_t rebuilds = 0;         // neighbour rebuilds inside the step loop
+  unsigned long long* d_maxdep = nullptr;
+  unsigned long long* h_maxdep = nullptr;
   // MechFraserSolve's CSV snapshots (out_<time>.csv), when a prefix is set
   bool csv_on = false;
   std::string csv_prefix;
@@ -208,6 +216,27 @@ __global__ void k_place_rigid(int32_t ne, int32_t first, const int32_t* inv,
   F.id[s] = zone;
   F.nrm[s] = normal[e];
 }
+// the largest plastic-strain increment since the last rebuild: non-negative
+// doubles order like their bit patterns, so one 64-bit atomicMax per warp
+__global__ void k_max_dep(int64_t n, const double* eps, const double* eps_rb,
+                          unsigned long long* out) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double v = 0.0;
+  if (i < n) {
+    v = eps[i] - eps_rb[i];
+    if (!(v > 0.0)) v = 0.0;
+  }
+  unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long c = __shfl_xor_sync(0xffffffffu, b, o);
+    b = c > b ? c : b;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(out, b);
+}
+__global__ void k_copy_d(int64_t n, const double* src, double* dst) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[i];
+}
 inline int nblk(int64_t n, int t = 256) { return (int)((n + t - 1) / t); }
 }  // namespace
 
@@ -247,7 +276,7 @@ static void free_fields(Fields& F) {
   void* ptrs[] = {F.xm, F.vd, F.u, F.a, F.sig6, F.ss6, F.eps6, F.sr6, F.rr6, F.p, F.seq, F.eps_p,
                   F.sy, F.eff, F.dep, F.drho, F.eint, F.T, F.Ta, F.Tb, F.dTdt, F.kT, F.cpT,
                   F.id, F.bct, F.perm, F.nw, F.xh, F.p32, F.v32, F.ss32, F.th32, F.pwn,
-                  F.nrm, F.cf};
+                  F.nrm, F.cf, F.qf, F.eps_rb};
   for (void* p : ptrs) if (p) cudaFree(p);
   F = Fields{};
 }
@@ -286,6 +315,12 @@ static StepParams make_params(const wf_domain* d) {
   }
   P.mu_s = d->mu_s;
   P.mu_d = d->mu_d;
+  P.contact_law = d->contact_law;
+  P.c_kappa = d->c_kappa;
+  P.c_dx = d->c_dx;
+  P.c_vreg = d->c_vreg;
+  P.c_eta = d->c_eta;
+  P.Kbulk = d->mat.E / (3.0 * (1.0 - 2.0 * d->mat.nu));
   P.totmass = d->totmass;
   P.id_free_surf = 1;              // MechFraserSolve, SolverFraser.cu:118
   P.cnb = d->cnb;
@@ -420,8 +455,87 @@ static int rebuild(wf_domain* d, bool use_current) {
   d->cur = 1 - d->cur;
   launch_nblist(n, d->npad, d->pf2, d->grid, d->cell_count, d->nb, d->nbc, d->d_status, s);
   d->launches += 8;
+  if (d->F[d->cur].eps_rb) {       // adaptive rebuild: the strain this list was built at
+    k_copy_d<<<nblk(n), 256, 0, s>>>(n, d->F[d->cur].eps_p, d->F[d->cur].eps_rb);
+    d->launches += 1;
+  }
   WF_CUDA_OK(cudaGetLastError());
   d->nb_built = true;
+  return WF_OK;
+}
+
+// The triangles of each tool binned once in the tool's frame as it stands
+// now (contact law 1): cells of 2h over the tool's box grown by h, each
+// triangle listed in every cell its box grown by h touches (ascending
+// triangle index within a cell), so every triangle within h of a point is
+// listed in the point's cell.
+static int build_tool_bins(wf_domain* d) {
+  const double cs = 2.0 * d->h, margin = d->h * (1.0 + 1e-6) + 1e-12;
+  for (MeshDev& M : d->meshes) {
+    std::vector<double4> nd(M.nn);
+    std::vector<int32_t> en(3 * (size_t)M.ne);
+    WF_CUDA_OK(cudaMemcpyAsync(nd.data(), M.node, sizeof(double4) * M.nn, cudaMemcpyDeviceToHost, d->stream));
+    WF_CUDA_OK(cudaMemcpyAsync(en.data(), M.elnode, sizeof(int32_t) * 3 * M.ne, cudaMemcpyDeviceToHost, d->stream));
+    WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (const double4& p : nd) {
+      const double c[3] = {p.x, p.y, p.z};
+      for (int k = 0; k < 3; k++) { lo[k] = std::min(lo[k], c[k]); hi[k] = std::max(hi[k], c[k]); }
+    }
+    int64_t ncell = 1;
+    for (int k = 0; k < 3; k++) {
+      M.gmin[k] = lo[k] - margin - cs;
+      M.dims[k] = (int32_t)std::ceil((hi[k] + margin + cs - M.gmin[k]) / cs) + 1;
+      ncell *= M.dims[k];
+    }
+    if (ncell > (int64_t)64 << 20) return wf_fail(d, WF_ERR_ARG, "tool bin grid too large");
+    M.cs = cs;
+    M.org[0] = nd[0].x; M.org[1] = nd[0].y; M.org[2] = nd[0].z;
+    std::vector<int32_t> start((size_t)ncell + 1, 0), list;
+    auto range = [&](int e, int r0[3], int r1[3]) {
+      for (int k = 0; k < 3; k++) {
+        double a = 1e300, b = -1e300;
+        for (int q = 0; q < 3; q++) {
+          const double4& p = nd[en[3 * e + q]];
+          const double c = k == 0 ? p.x : (k == 1 ? p.y : p.z);
+          a = std::min(a, c);
+          b = std::max(b, c);
+        }
+        r0[k] = std::max(0, (int)std::floor((a - margin - M.gmin[k]) / cs));
+        r1[k] = std::min(M.dims[k] - 1, (int)std::floor((b + margin - M.gmin[k]) / cs));
+      }
+    };
+    for (int pass = 0; pass < 2; pass++) {
+      std::vector<int32_t> fill;
+      if (pass == 1) {
+        for (int64_t c = 0; c < ncell; c++) start[c + 1] += start[c];
+        list.resize(start[ncell]);
+        fill.assign(start.begin(), start.end() - 1);
+      }
+      for (int e = 0; e < M.ne; e++) {
+        int r0[3], r1[3];
+        range(e, r0, r1);
+        for (int z = r0[2]; z <= r1[2]; z++)
+          for (int y = r0[1]; y <= r1[1]; y++)
+            for (int x = r0[0]; x <= r1[0]; x++) {
+              const int64_t c = ((int64_t)z * M.dims[1] + y) * M.dims[0] + x;
+              if (pass == 0) start[c + 1]++;
+              else list[fill[c]++] = e;
+            }
+      }
+    }
+    if (M.cstart) cudaFree(M.cstart);
+    if (M.ctri) cudaFree(M.ctri);
+    M.cstart = nullptr;
+    M.ctri = nullptr;
+    if (dalloc(&M.cstart, ncell + 1, d->stream) || dalloc(&M.ctri, std::max<int64_t>(1, (int64_t)list.size()), d->stream))
+      return wf_fail(d, WF_ERR_ALLOC, "tool bins");
+    WF_CUDA_OK(cudaMemcpyAsync(M.cstart, start.data(), sizeof(int32_t) * (ncell + 1), cudaMemcpyHostToDevice, d->stream));
+    if (!list.empty())
+      WF_CUDA_OK(cudaMemcpyAsync(M.ctri, list.data(), sizeof(int32_t) * list.size(), cudaMemcpyHostToDevice, d->stream));
+    WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+  }
+  d->bins_built = true;
   return WF_OK;
 }
 
@@ -479,6 +593,17 @@ static int solve_begin(wf_domain* d, double dt_out) {
     d->totmass = 0.0;                              // WeldFormGPU.cu:808-820, in index order
     for (double mm : d->h_mass) d->totmass += mm;
     launch_mesh_plane(make_params(d), d->stream);  // CalcSpheresKernel, :129-141
+    if (d->contact_law == 1) {
+      if (!(d->c_dx > 0.0)) return wf_fail(d, WF_ERR_STATE, "contact law 1 needs the option contact_dx");
+      // the triangle bins follow the tool by translation only
+      for (const MeshDev& M : d->meshes)
+        if (M.mw[0] != 0.0 || M.mw[1] != 0.0 || M.mw[2] != 0.0)
+          return wf_fail(d, WF_ERR_STATE, "contact law 1 takes translating tools only (angular velocity 0)");
+      if (!d->bins_built) {
+        rc = build_tool_bins(d);
+        if (rc) return rc;
+      }
+    }
   }
   if (d->precision == 1) k_mixed_init<<<nblk(d->n), 256, 0, d->stream>>>(d->n, d->F[d->cur]);
   WF_CUDA_OK(cudaGetLastError());
@@ -489,9 +614,27 @@ static int solve_begin(wf_domain* d, double dt_out) {
 
 static int solve_step(wf_domain* d) {
   cudaStream_t s = d->stream;
-  if (d->ts_i == 0 && (d->is_yielding || !d->rebuild_after_yield)) {   // :166-182
+  bool rb;
+  if (d->rb_dep > 0.0) {
+    // adaptive: rebuild once the plastic strain grew by rb_dep anywhere since
+    // the last rebuild (one device reduction and a 8-byte read per step)
+    const Fields& F0 = d->F[d->cur];
+    WF_CUDA_OK(cudaMemsetAsync(d->d_maxdep, 0, sizeof(unsigned long long), s));
+    k_max_dep<<<nblk(d->n), 256, 0, s>>>(d->n, F0.eps_p, F0.eps_rb, d->d_maxdep);
+    WF_CUDA_OK(cudaMemcpyAsync(d->h_maxdep, d->d_maxdep, sizeof(unsigned long long),
+                               cudaMemcpyDeviceToHost, s));
+    WF_CUDA_OK(cudaStreamSynchronize(s));
+    double mx;
+    memcpy(&mx, d->h_maxdep, sizeof mx);
+    d->launches += 1;
+    rb = mx > d->rb_dep;
+  } else {
+    rb = d->ts_i == 0 && (d->is_yielding || !d->rebuild_after_yield);   // :166-182
+  }
+  if (rb) {
     int rc = rebuild(d, d->rebuild_current != 0);
     if (rc) return rc;
+    d->rebuilds++;
   }
   StepParams P = make_params(d);
   const Fields& F = d->F[d->cur];
@@ -627,9 +770,11 @@ int wf_destroy(wf_domain* d) {
   if (d->stream) cudaStreamSynchronize(d->stream);
   for (int k = 0; k < 2; k++) free_fields(d->F[k]);
   for (MeshDev& M : d->meshes) {
-    void* mp[] = {M.node, M.node_v, M.centroid, M.normal, M.elnode, M.pplane};
+    void* mp[] = {M.node, M.node_v, M.centroid, M.normal, M.elnode, M.pplane, M.cstart, M.ctri};
     for (void* p : mp) if (p) cudaFree(p);
   }
+  if (d->d_maxdep) cudaFree(d->d_maxdep);
+  if (d->h_maxdep) cudaFreeHost(d->h_maxdep);
   if (d->cnb) cudaFree(d->cnb);
   if (d->ccnt) cudaFree(d->ccnt);
   void* ptrs[] = {d->vd2, d->v32b, d->a32, d->sigr32, d->mlp_w, d->mlp_packed, d->log_x,
@@ -779,9 +924,18 @@ int wf_set_csv_output(wf_domain* d, const char* prefix) {
 
 int wf_set_contact(wf_domain* d, double mu_static, double mu_dynamic, int law) {
   if (!d) return WF_ERR_ARG;
-  if (law != 0) return wf_fail(d, WF_ERR_ARG, "contact law must be 0 (the reference's penalty law)");
+  if (law != 0 && law != 1)
+    return wf_fail(d, WF_ERR_ARG, "contact law must be 0 (the reference's) or 1 (binned triangles)");
   if (!(mu_static >= 0.0) || !(mu_dynamic >= 0.0))
     return wf_fail(d, WF_ERR_ARG, "friction coefficients must be >= 0");
+  if (law == 1) {
+    for (const MeshDev& M : d->meshes)
+      if (M.mw[0] != 0.0 || M.mw[1] != 0.0 || M.mw[2] != 0.0)
+        return wf_fail(d, WF_ERR_ARG, "contact law 1 takes translating tools only");
+    if (!d->F[0].qf)
+      for (int f = 0; f < 2; f++)
+        if (dalloc(&d->F[f].qf, d->npad, d->stream)) return wf_fail(d, WF_ERR_ALLOC, "qf");
+  }
   d->mu_s = mu_static;
   d->mu_d = mu_dynamic;
   d->contact_law = law;
@@ -917,6 +1071,21 @@ int wf_set_option(wf_domain* d, const char* key, double v) {
   else if (k == "rebuild_current_positions") d->rebuild_current = v != 0;
   else if (k == "thermal") d->thermal = v != 0;
   else if (k == "fuse_heat") d->fuse_heat = v != 0;
+  else if (k == "contact_stiffness") d->c_kappa = v;
+  else if (k == "contact_dx") d->c_dx = v;
+  else if (k == "contact_vreg") d->c_vreg = v;
+  else if (k == "contact_heat_fraction") d->c_eta = v;
+  else if (k == "rebuild_strain_increment") {
+    if (!(v >= 0.0)) return wf_fail(d, WF_ERR_ARG, "rebuild_strain_increment must be >= 0");
+    if (v > 0.0 && !d->F[0].eps_rb) {
+      for (int f = 0; f < 2; f++)
+        if (dalloc(&d->F[f].eps_rb, d->npad, d->stream)) return wf_fail(d, WF_ERR_ALLOC, "eps_rb");
+      if (dalloc(&d->d_maxdep, 1, d->stream) ||
+          cudaMallocHost((void**)&d->h_maxdep, sizeof(unsigned long long)) != cudaSuccess)
+        return wf_fail(d, WF_ERR_ALLOC, "rebuild flag");
+    }
+    d->rb_dep = v;
+  }
   else if (k == "taylor_quinney") d->chi = v;
   else if (k == "newton_rtol") d->newton_rtol = v;
   else if (k == "newton_max_iter") d->newton_max_iter = (int)v;
@@ -1108,6 +1277,13 @@ int wf_get_field(wf_domain* d, const char* name, double* out) {
   if (s == "Ta") return g(F.Ta, 1, 0, 1);
   if (s == "Tb") return g(F.Tb, 1, 0, 1);
   if (s == "dTdt") return g(F.dTdt, 1, 0, 1);
+  if (s == "fric_heat") {                          // zero unless contact law 1
+    if (!F.qf) {
+      std::fill(out, out + n, 0.0);
+      return WF_OK;
+    }
+    return g(F.qf, 1, 0, 1);
+  }
   if (s == "normal" || s == "contforce") {         // zero until a rigid mesh is added
     const double4* src = s == "normal" ? F.nrm : F.cf;
     if (!src) {
@@ -1166,6 +1342,7 @@ int wf_get_scalar(wf_domain* d, const char* name, double* out) {
   if (s == "is_yielding") { *out = d->is_yielding; return WF_OK; }
   if (s == "isfirst") { *out = d->isfirst; return WF_OK; }
   if (s == "launches") { *out = (double)d->launches; return WF_OK; }
+  if (s == "rebuilds") { *out = (double)d->rebuilds; return WF_OK; }
   if (s == "newton_iters" || s == "newton_calls" || s == "mlp_used" || s == "status") {
     int rc = read_status(d);
     if (rc) return rc;

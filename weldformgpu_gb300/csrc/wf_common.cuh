@@ -83,6 +83,8 @@ struct Fields {
   // contact (allocated when a rigid mesh is added)
   double4* nrm;     // surface normal (solid particles) / element normal (rigid particles)
   double4* cf;      // contact force of the last contact (contforce)
+  double* qf;       // frictional heat into the particle (W), contact law 1
+  double* eps_rb;   // plastic strain at the last neighbour rebuild (adaptive rebuild)
 };
 
 // A rigid triangle mesh on the device (TriMesh_d, src/cuda/Mesh.cuh:19-54);
@@ -96,6 +98,12 @@ struct MeshDev {
   double* pplane;     // plane coefficient n . node
   int32_t nn, ne, first, zone;
   double mv[3], mw[3];  // translational and angular velocity (m_v, m_w)
+  // contact law 1: triangles binned once in the frame of the tool as added
+  // (a translating tool: the frame offset is node[0] - org)
+  double org[3], gmin[3], cs;   // node 0 as added, bin grid origin and cell size
+  int32_t dims[3];
+  int32_t* cstart;              // [cells + 1] CSR offsets
+  int32_t* ctri;                // triangle indices, ascending within a cell
 };
 #define WF_CONT_NB 20     // contact neighbours per particle (MAX_NB_COUNT, src/cuda/Contact.cu:7)
 
@@ -129,6 +137,8 @@ struct StepParams {
   int32_t csid[WF_MAX_MESH];
   MeshDev mesh[WF_MAX_MESH];   // ncsid meshes, zone ids in csid
   double mu_s, mu_d;    // static / dynamic friction coefficients
+  int contact_law;      // 0 the reference's penalty law, 1 binned triangles (kappa K / dx)
+  double c_kappa, c_dx, c_vreg, c_eta, Kbulk;   // law 1 constants, bulk modulus
   double totmass;       // sum of all particle masses (WeldFormGPU.cu:808-820)
   int32_t id_free_surf; // 1, the id of free-surface particles
   int32_t* cnb;         // contact neighbours [WF_CONT_NB * npad] (slot indices)

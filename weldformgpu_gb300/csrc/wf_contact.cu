@@ -156,6 +156,121 @@ __global__ void __launch_bounds__(128) k_contact_force(StepParams P, Fields F, f
   F.cf[i] = d4(cf);
 }
 
+// Closest point of triangle abc to p (Ericson, Real-Time Collision Detection,
+// 5.1.5: Voronoi regions of the vertices, edges and face).
+__device__ V3 closest_on_tri(V3 p, V3 a, V3 b, V3 c) {
+  const V3 ab = b - a, ac = c - a, ap = p - a;
+  const double d1 = dot(ab, ap), d2 = dot(ac, ap);
+  if (d1 <= 0.0 && d2 <= 0.0) return a;
+  const V3 bp = p - b;
+  const double d3 = dot(ab, bp), d4 = dot(ac, bp);
+  if (d3 >= 0.0 && d4 <= d3) return b;
+  const double vc = d1 * d4 - d3 * d2;
+  if (vc <= 0.0 && d1 >= 0.0 && d3 <= 0.0) return a + scale(ab, d1 / (d1 - d3));
+  const V3 cp = p - c;
+  const double d5 = dot(ab, cp), d6 = dot(ac, cp);
+  if (d6 >= 0.0 && d5 <= d6) return c;
+  const double vb = d5 * d2 - d1 * d6;
+  if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) return a + scale(ac, d2 / (d2 - d6));
+  const double va = d3 * d6 - d5 * d4;
+  if (va <= 0.0 && (d4 - d3) >= 0.0 && (d5 - d6) >= 0.0)
+    return b + scale(c - b, (d4 - d3) / ((d4 - d3) + (d5 - d6)));
+  const double denom = 1.0 / (va + vb + vc);
+  return (a + scale(ab, vb * denom)) + scale(ac, vc * denom);
+}
+
+// Contact law 1 (the 2M-particle contact workload; no reference
+// counterpart).  A solid particle looks up its cell in each tool's triangle
+// bins (built once in the tool's frame; the frame moves with node 0) and takes
+// the nearest triangle whose closest point lies within h (ties: first mesh,
+// lowest triangle index).  With the gap g = (x - q).n along the face's outward
+// normal and the penetration delta = dx/2 - g > 0 the normal force is
+// kappa K dx delta (pressure kappa K / dx on the face dx^2); friction is
+// Coulomb, regularised below v_reg: F_t = -mu F_n v_t / max(|v_t|, v_reg);
+// eta of the frictional power heats the particle.  Mixed form: the
+// acceleration comes from and returns to the FP32 array.
+__global__ void __launch_bounds__(128) k_contact_law1(StepParams P, Fields F, float4* a32) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= P.n || F.perm[i] >= P.n_solid) return;
+  const double4 x4 = F.xm[i];
+  const V3 xi = mk(x4);
+  double best = P.h * P.h;
+  int bm = -1, be = -1;
+  V3 bq = mk(0.0, 0.0, 0.0);
+  for (int m = 0; m < P.ncsid; m++) {
+    const MeshDev& M = P.mesh[m];
+    const double4 n0 = M.node[0];
+    const V3 xt = xi - (mk(n0) - mk(M.org[0], M.org[1], M.org[2]));
+    // cell coordinates compared in double first: a particle far outside the
+    // grid (or a NaN position) is skipped before any integer conversion
+    const double fx = floor((xt.x - M.gmin[0]) / M.cs);
+    const double fy = floor((xt.y - M.gmin[1]) / M.cs);
+    const double fz = floor((xt.z - M.gmin[2]) / M.cs);
+    if (!(fx >= 0.0 && fy >= 0.0 && fz >= 0.0 && fx < (double)M.dims[0] &&
+          fy < (double)M.dims[1] && fz < (double)M.dims[2]))
+      continue;
+    const int cell = ((int)fz * M.dims[1] + (int)fy) * M.dims[0] + (int)fx;
+    for (int t = M.cstart[cell]; t < M.cstart[cell + 1]; t++) {
+      const int e = M.ctri[t];
+      const int32_t* en = M.elnode + 3 * e;
+      const V3 q = closest_on_tri(xi, mk(M.node[en[0]]), mk(M.node[en[1]]), mk(M.node[en[2]]));
+      const V3 dv = xi - q;
+      const double d2 = dot(dv, dv);
+      if (d2 < best || (d2 == best && bm == m && e < be)) {
+        best = d2; bm = m; be = e; bq = q;
+      }
+    }
+  }
+  V3 f = mk(0.0, 0.0, 0.0);
+  double qf = 0.0;
+  int cnt = 0;
+  if (bm >= 0) {
+    const MeshDev& M = P.mesh[bm];
+    // contact normal: from the nearest surface point to the particle (the
+    // face normal inside a face, continuous across edges and vertices); the
+    // face normal and its signed gap for a centre behind the face
+    const V3 dv = xi - bq;
+    const double dist = sqrt(best);
+    const double gf = dot(dv, mk(M.normal[be]));
+    V3 n;
+    double g;
+    if (gf >= 0.0 && dist > 0.0) {
+      n = divide(dv, dist);
+      g = dist;
+    } else {
+      n = mk(M.normal[be]);
+      g = gf;
+    }
+    const double delta = 0.5 * P.c_dx - g;
+    if (delta > 0.0) {
+      const double fn = P.c_kappa * P.Kbulk * P.c_dx * delta;
+      f = scale(n, fn);
+      const V3 vrel = mk(F.vd[i]) - mk(M.mv[0], M.mv[1], M.mv[2]);
+      const V3 vt = vrel - scale(n, dot(vrel, n));
+      const double vtl = len(vt);
+      if (P.mu_s > 0.0) {
+        const double s = P.mu_s * fn / (vtl > P.c_vreg ? vtl : P.c_vreg);
+        f = f - scale(vt, s);
+        qf = P.c_eta * s * vtl * vtl;
+      }
+      V3 a;
+      if (a32) {
+        const float4 af = a32[i];
+        a = mk(af.x, af.y, af.z);
+      } else {
+        a = mk(F.a[i]);
+      }
+      a = a + divide(f, x4.w);
+      if (a32) a32[i] = make_float4((float)a.x, (float)a.y, (float)a.z, 0.f);
+      else F.a[i] = d4(a);
+      cnt = 1;
+    }
+  }
+  F.cf[i] = d4(f);
+  F.qf[i] = qf;
+  P.ccnt[i] = cnt;
+}
+
 // TriMesh_d::Move: node velocity m_v + m_w x node, then node += v dt
 __global__ void k_mesh_move(MeshDev M, double dt) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -205,6 +320,10 @@ inline int blocks_for(int64_t n, int t) { return (int)((n + t - 1) / t); }
 
 void launch_contact_stage(const StepParams& P, const Fields& F, const NbBuffers& N, bool list,
                           float4* a32, cudaStream_t s) {
+  if (P.contact_law == 1) {
+    k_contact_law1<<<blocks_for(P.n, 128), 128, 0, s>>>(P, F, a32);
+    return;
+  }
   k_surface<<<blocks_for(P.n, 128), 128, 0, s>>>(P, F, N.nb, N.cnt);
   if (list) k_contact_nb<<<blocks_for(P.n, 128), 128, 0, s>>>(P, F, N.nb, N.cnt);
   k_contact_force<<<blocks_for(P.n, 128), 128, 0, s>>>(P, F, a32);

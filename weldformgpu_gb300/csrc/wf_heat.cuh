@@ -19,6 +19,7 @@ __device__ __forceinline__ double heat_rate_mixed(const StepParams& P, const Fie
     const double dep = F.dep[i];
     if (dep > 0.0) sm += P.chif * (float)F.sy[i] * (float)dep / (rf * cpf * P.dtf);
   }
+  if (F.qf && F.qf[i] > 0.0) sm += (float)F.qf[i] / ((float)mass * cpf);   // frictional heat
   if (F.bct[i] == 1) {
     const float mf = (float)mass;
     const float dS2 = powf(mf / rf, 0.666666666f);

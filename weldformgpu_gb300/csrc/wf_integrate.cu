@@ -156,6 +156,7 @@ __global__ void __launch_bounds__(128) k_heat_rate(StepParams P, Fields F,
     const double dep = F.dep[i];
     if (dep > 0.0) s += P.chi * F.sy[i] * dep / (rhoi * F.cpT[i] * P.dt);
   }
+  if (F.qf && F.qf[i] > 0.0) s += F.qf[i] / (xi.w * F.cpT[i]);   // frictional heat, law 1
   if (F.bct[i] == 1) {
     const double dS2 = pow(xi.w / rhoi, 0.666666666);
     const double q_conv = P.h_conv * dS2 * (P.T_inf - Ti) / xi.w;

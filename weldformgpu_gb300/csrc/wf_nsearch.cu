@@ -195,7 +195,8 @@ __global__ void k_reorder(int64_t n, const int32_t* __restrict__ s_src, const Fi
   g1(B.id, A.id, k, s); g1(B.bct, A.bct, k, s); g1(B.nw, A.nw, k, s); g1(B.xh, A.xh, k, s);
   g1(B.p32, A.p32, k, s); g1(B.v32, A.v32, k, s); g6f(B.ss32, A.ss32, k, s);
   g1(B.th32, A.th32, k, s); g1(B.pwn, A.pwn, k, s);
-  g1(B.nrm, A.nrm, k, s); g1(B.cf, A.cf, k, s);
+  g1(B.nrm, A.nrm, k, s); g1(B.cf, A.cf, k, s); g1(B.qf, A.qf, k, s);
+  g1(B.eps_rb, A.eps_rb, k, s);
   int32_t o = A.perm[s];
   B.perm[k] = o;
   inv[o] = (int32_t)k;

@@ -3,6 +3,7 @@
 //
 // The generators reproduce the reference's floating-point sequence (running
 // sums, not products) so that particle positions are bit-identical.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdlib>
@@ -178,6 +179,70 @@ int64_t wf_gen_cylinder_uniform(double Rxy, double Lz, double r, double density,
   }
   if (mass && cnt > 0) *mass = kPi * Rxy * Rxy * Lz * density / (double)cnt;
   return cnt;
+}
+
+// Icosphere tool of radius R about `center` (the rigid indenter of the
+// 2M-particle contact benchmark: the lower half of a ~10k-triangle sphere).
+// The icosahedron's 20 faces are split `level` times into 4 (edge midpoints
+// pushed to the sphere; shared midpoints created once, keyed by the edge's
+// node pair); faces are ordered for outward normals.  lower_half keeps the
+// faces whose centroid lies at or below center[2], and their nodes (renumbered
+// in order of first use).  Two-call protocol: returns the face count and
+// *n_nodes; fills nodes (3 n_nodes) and tris (3 per face) when not NULL.
+int64_t wf_gen_icosphere(double R, const double* center, int level, int lower_half,
+                         double* nodes, int32_t* tris, int64_t* n_nodes) {
+  if (!(R > 0.0) || !center || level < 0 || level > 8) return -1;
+  const double t = (1.0 + std::sqrt(5.0)) / 2.0;
+  std::vector<double> v = {-1, t, 0, 1, t, 0, -1, -t, 0, 1, -t, 0, 0, -1, t, 0, 1, t,
+                           0, -1, -t, 0, 1, -t, t, 0, -1, t, 0, 1, -t, 0, -1, -t, 0, 1};
+  for (size_t k = 0; k < v.size(); k += 3) {
+    const double s = 1.0 / std::sqrt(v[k] * v[k] + v[k + 1] * v[k + 1] + v[k + 2] * v[k + 2]);
+    v[k] *= s; v[k + 1] *= s; v[k + 2] *= s;
+  }
+  std::vector<int32_t> f = {0, 11, 5, 0, 5, 1, 0, 1, 7, 0, 7, 10, 0, 10, 11, 1, 5, 9, 5, 11, 4,
+                            11, 10, 2, 10, 7, 6, 7, 1, 8, 3, 9, 4, 3, 4, 2, 3, 2, 6, 3, 6, 8,
+                            3, 8, 9, 4, 9, 5, 2, 4, 11, 6, 2, 10, 8, 6, 7, 9, 8, 1};
+  for (int l = 0; l < level; l++) {
+    std::map<std::pair<int32_t, int32_t>, int32_t> mid;
+    auto midpoint = [&](int32_t a, int32_t b) {
+      const std::pair<int32_t, int32_t> key(std::min(a, b), std::max(a, b));
+      auto it = mid.find(key);
+      if (it != mid.end()) return it->second;
+      double p[3] = {0.5 * (v[3 * a] + v[3 * b]), 0.5 * (v[3 * a + 1] + v[3 * b + 1]),
+                     0.5 * (v[3 * a + 2] + v[3 * b + 2])};
+      const double s = 1.0 / std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+      const int32_t id = (int32_t)(v.size() / 3);
+      v.push_back(p[0] * s); v.push_back(p[1] * s); v.push_back(p[2] * s);
+      mid[key] = id;
+      return id;
+    };
+    std::vector<int32_t> g;
+    g.reserve(f.size() * 4);
+    for (size_t k = 0; k < f.size(); k += 3) {
+      const int32_t a = f[k], b = f[k + 1], c = f[k + 2];
+      const int32_t ab = midpoint(a, b), bc = midpoint(b, c), ca = midpoint(c, a);
+      const int32_t nf[12] = {a, ab, ca, b, bc, ab, c, ca, bc, ab, bc, ca};
+      g.insert(g.end(), nf, nf + 12);
+    }
+    f.swap(g);
+  }
+  std::vector<int32_t> keep, remap(v.size() / 3, -1);
+  int32_t nn = 0;
+  for (size_t k = 0; k < f.size(); k += 3) {
+    const double cz = (v[3 * f[k] + 2] + v[3 * f[k + 1] + 2] + v[3 * f[k + 2] + 2]) / 3.0;
+    if (lower_half && cz > 0.0) continue;
+    for (int q = 0; q < 3; q++) {
+      if (remap[f[k + q]] < 0) remap[f[k + q]] = nn++;
+      keep.push_back(remap[f[k + q]]);
+    }
+  }
+  if (n_nodes) *n_nodes = nn;
+  if (nodes)
+    for (size_t q = 0; q < remap.size(); q++)
+      if (remap[q] >= 0)
+        for (int k = 0; k < 3; k++) nodes[3 * remap[q] + k] = center[k] + R * v[3 * q + k];
+  if (tris) std::copy(keep.begin(), keep.end(), tris);
+  return (int64_t)(keep.size() / 3);
 }
 
 // Domain::AssignZone (src/Domain.cpp:989-1005): inclusive box test.

@@ -97,6 +97,48 @@ def contact_cylinder(R=0.005, H=0.010, dx=0.0005, dens=10, v_plane=-10.0, gap=1.
     return sc
 
 
+def indent_block(L=(0.008, 0.008, 0.003), dx=0.00025, R=0.003, level=3, v_tool=-5.0, mu=0.3,
+                 gap=1.0e-7, thermal=True, zone=7, rebuild_increment=0.05):
+    """A block indented by a rigid lower-half icosphere (the shape of the
+    2M-particle contact benchmark, BASELINE config 5: block 200 x 200 x 50 dx,
+    dx = 0.25 mm, R = 10 mm, ~10k triangles, -5 m/s): contact law 1 (penalty
+    0.1 K / dx, friction mu, cell-binned triangle query, frictional heat), JC
+    aluminium, neighbour rebuild at a plastic-strain increment.  The bottom
+    layer is fixed (zone 2); the tool starts `gap` outside contact range."""
+    rho, E, nu = 2700.0, 70e9, 0.33
+    x, mass = S.gen_box_cubic((0.0, 0.0, 0.0), L, dx / 2.0, rho)
+    ns = len(x)
+    nodes, tris = S.gen_icosphere(R, (0.0, 0.0, 0.0), level, True)
+    top = x[:, 2].max()
+    shift = np.array([L[0] / 2.0, L[1] / 2.0, top + dx / 2.0 + gap - nodes[:, 2].min()])
+    nodes = nodes + shift
+    ne = len(tris)
+    n = ns + ne
+    ids = np.zeros(n, np.int32)
+    nw = np.zeros(n, np.uint8)
+    S.assign_zone(x, (-1, -1, -1), (1, 1, x[:, 2].min() + 0.5 * dx), 2, ids[:ns], nw[:ns])
+    ids[ns:] = zone
+    mat = _abi.WfMaterial(model=_abi.WF_JOHNSON_COOK, E=E, nu=nu, sy0=324e6, A=324e6, B=114e6,
+                          n=0.42, C=0.002, eps0=1.0, m=1.34, Tm=582.0, Tt=20.0)
+    K = E / (3.0 * (1.0 - 2.0 * nu))
+    G = E / (2.0 * (1.0 + nu))
+    Cs = math.sqrt(K / rho)
+    h = 1.2 * dx
+    opts = {"contact_dx": dx, "return_map": 1, "rebuild_current_positions": 1,
+            "rebuild_strain_increment": rebuild_increment}
+    sc = dict(n=n, n_solid=ns, x=np.vstack([x, np.zeros((ne, 3))]),
+              m=np.concatenate([np.full(ns, mass), np.zeros(ne)]), ids=ids, not_write=nw,
+              h=h, rho=rho, G=G, sy=324e6, Cs=Cs, dt=0.4 * h / Cs, alpha=1.0, beta=0.0, mat=mat,
+              T=np.full(n, 20.0), bcs=[(2, (0.0, 0.0, 0.0)), (zone, (0.0, 0.0, v_tool))], K=K,
+              dx=dx, mesh=dict(nodes=nodes, tris=tris, normals=None, zone=zone, first=ns,
+                               vel=(0.0, 0.0, v_tool), angvel=(0.0, 0.0, 0.0)),
+              mu=(mu, mu), law=1, options=opts)
+    if thermal:
+        sc["k"], sc["cp"] = 167.0, 896.0
+        opts.update(thermal=1, taylor_quinney=0.9)
+    return sc
+
+
 def load(dom, sc, options=None):
     """Applies a scenario through the Domain_d setters (product or oracle)."""
     n = sc["n"]
@@ -124,8 +166,8 @@ def load(dom, sc, options=None):
         ms = sc["mesh"]
         dom.add_trimesh(ms["nodes"], ms["tris"], ms["zone"], ms["first"], ms["vel"], ms["angvel"],
                         normals=ms["normals"])
-        dom.set_contact(sc["mu"][0], sc["mu"][1])
-    for k, v in (options or {}).items():
+        dom.set_contact(sc["mu"][0], sc["mu"][1], sc.get("law", 0))
+    for k, v in dict(sc.get("options", {}), **(options or {})).items():
         dom.set_option(k, float(v))
     return dom
 

@@ -67,6 +67,22 @@ def gen_cylinder_uniform(Rxy, Lz, r, density, ang=2.0 * np.pi, rows=1, r_i=0.0, 
     return x.reshape(n, 3), ids, m.value
 
 
+def gen_icosphere(R, center, level, lower_half=True):
+    """Icosphere tool (outward normals): (nodes[nn,3], tris[ne,3])."""
+    lib_ = _L()
+    fn = lib_.wf_gen_icosphere
+    fn.restype = C.c_int64
+    fn.argtypes = [C.c_double, C.POINTER(C.c_double), C.c_int, C.c_int, C.POINTER(C.c_double),
+                   C.POINTER(C.c_int32), C.POINTER(C.c_int64)]
+    c = np.asarray(center, dtype=np.float64)
+    nn = C.c_int64()
+    ne = fn(R, _p(c), int(level), int(lower_half), None, None, C.byref(nn))
+    nodes = np.empty(3 * nn.value)
+    tris = np.empty(3 * ne, np.int32)
+    fn(R, _p(c), int(level), int(lower_half), _p(nodes), _p(tris, C.c_int32), C.byref(nn))
+    return nodes.reshape(-1, 3), tris.reshape(-1, 3)
+
+
 def gen_cylinder_lattice(R, H, dx, jitter, seed):
     """Jittered cubic lattice inside a cylinder (the compression benchmarks' workload)."""
     lib_ = _L()
