@@ -47,6 +47,8 @@ def lib():
         L.wfo_set_field.restype = C.c_int
         L.wfo_set_field.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_double)]
         L.wfo_set_threads.restype = C.c_int
+        L.wfo_grad_kernel.restype = C.c_double
+        L.wfo_grad_kernel.argtypes = [C.c_double, C.c_double]
         L.wfo_set_threads.argtypes = [C.c_int]
         L.wfo_set_mlp_params.restype = C.c_int
         L.wfo_set_mlp_params.argtypes = [C.c_void_p, C.POINTER(C.c_double)]

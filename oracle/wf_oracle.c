@@ -1137,6 +1137,8 @@ int wfo_find_neighbors(wfo_domain* d) {
   return nb_search_from(d, d->x_h);
 }
 
+double wfo_grad_kernel(double q, double h) { return grad_kernel(q, h); }
+
 int wfo_run_stage(wfo_domain* d, const char* s) {
   if (!d || !s) return WF_ERR_ARG;
   if (!strcmp(s, "density")) stage_density(d);

@@ -71,6 +71,8 @@ int wfo_find_neighbors(wfo_domain* d);
  * ("density", "update_density", "rates", "pressure", "stress", "accel",
  * "bc", "update_pos", "update_vel", "thermal", "energy"). */
 int wfo_run_stage(wfo_domain* d, const char* stage);
+/* GradKernel (cubic spline, Dim 3): the scalar GK with grad W = GK * x_ij. */
+double wfo_grad_kernel(double q, double h);
 
 int wfo_get_field(wfo_domain* d, const char* name, double* out);
 int wfo_get_field_i32(wfo_domain* d, const char* name, int32_t* out);

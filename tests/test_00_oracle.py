@@ -182,6 +182,179 @@ def test_contact_law1_known_answers(case):
         assert np.abs(f).max() > 0.0 and qf > 0.0
 
 
+# ---- analytic known answers of the SPH discretisation --------------------
+DX, H_DX = 1.0e-3, 1.2
+
+
+def lattice_moment():
+    """kappa with sum_j V_j GK_ij x_ij x_ij^T = -kappa I on the cubic lattice
+    at h = 1.2 dx (exactly -I for the continuous kernel)."""
+    L = O.lib()
+    g = np.arange(-3, 4)
+    X = np.array(np.meshgrid(g, g, g, indexing="ij")).reshape(3, -1).T * DX
+    X = X[np.any(X != 0, axis=1)]
+    h = H_DX * DX
+    GK = np.array([L.wfo_grad_kernel(q, h) for q in np.linalg.norm(X, axis=1) / h])
+    M = (DX ** 3 * GK[:, None, None] * X[:, :, None] * X[:, None, :]).sum(0)
+    assert np.abs(M - M[0, 0] * np.eye(3)).max() < 1e-12       # isotropic
+    return -M[0, 0]
+
+
+def elastic_box(dims, rho=2700.0, E=70e9, nu=0.33, ids=None):
+    x, m = O.gen_box_cubic((0.0, 0.0, 0.0), tuple(k * DX for k in dims), DX / 2, rho)
+    n = len(x)
+    K, G = E / (3 * (1 - 2 * nu)), E / (2 * (1 + nu))
+    Cs = np.sqrt(K / rho)
+    h = H_DX * DX
+    d = O.OracleDomain(n)
+    d.set_h(h)
+    d.set_density(rho)
+    d.set_shear_modulus(G)
+    d.set_sigma_y(1e12)
+    d.set_cs(np.full(n, Cs))
+    d.set_positions(x.ravel())
+    d.set_mass(np.full(n, m))
+    d.set_id(np.zeros(n, np.int32) if ids is None else ids(x))
+    d.set_not_write_surf_id(np.zeros(n, np.uint8))
+    d.set_time_step(0.4 * h / Cs)
+    d.set_artificial_viscosity(1.0, 0.0)
+    d.set_material(_abi.WfMaterial(model=_abi.WF_BILINEAR, E=E, nu=nu, sy0=1e12, Et=0.0))
+    d.set_temperature(np.full(n, 20.0))
+    return d, x, dict(K=K, G=G, rho=rho, E=E, dt=0.4 * h / Cs)
+
+
+def interior(x, margin):
+    c = 0.5 * (x.min(axis=0) + x.max(axis=0))
+    half = 0.5 * (x.max(axis=0) - x.min(axis=0))
+    return np.all(np.abs(x - c) <= half - margin, axis=1)
+
+
+def test_kernel_gradient_moment_is_minus_three():
+    """int grad W . x dV = -3 int W dV = -3 for the oracle's GradKernel (cubic
+    spline, Functions.cu:76-88), by quadrature over the support; and the
+    lattice moment at h = 1.2 dx is within 2 % of the continuous one."""
+    from scipy.integrate import quad
+    L = O.lib()
+    for h in (1.0, 1.2e-3):
+        f = lambda r: 4.0 * np.pi * r ** 4 * L.wfo_grad_kernel(r / h, h)   # noqa: E731
+        val = quad(f, 0.0, h, epsabs=0, epsrel=1e-13)[0] + quad(f, h, 2 * h, epsabs=0,
+                                                                 epsrel=1e-13)[0]
+        assert abs(val + 3.0) < 1e-10, (h, val)
+    assert abs(lattice_moment() - 1.0) < 0.02
+
+
+def test_linear_velocity_field_rates_and_density_on_lattice():
+    """v = L x on a cubic lattice: interior strain rate kappa sym(L), rotation
+    rate kappa/2 (L - L^T) with the reference's sign flip of the xz entry
+    (InteractionAlt.cu:362), density rate -kappa rho tr(L) (continuity)."""
+    kappa = lattice_moment()
+    d, x, p = elastic_box((12, 12, 12))
+    Lg = np.array([[1.0, 0.3, -0.2], [0.5, -0.7, 0.4], [0.1, 0.6, 0.2]]) * 100.0
+    d.set_velocities(np.ascontiguousarray(x @ Lg.T).ravel())
+    d.find_neighbors()
+    d.run_stage("density")
+    d.run_stage("rates")
+    inner = interior(x, 2.5 * DX)
+    assert inner.sum() == 216
+    S = 0.5 * (Lg + Lg.T) * kappa
+    exp_sr = [S[0, 0], S[1, 1], S[2, 2], S[0, 1], S[1, 2], S[0, 2]]
+    W = 0.5 * kappa * (Lg - Lg.T)
+    exp_rr = [0.0, 0.0, 0.0, W[0, 1], W[1, 2], -W[0, 2]]
+    np.testing.assert_allclose(d.get_field("strrate")[inner], np.tile(exp_sr, (216, 1)),
+                               rtol=1e-10, atol=1e-10 * np.abs(exp_sr).max())
+    np.testing.assert_allclose(d.get_field("rotrate")[inner], np.tile(exp_rr, (216, 1)),
+                               rtol=1e-10, atol=1e-10 * np.abs(exp_rr).max())
+    np.testing.assert_allclose(d.get_field("drho")[inner], -kappa * p["rho"] * np.trace(Lg),
+                               rtol=1e-10)
+
+
+def test_uniaxial_strain_rate_gives_p_wave_modulus():
+    """One stress update under v = (e x, 0, 0): sigma_xx = (K + 4G/3) kappa e dt,
+    sigma_yy = sigma_zz = (K - 2G/3) kappa e dt (EOS pressure from the density
+    increment, deviatoric Hooke increment; rates see the updated density)."""
+    kappa = lattice_moment()
+    d, x, p = elastic_box((12, 12, 12))
+    e = -100.0
+    v = np.zeros_like(x)
+    v[:, 0] = e * x[:, 0]
+    d.set_velocities(v.ravel())
+    d.find_neighbors()
+    for stage in ("density", "update_density", "rates", "pressure", "stress"):
+        d.run_stage(stage)
+    # neighbours whose own neighbourhoods are complete (their density exact)
+    inner = interior(x, 4.0 * DX)
+    assert inner.sum() == 64
+    K, G, dt = p["K"], p["G"], p["dt"]
+    de = kappa * e * dt
+    vol = 1.0 / (1.0 - de)                       # V_j = m / rho_new
+    sg = d.get_field("sigma")[inner]
+    np.testing.assert_allclose(sg[:, 0], K * de + 4.0 / 3.0 * G * de * vol, rtol=1e-9)
+    np.testing.assert_allclose(sg[:, 1], K * de - 2.0 / 3.0 * G * de * vol, rtol=1e-9)
+    np.testing.assert_allclose(sg[:, 2], K * de - 2.0 / 3.0 * G * de * vol, rtol=1e-9)
+    assert np.abs(sg[:, 3:]).max() < 1e-9 * abs(sg[:, 0]).max()
+
+
+def test_elastic_wave_front_speed():
+    """A face pushed at 1 m/s into an elastic block (28 x 28 cross-section):
+    the half-amplitude front on the centre line, before the lateral release
+    waves reach it, travels at the longitudinal speed sqrt((K + 4G/3)/rho)
+    within 5 % (the bar speed sqrt(E/rho) is 18 % lower)."""
+    O.set_threads(os.cpu_count() or 1)
+    d, x, p = elastic_box((40, 28, 28), ids=lambda x: np.where(x[:, 0] < 2 * DX, 2, 0).astype(
+        np.int32))
+    d.add_velocity_bc(2, 1.0, 0.0, 0.0)
+    cL = np.sqrt((p["K"] + 4.0 * p["G"] / 3.0) / p["rho"])
+    c = 0.5 * (x.min(axis=0) + x.max(axis=0))
+    line = (np.abs(x[:, 1] - c[1]) < 0.6 * DX) & (np.abs(x[:, 2] - c[2]) < 0.6 * DX)
+    order = np.argsort(x[line, 0])
+    xl = x[line, 0][order]
+    t, f = [], []
+    d.step(6)
+    for _ in range(8):
+        d.step(2)
+        vx = d.get_field("v")[line, 0][order]
+        k = np.nonzero(vx >= 0.5)[0].max()
+        t.append(d.get_scalar("time"))
+        f.append(xl[k] + (vx[k] - 0.5) / (vx[k] - vx[k + 1]) * DX)
+    speed = np.polyfit(t, f, 1)[0]
+    assert abs(speed / cL - 1.0) < 0.05, (speed, cL)
+    assert speed > 1.1 * np.sqrt(p["E"] / p["rho"])
+
+
+def test_heat_conduction_step_matches_erfc():
+    """Heat-only solve (ThermalSolve) of a temperature step in a steel bar
+    (48 x 12 x 12 dx): along the centre line the profile follows
+    T0 + (T1 - T0)/2 erfc((x - xm)/(2 sqrt(kappa alpha t))) within 1.5 % of the
+    step after 100 steps (diffusion length 3 dx)."""
+    from scipy.special import erfc
+    kappa = lattice_moment()
+    rho, cp, k = 7850.0, 460.0, 50.0
+    alpha = k / (rho * cp)
+    x, m = O.gen_box_cubic((0.0, 0.0, 0.0), (48 * DX, 12 * DX, 12 * DX), DX / 2, rho)
+    n = len(x)
+    xm, T0, T1 = 24 * DX, 20.0, 120.0
+    dt = 0.1 * DX * DX / alpha
+    d = O.OracleDomain(n)
+    d.set_h(H_DX * DX)
+    d.set_density(rho)
+    d.set_positions(x.ravel())
+    d.set_mass(np.full(n, m))
+    d.set_conductivity(k)
+    d.set_heat_cap(cp)
+    d.set_temperature(np.where(x[:, 0] < xm, T1, T0))
+    d.set_thermal_bc(np.zeros(n, np.int32))
+    d.set_convection(0.0, T0)
+    d.set_time_step(dt)
+    d.thermal_solve(100 * dt * (1.0 - 1e-9))
+    assert d.get_scalar("step") == 100
+    t = d.get_scalar("time")
+    c = 0.5 * (x.min(axis=0) + x.max(axis=0))
+    line = (np.abs(x[:, 1] - c[1]) < 0.6 * DX) & (np.abs(x[:, 2] - c[2]) < 0.6 * DX)
+    mid = line & (np.abs(x[:, 0] - xm) < 12 * DX)
+    exact = T0 + 0.5 * (T1 - T0) * erfc((x[mid, 0] - xm) / (2.0 * np.sqrt(kappa * alpha * t)))
+    assert np.abs(d.get_field("T")[mid] - exact).max() < 0.015 * (T1 - T0)
+
+
 def test_jc_yield_table_and_newton_residual():
     """KATs: JC sigma_y from the formula; Newton converges to 1e-10 relative."""
     sc = S.compression_cylinder(material="jc", vz_top=-10.0)
