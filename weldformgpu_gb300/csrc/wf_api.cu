@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -33,6 +34,8 @@ enum { KID_NONE = 0, KID_DENSITY = 1, KID_STRESS = 2, KID_ACCEL = 3, KID_INTEGRA
 struct wf_domain {
   int64_t n = 0, n_solid = 0, npad = 0;
   cudaStream_t stream = nullptr;
+  char* arena = nullptr;        // fixed-size device arrays, one allocation
+  size_t arena_bytes = 0;
   // uniform scalars (the reference's setters fill every particle with one value)
   double h = 0, rho0 = 0, G = 0, Cs = 0, dt = 0, alpha = 1.0, beta = 0.0;
   double h_conv = 100.0, T_inf = 0.0;
@@ -253,30 +256,49 @@ static cudaError_t dalloc(T** p, int64_t count, cudaStream_t s) {
   return e;
 }
 
-static int alloc_fields(wf_domain* d, Fields& F) {
+// One device allocation holds every fixed-size per-particle array of a domain
+// (both field buffers, the mixed-form mirrors, the neighbour lists, the
+// search's sort arrays): wf_create makes one cudaMalloc and one zero fill
+// instead of ~90 of each, and wf_destroy one cudaFree.  Offsets are 256-byte
+// aligned.  Arrays whose size is known later (contact, cell tables, logs)
+// keep their own allocations.
+struct Arena {
+  uintptr_t base = 0;  // 0 in the sizing pass
+  size_t off = 0;
+  template <class T>
+  void take(T** p, int64_t count) {
+    off = (off + 255) & ~(size_t)255;
+    *p = reinterpret_cast<T*>(base + off);
+    off += sizeof(T) * (size_t)std::max<int64_t>(count, 1);
+  }
+};
+
+static void layout_arena(wf_domain* d, Arena& A) {
   const int64_t n = d->npad;
-  WF_CUDA_OK(dalloc(&F.xm, n, d->stream)); WF_CUDA_OK(dalloc(&F.vd, n, d->stream));
-  WF_CUDA_OK(dalloc(&F.u, n, d->stream)); WF_CUDA_OK(dalloc(&F.a, n, d->stream));
-  WF_CUDA_OK(dalloc(&F.sig6, 6 * n, d->stream)); WF_CUDA_OK(dalloc(&F.ss6, 6 * n, d->stream));
-  WF_CUDA_OK(dalloc(&F.eps6, 6 * n, d->stream)); WF_CUDA_OK(dalloc(&F.sr6, 6 * n, d->stream));
-  WF_CUDA_OK(dalloc(&F.rr6, 6 * n, d->stream));
-  WF_CUDA_OK(dalloc(&F.p, n, d->stream)); WF_CUDA_OK(dalloc(&F.seq, n, d->stream)); WF_CUDA_OK(dalloc(&F.eps_p, n, d->stream));
-  WF_CUDA_OK(dalloc(&F.sy, n, d->stream)); WF_CUDA_OK(dalloc(&F.eff, n, d->stream)); WF_CUDA_OK(dalloc(&F.dep, n, d->stream));
-  WF_CUDA_OK(dalloc(&F.drho, n, d->stream)); WF_CUDA_OK(dalloc(&F.eint, n, d->stream));
-  WF_CUDA_OK(dalloc(&F.T, n, d->stream)); WF_CUDA_OK(dalloc(&F.Ta, n, d->stream)); WF_CUDA_OK(dalloc(&F.Tb, n, d->stream));
-  WF_CUDA_OK(dalloc(&F.dTdt, n, d->stream)); WF_CUDA_OK(dalloc(&F.kT, n, d->stream)); WF_CUDA_OK(dalloc(&F.cpT, n, d->stream));
-  WF_CUDA_OK(dalloc(&F.id, n, d->stream)); WF_CUDA_OK(dalloc(&F.bct, n, d->stream)); WF_CUDA_OK(dalloc(&F.perm, n, d->stream));
-  WF_CUDA_OK(dalloc(&F.nw, n, d->stream)); WF_CUDA_OK(dalloc(&F.xh, n, d->stream));
-  WF_CUDA_OK(dalloc(&F.p32, n, d->stream)); WF_CUDA_OK(dalloc(&F.v32, n, d->stream)); WF_CUDA_OK(dalloc(&F.ss32, 6 * n, d->stream));
-  WF_CUDA_OK(dalloc(&F.th32, n, d->stream)); WF_CUDA_OK(dalloc(&F.pwn, n, d->stream));
-  return WF_OK;
+  for (int k = 0; k < 2; k++) {
+    Fields& F = d->F[k];
+    A.take(&F.xm, n); A.take(&F.vd, n); A.take(&F.u, n); A.take(&F.a, n);
+    A.take(&F.sig6, 6 * n); A.take(&F.ss6, 6 * n); A.take(&F.eps6, 6 * n);
+    A.take(&F.sr6, 6 * n); A.take(&F.rr6, 6 * n);
+    A.take(&F.p, n); A.take(&F.seq, n); A.take(&F.eps_p, n); A.take(&F.sy, n);
+    A.take(&F.eff, n); A.take(&F.dep, n); A.take(&F.drho, n); A.take(&F.eint, n);
+    A.take(&F.T, n); A.take(&F.Ta, n); A.take(&F.Tb, n); A.take(&F.dTdt, n);
+    A.take(&F.kT, n); A.take(&F.cpT, n);
+    A.take(&F.id, n); A.take(&F.bct, n); A.take(&F.perm, n); A.take(&F.nw, n);
+    A.take(&F.xh, n); A.take(&F.p32, n); A.take(&F.v32, n); A.take(&F.ss32, 6 * n);
+    A.take(&F.th32, n); A.take(&F.pwn, n);
+  }
+  A.take(&d->vd2, n); A.take(&d->v32b, n); A.take(&d->a32, n); A.take(&d->sigr32, 8 * n);
+  A.take(&d->nb, (int64_t)WF_NB_ALLOC * n); A.take(&d->nbc, n); A.take(&d->inv, n);
+  A.take(&d->pf, n); A.take(&d->pf2, n); A.take(&d->cellid, n); A.take(&d->s_src, n);
+  A.take(&d->s_orig, n); A.take(&d->d_mm, 8); A.take(&d->d_status, 8);
+  A.take(&d->d_stage, 6 * n); A.take(&d->mlp_w, WF_MLP_NPARAM);
+  A.take(&d->mlp_packed, (int64_t)wf_mlp_packed_bytes());
 }
 
+// the field arrays allocated on demand (contact, adaptive rebuild)
 static void free_fields(Fields& F) {
-  void* ptrs[] = {F.xm, F.vd, F.u, F.a, F.sig6, F.ss6, F.eps6, F.sr6, F.rr6, F.p, F.seq, F.eps_p,
-                  F.sy, F.eff, F.dep, F.drho, F.eint, F.T, F.Ta, F.Tb, F.dTdt, F.kT, F.cpT,
-                  F.id, F.bct, F.perm, F.nw, F.xh, F.p32, F.v32, F.ss32, F.th32, F.pwn,
-                  F.nrm, F.cf, F.qf, F.eps_rb};
+  void* ptrs[] = {F.nrm, F.cf, F.qf, F.eps_rb};
   for (void* p : ptrs) if (p) cudaFree(p);
   F = Fields{};
 }
@@ -745,18 +767,20 @@ int wf_create(wf_domain** out, int64_t n) {
   auto bail = [&](int code) { wf_destroy(d); return code; };
   if (cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking) != cudaSuccess)
     return bail(WF_ERR_CUDA);
-  for (int k = 0; k < 2; k++) {
-    rc = alloc_fields(d, d->F[k]);
-    if (rc) return bail(rc);
+  {
+    Arena size;
+    layout_arena(d, size);
+    d->arena_bytes = size.off;
+    if (cudaMalloc((void**)&d->arena, d->arena_bytes) != cudaSuccess) {
+      d->arena = nullptr;
+      return bail(WF_ERR_ALLOC);
+    }
+    if (cudaMemsetAsync(d->arena, 0, d->arena_bytes, d->stream) != cudaSuccess)
+      return bail(WF_ERR_CUDA);
+    Arena place;
+    place.base = reinterpret_cast<uintptr_t>(d->arena);
+    layout_arena(d, place);
   }
-  if (dalloc(&d->vd2, d->npad, d->stream) || dalloc(&d->v32b, d->npad, d->stream) || dalloc(&d->a32, d->npad, d->stream) || dalloc(&d->sigr32, 8 * d->npad, d->stream) ||
-      dalloc(&d->nb, (int64_t)WF_NB_ALLOC * d->npad, d->stream) || dalloc(&d->nbc, d->npad, d->stream) ||
-      dalloc(&d->inv, d->npad, d->stream) || dalloc(&d->pf, d->npad, d->stream) || dalloc(&d->pf2, d->npad, d->stream) ||
-      dalloc(&d->cellid, d->npad, d->stream) || dalloc(&d->s_src, d->npad, d->stream) || dalloc(&d->s_orig, d->npad, d->stream) ||
-      dalloc(&d->d_mm, 8, d->stream) || dalloc(&d->d_status, 8, d->stream) || dalloc(&d->d_stage, 6 * d->npad, d->stream) ||
-      dalloc(&d->mlp_w, WF_MLP_NPARAM, d->stream) ||
-      dalloc(&d->mlp_packed, (int64_t)wf_mlp_packed_bytes(), d->stream))
-    return bail(WF_ERR_ALLOC);
   if (cudaMallocHost((void**)&d->h_status, 8 * sizeof(int)) != cudaSuccess) return bail(WF_ERR_ALLOC);
   k_iota<<<nblk(n), 256, 0, d->stream>>>(n, d->F[0].perm, d->inv);
   k_fill_d<<<nblk(n), 256, 0, d->stream>>>(n, -1.0, d->F[0].pwn, 1, 0);
@@ -777,10 +801,8 @@ int wf_destroy(wf_domain* d) {
   if (d->h_maxdep) cudaFreeHost(d->h_maxdep);
   if (d->cnb) cudaFree(d->cnb);
   if (d->ccnt) cudaFree(d->ccnt);
-  void* ptrs[] = {d->vd2, d->v32b, d->a32, d->sigr32, d->mlp_w, d->mlp_packed, d->log_x,
-                  d->log_y, d->log_count, d->nb, d->nbc, d->inv, d->pf, d->pf2,
-                  d->cellid, d->cell_count, d->cell_cursor, d->scan_tmp, d->s_src, d->s_orig,
-                  d->d_mm, d->d_status, d->d_stage};
+  void* ptrs[] = {d->log_x, d->log_y, d->log_count, d->cell_count, d->cell_cursor,
+                  d->scan_tmp, d->arena};
   for (void* p : ptrs) if (p) cudaFree(p);
   if (d->h_status) cudaFreeHost(d->h_status);
   for (cudaEvent_t e : d->ev_pool) cudaEventDestroy(e);
