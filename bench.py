@@ -298,6 +298,90 @@ def reduce_max(dist, v):
     return float(t.item())
 
 
+def indentation_domain(sc, form, shift_t, state=None):
+    """The indentation workload's domain: the tool's nodes moved by its velocity
+    times `shift_t` (the tool translates at constant velocity, so this is where
+    a run of that length leaves it), particle state restored from `state`."""
+    sc2 = dict(sc)
+    ms = dict(sc["mesh"])
+    ms["nodes"] = ms["nodes"] + np.asarray(ms["vel"]) * shift_t
+    sc2["mesh"] = ms
+    opts = base_options()
+    opts["precision"] = 1 if form == "mixed" else 0
+    d = build_domain(sc2, opts)
+    if state is not None:
+        d.restore(state)
+    return d
+
+
+def bench_indentation(args):
+    """Config-5 shape (--size full): block 200 x 200 x 50 at dx = 0.25 mm (2.0M particles;
+    medium 100 x 100 x 50, small 50 x 50 x 25)
+    indented by the lower half of a level-5 icosphere (R = 10 mm, 10,304
+    triangles) at -5 m/s; contact law 1 (0.1 K/dx penalty, mu = 0.3,
+    frictional heat), JC, coupled heat, neighbour rebuild at a plastic-strain
+    increment of 0.05.  The mixed form runs `--preload` steps from rest to
+    develop the contact; both forms are timed from that state."""
+    from weldformgpu_gb300 import scenarios as S
+    L = {"full": (0.05, 0.05, 0.0125), "medium": (0.025, 0.025, 0.0125),
+         "small": (0.0125, 0.0125, 0.00625)}[args.size]
+    sc = S.indent_block(L=L, dx=0.00025, R=0.01, level=5, v_tool=-5.0, mu=0.3, thermal=True,
+                        rebuild_increment=0.05)
+    ns, ne = sc["n_solid"], len(sc["mesh"]["tris"])
+    preload = args.preload if args.preload != 4000 else 1000
+    d = indentation_domain(sc, "mixed", 0.0)
+    d.step(preload)
+    state = d.checkpoint()
+    t_pre = state["_time"]
+    contacts_pre = int((d.get_field_i32("cont_count") > 0).sum())
+    d.close()
+    forms = [f for f in ("mixed", "fp64") if f in args.forms.split(",")]
+    out = {}
+    for form in forms:
+        steps = args.steps if form == "mixed" else max(3, args.steps // 20)
+        d = indentation_domain(sc, form, t_pre, state)
+        d.step(max(args.warmup, 3))
+        kms = per_kernel_ms(d, ["density", "stress", "accel", "integrate", "thermal"], reps=5)
+        d.set_option("profile_kernel", 7)
+        _, cms, cl, _ = d.time_steps(5)
+        kms["contact"] = cms / max(cl / 2, 1)          # two timed scopes per step
+        d.set_option("profile_kernel", 0)
+        r0 = d.get_scalar("rebuilds")
+        with ClockSampler() as clk, ProfilerRange():
+            elapsed, _, _, launches = d.time_steps(steps)
+        out[form] = dict(value=ns * steps / (elapsed / 1e3), ms_per_step=elapsed / steps,
+                         per_kernel_ms=kms, launches=launches, clocks=clk.summary(),
+                         rebuilds_per_step=(d.get_scalar("rebuilds") - r0) / steps,
+                         contacts=int((d.get_field_i32("cont_count") > 0).sum()))
+        d.close()
+    line = {"workload": "indentation_block%dx%dx%d_dx0.25mm_icosphere_R10mm_level5" % tuple(
+                int(round(v / 0.00025)) for v in L),
+            "metric": "particle-steps/s (solid particles), mixed vs plain FP64 on 1 GB300",
+            "unit": UNIT, "value": out["mixed"]["value"], "ms_per_step": out["mixed"]["ms_per_step"],
+            "steps": args.steps, "n_gpus": 1, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"solid_particles": ns, "rigid_particles": ne, "triangles": ne,
+                       "dx_m": sc["dx"], "dt_s": sc["dt"], "tool_velocity_m_s": -5.0,
+                       "contact": "law 1: 0.1 K/dx penalty, mu 0.3, frictional heat",
+                       "rebuild": "plastic-strain increment 0.05", "preload_steps": preload,
+                       "contacts_at_start": contacts_pre},
+            "mixed": out["mixed"]}
+    if "fp64" in out:
+        # parity of the two forms over 20 steps from the same state
+        fields = {}
+        for form in ("mixed", "fp64"):
+            d = indentation_domain(sc, form, t_pre, state)
+            d.step(20)
+            fields[form] = {f: d.get_field(f) for f in ("u", "pl_strain", "sigma_eq", "T",
+                                                        "contforce")}
+            d.close()
+        line["plain_fp64"] = out["fp64"]
+        line["speedup_vs_plain_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+        line["rel_l2_vs_fp64_after_20_steps"] = {
+            f: rel_l2(fields["mixed"][f] - (20.0 if f == "T" else 0.0),
+                      fields["fp64"][f] - (20.0 if f == "T" else 0.0)) for f in fields["mixed"]}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -314,8 +398,16 @@ def main():
     ap.add_argument("--no-mlp", action="store_true", help="time the mixed form without the MLP")
     ap.add_argument("--preload", type=int, default=4000,
                     help="steps run (mixed form) before the timed runs, to reach plasticity")
+    ap.add_argument("--workload", default="compression", choices=["compression", "indentation"],
+                    help="compression: the metric's workload; indentation: the 2M-particle "
+                         "contact case (a separate line, not the metric)")
     args = ap.parse_args()
     warmup = max(args.warmup, 3)
+    if args.workload == "indentation":
+        from weldformgpu_gb300 import build as Bld
+        Bld.build()
+        bench_indentation(args)
+        return
     rank, ws, dist = dist_setup(args.gpus)
 
     from weldformgpu_gb300 import build as B

@@ -181,7 +181,9 @@ int wf_get_field_i32(wf_domain* d, const char* name, int32_t* out);
 int wf_get_neighbors(wf_domain* d, int32_t* counts, int32_t* lists);
 /* "time", "step", "is_yielding", "isfirst", "launches", "rebuilds" (neighbour
  * rebuilds inside the step loop), "newton_iters", "newton_calls", "mlp_used",
- * "status", "int_energy_sum". */
+ * "status", "int_energy_sum", "contact_tests32" / "contact_tests64" (contact
+ * law 1: triangle tests in the FP32 search and the FP64 decision, since
+ * creation). */
 int wf_get_scalar(wf_domain* d, const char* name, double* out);
 /* Checkpoint / restart (no reference counterpart: the reference's CSV
  * snapshots are not restartable).  wf_set_field writes a state field in the

@@ -72,6 +72,7 @@ struct wf_domain {
   int* d_mm = nullptr;
   int* d_status = nullptr;     // [0] bits, [1] yield flag, [2..3] newton iters, [4..5] calls
   int* h_status = nullptr;     // pinned mirror
+  unsigned long long* d_cstat = nullptr;   // contact law 1 triangle-test counters
   double* d_stage = nullptr;   // staging for ABI copies (6 doubles per particle)
   // solver state
   bool started = false, nb_built = false, is_yielding = false, isfirst = true;
@@ -220,21 +221,33 @@ __global__ void k_place_rigid(int32_t ne, int32_t first, const int32_t* inv,
   F.nrm[s] = normal[e];
 }
 // the largest plastic-strain increment since the last rebuild: non-negative
-// doubles order like their bit patterns, so one 64-bit atomicMax per warp
-__global__ void k_max_dep(int64_t n, const double* eps, const double* eps_rb,
-                          unsigned long long* out) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  double v = 0.0;
-  if (i < n) {
-    v = eps[i] - eps_rb[i];
+// doubles order like their bit patterns.  Grid-stride over at most
+// kMaxDepBlocks blocks, reduced per warp and then per block, so one 64-bit
+// atomicMax per block (one per warp serialised 63k atomics on one address at
+// 2M particles: 44 us).
+constexpr int kMaxDepBlocks = 1024;
+__global__ void __launch_bounds__(256) k_max_dep(int64_t n, const double* eps,
+                                                 const double* eps_rb,
+                                                 unsigned long long* out) {
+  __shared__ unsigned long long wmax[8];
+  unsigned long long b = 0ull;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double v = eps[i] - eps_rb[i];
     if (!(v > 0.0)) v = 0.0;
+    const unsigned long long c = (unsigned long long)__double_as_longlong(v);
+    b = c > b ? c : b;
   }
-  unsigned long long b = (unsigned long long)__double_as_longlong(v);
   for (int o = 16; o > 0; o >>= 1) {
     const unsigned long long c = __shfl_xor_sync(0xffffffffu, b, o);
     b = c > b ? c : b;
   }
-  if ((threadIdx.x & 31) == 0) atomicMax(out, b);
+  if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = b;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) b = wmax[w] > b ? wmax[w] : b;
+    atomicMax(out, b);
+  }
 }
 __global__ void k_copy_d(int64_t n, const double* src, double* dst) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -291,7 +304,7 @@ static void layout_arena(wf_domain* d, Arena& A) {
   A.take(&d->vd2, n); A.take(&d->v32b, n); A.take(&d->a32, n); A.take(&d->sigr32, 8 * n);
   A.take(&d->nb, (int64_t)WF_NB_ALLOC * n); A.take(&d->nbc, n); A.take(&d->inv, n);
   A.take(&d->pf, n); A.take(&d->pf2, n); A.take(&d->cellid, n); A.take(&d->s_src, n);
-  A.take(&d->s_orig, n); A.take(&d->d_mm, 8); A.take(&d->d_status, 8);
+  A.take(&d->s_orig, n); A.take(&d->d_mm, 8); A.take(&d->d_status, 8); A.take(&d->d_cstat, 2);
   A.take(&d->d_stage, 6 * n); A.take(&d->mlp_w, WF_MLP_NPARAM);
   A.take(&d->mlp_packed, (int64_t)wf_mlp_packed_bytes());
 }
@@ -347,6 +360,7 @@ static StepParams make_params(const wf_domain* d) {
   P.id_free_surf = 1;              // MechFraserSolve, SolverFraser.cu:118
   P.cnb = d->cnb;
   P.ccnt = d->ccnt;
+  P.cstat = d->d_cstat;
   P.nbc = (int)d->bc_zone.size();
   for (int b = 0; b < P.nbc; b++) {
     P.bc_zone[b] = d->bc_zone[b];
@@ -512,7 +526,15 @@ static int build_tool_bins(wf_domain* d) {
     }
     if (ncell > (int64_t)64 << 20) return wf_fail(d, WF_ERR_ARG, "tool bin grid too large");
     M.cs = cs;
+    M.inv_cs = 1.0 / cs;
     M.org[0] = nd[0].x; M.org[1] = nd[0].y; M.org[2] = nd[0].z;
+    for (int k = 0; k < 3; k++) {
+      M.glo[k] = (float)(M.gmin[k] - cs);
+      M.ghi[k] = (float)(M.gmin[k] + (M.dims[k] + 1) * cs);
+    }
+    if (!M.off32 && dalloc(&M.off32, 1, d->stream) != cudaSuccess)
+      return wf_fail(d, WF_ERR_ALLOC, "tool offset");
+    WF_CUDA_OK(cudaMemsetAsync(M.off32, 0, sizeof(float4), d->stream));
     std::vector<int32_t> start((size_t)ncell + 1, 0), list;
     auto range = [&](int e, int r0[3], int r1[3]) {
       for (int k = 0; k < 3; k++) {
@@ -555,6 +577,34 @@ static int build_tool_bins(wf_domain* d) {
     WF_CUDA_OK(cudaMemcpyAsync(M.cstart, start.data(), sizeof(int32_t) * (ncell + 1), cudaMemcpyHostToDevice, d->stream));
     if (!list.empty())
       WF_CUDA_OK(cudaMemcpyAsync(M.ctri, list.data(), sizeof(int32_t) * list.size(), cudaMemcpyHostToDevice, d->stream));
+    WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+    // FP32 vertex coordinates relative to node 0 for the FP32 triangle search,
+    // stored per bin entry so a cell's triangles are read contiguously, and
+    // the search tolerance: 1e-3 h plus 1e-6 of the tool's extent (16 FP32
+    // ulps of the largest relative coordinate), far above the FP32 distance
+    // error
+    double ext = 0.0;
+    for (int q = 0; q < M.nn; q++)
+      ext = std::max(ext, std::max(std::fabs(nd[q].x - nd[0].x),
+                                   std::max(std::fabs(nd[q].y - nd[0].y), std::fabs(nd[q].z - nd[0].z))));
+    M.tol32 = (float)(1e-3 * d->h + 1e-6 * (ext + 2.0 * d->h));
+    std::vector<float4> cv(3 * std::max<size_t>(1, list.size()));
+    for (size_t t = 0; t < list.size(); t++) {
+      const int e = list[t];
+      for (int k = 0; k < 3; k++) {
+        const double4& p = nd[en[3 * e + k]];
+        float w = 0.f;
+        if (k == 0) memcpy(&w, &e, sizeof w);   // the triangle index's bits
+        cv[3 * t + k] = make_float4((float)(p.x - nd[0].x), (float)(p.y - nd[0].y),
+                                    (float)(p.z - nd[0].z), w);
+      }
+    }
+    if (M.cvert) cudaFree(M.cvert);
+    M.cvert = nullptr;
+    if (dalloc(&M.cvert, (int64_t)cv.size(), d->stream) != cudaSuccess)
+      return wf_fail(d, WF_ERR_ALLOC, "tool bin vertices");
+    WF_CUDA_OK(cudaMemcpyAsync(M.cvert, cv.data(), sizeof(float4) * cv.size(), cudaMemcpyHostToDevice,
+                               d->stream));
     WF_CUDA_OK(cudaStreamSynchronize(d->stream));
   }
   d->bins_built = true;
@@ -621,6 +671,9 @@ static int solve_begin(wf_domain* d, double dt_out) {
       for (const MeshDev& M : d->meshes)
         if (M.mw[0] != 0.0 || M.mw[1] != 0.0 || M.mw[2] != 0.0)
           return wf_fail(d, WF_ERR_STATE, "contact law 1 takes translating tools only (angular velocity 0)");
+      for (const MeshDev& M : d->meshes)
+        if (M.ne >= (1 << 24))
+          return wf_fail(d, WF_ERR_ARG, "contact law 1 takes meshes of fewer than 2^24 triangles");
       if (!d->bins_built) {
         rc = build_tool_bins(d);
         if (rc) return rc;
@@ -642,7 +695,8 @@ static int solve_step(wf_domain* d) {
     // the last rebuild (one device reduction and a 8-byte read per step)
     const Fields& F0 = d->F[d->cur];
     WF_CUDA_OK(cudaMemsetAsync(d->d_maxdep, 0, sizeof(unsigned long long), s));
-    k_max_dep<<<nblk(d->n), 256, 0, s>>>(d->n, F0.eps_p, F0.eps_rb, d->d_maxdep);
+    k_max_dep<<<std::min(nblk(d->n), kMaxDepBlocks), 256, 0, s>>>(d->n, F0.eps_p, F0.eps_rb,
+                                                                 d->d_maxdep);
     WF_CUDA_OK(cudaMemcpyAsync(d->h_maxdep, d->d_maxdep, sizeof(unsigned long long),
                                cudaMemcpyDeviceToHost, s));
     WF_CUDA_OK(cudaStreamSynchronize(s));
@@ -794,7 +848,8 @@ int wf_destroy(wf_domain* d) {
   if (d->stream) cudaStreamSynchronize(d->stream);
   for (int k = 0; k < 2; k++) free_fields(d->F[k]);
   for (MeshDev& M : d->meshes) {
-    void* mp[] = {M.node, M.node_v, M.centroid, M.normal, M.elnode, M.pplane, M.cstart, M.ctri};
+    void* mp[] = {M.node, M.node_v, M.centroid, M.normal, M.elnode, M.pplane, M.cstart, M.ctri,
+                  M.off32, M.cvert};
     for (void* p : mp) if (p) cudaFree(p);
   }
   if (d->d_maxdep) cudaFree(d->d_maxdep);
@@ -1365,6 +1420,13 @@ int wf_get_scalar(wf_domain* d, const char* name, double* out) {
   if (s == "isfirst") { *out = d->isfirst; return WF_OK; }
   if (s == "launches") { *out = (double)d->launches; return WF_OK; }
   if (s == "rebuilds") { *out = (double)d->rebuilds; return WF_OK; }
+  if (s == "contact_tests32" || s == "contact_tests64") {   // law 1, since creation
+    unsigned long long c[2];
+    WF_CUDA_OK(cudaMemcpyAsync(c, d->d_cstat, sizeof c, cudaMemcpyDeviceToHost, d->stream));
+    WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+    *out = (double)c[s == "contact_tests32" ? 0 : 1];
+    return WF_OK;
+  }
   if (s == "newton_iters" || s == "newton_calls" || s == "mlp_used" || s == "status") {
     int rc = read_status(d);
     if (rc) return rc;

@@ -101,9 +101,16 @@ struct MeshDev {
   // contact law 1: triangles binned once in the frame of the tool as added
   // (a translating tool: the frame offset is node[0] - org)
   double org[3], gmin[3], cs;   // node 0 as added, bin grid origin and cell size
+  double inv_cs;                // 1 / cs
+  float glo[3], ghi[3];         // grid bounds widened by one cell (the FP32 early-out)
   int32_t dims[3];
   int32_t* cstart;              // [cells + 1] CSR offsets
   int32_t* ctri;                // triangle indices, ascending within a cell
+  float4* off32;                // node[0] - org in FP32, written by the mesh motion
+  float4* cvert;                // per bin entry: its triangle's vertices - node[0] in FP32
+                                // (fixed for a translating tool), 3 float4; .w of the
+                                // first holds the triangle index
+  float tol32;                  // FP32 search tolerance in distance (see k_contact_law1)
 };
 #define WF_CONT_NB 20     // contact neighbours per particle (MAX_NB_COUNT, src/cuda/Contact.cu:7)
 
@@ -143,6 +150,7 @@ struct StepParams {
   int32_t id_free_surf; // 1, the id of free-surface particles
   int32_t* cnb;         // contact neighbours [WF_CONT_NB * npad] (slot indices)
   int32_t* ccnt;        // contact neighbour counts [npad]
+  unsigned long long* cstat;  // contact law 1 counters: [0] FP32 triangle tests, [1] FP64 ones
   int nbc;
   int32_t bc_zone[WF_MAX_BC];
   double bc_v[WF_MAX_BC][3];

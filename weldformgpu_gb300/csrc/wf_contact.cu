@@ -179,12 +179,68 @@ __device__ V3 closest_on_tri(V3 p, V3 a, V3 b, V3 c) {
   return (a + scale(ab, vb * denom)) + scale(ac, vc * denom);
 }
 
+// The same closest-point rule in FP32 on tool-relative coordinates; returns
+// the squared distance.  Used only to choose which triangles the FP64 rule
+// evaluates (the FP64 pipe runs at 1/64 of the FP32 rate on this GPU).
+__device__ __forceinline__ float3 f3sub(float3 a, float3 b) {
+  return make_float3(a.x - b.x, a.y - b.y, a.z - b.z);
+}
+__device__ __forceinline__ float f3dot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 f3axpy(float3 a, float3 d, float t) {
+  return make_float3(a.x + d.x * t, a.y + d.y * t, a.z + d.z * t);
+}
+__device__ float closest_sq32(float3 p, float3 a, float3 b, float3 c) {
+  const float3 ab = f3sub(b, a), ac = f3sub(c, a), ap = f3sub(p, a);
+  const float d1 = f3dot(ab, ap), d2 = f3dot(ac, ap);
+  float3 q;
+  const float3 bp = f3sub(p, b), cp = f3sub(p, c);
+  const float d3 = f3dot(ab, bp), d4 = f3dot(ac, bp);
+  const float d5 = f3dot(ab, cp), d6 = f3dot(ac, cp);
+  const float vc = d1 * d4 - d3 * d2, vb = d5 * d2 - d1 * d6, va = d3 * d6 - d5 * d4;
+  if (d1 <= 0.f && d2 <= 0.f) q = a;
+  else if (d3 >= 0.f && d4 <= d3) q = b;
+  else if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) q = f3axpy(a, ab, d1 / (d1 - d3));
+  else if (d6 >= 0.f && d5 <= d6) q = c;
+  else if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) q = f3axpy(a, ac, d2 / (d2 - d6));
+  else if (va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f)
+    q = f3axpy(b, f3sub(c, b), (d4 - d3) / ((d4 - d3) + (d5 - d6)));
+  else {
+    const float den = 1.f / (va + vb + vc);
+    q = f3axpy(f3axpy(a, ab, vb * den), ac, vc * den);
+  }
+  const float3 dq = f3sub(p, q);
+  return f3dot(dq, dq);
+}
+
+__device__ __forceinline__ float3 rel32(const float4* r, int q) {
+  const float4 v = r[q];
+  return make_float3(v.x, v.y, v.z);
+}
+
+// The particle's cell in mesh M's bins, or -1 outside the grid (compared in
+// double first: a particle far outside the grid, or a NaN position, is
+// skipped before any integer conversion; the bins carry a margin of h, so the
+// rounding of the product cannot lose a triangle within h).
+__device__ __forceinline__ int tool_cell(const MeshDev& M, V3 xi) {
+  const double4 n0 = M.node[0];
+  const V3 xt = xi - (mk(n0) - mk(M.org[0], M.org[1], M.org[2]));
+  const double fx = floor((xt.x - M.gmin[0]) * M.inv_cs);
+  const double fy = floor((xt.y - M.gmin[1]) * M.inv_cs);
+  const double fz = floor((xt.z - M.gmin[2]) * M.inv_cs);
+  if (!(fx >= 0.0 && fy >= 0.0 && fz >= 0.0 && fx < (double)M.dims[0] &&
+        fy < (double)M.dims[1] && fz < (double)M.dims[2]))
+    return -1;
+  return ((int)fz * M.dims[1] + (int)fy) * M.dims[0] + (int)fx;
+}
+
 // Contact law 1 (the 2M-particle contact workload; no reference
 // counterpart).  A solid particle looks up its cell in each tool's triangle
 // bins (built once in the tool's frame; the frame moves with node 0) and takes
-// the nearest triangle whose closest point lies within h (ties: first mesh,
-// lowest triangle index).  With the gap g = (x - q).n along the face's outward
-// normal and the penetration delta = dx/2 - g > 0 the normal force is
+// the nearest triangle whose closest point q lies within h (ties: first mesh,
+// lowest triangle index), searched in FP32 and decided in FP64.  With the gap
+// g = |x - q| along n = (x - q)/g (the face normal and the signed gap for a
+// centre behind the face) and the penetration delta = dx/2 - g > 0 the normal
+// force is
 // kappa K dx delta (pressure kappa K / dx on the face dx^2); friction is
 // Coulomb, regularised below v_reg: F_t = -mu F_n v_t / max(|v_t|, v_reg);
 // eta of the frictional power heats the particle.  Mixed form: the
@@ -192,33 +248,121 @@ __device__ V3 closest_on_tri(V3 p, V3 a, V3 b, V3 c) {
 __global__ void __launch_bounds__(128) k_contact_law1(StepParams P, Fields F, float4* a32) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= P.n || F.perm[i] >= P.n_solid) return;
+  // FP32 early-out against each tool's bin grid widened by one cell (far
+  // larger than FP32 rounding): most particles are nowhere near a tool and
+  // skip all FP64 work.  The mixed form keeps an FP32 position mirror.
+  float px, py, pz;
+  if (a32) {
+    const float4 p = F.p32[i];
+    px = p.x; py = p.y; pz = p.z;
+  } else {
+    const double4 p = F.xm[i];
+    px = (float)p.x; py = (float)p.y; pz = (float)p.z;
+  }
+  bool near = false;
+  for (int m = 0; m < P.ncsid; m++) {
+    const MeshDev& M = P.mesh[m];
+    const float4 o = M.off32[0];
+    const float tx = px - o.x, ty = py - o.y, tz = pz - o.z;
+    near |= tx >= M.glo[0] && tx <= M.ghi[0] && ty >= M.glo[1] && ty <= M.ghi[1] &&
+            tz >= M.glo[2] && tz <= M.ghi[2];
+  }
+  if (!near) {
+    F.cf[i] = make_double4(0.0, 0.0, 0.0, 0.0);
+    F.qf[i] = 0.0;
+    P.ccnt[i] = 0;
+    return;
+  }
   const double4 x4 = F.xm[i];
   const V3 xi = mk(x4);
+  // Pass 1, FP32: the smallest squared distance over the candidate triangles,
+  // in coordinates relative to each tool's node 0 (each bin entry carries its
+  // triangle's FP32 vertices, so the loads of successive entries overlap).
+  float m32 = P.hf * P.hf, tol = 0.f;
+  unsigned n32 = 0, n64 = 0;
+  for (int m = 0; m < P.ncsid; m++) {
+    const MeshDev& M = P.mesh[m];
+    const int cell = tool_cell(M, xi);
+    if (cell < 0) continue;
+    tol = fmaxf(tol, M.tol32);
+    const double4 n0 = M.node[0];
+    const float3 pr = make_float3((float)(xi.x - n0.x), (float)(xi.y - n0.y), (float)(xi.z - n0.z));
+    const int t0 = M.cstart[cell], t1 = M.cstart[cell + 1];
+    n32 += (unsigned)(t1 - t0);
+#pragma unroll 4
+    for (int t = t0; t < t1; t++) {
+      const float4* v = M.cvert + 3 * (int64_t)t;
+      m32 = fminf(m32, closest_sq32(pr, rel32(v, 0), rel32(v, 1), rel32(v, 2)));
+    }
+  }
+  // Pass 2, FP64: the triangles within tol (in distance) of that minimum, in
+  // the order and with the tie rule of a scan of every triangle.  tol is far
+  // above the FP32 distance error, so the FP64 minimum is always among them.
+  // Candidates are collected first (FP32) and evaluated together: inside the
+  // scan, lanes pass the filter at different entries and a warp would run the
+  // FP64 test once per such entry.  A lane with more than kCand candidates
+  // (never seen on tessellated tools) scans again in FP64.
+  constexpr int kCand = 8;
+  const float lim = sqrtf(m32) + tol;
+  const float thr = lim * lim;
+  int cand[kCand];
+  int ncand = 0;
+  for (int m = 0; m < P.ncsid; m++) {
+    const MeshDev& M = P.mesh[m];
+    const int cell = tool_cell(M, xi);
+    if (cell < 0) continue;
+    const double4 n0 = M.node[0];
+    const float3 pr = make_float3((float)(xi.x - n0.x), (float)(xi.y - n0.y), (float)(xi.z - n0.z));
+    const int t1 = M.cstart[cell + 1];
+#pragma unroll 4
+    for (int t = M.cstart[cell]; t < t1; t++) {
+      const float4* v = M.cvert + 3 * (int64_t)t;
+      const float4 v0 = v[0];
+      if (closest_sq32(pr, make_float3(v0.x, v0.y, v0.z), rel32(v, 1), rel32(v, 2)) > thr)
+        continue;
+      if (ncand < kCand) cand[ncand] = (m << 24) | __float_as_int(v0.w);
+      ncand++;
+    }
+  }
   double best = P.h * P.h;
   int bm = -1, be = -1;
   V3 bq = mk(0.0, 0.0, 0.0);
-  for (int m = 0; m < P.ncsid; m++) {
+  auto consider = [&](int m, int e) {
     const MeshDev& M = P.mesh[m];
-    const double4 n0 = M.node[0];
-    const V3 xt = xi - (mk(n0) - mk(M.org[0], M.org[1], M.org[2]));
-    // cell coordinates compared in double first: a particle far outside the
-    // grid (or a NaN position) is skipped before any integer conversion
-    const double fx = floor((xt.x - M.gmin[0]) / M.cs);
-    const double fy = floor((xt.y - M.gmin[1]) / M.cs);
-    const double fz = floor((xt.z - M.gmin[2]) / M.cs);
-    if (!(fx >= 0.0 && fy >= 0.0 && fz >= 0.0 && fx < (double)M.dims[0] &&
-          fy < (double)M.dims[1] && fz < (double)M.dims[2]))
-      continue;
-    const int cell = ((int)fz * M.dims[1] + (int)fy) * M.dims[0] + (int)fx;
-    for (int t = M.cstart[cell]; t < M.cstart[cell + 1]; t++) {
-      const int e = M.ctri[t];
-      const int32_t* en = M.elnode + 3 * e;
-      const V3 q = closest_on_tri(xi, mk(M.node[en[0]]), mk(M.node[en[1]]), mk(M.node[en[2]]));
-      const V3 dv = xi - q;
-      const double d2 = dot(dv, dv);
-      if (d2 < best || (d2 == best && bm == m && e < be)) {
-        best = d2; bm = m; be = e; bq = q;
+    const int32_t* en = M.elnode + 3 * e;
+    const V3 q = closest_on_tri(xi, mk(M.node[en[0]]), mk(M.node[en[1]]), mk(M.node[en[2]]));
+    const V3 dv = xi - q;
+    const double d2 = dot(dv, dv);
+    if (d2 < best || (d2 == best && bm == m && e < be)) {
+      best = d2; bm = m; be = e; bq = q;
+    }
+  };
+  if (ncand <= kCand) {
+    for (int k = 0; k < ncand; k++) consider(cand[k] >> 24, cand[k] & 0xffffff);
+    n64 += (unsigned)ncand;
+  } else {
+    for (int m = 0; m < P.ncsid; m++) {
+      const MeshDev& M = P.mesh[m];
+      const int cell = tool_cell(M, xi);
+      if (cell < 0) continue;
+      const double4 n0 = M.node[0];
+      const float3 pr = make_float3((float)(xi.x - n0.x), (float)(xi.y - n0.y), (float)(xi.z - n0.z));
+      for (int t = M.cstart[cell]; t < M.cstart[cell + 1]; t++) {
+        const float4* v = M.cvert + 3 * (int64_t)t;
+        const float4 v0 = v[0];
+        if (closest_sq32(pr, make_float3(v0.x, v0.y, v0.z), rel32(v, 1), rel32(v, 2)) > thr)
+          continue;
+        consider(m, __float_as_int(v0.w));
+        n64++;
       }
+    }
+  }
+  {
+    const unsigned mask = __activemask();
+    const unsigned s32 = __reduce_add_sync(mask, n32), s64 = __reduce_add_sync(mask, n64);
+    if ((int)(threadIdx.x & 31) == __ffs(mask) - 1 && s32) {
+      atomicAdd(P.cstat, (unsigned long long)s32);
+      atomicAdd(P.cstat + 1, (unsigned long long)s64);
     }
   }
   V3 f = mk(0.0, 0.0, 0.0);
@@ -279,7 +423,11 @@ __global__ void k_mesh_move(MeshDev M, double dt) {
   const V3 vr = cross(mk(M.mw[0], M.mw[1], M.mw[2]), nd);
   const V3 nv = mk(M.mv[0], M.mv[1], M.mv[2]) + vr;
   M.node_v[q] = d4(nv);
-  M.node[q] = d4(nd + scale(nv, dt));
+  const V3 moved = nd + scale(nv, dt);
+  M.node[q] = d4(moved);
+  if (q == 0 && M.off32)   // the tool frame's offset for the law-1 early-out
+    M.off32[0] = make_float4((float)(moved.x - M.org[0]), (float)(moved.y - M.org[1]),
+                             (float)(moved.z - M.org[2]), 0.f);
 }
 
 // CalcCentroids, CalcNormals and UpdatePlaneCoeff of one element from the
