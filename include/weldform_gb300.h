@@ -274,7 +274,8 @@ int wf_set_mlp_weights(wf_domain* d, const float* params);
 /* (features, dlambda/dlambda_radial) pairs logged by the plain FP64 solver
  * while option "log_return_map" (capacity) is set: copies up to cap pairs */
 int wf_get_return_map_log(wf_domain* d, float* X, float* Y, int64_t cap, int64_t* count);
-/* Y = network(X) for n samples, BF16 tensor cores (FP32 accumulate) or FP32 */
+/* Y = network(X) for n samples: use_tensor_cores != 0 runs the tcgen05 path of
+ * the solver (BF16 operands, FP32 accumulation), 0 an FP32 reference kernel. */
 int wf_mlp_infer(const float* params, const float* X, int64_t n, int use_tensor_cores, float* Y);
 /* mean-squared-error loss and its gradient over n samples (training kernels) */
 int wf_mlp_grad(const float* params, const float* X, const float* Y, int64_t n, float* grad,

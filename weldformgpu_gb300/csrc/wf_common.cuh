@@ -43,6 +43,7 @@ __device__ __forceinline__ void nb_block(const int32_t* __restrict__ nb, int64_t
 #define WF_STATUS_NAN       1   // a kernel produced NaN/Inf in the stress state
 #define WF_STATUS_NB_CAP    2   // some particle hit WF_MAX_NEIGHBORS (list truncated)
 #define WF_STATUS_GRID      4   // a particle fell outside the search grid
+#define WF_STATUS_MMA_WAIT  8   // a tensor-core completion wait ran out (result discarded)
 
 // All per-slot arrays that move with the particles at a reorder.
 struct Fields {

@@ -1,6 +1,6 @@
 // wf_mlp.cu — the learned warm start of the Johnson-Cook return map:
 // synthetic (state, converged increment) pairs, FP32 training kernels
-// (forward, backward, Adam), BF16 tensor-core inference, and a kernel that
+// (forward, backward, Adam), BF16 tcgen05 tensor-core inference, and a kernel that
 // counts Newton iterations with and without the network.
 //
 // No counterpart in the reference: its return map is a one-shot radial
@@ -20,34 +20,39 @@
 namespace {
 
 // ---- parameter packing for the tensor-core kernels ---------------------------
-__global__ void k_mlp_pack(const float* __restrict__ P, MlpPacked* __restrict__ out) {
-  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  const int w = threadIdx.x >> 5;          // 0..7: n-tile
+// The tcgen05 weight image (mlp_umma_cta): B1 = [W1 | b1 | 0] and B2 = W2 in
+// BF16, K-major core-matrix order, then b2, W3 and b3 in FP32.
+__global__ void k_mlp_pack_umma(const float* __restrict__ P, uint8_t* __restrict__ out) {
   const float* W1 = P + WF_MLP_OFF_W1;
   const float* b1 = P + WF_MLP_OFF_B1;
   const float* W2 = P + WF_MLP_OFF_W2;
-  const int n = 8 * w + g;
-  auto w1x = [&](int k) { return k < 4 ? W1[n * 4 + k] : (k == 4 ? b1[n] : 0.0f); };
-  out->b1[w][lane] = make_uint2(bf16x2(w1x(2 * t), w1x(2 * t + 1)), bf16x2(w1x(2 * t + 8), w1x(2 * t + 9)));
-  for (int kk = 0; kk < 4; kk++) {
-    const int k0 = 16 * kk + 2 * t;
-    out->b2[kk][w][lane] = make_uint2(bf16x2(W2[n * WF_MLP_H + k0], W2[n * WF_MLP_H + k0 + 1]),
-                                      bf16x2(W2[n * WF_MLP_H + k0 + 8], W2[n * WF_MLP_H + k0 + 9]));
+  for (int k = threadIdx.x; k < WF_UMMA_IMAGE / 4; k += blockDim.x)
+    reinterpret_cast<uint32_t*>(out)[k] = 0u;
+  __syncthreads();
+  for (int e = threadIdx.x; e < WF_MLP_H * 16; e += blockDim.x) {
+    const int n = e / 16, k = e % 16;
+    const float v = k < 4 ? W1[n * 4 + k] : (k == 4 ? b1[n] : 0.0f);
+    *reinterpret_cast<__nv_bfloat16*>(out + WF_UMMA_B1 + umma_kmajor_off(n, k, 16)) =
+        __float2bfloat16_rn(v);
+  }
+  for (int e = threadIdx.x; e < WF_MLP_H * WF_MLP_H; e += blockDim.x) {
+    const int n = e / WF_MLP_H, k = e % WF_MLP_H;
+    *reinterpret_cast<__nv_bfloat16*>(out + WF_UMMA_B2 + umma_kmajor_off(n, k, WF_MLP_H)) =
+        __float2bfloat16_rn(W2[n * WF_MLP_H + k]);
   }
   for (int k = threadIdx.x; k < WF_MLP_H; k += blockDim.x) {
-    out->bias2[k] = P[WF_MLP_OFF_B2 + k];
-    out->w3[k] = P[WF_MLP_OFF_W3 + k];
+    reinterpret_cast<float*>(out + WF_UMMA_BIAS2)[k] = P[WF_MLP_OFF_B2 + k];
+    reinterpret_cast<float*>(out + WF_UMMA_W3)[k] = P[WF_MLP_OFF_W3 + k];
   }
-  if (threadIdx.x == 0) out->b3 = P[WF_MLP_OFF_B3];
+  if (threadIdx.x == 0) *reinterpret_cast<float*>(out + WF_UMMA_B3) = P[WF_MLP_OFF_B3];
 }
 
 // ---- standalone inference ---------------------------------------------------
-__global__ void k_mlp_infer_tc(const MlpPacked* __restrict__ Wg, const float4* __restrict__ X,
-                               int64_t n, float* __restrict__ Y) {
-  __shared__ MlpPacked W;
-  for (int k = threadIdx.x; k < WF_MLP_PACKED_WORDS; k += blockDim.x)
-    reinterpret_cast<uint32_t*>(&W)[k] = reinterpret_cast<const uint32_t*>(Wg)[k];
-  __syncthreads();
+__global__ void __launch_bounds__(128) k_mlp_infer_umma(const uint4* __restrict__ image,
+                                                        const float4* __restrict__ X, int64_t n,
+                                                        float* __restrict__ Y, int* status) {
+  extern __shared__ __align__(1024) uint8_t smu[];
+  mlp_umma_begin(smu, image);
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const bool valid = i < n;
   float f[4] = {0.f, 0.f, 0.f, 0.f};
@@ -55,8 +60,7 @@ __global__ void k_mlp_infer_tc(const MlpPacked* __restrict__ Wg, const float4* _
     const float4 x = X[i];
     f[0] = x.x; f[1] = x.y; f[2] = x.z; f[3] = x.w;
   }
-  __syncwarp();
-  const float y = mlp_tc_warp(W, f, valid);
+  const float y = mlp_umma_cta(smu, f, valid, status);
   if (valid) Y[i] = y;
 }
 
@@ -131,17 +135,15 @@ __global__ void k_mlp_synth(StepParams P, double G, int64_t n, uint64_t seed, fl
   iters[i] = it;
 }
 
-// Newton iterations from the radial start (W == nullptr) or the network's start
-__global__ void k_mlp_newton_iters(StepParams P, double G, const MlpPacked* __restrict__ Wg,
-                                   const float4* __restrict__ S, int64_t n,
-                                   int32_t* __restrict__ iters, int32_t* __restrict__ used,
-                                   float* __restrict__ dl_out) {
-  __shared__ MlpPacked W;
-  if (Wg) {
-    for (int k = threadIdx.x; k < WF_MLP_PACKED_WORDS; k += blockDim.x)
-      reinterpret_cast<uint32_t*>(&W)[k] = reinterpret_cast<const uint32_t*>(Wg)[k];
-  }
-  __syncthreads();
+// Newton iterations from the radial start (image == nullptr) or the network's start
+__global__ void __launch_bounds__(128) k_mlp_newton_iters(StepParams P, double G,
+                                                          const uint4* __restrict__ image,
+                                                          const float4* __restrict__ S, int64_t n,
+                                                          int32_t* __restrict__ iters,
+                                                          int32_t* __restrict__ used,
+                                                          float* __restrict__ dl_out, int* status) {
+  extern __shared__ __align__(1024) uint8_t smu[];
+  mlp_umma_begin(smu, image);
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const bool valid = i < n;
   const float4 s = valid ? S[i] : make_float4(1.f, 1e-2f, 1.f, 20.f);
@@ -152,11 +154,10 @@ __global__ void k_mlp_newton_iters(StepParams P, double G, const MlpPacked* __re
   const double st = (double)s.x * sy0;
   double ratio = -1.0;
   int use = 0;
-  if (Wg) {
+  if (image) {
     float f[4];
     mlp_features(s.x, (double)s.y, s.z, (float)Th, f);
-    __syncwarp();
-    const float y = mlp_tc_warp(W, f, valid);
+    const float y = mlp_umma_cta(smu, f, valid, status);
     const float yc = mlp_accept(y);
     if (yc > 0.0f) { ratio = (double)yc; use = 1; }
   }
@@ -333,10 +334,10 @@ inline int nb(int64_t n, int t) { return (int)((n + t - 1) / t); }
 
 // packs FP32 parameters into the BF16 fragment image used by the kernels
 int wf_mlp_pack_device(const float* dparams, void* dpacked, cudaStream_t s) {
-  k_mlp_pack<<<1, 256, 0, s>>>(dparams, (MlpPacked*)dpacked);
+  k_mlp_pack_umma<<<1, 256, 0, s>>>(dparams, (uint8_t*)dpacked);
   return cudaGetLastError() == cudaSuccess ? WF_OK : WF_ERR_CUDA;
 }
-size_t wf_mlp_packed_bytes() { return sizeof(MlpPacked); }
+size_t wf_mlp_packed_bytes() { return WF_UMMA_IMAGE; }
 
 extern "C" {
 
@@ -346,13 +347,19 @@ int wf_mlp_infer(const float* params, const float* X, int64_t n, int use_tensor_
   float* dP = B.get<float>(WF_MLP_NPARAM);
   float4* dX = B.get<float4>(n);
   float* dY = B.get<float>(n);
-  MlpPacked* dW = B.get<MlpPacked>(1);
-  if (!dP || !dX || !dY || !dW) return WF_ERR_ALLOC;
+  if (!dP || !dX || !dY) return WF_ERR_ALLOC;
   cudaMemcpy(dP, params, sizeof(float) * WF_MLP_NPARAM, cudaMemcpyHostToDevice);
   cudaMemcpy(dX, X, sizeof(float) * 4 * n, cudaMemcpyHostToDevice);
   if (use_tensor_cores) {
-    k_mlp_pack<<<1, 256>>>(dP, dW);
-    k_mlp_infer_tc<<<nb(n, 128), 128>>>(dW, dX, n, dY);
+    uint4* dI = B.get<uint4>(WF_UMMA_IMAGE / 16);
+    int* dS = B.get<int>(1);
+    if (!dI || !dS) return WF_ERR_ALLOC;
+    cudaMemset(dS, 0, sizeof(int));
+    k_mlp_pack_umma<<<1, 256>>>(dP, (uint8_t*)dI);
+    k_mlp_infer_umma<<<nb(n, 128), 128, WF_UMMA_SMEM>>>(dI, dX, n, dY, dS);
+    int st = 0;
+    cudaMemcpy(&st, dS, sizeof(int), cudaMemcpyDeviceToHost);
+    if (st & WF_STATUS_MMA_WAIT) return WF_ERR_CUDA;
   } else {
     k_mlp_infer_f32<<<nb(n, 128), 128>>>(dP, dX, n, dY);
   }
@@ -460,18 +467,24 @@ int wf_mlp_newton_iters(const wf_material* mat, double G, const float* params, c
   int32_t* dU = B.get<int32_t>(n);
   float* dD = B.get<float>(n);
   float* dP = B.get<float>(WF_MLP_NPARAM);
-  MlpPacked* dW = B.get<MlpPacked>(1);
-  if (!dS || !dI || !dU || !dD || !dP || !dW) return WF_ERR_ALLOC;
+  uint4* dW = B.get<uint4>(WF_UMMA_IMAGE / 16);
+  int* dSt = B.get<int>(1);
+  if (!dS || !dI || !dU || !dD || !dP || !dW || !dSt) return WF_ERR_ALLOC;
   cudaMemcpy(dS, states, sizeof(float) * 4 * n, cudaMemcpyHostToDevice);
+  cudaMemset(dSt, 0, sizeof(int));
   if (params) {
     cudaMemcpy(dP, params, sizeof(float) * WF_MLP_NPARAM, cudaMemcpyHostToDevice);
-    k_mlp_pack<<<1, 256>>>(dP, dW);
+    k_mlp_pack_umma<<<1, 256>>>(dP, (uint8_t*)dW);
   }
   StepParams P = jc_params(mat, rtol);
-  k_mlp_newton_iters<<<nb(n, 128), 128>>>(P, G, params ? dW : nullptr, dS, n, dI, dU, dD);
+  k_mlp_newton_iters<<<nb(n, 128), 128, params ? WF_UMMA_SMEM : 0>>>(
+      P, G, params ? dW : nullptr, dS, n, dI, dU, dD, dSt);
   cudaMemcpy(iters, dI, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
   cudaMemcpy(used, dU, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
   if (cudaMemcpy(dl, dD, sizeof(float) * n, cudaMemcpyDeviceToHost) != cudaSuccess) return WF_ERR_CUDA;
+  int st = 0;
+  cudaMemcpy(&st, dSt, sizeof(int), cudaMemcpyDeviceToHost);
+  if (st & WF_STATUS_MMA_WAIT) return WF_ERR_CUDA;
   return cudaGetLastError() == cudaSuccess ? WF_OK : WF_ERR_CUDA;
 }
 

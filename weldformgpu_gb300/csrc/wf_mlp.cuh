@@ -10,6 +10,8 @@
 //   f3 = homologous temperature
 //   y  = dlambda / dlambda_radial, where dlambda_radial = (sigma_trial - sigma_y0) / 3G
 // A prediction outside (0, 1] is ignored and Newton starts from the radial value.
+// Inference runs on the 5th-generation tensor cores (tcgen05, mlp_umma_cta)
+// for a block's 128 particles at once, inside the stress kernel.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -39,32 +41,6 @@ __device__ __forceinline__ float mlp_accept(float y) {
   return 0.0f;
 }
 
-// ---------------------------------------------------------------------------
-// BF16 tensor-core inference (mma.sync m16n8k16, FP32 accumulation).
-//
-// One warp evaluates the network for its 32 particles: rows of the A operand
-// are particles (two m-tiles of 16), columns are input features.  Layer 1 has
-// K = 16 (4 features, a constant 1 that carries the bias b1, zeros); layer 2
-// has K = 64 in 4 k-steps; both have N = 64 in 8 n-tiles.  The FP32 layer-1
-// accumulator fragments become the BF16 A fragments of layer 2 without data
-// movement (for m16n8k16 the C layout of n-tiles 2k, 2k+1 is the A layout of
-// k-step k).  Layer 3 (N = 1) is a dot product reduced across each quad.
-//
-// Fragment layouts (PTX ISA, mma.m16n8k16 with .bf16): lane = 4 g + t;
-//   A regs: {A[g][2t..2t+1]}, {A[g+8][2t..]}, {A[g][2t+8..]}, {A[g+8][2t+8..]}
-//   B regs: {B[2t..2t+1][g]}, {B[2t+8..2t+9][g]}
-//   C/D:    C[g][2t], C[g][2t+1], C[g+8][2t], C[g+8][2t+1]
-// ---------------------------------------------------------------------------
-struct MlpPacked {
-  uint2 b1[8][32];       // layer-1 B fragments per n-tile and lane (W1 | b1)
-  uint2 b2[4][8][32];    // layer-2 B fragments per k-step, n-tile and lane
-  float bias2[WF_MLP_H];
-  float w3[WF_MLP_H];
-  float b3;
-  float pad[3];
-};
-#define WF_MLP_PACKED_WORDS ((int)(sizeof(MlpPacked) / 4))
-
 __device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
   __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
   return *reinterpret_cast<uint32_t*>(&v);
@@ -80,9 +56,8 @@ __device__ __forceinline__ float silu_tanh(float z) {
   return fmaf(h, t, h);
 }
 
-// Two SiLUs in BF16 for a pair of layer-1 outputs that become one BF16x2 A
-// operand of layer 2 anyway: tanh.approx.bf16x2 handles both values in one
-// MUFU operation.
+// Two SiLUs in BF16: tanh.approx.bf16x2 handles both values in one MUFU
+// operation.
 __device__ __forceinline__ uint32_t silu_bf16x2(float z0, float z1) {
   const uint32_t h = bf16x2(0.5f * z0, 0.5f * z1);
   uint32_t t, r;
@@ -91,72 +66,135 @@ __device__ __forceinline__ uint32_t silu_bf16x2(float z0, float z1) {
   return r;
 }
 
-__device__ __forceinline__ void mma_bf16_16816(float c[4], const uint32_t a[4], uint2 b) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
-      "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y));
+// ---------------------------------------------------------------------------
+// tcgen05 inference: one CTA of 128 threads evaluates the network for its 128
+// particles, row m of every matrix being thread m's particle.
+//   layer 1: D1 (128 x 64, FP32 in tensor memory) = A1 (128 x 16) x B1^T,
+//            A1 row = [f0 f1 f2 f3 1 0 ...], B1 row n = [W1[n][0..3] b1[n] 0 ...]
+//   layer 2: D2 (128 x 64) = A2 (128 x 64) x B2^T, A2 = SiLU(D1) in BF16,
+//            B2 = W2; four MMAs of K = 16 accumulate in the same 64 columns
+//   layer 3: each thread reads its row of D2, adds b2, applies SiLU and
+//            takes the dot product with W3 (FP32).
+// One thread issues the MMAs and commits them to an mbarrier; every thread
+// waits (bounded) and reads its own row with tcgen05.ld.  The 64 tensor-
+// memory columns are allocated and freed inside the call.
+//
+// Dynamic shared memory (bytes): the weight image (copied from the packed
+// parameters, MlpUmma), then the two A operands, the mbarrier and the
+// tensor-memory address.  K-major, no swizzle (wf_umma.cuh).
+// ---------------------------------------------------------------------------
+#include "wf_common.cuh"
+#include "wf_umma.cuh"
+#define WF_UMMA_B1 0          // 64 x 16 BF16 (SBO 256)
+#define WF_UMMA_B2 2048       // 64 x 64 BF16 (SBO 1024)
+#define WF_UMMA_BIAS2 10240   // 64 floats
+#define WF_UMMA_W3 10496      // 64 floats
+#define WF_UMMA_B3 10752      // 1 float
+#define WF_UMMA_IMAGE 10880   // bytes of the packed weight image (a multiple of 128)
+#define WF_UMMA_A1 10880      // 128 x 16 BF16 (SBO 256)
+#define WF_UMMA_A2 14976      // 128 x 64 BF16 (SBO 1024)
+#define WF_UMMA_MBAR 31360    // mbarrier, 8 bytes
+#define WF_UMMA_TSLOT 31368   // tensor-memory base address, 4 bytes
+#define WF_UMMA_SMEM 31488    // dynamic shared memory of a kernel that runs the MLP
+
+// byte offset of BF16 element (r, k) of a K-major operand with K columns
+__host__ __device__ __forceinline__ int umma_kmajor_off(int r, int k, int K) {
+  return (r >> 3) * (K * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2;
 }
 
-// Warp-collective: every lane of the warp must call it, convergent.  Lanes
-// with want == false pass dummy features; returns the network output for the
-// calling lane's particle, or -1 when no lane of the warp wants a prediction.
-__device__ __forceinline__ float mlp_tc_warp(const MlpPacked& W, const float f[4], bool want) {
-  const unsigned full = 0xffffffffu;
-  if (__ballot_sync(full, want) == 0u) return -1.0f;
-  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  float out = 0.0f;
-#pragma unroll
-  for (int mt = 0; mt < 2; mt++) {
-    // layer-1 A fragment: feature columns 2t, 2t+1 of particles mt*16+g and mt*16+g+8
-    uint32_t a1[4];
-#pragma unroll
-    for (int half = 0; half < 2; half++) {
-      const int src = mt * 16 + g + half * 8;
-      const float f0 = __shfl_sync(full, f[0], src), f1 = __shfl_sync(full, f[1], src);
-      const float f2 = __shfl_sync(full, f[2], src), f3 = __shfl_sync(full, f[3], src);
-      const float c0 = t == 0 ? f0 : (t == 1 ? f2 : (t == 2 ? 1.0f : 0.0f));
-      const float c1 = t == 0 ? f1 : (t == 1 ? f3 : 0.0f);
-      a1[half] = bf16x2(c0, c1);
-    }
-    a1[2] = 0u;
-    a1[3] = 0u;
-    float acc1[8][4];
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-      acc1[j][0] = acc1[j][1] = acc1[j][2] = acc1[j][3] = 0.0f;
-      mma_bf16_16816(acc1[j], a1, W.b1[j][lane]);
-    }
-    // SiLU, then the accumulators of n-tiles 2k, 2k+1 are the A fragment of k-step k
-    uint32_t a2[4][4];
-#pragma unroll
-    for (int kk = 0; kk < 4; kk++) {
-      a2[kk][0] = silu_bf16x2(acc1[2 * kk][0], acc1[2 * kk][1]);
-      a2[kk][1] = silu_bf16x2(acc1[2 * kk][2], acc1[2 * kk][3]);
-      a2[kk][2] = silu_bf16x2(acc1[2 * kk + 1][0], acc1[2 * kk + 1][1]);
-      a2[kk][3] = silu_bf16x2(acc1[2 * kk + 1][2], acc1[2 * kk + 1][3]);
-    }
-    float y0 = 0.0f, y1 = 0.0f;   // rows g and g+8 of this m-tile
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-      const int col = 8 * j + 2 * t;
-      float acc2[4] = {W.bias2[col], W.bias2[col + 1], W.bias2[col], W.bias2[col + 1]};
-#pragma unroll
-      for (int kk = 0; kk < 4; kk++) mma_bf16_16816(acc2, a2[kk], W.b2[kk][j][lane]);
-      y0 += W.w3[col] * silu_tanh(acc2[0]) + W.w3[col + 1] * silu_tanh(acc2[1]);
-      y1 += W.w3[col] * silu_tanh(acc2[2]) + W.w3[col + 1] * silu_tanh(acc2[3]);
-    }
-    y0 += __shfl_xor_sync(full, y0, 1);
-    y0 += __shfl_xor_sync(full, y0, 2);
-    y1 += __shfl_xor_sync(full, y1, 1);
-    y1 += __shfl_xor_sync(full, y1, 2);
-    // particle p = mt*16 + half*8 + r sits in row r (+8 for half 1) of quad r
-    const float v0 = __shfl_sync(full, y0, 4 * (lane & 7));
-    const float v1 = __shfl_sync(full, y1, 4 * (lane & 7));
-    if ((lane >> 4) == mt) out = ((lane >> 3) & 1) ? v1 : v0;
+// Kernel entry of every kernel that contains the MLP (all threads of the
+// block, before anything else): with the network on (image != nullptr) copies
+// the weight image into dynamic shared memory, initialises the mbarrier and
+// allocates the 64 tensor-memory columns; in every case warp 0 gives up the
+// allocation permit so further CTAs can start on the SM.  Ends with a barrier.
+__device__ __forceinline__ void mlp_umma_begin(uint8_t* sm, const uint4* __restrict__ image) {
+  if (image) {
+    for (int k = threadIdx.x; k < WF_UMMA_IMAGE / 16; k += blockDim.x)
+      reinterpret_cast<uint4*>(sm)[k] = image[k];
+    if (threadIdx.x == 0) umma::mbar_init(umma::smem_addr(sm) + WF_UMMA_MBAR, 1);
   }
-  return out + W.b3;
+  if (threadIdx.x < 32) {
+    if (image) umma::tmem_alloc(umma::smem_addr(sm) + WF_UMMA_TSLOT, 64);
+    umma::relinquish_permit();
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+}
+
+// Block-collective, once per kernel after mlp_umma_begin(sm, image != nullptr):
+// blockDim.x == 128 and every thread calls it at the same point.  Frees the
+// tensor memory.  Returns the network output for the calling thread's row,
+// or -1 when no thread of the block wants a prediction or a completion wait
+// ran out (then WF_STATUS_MMA_WAIT is set in *status).
+static __device__ __forceinline__ float mlp_umma_cta(uint8_t* sm, const float f[4], bool want,
+                                                     int* status) {
+  constexpr int kWaitLimit = 1 << 20;
+  constexpr uint32_t kId = umma::idesc_bf16_f32(128, 64);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(sm + WF_UMMA_TSLOT);
+  if (!__syncthreads_or(want)) {
+    if (warp == 0) umma::tmem_dealloc(tmem, 64);
+    return -1.0f;
+  }
+  const uint32_t s0 = umma::smem_addr(sm);
+  const uint32_t mbar = s0 + WF_UMMA_MBAR;
+  uint4* a1 = reinterpret_cast<uint4*>(sm + WF_UMMA_A1 + umma_kmajor_off(tid, 0, 16));
+  a1[0] = make_uint4(bf16x2(f[0], f[1]), bf16x2(f[2], f[3]), bf16x2(1.0f, 0.0f), 0u);
+  a1[8] = make_uint4(0u, 0u, 0u, 0u);            // columns 8..15, the next core matrix
+  umma::fence_async_smem();
+  __syncthreads();
+  umma::fence_after_sync();
+  if (tid == 0) {
+    umma::mma_bf16(tmem, umma::smem_desc(s0 + WF_UMMA_A1, 128, 256),
+                   umma::smem_desc(s0 + WF_UMMA_B1, 128, 256), kId, 0u);
+    umma::commit(mbar);
+  }
+  bool ok = umma::mbar_wait(mbar, 0, kWaitLimit);
+  umma::fence_after_sync();
+  const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);   // this warp's 32 lanes
+  uint4* a2 = reinterpret_cast<uint4*>(sm + WF_UMMA_A2 + umma_kmajor_off(tid, 0, 64));
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    float v[16];
+    umma::ld16(trow + 16 * c, v);
+    uint32_t r[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) r[j] = silu_bf16x2(v[2 * j], v[2 * j + 1]);
+    a2[16 * c] = make_uint4(r[0], r[1], r[2], r[3]);       // columns 16c .. 16c+7
+    a2[16 * c + 8] = make_uint4(r[4], r[5], r[6], r[7]);   // columns 16c+8 .. 16c+15
+  }
+  umma::fence_async_smem();
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  if (tid == 0) {
+#pragma unroll
+    for (int kk = 0; kk < 4; kk++)
+      umma::mma_bf16(tmem, umma::smem_desc(s0 + WF_UMMA_A2 + 256 * kk, 128, 1024),
+                     umma::smem_desc(s0 + WF_UMMA_B2 + 256 * kk, 128, 1024), kId, kk > 0 ? 1u : 0u);
+    umma::commit(mbar);
+  }
+  ok = umma::mbar_wait(mbar, 1, kWaitLimit) && ok;
+  umma::fence_after_sync();
+  const float* bias2 = reinterpret_cast<const float*>(sm + WF_UMMA_BIAS2);
+  const float* w3 = reinterpret_cast<const float*>(sm + WF_UMMA_W3);
+  float y = 0.0f;
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    float v[16];
+    umma::ld16(trow + 16 * c, v);
+#pragma unroll
+    for (int j = 0; j < 16; j++) y += w3[16 * c + j] * silu_tanh(v[j] + bias2[16 * c + j]);
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) umma::tmem_dealloc(tmem, 64);
+  if (!ok) {
+    if (tid == 0) atomicOr(status, WF_STATUS_MMA_WAIT);
+    return -1.0f;
+  }
+  return y + *reinterpret_cast<const float*>(sm + WF_UMMA_B3);
 }
 
 __device__ __forceinline__ void mlp_features(float ratio, double eps_p, float eff, float Th,

@@ -219,17 +219,12 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
                                                   const int32_t* __restrict__ nb,
                                                   const int32_t* __restrict__ cnt,
                                                   int* __restrict__ status,
-                                                  const MlpPacked* __restrict__ mlp) {
-  // The MLP runs on tensor cores with warp-collective mma.sync: every lane of
-  // a warp must reach it, so out-of-range and non-solid lanes are predicated
-  // rather than returned before that point.
-  extern __shared__ uint32_t smlp[];
-  const MlpPacked& Wm = *reinterpret_cast<const MlpPacked*>(smlp);
-  if (mlp) {
-    for (int k = threadIdx.x; k < WF_MLP_PACKED_WORDS; k += blockDim.x)
-      smlp[k] = reinterpret_cast<const uint32_t*>(mlp)[k];
-    __syncthreads();
-  }
+                                                  const uint4* __restrict__ mlp) {
+  // The MLP runs on the tensor cores (tcgen05) for the block's 128 particles
+  // at once: every thread of the block must reach it, so out-of-range and
+  // non-solid threads are predicated rather than returned before that point.
+  extern __shared__ __align__(1024) uint8_t smlp[];
+  mlp_umma_begin(smlp, mlp);
   const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const bool valid = i0 < P.n;
   const int64_t i = valid ? i0 : 0;
@@ -340,8 +335,7 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
     const bool want = solid && jc_newton && st > sy0f;
     float f[4] = {0.f, 0.f, 0.f, 0.f};
     if (want) mlp_features(st / sy0f, eps_p, eff, Th, f);
-    __syncwarp();
-    const float y = mlp_tc_warp(Wm, f, want);
+    const float y = mlp_umma_cta(smlp, f, want, status);
     const float yc = mlp_accept(y);
     if (want && yc > 0.0f) ratio = (double)yc;
     if (!solid) return;
@@ -515,8 +509,8 @@ void launch_fp32_density_heat(const StepParams& P, const Fields& F, double4* vd2
 }
 void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b, float* sigr32,
                         const NbBuffers& N, int* status, const void* mlp_packed, cudaStream_t s) {
-  const MlpPacked* W = reinterpret_cast<const MlpPacked*>(mlp_packed);
-  size_t smem = W ? sizeof(MlpPacked) : 0;
+  const uint4* W = reinterpret_cast<const uint4*>(mlp_packed);
+  size_t smem = W ? WF_UMMA_SMEM : 0;
   k_stress32<<<blocks_for(P.n, 128), 128, smem, s>>>(P, F, v32b, sigr32, N.nb, N.cnt, status, W);
 }
 void launch_fp32_accel(const StepParams& P, const Fields& F, const float4* v32b,
