@@ -798,6 +798,8 @@ static int finish(wf_domain* d) {
   if (rc) return rc;
   WF_CUDA_OK(cudaGetLastError());
   if (d->h_status[0] & WF_STATUS_NAN) return wf_fail(d, WF_ERR_NUMERIC, "non-finite stress detected");
+  if (d->h_status[0] & WF_STATUS_MMA_WAIT)
+    return wf_fail(d, WF_ERR_CUDA, "a tensor-core completion wait ran out (warm-start network)");
   return WF_OK;
 }
 

@@ -93,8 +93,9 @@ __device__ __forceinline__ uint32_t silu_bf16x2(float z0, float z1) {
 #define WF_UMMA_IMAGE 10880   // bytes of the packed weight image (a multiple of 128)
 #define WF_UMMA_A1 10880      // 128 x 16 BF16 (SBO 256)
 #define WF_UMMA_A2 14976      // 128 x 64 BF16 (SBO 1024)
-#define WF_UMMA_MBAR 31360    // mbarrier, 8 bytes
+#define WF_UMMA_MBAR 31360    // mbarrier of the MMAs, 8 bytes
 #define WF_UMMA_TSLOT 31368   // tensor-memory base address, 4 bytes
+#define WF_UMMA_MBAR_W 31376  // mbarrier of the weight-image copy, 8 bytes
 #define WF_UMMA_SMEM 31488    // dynamic shared memory of a kernel that runs the MLP
 
 // byte offset of BF16 element (r, k) of a K-major operand with K columns
@@ -103,23 +104,32 @@ __host__ __device__ __forceinline__ int umma_kmajor_off(int r, int k, int K) {
 }
 
 // Kernel entry of every kernel that contains the MLP (all threads of the
-// block, before anything else): with the network on (image != nullptr) copies
-// the weight image into dynamic shared memory, initialises the mbarrier and
-// allocates the 64 tensor-memory columns; in every case warp 0 gives up the
-// allocation permit so further CTAs can start on the SM.  Ends with a barrier.
-__device__ __forceinline__ void mlp_umma_begin(uint8_t* sm, const uint4* __restrict__ image) {
-  if (image) {
-    for (int k = threadIdx.x; k < WF_UMMA_IMAGE / 16; k += blockDim.x)
-      reinterpret_cast<uint4*>(sm)[k] = image[k];
-    if (threadIdx.x == 0) umma::mbar_init(umma::smem_addr(sm) + WF_UMMA_MBAR, 1);
+// block, before anything else): with the network on (image != nullptr) one
+// thread starts a bulk copy of the weight image into dynamic shared memory
+// and initialises the mbarriers, and warp 0 allocates the 64 tensor-memory
+// columns; in every case warp 0 gives up the allocation permit so further
+// CTAs can start on the SM.  Ends once the image has arrived.  The image must
+// be 16-byte aligned (WF_UMMA_IMAGE is a multiple of 16).  Returns false
+// (and sets WF_STATUS_MMA_WAIT) if the copy's wait ran out.
+__device__ __forceinline__ bool mlp_umma_begin(uint8_t* sm, const uint4* __restrict__ image,
+                                               int* status) {
+  const uint32_t s0 = umma::smem_addr(sm);
+  if (image && threadIdx.x == 0) {
+    umma::mbar_init(s0 + WF_UMMA_MBAR, 1);
+    umma::mbar_init(s0 + WF_UMMA_MBAR_W, 1);
+    umma::bulk_load(s0, image, WF_UMMA_IMAGE, s0 + WF_UMMA_MBAR_W);
   }
   if (threadIdx.x < 32) {
-    if (image) umma::tmem_alloc(umma::smem_addr(sm) + WF_UMMA_TSLOT, 64);
+    if (image) umma::tmem_alloc(s0 + WF_UMMA_TSLOT, 64);
     umma::relinquish_permit();
   }
   umma::fence_before_sync();
   __syncthreads();
   umma::fence_after_sync();
+  if (!image) return true;
+  const bool ok = umma::mbar_wait(s0 + WF_UMMA_MBAR_W, 0, 1 << 20);
+  if (!ok && threadIdx.x == 0) atomicOr(status, WF_STATUS_MMA_WAIT);
+  return ok;
 }
 
 // Block-collective, once per kernel after mlp_umma_begin(sm, image != nullptr):

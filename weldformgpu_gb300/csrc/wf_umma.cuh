@@ -99,6 +99,19 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar_saddr, uint32_t parity, 
   return false;
 }
 
+// One bulk copy (TMA, untiled) of `bytes` from global to shared memory whose
+// completion is counted on the mbarrier: the issuing thread arrives once and
+// announces the byte count.  Both addresses 16-byte aligned, bytes a
+// multiple of 16.
+__device__ __forceinline__ void bulk_load(uint32_t dst_saddr, const void* src, uint32_t bytes,
+                                          uint32_t mbar_saddr) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+               :: "r"(mbar_saddr), "r"(bytes) : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      :: "r"(dst_saddr), "l"(src), "r"(bytes), "r"(mbar_saddr) : "memory");
+}
+
 // 16 consecutive 32-bit columns of the calling thread's tensor-memory lane
 // (the warp's quadrant of lanes is fixed by the lane field of taddr).  The
 // load and its wait are one asm statement, so no use of the registers can be
