@@ -90,6 +90,7 @@ struct wf_domain {
   bool bins_built = false;
   // adaptive rebuild at a plastic-strain increment (0: the reference's cadence)
   double rb_dep = 0.0;
+  double k_cond = 0.0;          // conductivity (wf_set_conductivity: uniform)
   int64_t rebuilds = 0;         // neighbour rebuilds inside the step loop
   unsigned long long* d_maxdep = nullptr;
   unsigned long long* h_maxdep = nullptr;
@@ -199,7 +200,7 @@ __global__ void k_mixed_init(int64_t n, Fields F) {
   for (int c = 0; c < 6; c++) F.ss32[s * 6 + c] = (float)F.ss6[s * 6 + c];
   const double T = F.T[s];
   const float thi = (float)T;
-  F.th32[s] = make_float4(thi, (float)(T - (double)thi), (float)F.kT[s], (float)v.w);
+  F.th32[s] = make_float2(thi, (float)(T - (double)thi));
 }
 // FP64 copy of the FP32 deviatoric state (mixed -> plain switch)
 __global__ void k_mixed_to_fp64(int64_t n, Fields F) {
@@ -398,6 +399,7 @@ static StepParams make_params(const wf_domain* d) {
   P.Cf = (float)P.gkC;
   P.Chf = (float)(P.gkC / P.h);
   P.Csf = (float)P.Cs;
+  P.k2f = (float)(2.0 * d->k_cond);
   P.alphaf = (float)P.alpha;
   P.betaf = (float)P.beta;
   P.epsf = (float)(0.01 * P.h * P.h);
@@ -918,6 +920,7 @@ int wf_set_sigma_y(wf_domain* d, double sy) {
 }
 int wf_set_conductivity(wf_domain* d, double k) {
   if (!d) return WF_ERR_ARG;
+  d->k_cond = k;   // one value for every particle
   return fill_d(d, k, CF(d).kT, 1, 0);
 }
 int wf_set_heat_cap(wf_domain* d, double cp) {

@@ -79,7 +79,7 @@ struct Fields {
   float4* p32;      // position xyz, mass w
   float4* v32;      // velocity xyz, density w
   float* ss32;      // deviatoric stress FP32 state (mixed form), 6 per slot
-  float4* th32;     // heat-flux mirror (mixed form): T as a float pair (hi, lo), k, rho
+  float2* th32;     // heat-flux mirror (mixed form): T as a float pair (hi, lo)
   double* pwn;      // cached eps_p^n of the Johnson-Cook law (< 0: not cached yet)
   // contact (allocated when a rigid mesh is added)
   double4* nrm;     // surface normal (solid particles) / element normal (rigid particles)
@@ -165,6 +165,7 @@ struct StepParams {
   // FP32 constants for the mixed form, computed once on the host: on GB300 a
   // per-thread FP64 division or conversion costs as much as an FP32 pair loop
   float hf, invhf, Cf, Chf, Csf, alphaf, betaf, epsf, dtf, G2f, mlp_scale;
+  float k2f;        // 2 k: the pair conductivity 4 k_i k_j / (k_i + k_j) of a uniform k
   // Johnson-Cook constants of the FP32 increment form of the Newton return map
   float G3f, jcAf, jcBf, jcnf, binf[5];
   float jcTtf, jcinvdTf, jcCf, jcinveps0f, jcmf;   // T_t, 1/(T_m - T_t), C, 1/eps_0, m

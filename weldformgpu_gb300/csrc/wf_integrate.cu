@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(256) k_integrate(StepParams P, Fields F,
     F.v32[i] = make_float4((float)vx, (float)vy, (float)vz, (float)v4.w);
     const double T = F.T[i];
     const float thi = (float)T;
-    F.th32[i] = make_float4(thi, (float)(T - (double)thi), (float)F.kT[i], (float)v4.w);
+    F.th32[i] = make_float2(thi, (float)(T - (double)thi));
     return;
   }
   const double dt = P.dt;
@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(128) k_heat_rate(StepParams P, Fields F,
   } else {
     // temperature differences from the (hi, lo) float pair: exact to ~1e-14 of T
     const float4 pi = F.p32[i];
-    const float4 ti = F.th32[i];
+    const float2 ti = F.th32[i];
     const float invh = P.invhf, C = P.Cf, Ch = P.Chf;
     float sf = 0.0f;
     int4 lo = make_int4(0, 0, 0, 0), hi = lo;
@@ -130,11 +130,14 @@ __global__ void __launch_bounds__(128) k_heat_rate(StepParams P, Fields F,
       if (m > WF_NB_BLK) nb_block(nb, P.npad, i, b + 1, lo, hi);
 #pragma unroll
       for (int h = 0; h < WF_NB_BLK; h += 4) {
-        float4 pj[4], tj[4];
+        float4 pj[4];
+        float2 tj[4];
+        float rj[4];
 #pragma unroll
         for (int u = 0; u < 4; u++) {
           pj[u] = F.p32[js[h + u]];
           tj[u] = F.th32[js[h + u]];
+          rj[u] = F.v32[js[h + u]].w;
         }
 #pragma unroll
         for (int u = 0; u < 4; u++) {
@@ -143,12 +146,11 @@ __global__ void __launch_bounds__(128) k_heat_rate(StepParams P, Fields F,
           const float xx = pi.x - pj[u].x, xy = pi.y - pj[u].y, xz = pi.z - pj[u].z;
           // x.(GK x) / r^2 = GK
           const float GK = gk32_r2(xx * xx + xy * xy + xz * xz, invh, Ch, C);
-          sf += __fdividef(pj[u].w, tj[u].w) * __fdividef(4.0f * ti.z * tj[u].z, ti.z + tj[u].z) *
-                dT * GK;
+          sf += __fdividef(pj[u].w, rj[u]) * dT * GK;
         }
       }
     }
-    F.dTdt[i] = heat_rate_mixed(P, F, i, sf, rhoi, xi.w, Ti, plastic_heat);
+    F.dTdt[i] = heat_rate_mixed(P, F, i, P.k2f * sf, rhoi, xi.w, Ti, plastic_heat);
     return;
   }
   s *= 1. / (rhoi * F.cpT[i]);
@@ -173,10 +175,7 @@ __global__ void __launch_bounds__(256) k_heat_leapfrog(StepParams P, Fields F, i
   const double T = heat_leapfrog_one(P, F, i, F.dTdt[i], first);
   if (mixed && !first) {
     const float thi = (float)T;
-    float4 t = F.th32[i];
-    t.x = thi;
-    t.y = (float)(T - (double)thi);
-    F.th32[i] = t;
+    F.th32[i] = make_float2(thi, (float)(T - (double)thi));
   }
 }
 

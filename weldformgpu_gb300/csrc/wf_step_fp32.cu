@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(128) k_density_heat32(StepParams P, Fields F,
   if (i >= P.n) return;
   const float4 pi = F.p32[i];
   const float4 vi = F.v32[i];
-  const float4 ti = F.th32[i];
+  const float2 ti = F.th32[i];
   const double4 vdi = F.vd[i];
   const bool solid = F.perm[i] < P.n_solid;
   const float invh = P.invhf, C = P.Cf, Ch = P.Chf;
@@ -116,7 +116,8 @@ __global__ void __launch_bounds__(128) k_density_heat32(StepParams P, Fields F,
     if (m > WF_NB_BLK) nb_block(nb, P.npad, i, b + 1, lo, hi);
 #pragma unroll
     for (int h = 0; h < WF_NB_BLK; h += 4) {
-      float4 pj[4], vj[4], tj[4];
+      float4 pj[4], vj[4];
+      float2 tj[4];
 #pragma unroll
       for (int q = 0; q < 4; q++) {
         pj[q] = F.p32[js[h + q]];
@@ -129,9 +130,10 @@ __global__ void __launch_bounds__(128) k_density_heat32(StepParams P, Fields F,
         const float xx = pi.x - pj[q].x, xy = pi.y - pj[q].y, xz = pi.z - pj[q].z;
         const float GK = gk32_r2(xx * xx + xy * xy + xz * xz, invh, Ch, C);
         const float mr = __fdividef(pj[q].w, vj[q].w);   // m_j / rho_j
-        // heat flux (every particle, no contact filter)
+        // heat flux (every particle, no contact filter); the pair
+        // conductivity 4 k_i k_j / (k_i + k_j) = 2k multiplies the sum
         const float dT = (ti.x - tj[q].x) + (ti.y - tj[q].y);
-        sf += mr * __fdividef(4.0f * ti.z * tj[q].z, ti.z + tj[q].z) * dT * GK;
+        sf += mr * dT * GK;
         // density rate (solid particles, contact filter)
         if (solid && !(P.contact && !pass_ij(P, idi, F.id[js[h + q]]))) {
           const float vx = vi.x - vj[q].x, vy = vi.y - vj[q].y, vz = vi.z - vj[q].z;
@@ -141,7 +143,7 @@ __global__ void __launch_bounds__(128) k_density_heat32(StepParams P, Fields F,
     }
   }
   // heat of the previous step: rate and leapfrog, own particle only
-  const double dTdt = heat_rate_mixed(P, F, i, sf, vdi.w, (double)pi.w, F.T[i], plastic_heat);
+  const double dTdt = heat_rate_mixed(P, F, i, P.k2f * sf, vdi.w, (double)pi.w, F.T[i], plastic_heat);
   F.dTdt[i] = dTdt;
   heat_leapfrog_one(P, F, i, dTdt, first);
   // density of this step
