@@ -40,7 +40,7 @@ WORKLOAD = "jc_thermomech_compression_R25mm_H50mm_dx0.5mm"
 # mixed form the density launch also runs the previous step's heat pass
 # (k_density_heat32); "thermal" there is only the heat pass of a call's last step.
 BYTES_MODEL = {
-    "mixed": {"density": 224, "stress": 248, "accel": 104, "integrate": 328, "thermal": 96},
+    "mixed": {"density": 216, "stress": 248, "accel": 96, "integrate": 320, "thermal": 88},
     "fp64": {"density": 120, "stress": 416, "accel": 144, "integrate": 264, "thermal": 112},
 }
 NB_INDEX_BYTES = 4  # per neighbour per pair pass
