@@ -170,12 +170,17 @@ class Domain_d:
         return e.value, k.value, kl.value, tl.value
 
     # ---- outputs --------------------------------------------------------
-    def get_field(self, name):
+    def get_field(self, name, out=None):
+        """A state field in the caller's order; `out` (float64, n x components,
+        C-contiguous, e.g. in pinned host memory) receives it if given."""
         c = _abi.FIELD_COMPONENTS.get(name, 1)
-        out = np.empty(self.n * c, dtype=np.float64)
+        if out is None:
+            out = np.empty(self.n * c, dtype=np.float64)
+        elif out.dtype != np.float64 or out.size != self.n * c or not out.flags.c_contiguous:
+            raise ValueError("get_field(%s): out must be %d contiguous float64" % (name, self.n * c))
         self._ck(self.L.wf_get_field(self.h, name.encode(), _ptr(out, C.c_double)),
                  "wf_get_field(%s)" % name)
-        return out.reshape(self.n, c) if c > 1 else out
+        return out.reshape(self.n, c) if c > 1 else out.reshape(self.n)
 
     def set_field(self, name, values):
         """Writes a state field (caller's order); see wf_set_field."""
