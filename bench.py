@@ -403,6 +403,43 @@ def bench_indentation(args):
     print(json.dumps(line))
 
 
+def bench_heat(args):
+    """Config-2 shape: heat conduction only (ThermalSolve) in a 100^3-particle
+    steel box (dx = 0.1 mm, 1.0M particles), Gaussian hot spot, convection on
+    the outer layer, dt = 0.1 dx^2 rho c_p / k.  Plain FP64 against the mixed
+    form (FP32 flux, FP64 temperature accumulation).  Each solve call starts
+    with one neighbour search (as the reference's ThermalSolve) and is timed
+    with the host clock around the call after one warm-up call."""
+    from weldformgpu_gb300 import Domain_d
+    from weldformgpu_gb300 import scenarios as S
+    sc = S.heat_box(n_side=100)
+    n = sc["n"]
+    steps = max(args.steps, 20) * 2
+    out, T = {}, {}
+    for form in ("mixed", "fp64"):
+        d = S.load_heat(Domain_d(n), sc)
+        d.set_option("precision", 1 if form == "mixed" else 0)
+        d.thermal_solve(5 * sc["dt"])
+        t0 = time.perf_counter()
+        d.thermal_solve(steps * sc["dt"] * (1.0 - 1e-9))
+        el = time.perf_counter() - t0
+        T[form] = d.get_field("T")
+        out[form] = dict(value=n * steps / el, ms_per_step=1e3 * el / steps,
+                         steps=int(d.get_scalar("step")) - 5)
+        d.close()
+    line = {"workload": "heat_conduction_box100x100x100_dx0.1mm", "unit": UNIT,
+            "metric": "particle-steps/s, mixed (FP32 flux) vs plain FP64 on 1 GB300",
+            "value": out["mixed"]["value"], "ms_per_step": out["mixed"]["ms_per_step"],
+            "steps": steps, "n_gpus": 1, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"particles": n, "dx_m": sc["dx"], "dt_s": sc["dt"],
+                       "timing": "host clock around one ThermalSolve call of `steps` steps, "
+                                 "including its initial neighbour search"},
+            "mixed": out["mixed"], "plain_fp64": out["fp64"],
+            "speedup_vs_plain_fp64": out["mixed"]["value"] / out["fp64"]["value"],
+            "rel_l2_vs_fp64": rel_l2(T["mixed"] - sc["T"], T["fp64"] - sc["T"])}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -419,15 +456,17 @@ def main():
     ap.add_argument("--no-mlp", action="store_true", help="time the mixed form without the MLP")
     ap.add_argument("--preload", type=int, default=4000,
                     help="steps run (mixed form) before the timed runs, to reach plasticity")
-    ap.add_argument("--workload", default="compression", choices=["compression", "indentation"],
+    ap.add_argument("--workload", default="compression",
+                    choices=["compression", "indentation", "heat"],
                     help="compression: the metric's workload; indentation: the 2M-particle "
-                         "contact case (a separate line, not the metric)")
+                         "contact case; heat: the 1M-particle heat-only case (separate "
+                         "lines, not the metric)")
     args = ap.parse_args()
     warmup = max(args.warmup, 3)
-    if args.workload == "indentation":
+    if args.workload in ("indentation", "heat"):
         from weldformgpu_gb300 import build as Bld
         Bld.build()
-        bench_indentation(args)
+        (bench_indentation if args.workload == "indentation" else bench_heat)(args)
         return
     rank, ws, dist = dist_setup(args.gpus)
 
