@@ -107,8 +107,9 @@ int wf_set_convection(wf_domain* d, double h_conv, double T_inf); /* h_conv_doub
  * friction -mu_static F_n v_t / max(|v_t|, contact_vreg) and frictional heat
  * contact_heat_fraction * mu_static F_n |v_t|^2 / max(|v_t|, contact_vreg)
  * into the particle ("fric_heat", W).  Law 1 needs the option contact_dx and
- * tools that translate only (angular velocity 0); the solve fails with
- * WF_ERR_STATE otherwise. */
+ * tools that translate only (angular velocity 0): wf_set_contact fails with
+ * WF_ERR_ARG when a rotating mesh is already added, and the solve fails with
+ * WF_ERR_STATE when contact_dx is missing or a rotating mesh came later. */
 int wf_set_contact(wf_domain* d, double mu_static, double mu_dynamic, int law);
 /* A rigid triangle mesh (TriMesh_d, src/cuda/Mesh.cuh:19-54) as main adds it
  * (AddTrimeshParticles + AssignTrimeshAddress + SetMeshVel,

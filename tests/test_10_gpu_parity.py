@@ -295,6 +295,37 @@ def test_contact_law1_mixed_within_1e3():
     assert rel_l2(gm.get_field("T") - 20.0, g64.get_field("T") - 20.0) < 1e-3
 
 
+def test_contact_law1_rejects_missing_dx_and_rotating_tools():
+    """Law 1 needs contact_dx and a tool that only translates (its triangle
+    bins follow the tool by translation): the solve fails with WF_ERR_STATE
+    before any step, and leaves the domain usable once fixed."""
+    from weldformgpu_gb300 import Domain_d
+    from weldformgpu_gb300.domain import WeldformError
+    sc = S.indent_block(L=(0.002, 0.002, 0.001), R=0.002, level=2)
+    opts = dict(sc["options"])
+    del opts["contact_dx"]
+    d = S.load(Domain_d(sc["n"]), dict(sc, options=opts))
+    with pytest.raises(WeldformError) as e:
+        d.step(1)
+    assert e.value.code == -3 and "contact_dx" in str(e.value)
+    d.set_option("contact_dx", sc["dx"])
+    d.step(1)
+    # a rotating tool: rejected by wf_set_contact when the mesh came first ...
+    ms = dict(sc["mesh"], angvel=(0.0, 0.0, 1.0))
+    with pytest.raises(WeldformError) as e:
+        S.load(Domain_d(sc["n"]), dict(sc, mesh=ms))
+    assert e.value.code == -1 and "translating" in str(e.value)
+    # ... and by the solve when the law was chosen first
+    r = S.load(Domain_d(sc["n"]), {k: v for k, v in sc.items() if k != "mesh"})
+    r.set_contact(sc["mu"][0], sc["mu"][1], 1)
+    r.add_trimesh(ms["nodes"], ms["tris"], ms["zone"], ms["first"], ms["vel"], ms["angvel"])
+    for k, v in sc["options"].items():
+        r.set_option(k, float(v))
+    with pytest.raises(WeldformError) as e:
+        r.step(1)
+    assert e.value.code == -3 and "angular velocity" in str(e.value)
+
+
 def test_mixed_fused_heat_matches_separate_heat_pass():
     """Mixed form: the heat pass fused into the next step's density pass gives
     the temperatures of the separate heat pass (to FP32 rounding), including
