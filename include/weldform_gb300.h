@@ -104,12 +104,13 @@ int wf_set_convection(wf_domain* d, double h_conv, double T_inf); /* h_conv_doub
  * with the tool), the gap to the nearest surface point along the direction
  * from that point (the face normal for a centre behind the face), penalty
  * F_n = contact_stiffness * K * contact_dx * (contact_dx/2 - gap), Coulomb
- * friction -mu_static F_n v_t / max(|v_t|, contact_vreg) and frictional heat
- * contact_heat_fraction * mu_static F_n |v_t|^2 / max(|v_t|, contact_vreg)
- * into the particle ("fric_heat", W).  Law 1 needs the option contact_dx and
- * tools that translate only (angular velocity 0): wf_set_contact fails with
- * WF_ERR_ARG when a rotating mesh is already added, and the solve fails with
- * WF_ERR_STATE when contact_dx is missing or a rotating mesh came later. */
+ * friction -mu_static F_n v_t / max(|v_t|, contact_vreg) with v_t the
+ * tangential velocity relative to the tool surface at the nearest point
+ * (m_v + m_w x q), and frictional heat contact_heat_fraction * mu_static F_n
+ * |v_t|^2 / max(|v_t|, contact_vreg) into the particle ("fric_heat", W).
+ * Translating tools are binned once, rotating ones again on the GPU every
+ * step.  Law 1 needs the option contact_dx (the solve fails with WF_ERR_STATE
+ * without it) and meshes of fewer than 2^24 triangles. */
 int wf_set_contact(wf_domain* d, double mu_static, double mu_dynamic, int law);
 /* A rigid triangle mesh (TriMesh_d, src/cuda/Mesh.cuh:19-54) as main adds it
  * (AddTrimeshParticles + AssignTrimeshAddress + SetMeshVel,

@@ -934,7 +934,9 @@ static void stage_contact_law1(wfo_domain* d) {
     if (!(delta > 0.0)) continue;
     const double fn = d->c_kappa * K * d->c_dx * delta;
     d3 f = d3_scale(n, fn);
-    const d3 vrel = d3_sub(d->v[i], d->mesh[bm].m_v);
+    /* relative to the tool surface at the nearest point: m_v + m_w x q */
+    const d3 vtool = d3_add(d->mesh[bm].m_v, d3_cross(d->mesh[bm].m_w, bq));
+    const d3 vrel = d3_sub(d->v[i], vtool);
     const d3 vt = d3_sub(vrel, d3_scale(n, d3_dot(vrel, n)));
     const double vtl = d3_len(vt);
     if (d->mu_s > 0.0) {
@@ -1349,10 +1351,6 @@ int wfo_set_option(wfo_domain* d, const char* key, double v) {
  * (0: the reference's penalty law, CalcContactForcesWang) */
 int wfo_set_contact(wfo_domain* d, double mu_static, double mu_dynamic, int law) {
   if (!d || law < 0 || law > 1 || !(mu_static >= 0.0) || !(mu_dynamic >= 0.0)) return WF_ERR_ARG;
-  if (law == 1)
-    for (int mi = 0; mi < d->trimesh_count; mi++)
-      if (d->mesh[mi].m_w.x != 0.0 || d->mesh[mi].m_w.y != 0.0 || d->mesh[mi].m_w.z != 0.0)
-        return fail(d, WF_ERR_ARG, "contact law 1 takes translating tools only");
   d->mu_s = mu_static;
   d->mu_d = mu_dynamic;
   d->contact_law = law;

@@ -295,10 +295,9 @@ def test_contact_law1_mixed_within_1e3():
     assert rel_l2(gm.get_field("T") - 20.0, g64.get_field("T") - 20.0) < 1e-3
 
 
-def test_contact_law1_rejects_missing_dx_and_rotating_tools():
-    """Law 1 needs contact_dx and a tool that only translates (its triangle
-    bins follow the tool by translation): the solve fails with WF_ERR_STATE
-    before any step, and leaves the domain usable once fixed."""
+def test_contact_law1_rejects_missing_dx():
+    """Law 1 needs contact_dx: the solve fails with WF_ERR_STATE before any
+    step and the domain is usable once it is set."""
     from weldformgpu_gb300 import Domain_d
     from weldformgpu_gb300.domain import WeldformError
     sc = S.indent_block(L=(0.002, 0.002, 0.001), R=0.002, level=2)
@@ -310,20 +309,29 @@ def test_contact_law1_rejects_missing_dx_and_rotating_tools():
     assert e.value.code == -3 and "contact_dx" in str(e.value)
     d.set_option("contact_dx", sc["dx"])
     d.step(1)
-    # a rotating tool: rejected by wf_set_contact when the mesh came first ...
-    ms = dict(sc["mesh"], angvel=(0.0, 0.0, 1.0))
-    with pytest.raises(WeldformError) as e:
-        S.load(Domain_d(sc["n"]), dict(sc, mesh=ms))
-    assert e.value.code == -1 and "translating" in str(e.value)
-    # ... and by the solve when the law was chosen first
-    r = S.load(Domain_d(sc["n"]), {k: v for k, v in sc.items() if k != "mesh"})
-    r.set_contact(sc["mu"][0], sc["mu"][1], 1)
-    r.add_trimesh(ms["nodes"], ms["tris"], ms["zone"], ms["first"], ms["vel"], ms["angvel"])
-    for k, v in sc["options"].items():
-        r.set_option(k, float(v))
-    with pytest.raises(WeldformError) as e:
-        r.step(1)
-    assert e.value.code == -3 and "angular velocity" in str(e.value)
+
+
+def test_contact_law1_rotating_tool_fp64_vs_oracle_and_mixed():
+    """A lower-half icosphere spinning at 2,000 rad/s about the z axis while it
+    indents the centred block: its bins are rebuilt on the GPU every step, the
+    friction and heat use the tool's surface velocity m_v + m_w x q.  Plain
+    FP64 against the oracle's scan of every triangle: 1e-9 (pow/log) with the
+    same contact set; the mixed form within 1e-3 of FP64."""
+    sc = S.indent_block(rebuild_increment=0.002, omega=2000.0)
+    o, g, gm = ora(sc), gpu(sc), gpu(sc, {"precision": 1})
+    for d in (o, g, gm):
+        d.step(600)
+    for f in LAW1_FIELDS:
+        err = rel_l2(g.get_field(f), o.get_field(f))
+        assert err < 1e-9, (f, err)
+    assert rel_l2(g.get_field("T") - 20.0, o.get_field("T") - 20.0) < 1e-9
+    assert np.array_equal(g.get_field_i32("cont_count"), o.get_field_i32("cont_count"))
+    cf = g.get_field("contforce")
+    assert (g.get_field_i32("cont_count") > 0).sum() >= 10
+    assert np.abs(cf[:, :2]).sum() > 0.2 * np.abs(cf[:, 2]).sum()   # the spin drags
+    for f in ("u", "pl_strain", "contforce", "fric_heat"):
+        err = rel_l2(gm.get_field(f), g.get_field(f))
+        assert err < 1e-3, (f, err)
 
 
 def test_mixed_fused_heat_matches_separate_heat_pass():

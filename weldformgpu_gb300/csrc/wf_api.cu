@@ -515,40 +515,85 @@ static int build_tool_bins(wf_domain* d) {
     WF_CUDA_OK(cudaMemcpyAsync(nd.data(), M.node, sizeof(double4) * M.nn, cudaMemcpyDeviceToHost, d->stream));
     WF_CUDA_OK(cudaMemcpyAsync(en.data(), M.elnode, sizeof(int32_t) * 3 * M.ne, cudaMemcpyDeviceToHost, d->stream));
     WF_CUDA_OK(cudaStreamSynchronize(d->stream));
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (const double4& p : nd) {
-      const double c[3] = {p.x, p.y, p.z};
-      for (int k = 0; k < 3; k++) { lo[k] = std::min(lo[k], c[k]); hi[k] = std::max(hi[k], c[k]); }
+    // node coordinates relative to node 0
+    std::vector<double> rel(3 * (size_t)M.nn);
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300}, ext = 0.0, rmax = 0.0;
+    for (int q = 0; q < M.nn; q++) {
+      const double c[3] = {nd[q].x - nd[0].x, nd[q].y - nd[0].y, nd[q].z - nd[0].z};
+      for (int k = 0; k < 3; k++) {
+        rel[3 * q + k] = c[k];
+        lo[k] = std::min(lo[k], c[k]);
+        hi[k] = std::max(hi[k], c[k]);
+        ext = std::max(ext, std::fabs(c[k]));
+      }
+      rmax = std::max(rmax, std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]));
+    }
+    M.rot = (M.mw[0] != 0.0 || M.mw[1] != 0.0 || M.mw[2] != 0.0) ? 1 : 0;
+    if (M.rot) {
+      // a box around node 0 that holds the tool in any orientation (the
+      // distances to node 0 do not change under the rigid motion; 1 % spare)
+      const double R = 1.01 * rmax;
+      for (int k = 0; k < 3; k++) { lo[k] = -R; hi[k] = R; }
+      ext = std::max(ext, R);
     }
     int64_t ncell = 1;
     for (int k = 0; k < 3; k++) {
-      M.gmin[k] = lo[k] - margin - cs;
-      M.dims[k] = (int32_t)std::ceil((hi[k] + margin + cs - M.gmin[k]) / cs) + 1;
+      M.grel[k] = lo[k] - margin - cs;
+      M.dims[k] = (int32_t)std::ceil((hi[k] + margin + cs - M.grel[k]) / cs) + 1;
       ncell *= M.dims[k];
     }
     if (ncell > (int64_t)64 << 20) return wf_fail(d, WF_ERR_ARG, "tool bin grid too large");
     M.cs = cs;
     M.inv_cs = 1.0 / cs;
-    M.org[0] = nd[0].x; M.org[1] = nd[0].y; M.org[2] = nd[0].z;
+    M.margin = margin;
     for (int k = 0; k < 3; k++) {
-      M.glo[k] = (float)(M.gmin[k] - cs);
-      M.ghi[k] = (float)(M.gmin[k] + (M.dims[k] + 1) * cs);
+      M.glo[k] = (float)(M.grel[k] - cs);
+      M.ghi[k] = (float)(M.grel[k] + (M.dims[k] + 1) * cs);
     }
     if (!M.off32 && dalloc(&M.off32, 1, d->stream) != cudaSuccess)
       return wf_fail(d, WF_ERR_ALLOC, "tool offset");
-    WF_CUDA_OK(cudaMemsetAsync(M.off32, 0, sizeof(float4), d->stream));
+    const float4 o = make_float4((float)nd[0].x, (float)nd[0].y, (float)nd[0].z, 0.f);
+    WF_CUDA_OK(cudaMemcpyAsync(M.off32, &o, sizeof(float4), cudaMemcpyHostToDevice, d->stream));
+    // FP32 search tolerance: 1e-3 h plus 1e-6 of the tool's extent (16 FP32
+    // ulps of the largest relative coordinate), far above the FP32 distance error
+    M.tol32 = (float)(1e-3 * d->h + 1e-6 * (ext + 2.0 * d->h));
+    for (void* p : {(void*)M.cstart, (void*)M.ctri, (void*)M.cvert, (void*)M.cursor, (void*)M.scan_tmp})
+      if (p) cudaFree(p);
+    M.cstart = nullptr; M.ctri = nullptr; M.cvert = nullptr; M.cursor = nullptr; M.scan_tmp = nullptr;
+    if (M.rot) {
+      // entries: a triangle's box spans at most its diameter along any axis in
+      // any orientation, so it touches at most (floor((D + 2 margin)/cs) + 2)^3 cells
+      int64_t cap = 0;
+      for (int e = 0; e < M.ne; e++) {
+        double dia = 0.0;
+        for (int a1 = 0; a1 < 3; a1++)
+          for (int a2 = a1 + 1; a2 < 3; a2++) {
+            const double* p1 = &rel[3 * en[3 * e + a1]];
+            const double* p2 = &rel[3 * en[3 * e + a2]];
+            dia = std::max(dia, std::sqrt((p1[0] - p2[0]) * (p1[0] - p2[0]) + (p1[1] - p2[1]) * (p1[1] - p2[1]) +
+                                          (p1[2] - p2[2]) * (p1[2] - p2[2])));
+          }
+        const int64_t span = (int64_t)std::floor((dia + 2.0 * margin) / cs) + 2;
+        cap += span * span * span;
+      }
+      M.cap = cap;
+      if (dalloc(&M.cstart, ncell + 1, d->stream) || dalloc(&M.cursor, ncell, d->stream) ||
+          dalloc(&M.scan_tmp, scan_tmp_words(ncell + 1), d->stream) ||
+          dalloc(&M.cvert, 3 * cap, d->stream))
+        return wf_fail(d, WF_ERR_ALLOC, "rotating tool bins");
+      continue;   // binned on the GPU before every contact stage
+    }
     std::vector<int32_t> start((size_t)ncell + 1, 0), list;
     auto range = [&](int e, int r0[3], int r1[3]) {
       for (int k = 0; k < 3; k++) {
         double a = 1e300, b = -1e300;
         for (int q = 0; q < 3; q++) {
-          const double4& p = nd[en[3 * e + q]];
-          const double c = k == 0 ? p.x : (k == 1 ? p.y : p.z);
+          const double c = rel[3 * en[3 * e + q] + k];
           a = std::min(a, c);
           b = std::max(b, c);
         }
-        r0[k] = std::max(0, (int)std::floor((a - margin - M.gmin[k]) / cs));
-        r1[k] = std::min(M.dims[k] - 1, (int)std::floor((b + margin - M.gmin[k]) / cs));
+        r0[k] = std::max(0, (int)std::floor((a - margin - M.grel[k]) / cs));
+        r1[k] = std::min(M.dims[k] - 1, (int)std::floor((b + margin - M.grel[k]) / cs));
       }
     };
     for (int pass = 0; pass < 2; pass++) {
@@ -570,39 +615,23 @@ static int build_tool_bins(wf_domain* d) {
             }
       }
     }
-    if (M.cstart) cudaFree(M.cstart);
-    if (M.ctri) cudaFree(M.ctri);
-    M.cstart = nullptr;
-    M.ctri = nullptr;
+    M.cap = (int64_t)list.size();
     if (dalloc(&M.cstart, ncell + 1, d->stream) || dalloc(&M.ctri, std::max<int64_t>(1, (int64_t)list.size()), d->stream))
       return wf_fail(d, WF_ERR_ALLOC, "tool bins");
     WF_CUDA_OK(cudaMemcpyAsync(M.cstart, start.data(), sizeof(int32_t) * (ncell + 1), cudaMemcpyHostToDevice, d->stream));
     if (!list.empty())
       WF_CUDA_OK(cudaMemcpyAsync(M.ctri, list.data(), sizeof(int32_t) * list.size(), cudaMemcpyHostToDevice, d->stream));
-    WF_CUDA_OK(cudaStreamSynchronize(d->stream));
-    // FP32 vertex coordinates relative to node 0 for the FP32 triangle search,
-    // stored per bin entry so a cell's triangles are read contiguously, and
-    // the search tolerance: 1e-3 h plus 1e-6 of the tool's extent (16 FP32
-    // ulps of the largest relative coordinate), far above the FP32 distance
-    // error
-    double ext = 0.0;
-    for (int q = 0; q < M.nn; q++)
-      ext = std::max(ext, std::max(std::fabs(nd[q].x - nd[0].x),
-                                   std::max(std::fabs(nd[q].y - nd[0].y), std::fabs(nd[q].z - nd[0].z))));
-    M.tol32 = (float)(1e-3 * d->h + 1e-6 * (ext + 2.0 * d->h));
+    // each entry carries its triangle's FP32 vertices relative to node 0
     std::vector<float4> cv(3 * std::max<size_t>(1, list.size()));
     for (size_t t = 0; t < list.size(); t++) {
       const int e = list[t];
       for (int k = 0; k < 3; k++) {
-        const double4& p = nd[en[3 * e + k]];
+        const double* p = &rel[3 * en[3 * e + k]];
         float w = 0.f;
         if (k == 0) memcpy(&w, &e, sizeof w);   // the triangle index's bits
-        cv[3 * t + k] = make_float4((float)(p.x - nd[0].x), (float)(p.y - nd[0].y),
-                                    (float)(p.z - nd[0].z), w);
+        cv[3 * t + k] = make_float4((float)p[0], (float)p[1], (float)p[2], w);
       }
     }
-    if (M.cvert) cudaFree(M.cvert);
-    M.cvert = nullptr;
     if (dalloc(&M.cvert, (int64_t)cv.size(), d->stream) != cudaSuccess)
       return wf_fail(d, WF_ERR_ALLOC, "tool bin vertices");
     WF_CUDA_OK(cudaMemcpyAsync(M.cvert, cv.data(), sizeof(float4) * cv.size(), cudaMemcpyHostToDevice,
@@ -669,10 +698,6 @@ static int solve_begin(wf_domain* d, double dt_out) {
     launch_mesh_plane(make_params(d), d->stream);  // CalcSpheresKernel, :129-141
     if (d->contact_law == 1) {
       if (!(d->c_dx > 0.0)) return wf_fail(d, WF_ERR_STATE, "contact law 1 needs the option contact_dx");
-      // the triangle bins follow the tool by translation only
-      for (const MeshDev& M : d->meshes)
-        if (M.mw[0] != 0.0 || M.mw[1] != 0.0 || M.mw[2] != 0.0)
-          return wf_fail(d, WF_ERR_STATE, "contact law 1 takes translating tools only (angular velocity 0)");
       for (const MeshDev& M : d->meshes)
         if (M.ne >= (1 << 24))
           return wf_fail(d, WF_ERR_ARG, "contact law 1 takes meshes of fewer than 2^24 triangles");
@@ -853,7 +878,7 @@ int wf_destroy(wf_domain* d) {
   for (int k = 0; k < 2; k++) free_fields(d->F[k]);
   for (MeshDev& M : d->meshes) {
     void* mp[] = {M.node, M.node_v, M.centroid, M.normal, M.elnode, M.pplane, M.cstart, M.ctri,
-                  M.off32, M.cvert};
+                  M.off32, M.cvert, M.cursor, M.scan_tmp};
     for (void* p : mp) if (p) cudaFree(p);
   }
   if (d->d_maxdep) cudaFree(d->d_maxdep);
@@ -1011,9 +1036,6 @@ int wf_set_contact(wf_domain* d, double mu_static, double mu_dynamic, int law) {
   if (!(mu_static >= 0.0) || !(mu_dynamic >= 0.0))
     return wf_fail(d, WF_ERR_ARG, "friction coefficients must be >= 0");
   if (law == 1) {
-    for (const MeshDev& M : d->meshes)
-      if (M.mw[0] != 0.0 || M.mw[1] != 0.0 || M.mw[2] != 0.0)
-        return wf_fail(d, WF_ERR_ARG, "contact law 1 takes translating tools only");
     if (!d->F[0].qf)
       for (int f = 0; f < 2; f++)
         if (dalloc(&d->F[f].qf, d->npad, d->stream)) return wf_fail(d, WF_ERR_ALLOC, "qf");

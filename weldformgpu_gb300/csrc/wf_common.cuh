@@ -99,15 +99,22 @@ struct MeshDev {
   double* pplane;     // plane coefficient n . node
   int32_t nn, ne, first, zone;
   double mv[3], mw[3];  // translational and angular velocity (m_v, m_w)
-  // contact law 1: triangles binned once in the frame of the tool as added
-  // (a translating tool: the frame offset is node[0] - org)
-  double org[3], gmin[3], cs;   // node 0 as added, bin grid origin and cell size
+  // contact law 1: triangles binned in cells whose coordinates are relative to
+  // node 0 (the tool's frame up to its rotation).  A translating tool is
+  // binned once; a rotating one (mw != 0) is binned again on the GPU every
+  // step in a fixed box that holds it in any orientation.
+  double grel[3], cs;           // bin grid origin relative to node 0, cell size
   double inv_cs;                // 1 / cs
-  float glo[3], ghi[3];         // grid bounds widened by one cell (the FP32 early-out)
+  double margin;                // binning margin (h and a little)
+  float glo[3], ghi[3];         // grid bounds widened by one cell, relative (FP32 early-out)
   int32_t dims[3];
+  int32_t rot;                  // 1: rotating, binned every step
+  int64_t cap;                  // bin entries allocated (cvert holds 3 * cap float4)
   int32_t* cstart;              // [cells + 1] CSR offsets
-  int32_t* ctri;                // triangle indices, ascending within a cell
-  float4* off32;                // node[0] - org in FP32, written by the mesh motion
+  int32_t* ctri;                // triangle indices, ascending within a cell (translating)
+  uint32_t* cursor;             // [cells] fill cursors (rotating)
+  uint32_t* scan_tmp;           // scan scratch (rotating)
+  float4* off32;                // node 0 in FP32, written by the mesh motion
   float4* cvert;                // per bin entry: its triangle's vertices - node[0] in FP32
                                 // (fixed for a translating tool), 3 float4; .w of the
                                 // first holds the triangle index

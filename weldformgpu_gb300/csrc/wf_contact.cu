@@ -12,6 +12,7 @@
 // One thread per particle (surface, list, force), per node (mesh motion) or
 // per element (element geometry, rigid particles).
 #include "wf_common.cuh"
+#include "wf_nsearch.cuh"
 
 namespace {
 
@@ -222,15 +223,65 @@ __device__ __forceinline__ float3 rel32(const float4* r, int q) {
 // skipped before any integer conversion; the bins carry a margin of h, so the
 // rounding of the product cannot lose a triangle within h).
 __device__ __forceinline__ int tool_cell(const MeshDev& M, V3 xi) {
-  const double4 n0 = M.node[0];
-  const V3 xt = xi - (mk(n0) - mk(M.org[0], M.org[1], M.org[2]));
-  const double fx = floor((xt.x - M.gmin[0]) * M.inv_cs);
-  const double fy = floor((xt.y - M.gmin[1]) * M.inv_cs);
-  const double fz = floor((xt.z - M.gmin[2]) * M.inv_cs);
+  const V3 r = xi - mk(M.node[0]);
+  const double fx = floor((r.x - M.grel[0]) * M.inv_cs);
+  const double fy = floor((r.y - M.grel[1]) * M.inv_cs);
+  const double fz = floor((r.z - M.grel[2]) * M.inv_cs);
   if (!(fx >= 0.0 && fy >= 0.0 && fz >= 0.0 && fx < (double)M.dims[0] &&
         fy < (double)M.dims[1] && fz < (double)M.dims[2]))
     return -1;
   return ((int)fz * M.dims[1] + (int)fy) * M.dims[0] + (int)fx;
+}
+
+// Bins of a rotating tool, rebuilt every step from the current nodes: every
+// triangle goes into each cell that its bounding box (relative to node 0)
+// widened by the margin touches, with its vertices relative to node 0 in
+// FP32.  Count, exclusive scan (cstart), fill; the order within a cell depends
+// on the atomics, which the search's explicit tie rule makes irrelevant.
+__device__ __forceinline__ void tri_cells(const MeshDev& M, int e, V3 rv[3], int r0[3], int r1[3]) {
+  const int32_t* en = M.elnode + 3 * e;
+  const V3 n0 = mk(M.node[0]);
+  for (int k = 0; k < 3; k++) rv[k] = mk(M.node[en[k]]) - n0;
+  const double lo[3] = {fmin(fmin(rv[0].x, rv[1].x), rv[2].x), fmin(fmin(rv[0].y, rv[1].y), rv[2].y),
+                        fmin(fmin(rv[0].z, rv[1].z), rv[2].z)};
+  const double hi[3] = {fmax(fmax(rv[0].x, rv[1].x), rv[2].x), fmax(fmax(rv[0].y, rv[1].y), rv[2].y),
+                        fmax(fmax(rv[0].z, rv[1].z), rv[2].z)};
+  for (int k = 0; k < 3; k++) {
+    const double a = floor((lo[k] - M.margin - M.grel[k]) * M.inv_cs);
+    const double b = floor((hi[k] + M.margin - M.grel[k]) * M.inv_cs);
+    // clamped in double before the conversion (NaN gives an empty range)
+    r0[k] = (int)fmin(fmax(a, 0.0), (double)M.dims[k]);
+    r1[k] = (int)fmax(fmin(b, (double)(M.dims[k] - 1)), -1.0);
+  }
+}
+__global__ void k_bins_count(MeshDev M) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= M.ne) return;
+  V3 rv[3];
+  int r0[3], r1[3];
+  tri_cells(M, e, rv, r0, r1);
+  uint32_t* cnt = reinterpret_cast<uint32_t*>(M.cstart);
+  for (int z = r0[2]; z <= r1[2]; z++)
+    for (int y = r0[1]; y <= r1[1]; y++)
+      for (int x = r0[0]; x <= r1[0]; x++)
+        atomicAdd(cnt + ((int64_t)z * M.dims[1] + y) * M.dims[0] + x, 1u);
+}
+__global__ void k_bins_fill(MeshDev M) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= M.ne) return;
+  V3 rv[3];
+  int r0[3], r1[3];
+  tri_cells(M, e, rv, r0, r1);
+  for (int z = r0[2]; z <= r1[2]; z++)
+    for (int y = r0[1]; y <= r1[1]; y++)
+      for (int x = r0[0]; x <= r1[0]; x++) {
+        const uint32_t pos = atomicAdd(M.cursor + ((int64_t)z * M.dims[1] + y) * M.dims[0] + x, 1u);
+        if ((int64_t)pos >= M.cap) continue;   // bounded by construction (cap)
+        float4* v = M.cvert + 3 * (int64_t)pos;
+        v[0] = make_float4((float)rv[0].x, (float)rv[0].y, (float)rv[0].z, __int_as_float(e));
+        v[1] = make_float4((float)rv[1].x, (float)rv[1].y, (float)rv[1].z, 0.f);
+        v[2] = make_float4((float)rv[2].x, (float)rv[2].y, (float)rv[2].z, 0.f);
+      }
 }
 
 // Contact law 1 (the 2M-particle contact workload; no reference
@@ -389,7 +440,9 @@ __global__ void __launch_bounds__(128) k_contact_law1(StepParams P, Fields F, fl
     if (delta > 0.0) {
       const double fn = P.c_kappa * P.Kbulk * P.c_dx * delta;
       f = scale(n, fn);
-      const V3 vrel = mk(F.vd[i]) - mk(M.mv[0], M.mv[1], M.mv[2]);
+      // relative to the tool surface at the nearest point: m_v + m_w x q
+      const V3 vtool = mk(M.mv[0], M.mv[1], M.mv[2]) + cross(mk(M.mw[0], M.mw[1], M.mw[2]), bq);
+      const V3 vrel = mk(F.vd[i]) - vtool;
       const V3 vt = vrel - scale(n, dot(vrel, n));
       const double vtl = len(vt);
       if (P.mu_s > 0.0) {
@@ -425,9 +478,8 @@ __global__ void k_mesh_move(MeshDev M, double dt) {
   M.node_v[q] = d4(nv);
   const V3 moved = nd + scale(nv, dt);
   M.node[q] = d4(moved);
-  if (q == 0 && M.off32)   // the tool frame's offset for the law-1 early-out
-    M.off32[0] = make_float4((float)(moved.x - M.org[0]), (float)(moved.y - M.org[1]),
-                             (float)(moved.z - M.org[2]), 0.f);
+  if (q == 0 && M.off32)   // node 0 in FP32 for the law-1 early-out
+    M.off32[0] = make_float4((float)moved.x, (float)moved.y, (float)moved.z, 0.f);
 }
 
 // CalcCentroids, CalcNormals and UpdatePlaneCoeff of one element from the
@@ -469,6 +521,16 @@ inline int blocks_for(int64_t n, int t) { return (int)((n + t - 1) / t); }
 void launch_contact_stage(const StepParams& P, const Fields& F, const NbBuffers& N, bool list,
                           float4* a32, cudaStream_t s) {
   if (P.contact_law == 1) {
+    for (int m = 0; m < P.ncsid; m++) {   // rotating tools: bins from the current nodes
+      const MeshDev& M = P.mesh[m];
+      if (!M.rot) continue;
+      const int64_t ncell = (int64_t)M.dims[0] * M.dims[1] * M.dims[2];
+      cudaMemsetAsync(M.cstart, 0, sizeof(uint32_t) * (ncell + 1), s);
+      k_bins_count<<<blocks_for(M.ne, 128), 128, 0, s>>>(M);
+      device_exclusive_scan(reinterpret_cast<uint32_t*>(M.cstart), ncell + 1, M.scan_tmp, s);
+      cudaMemcpyAsync(M.cursor, M.cstart, sizeof(uint32_t) * ncell, cudaMemcpyDeviceToDevice, s);
+      k_bins_fill<<<blocks_for(M.ne, 128), 128, 0, s>>>(M);
+    }
     k_contact_law1<<<blocks_for(P.n, 128), 128, 0, s>>>(P, F, a32);
     return;
   }

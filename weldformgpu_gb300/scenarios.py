@@ -98,19 +98,23 @@ def contact_cylinder(R=0.005, H=0.010, dx=0.0005, dens=10, v_plane=-10.0, gap=1.
 
 
 def indent_block(L=(0.008, 0.008, 0.003), dx=0.00025, R=0.003, level=3, v_tool=-5.0, mu=0.3,
-                 gap=1.0e-7, thermal=True, zone=7, rebuild_increment=0.05):
+                 gap=1.0e-7, thermal=True, zone=7, rebuild_increment=0.05, omega=0.0):
     """A block indented by a rigid lower-half icosphere (the shape of the
     2M-particle contact benchmark, BASELINE config 5: block 200 x 200 x 50 dx,
     dx = 0.25 mm, R = 10 mm, ~10k triangles, -5 m/s): contact law 1 (penalty
     0.1 K / dx, friction mu, cell-binned triangle query, frictional heat), JC
     aluminium, neighbour rebuild at a plastic-strain increment.  The bottom
-    layer is fixed (zone 2); the tool starts `gap` outside contact range."""
+    layer is fixed (zone 2); the tool starts `gap` outside contact range.
+    omega != 0 spins the tool about the z axis (rad/s): the block is then
+    centred on that axis (x, y in [-L/2, L/2]), as for a stirring tool."""
     rho, E, nu = 2700.0, 70e9, 0.33
-    x, mass = S.gen_box_cubic((0.0, 0.0, 0.0), L, dx / 2.0, rho)
+    x0 = (-L[0] / 2.0, -L[1] / 2.0, 0.0) if omega != 0.0 else (0.0, 0.0, 0.0)
+    x, mass = S.gen_box_cubic(x0, L, dx / 2.0, rho)
     ns = len(x)
     nodes, tris = S.gen_icosphere(R, (0.0, 0.0, 0.0), level, True)
     top = x[:, 2].max()
-    shift = np.array([L[0] / 2.0, L[1] / 2.0, top + dx / 2.0 + gap - nodes[:, 2].min()])
+    cxy = (0.0, 0.0) if omega != 0.0 else (L[0] / 2.0, L[1] / 2.0)
+    shift = np.array([cxy[0], cxy[1], top + dx / 2.0 + gap - nodes[:, 2].min()])
     nodes = nodes + shift
     ne = len(tris)
     n = ns + ne
@@ -131,7 +135,7 @@ def indent_block(L=(0.008, 0.008, 0.003), dx=0.00025, R=0.003, level=3, v_tool=-
               h=h, rho=rho, G=G, sy=324e6, Cs=Cs, dt=0.4 * h / Cs, alpha=1.0, beta=0.0, mat=mat,
               T=np.full(n, 20.0), bcs=[(2, (0.0, 0.0, 0.0)), (zone, (0.0, 0.0, v_tool))], K=K,
               dx=dx, mesh=dict(nodes=nodes, tris=tris, normals=None, zone=zone, first=ns,
-                               vel=(0.0, 0.0, v_tool), angvel=(0.0, 0.0, 0.0)),
+                               vel=(0.0, 0.0, v_tool), angvel=(0.0, 0.0, omega)),
               mu=(mu, mu), law=1, options=opts)
     if thermal:
         sc["k"], sc["cp"] = 167.0, 896.0
