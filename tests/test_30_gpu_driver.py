@@ -47,9 +47,10 @@ def _inputs():
     return cfg, zp
 
 
-def _api_domain(zp, mesh=None):
+def _api_domain(zp, mesh=None, law=0):
     """main's set-up (src/WeldFormGPU.cu:689-914) through the Python API;
-    mesh = (nodes, tris) of a file rigid body, else main's plane."""
+    mesh = (nodes, tris) of a file rigid body, else main's plane; law 1 with
+    contact_dx = 2 r as the driver's "law" key sets it."""
     from weldformgpu_gb300 import Domain_d
     x, mass = P.gen_cylinder_ref((0.0, 0.0, 0.0), R, H, r, rho)
     ns = len(x)
@@ -80,7 +81,9 @@ def _api_domain(zp, mesh=None):
     d.add_velocity_bc(2, 0.0, 0.0, 0.0)
     d.add_velocity_bc(10, 0.0, 0.0, -10.0)
     d.add_trimesh(nodes, tris, 10, ns, (0.0, 0.0, -10.0), normals=normals)
-    d.set_contact(0.3, 0.2)
+    d.set_contact(0.3, 0.2, law)
+    if law == 1:
+        d.set_option("contact_dx", 2 * r)
     d.mech_fraser_solve(SIM, OUT)
     return d, n
 
@@ -200,3 +203,35 @@ def test_json_driver_nastran_rigid_body(tmp_path):
     head, rows = _csv(out / "test.csv")
     np.testing.assert_allclose(rows[:, 1:4], d.get_field("x"), rtol=2e-6, atol=1e-12)
     assert (rows[:, 21] > 0).sum() > 20                       # in contact with the tool
+
+
+def test_json_driver_contact_law1(tmp_path):
+    """The extension key Contact[0].law = 1 runs the binned nearest-triangle law
+    (contact_dx = 2 r) and equals the same set-up through the API."""
+    from weldformgpu_gb300.domain import LIB_PATH, lib
+    lib()
+    L = ctypes.CDLL(LIB_PATH)
+    L.wf_run_json.restype = ctypes.c_int
+    L.wf_run_json.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int64]
+    cfg, zp = _inputs()
+    cfg["Contact"][0]["law"] = 1
+    # law 1 acts within dx/2 = r of the surface: the plate starts just outside
+    zp = zp - 1.2 * 2 * r - 1e-7 + r + 1e-6
+    cfg["RigidBodies"][0]["start"][2] = zp
+    inp = tmp_path / "law1.json"
+    inp.write_text(json.dumps(cfg, indent=1))
+    out = tmp_path / "run"
+    out.mkdir()
+    err = ctypes.create_string_buffer(512)
+    assert L.wf_run_json(str(inp).encode(), str(out).encode(), err, 512) == 0, err.value
+    head, rows = _csv(out / "test.csv")
+    d, n = _api_domain(zp, law=1)
+    np.testing.assert_allclose(rows[:, 1:4], d.get_field("x"), rtol=2e-6, atol=1e-12)
+    np.testing.assert_allclose(rows[:, 19], d.get_field("pl_strain"), rtol=2e-6, atol=1e-12)
+    cf = d.get_field("contforce")
+    assert (np.abs(cf).sum(axis=1) > 0).sum() > 20             # the plate touches
+    np.testing.assert_allclose(rows[:, 22:25], cf, rtol=2e-6, atol=1e-6 * np.abs(cf).max())
+    cfg["Contact"][0]["law"] = 2
+    inp.write_text(json.dumps(cfg))
+    assert L.wf_run_json(str(inp).encode(), str(out).encode(), err, 512) != 0
+    assert b"law" in err.value

@@ -333,7 +333,7 @@ bool run_input(const Json& root, const std::string& out_dir, const std::string& 
   std::vector<int32_t> tris;
   int64_t ne = 0;
   int rzone = 0;
-  double mu_s = 0.0, mu_d = 0.0;
+  double mu_s = 0.0, mu_d = 0.0, contact_law = 0.0;
   if (has_contact) {
     double rs[3] = {0, 0, 0}, rd[3] = {0, 0, 0};
     int dens = 10;
@@ -373,6 +373,11 @@ bool run_input(const Json& root, const std::string& out_dir, const std::string& 
     const Json* ct = contact ? contact->at(0) : nullptr;
     read_num(ct, "fricCoeffStatic", mu_s);
     read_num(ct, "fricCoeffDynamic", mu_d);
+    // extension: "law": 1 selects the binned nearest-triangle law (contact_dx =
+    // the particle spacing 2 r)
+    read_num(ct, "law", contact_law);
+    if (contact_law != 0.0 && contact_law != 1.0)
+      return run.fail(WF_ERR_ARG, "Contact law must be 0 or 1");
   }
   const int64_t n = ns + ne;
   // initial temperature (InitialConditions[0].Temp; main leaves T unset)
@@ -420,13 +425,19 @@ bool run_input(const Json& root, const std::string& out_dir, const std::string& 
                                    (int32_t)ne, normals.empty() ? nullptr : normals.data(),
                                    rzone, ns, mesh_v, w),
             "rigid plane") ||
-        !ok(run, d, wf_set_contact(d, mu_s, mu_d, 0), "contact"))
+        !ok(run, d, wf_set_contact(d, mu_s, mu_d, (int)contact_law), "contact"))
+      return false;
+    if (contact_law == 1.0 && !ok(run, d, wf_set_option(d, "contact_dx", 2.0 * r), "contact law 1"))
       return false;
   }
   // options the reference has no key for (documented extensions)
   std::string s;
   if (read_str(config, "precision", s) &&
       !ok(run, d, wf_set_option(d, "precision", s == "mixed" ? 1.0 : 0.0), "precision"))
+    return false;
+  double rb_inc = 0.0;
+  if (read_num(config, "rebuildStrainIncrement", rb_inc) &&
+      !ok(run, d, wf_set_option(d, "rebuild_strain_increment", rb_inc), "rebuildStrainIncrement"))
     return false;
   if (read_str(config, "returnMap", s) &&
       !ok(run, d, wf_set_option(d, "return_map", s == "newton" ? 1.0 : 0.0), "returnMap"))
