@@ -334,6 +334,23 @@ def test_contact_law1_rotating_tool_fp64_vs_oracle_and_mixed():
         assert err < 1e-3, (f, err)
 
 
+def test_set_positions_rejects_non_finite_and_keeps_state():
+    """A NaN or infinite coordinate fails with WF_ERR_ARG before anything is
+    written; valid positions then go in and read back unchanged."""
+    from weldformgpu_gb300 import Domain_d
+    from weldformgpu_gb300.domain import WeldformError
+    sc = S.compression_cylinder()
+    d = Domain_d(sc["n"])
+    for bad in (np.nan, np.inf):
+        x = sc["x"].copy()
+        x[5, 1] = bad
+        with pytest.raises(WeldformError) as e:
+            d.set_positions(x.ravel())
+        assert e.value.code == -1 and "non-finite" in str(e.value)
+    d.set_positions(np.ascontiguousarray(sc["x"]).ravel())
+    assert np.array_equal(d.get_field("x"), sc["x"])
+
+
 def test_mixed_fused_heat_matches_separate_heat_pass():
     """Mixed form: the heat pass fused into the next step's density pass gives
     the temperatures of the separate heat pass (to FP32 rounding), including

@@ -122,6 +122,12 @@ static int wf_fail(wf_domain* d, int code, const std::string& msg) {
 // small utility kernels: scatter/gather between caller order and slot order
 // ---------------------------------------------------------------------------
 namespace {
+// flag[0] = 1 if any of the count values is not finite
+__global__ void k_any_nonfinite(int64_t count, const double* v, int* flag) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool bad = i < count && !isfinite(v[i]);
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
 __global__ void k_scatter_d(int64_t n, const int32_t* inv, const double* src, int comps,
                             double* dst, int stride, int off) {
   int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -972,10 +978,20 @@ int wf_set_id(wf_domain* d, const int32_t* id) {
 }
 int wf_set_positions(wf_domain* d, const double* x) {
   if (!d || !x) return WF_ERR_ARG;
-  for (int64_t i = 0; i < 3 * d->n; i++)
-    if (!std::isfinite(x[i])) return wf_fail(d, WF_ERR_ARG, "non-finite position");
+  // staged and checked on the device before anything is written
+  WF_CUDA_OK(cudaMemcpyAsync(d->d_stage, x, sizeof(double) * 3 * d->n, cudaMemcpyHostToDevice,
+                             d->stream));
+  WF_CUDA_OK(cudaMemsetAsync(d->d_mm, 0, sizeof(int), d->stream));
+  k_any_nonfinite<<<nblk(3 * d->n), 256, 0, d->stream>>>(3 * d->n, d->d_stage, d->d_mm);
+  int bad = 0;
+  WF_CUDA_OK(cudaMemcpyAsync(&bad, d->d_mm, sizeof(int), cudaMemcpyDeviceToHost, d->stream));
+  WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+  if (bad) return wf_fail(d, WF_ERR_ARG, "non-finite position");
   d->x_set = true;
-  return upload_d(d, x, 3, (double*)CF(d).xm, 4, 0);
+  k_scatter_d<<<nblk(d->n), 256, 0, d->stream>>>(d->n, d->inv, d->d_stage, 3, (double*)CF(d).xm,
+                                                  4, 0);
+  WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+  return WF_OK;
 }
 int wf_set_velocities(wf_domain* d, const double* v) {
   if (!d || !v) return WF_ERR_ARG;
