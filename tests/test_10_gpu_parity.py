@@ -351,6 +351,24 @@ def test_set_positions_rejects_non_finite_and_keeps_state():
     assert np.array_equal(d.get_field("x"), sc["x"])
 
 
+def test_mixed_fused_integration_bit_identical_to_separate_pass():
+    """Mixed form without contact: the integration fused into the acceleration
+    pass (new positions to a second mirror) gives the separate integration
+    pass's results bit for bit, through neighbour rebuilds and coupled heat."""
+    sc = S.compression_cylinder(material="jc", vz_top=-10.0)
+    sc["k"], sc["cp"] = 167.0, 896.0
+    opts = {"return_map": 1, "thermal": 1, "taylor_quinney": 0.9, "precision": 1,
+            "rebuild_every": 5, "rebuild_current_positions": 1, "rebuild_after_yield": 0}
+    fused = gpu(sc, dict(opts, fuse_integrate=1))
+    sep = gpu(sc, dict(opts, fuse_integrate=0))
+    for n in (1, 7, 150):
+        fused.step(n)
+        sep.step(n)
+        for f in ("x", "u", "v", "a", "rho", "pl_strain", "sigma_eq", "T"):
+            assert np.array_equal(fused.get_field(f), sep.get_field(f)), (n, f)
+    assert sep.get_field("pl_strain").max() > 0.0
+
+
 def test_mixed_fused_heat_matches_separate_heat_pass():
     """Mixed form: the heat pass fused into the next step's density pass gives
     the temperatures of the separate heat pass (to FP32 rounding), including

@@ -79,6 +79,7 @@ struct wf_domain {
   // mixed form: the heat pass of the last step runs inside the next step's
   // density pass, or in finish() when the call ends first
   bool fuse_heat = true, heat_pending = false, heat_pending_first = false;
+  bool fuse_integrate = true;    // mixed form without contact: integration inside the accel pass
   // contact with rigid triangle meshes
   std::vector<MeshDev> meshes;
   double mu_s = 0.0, mu_d = 0.0, totmass = 0.0;
@@ -306,7 +307,7 @@ static void layout_arena(wf_domain* d, Arena& A) {
     A.take(&F.kT, n); A.take(&F.cpT, n);
     A.take(&F.id, n); A.take(&F.bct, n); A.take(&F.perm, n); A.take(&F.nw, n);
     A.take(&F.xh, n); A.take(&F.p32, n); A.take(&F.v32, n); A.take(&F.ss32, 6 * n);
-    A.take(&F.th32, n); A.take(&F.pwn, n);
+    A.take(&F.th32, n); A.take(&F.pwn, n); A.take(&F.p32n, n);
   }
   A.take(&d->vd2, n); A.take(&d->v32b, n); A.take(&d->a32, n); A.take(&d->sigr32, 8 * n);
   A.take(&d->nb, (int64_t)WF_NB_ALLOC * n); A.take(&d->nbc, n); A.take(&d->inv, n);
@@ -749,6 +750,7 @@ static int solve_step(wf_domain* d) {
   const Fields& F = d->F[d->cur];
   NbBuffers N{d->nb, d->nbc};
   const bool mixed = d->precision == 1;
+  bool integrated = false;
   if (!mixed) {
     { KTimer t(d, KID_DENSITY); launch_fp64_density(P, F, d->vd2, N, s); }          // :193-202
     { KTimer t(d, KID_STRESS); launch_fp64_stress(P, F, d->vd2, N, d->d_status, s); }  // :204-218
@@ -766,15 +768,25 @@ static int solve_step(wf_domain* d) {
     { KTimer t(d, KID_STRESS);
       launch_fp32_stress(P, F, d->v32b, d->sigr32, N, d->d_status,
                          (d->mlp_on && d->mlp_loaded) ? d->mlp_packed : nullptr, s); }
-    { KTimer t(d, KID_ACCEL); launch_fp32_accel(P, F, d->v32b, d->sigr32, d->a32, N, s); }
+    if (!P.contact && d->fuse_integrate) {
+      { KTimer t(d, KID_ACCEL); launch_fp32_accel_integrate(P, F, d->v32b, d->sigr32, d->vd2, N, s); }
+      std::swap(d->F[d->cur].p32, d->F[d->cur].p32n);   // the new positions become current
+      integrated = true;
+    } else {
+      KTimer t(d, KID_ACCEL);
+      launch_fp32_accel(P, F, d->v32b, d->sigr32, d->a32, N, s);
+    }
   }
   if (P.contact) {                                                                    // :233-257
     KTimer t(d, KID_CONTACT);
     launch_contact_stage(P, F, N, d->ts_i == 0, mixed ? d->a32 : nullptr, s);
     d->launches += d->ts_i == 0 ? 3 : 2;
   }
-  { KTimer t(d, KID_INTEGRATE); launch_integrate(P, F, d->vd2, mixed ? d->a32 : nullptr, s); }   // :273-287
-  d->launches += 4;
+  if (!integrated) {   // :273-287
+    KTimer t(d, KID_INTEGRATE);
+    launch_integrate(P, F, d->vd2, mixed ? d->a32 : nullptr, s);
+  }
+  d->launches += integrated ? 3 : 4;
   if (d->thermal) {                                                                   // :285
     if (mixed && d->fuse_heat) {
       d->heat_pending = true;
@@ -1191,6 +1203,7 @@ int wf_set_option(wf_domain* d, const char* key, double v) {
   else if (k == "rebuild_current_positions") d->rebuild_current = v != 0;
   else if (k == "thermal") d->thermal = v != 0;
   else if (k == "fuse_heat") d->fuse_heat = v != 0;
+  else if (k == "fuse_integrate") d->fuse_integrate = v != 0;
   else if (k == "contact_stiffness") d->c_kappa = v;
   else if (k == "contact_dx") d->c_dx = v;
   else if (k == "contact_vreg") d->c_vreg = v;

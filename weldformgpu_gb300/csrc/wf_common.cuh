@@ -80,6 +80,7 @@ struct Fields {
   float4* v32;      // velocity xyz, density w
   float* ss32;      // deviatoric stress FP32 state (mixed form), 6 per slot
   float2* th32;     // heat-flux mirror (mixed form): T as a float pair (hi, lo)
+  float4* p32n;     // next positions of the fused acceleration + integration pass
   double* pwn;      // cached eps_p^n of the Johnson-Cook law (< 0: not cached yet)
   // contact (allocated when a rigid mesh is added)
   double4* nrm;     // surface normal (solid particles) / element normal (rigid particles)
@@ -282,3 +283,6 @@ void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b
                         cudaStream_t s);
 void launch_fp32_accel(const StepParams& P, const Fields& F, const float4* v32b,
                        const float* sigr32, float4* a32, const NbBuffers& N, cudaStream_t s);
+void launch_fp32_accel_integrate(const StepParams& P, const Fields& F, const float4* v32b,
+                                 const float* sigr32, const double4* vd2, const NbBuffers& N,
+                                 cudaStream_t s);

@@ -4,17 +4,9 @@
 // updates round exactly like the reference (--fmad=false).
 #include "wf_common.cuh"
 #include "wf_heat.cuh"
+#include "wf_integrate.cuh"
 
 namespace {
-
-__device__ __forceinline__ void apply_bc(const StepParams& P, int32_t id, double& vx, double& vy,
-                                         double& vz, double& ax, double& ay, double& az) {
-  for (int b = 0; b < P.nbc; b++)
-    if (id == P.bc_zone[b]) {
-      ax = 0.0; ay = 0.0; az = 0.0;
-      vx = P.bc_v[b][0]; vy = P.bc_v[b][1]; vz = P.bc_v[b][2];
-    }
-}
 
 // ---- D: BC, UpdatePosFraser, UpdateVel, BC, CalcIntEnergy ---------------
 // GeneralAfter/ApplyBCVel (src/WeldFormGPU.cu:103-106, src/cuda/Mechanical.cu:572-584),
@@ -25,44 +17,18 @@ __global__ void __launch_bounds__(256) k_integrate(StepParams P, Fields F,
                                                    const float4* __restrict__ a32) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= P.n) return;
-  const bool mixed = a32 != nullptr;
-  double4 xm = F.xm[i];
-  const double4 v4 = vd2[i];
-  double4 a4;
-  if (mixed) {
+  if (a32) {
     // rigid (non-solid) slots keep the acceleration the BCs left (zero)
     const float4 af = F.perm[i] < P.n_solid ? a32[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    a4 = make_double4(af.x, af.y, af.z, 0.0);
-  } else {
-    a4 = F.a[i];
+    integrate_mixed_one(P, F, vd2, i, af, F.p32);
+    return;
   }
+  double4 xm = F.xm[i];
+  const double4 v4 = vd2[i];
+  const double4 a4 = F.a[i];
   const int32_t id = F.id[i];
   double vx = v4.x, vy = v4.y, vz = v4.z, ax = a4.x, ay = a4.y, az = a4.z;
   apply_bc(P, id, vx, vy, vz, ax, ay, az);
-  if (mixed) {
-    // the increments in FP32 (relative error ~1e-7 of the increment), added
-    // to the FP64 positions, displacements and velocities
-    const float dtf = P.dtf, hdt2 = 0.5f * P.dtf * P.dtf;
-    const float fax = (float)ax, fay = (float)ay, faz = (float)az;
-    const double ux = (double)((float)vx * dtf + fax * hdt2);
-    const double uy = (double)((float)vy * dtf + fay * hdt2);
-    const double uz = (double)((float)vz * dtf + faz * hdt2);
-    xm.x += ux; xm.y += uy; xm.z += uz;
-    double4 u = F.u[i];
-    u.x += ux; u.y += uy; u.z += uz;
-    vx += (double)(fax * dtf); vy += (double)(fay * dtf); vz += (double)(faz * dtf);
-    apply_bc(P, id, vx, vy, vz, ax, ay, az);
-    F.xm[i] = xm;
-    F.vd[i] = make_double4(vx, vy, vz, v4.w);
-    F.u[i] = u;
-    F.a[i] = make_double4(ax, ay, az, 0.0);
-    F.p32[i] = make_float4((float)xm.x, (float)xm.y, (float)xm.z, (float)xm.w);
-    F.v32[i] = make_float4((float)vx, (float)vy, (float)vz, (float)v4.w);
-    const double T = F.T[i];
-    const float thi = (float)T;
-    F.th32[i] = make_float2(thi, (float)(T - (double)thi));
-    return;
-  }
   const double dt = P.dt;
   const double ux = vx * dt + ((ax * 0.5) * dt) * dt;
   const double uy = vy * dt + ((ay * 0.5) * dt) * dt;

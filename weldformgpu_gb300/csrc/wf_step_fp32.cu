@@ -11,6 +11,7 @@
 // FP64 division or conversion costs as much as the whole FP32 pair loop.
 #include "wf_common.cuh"
 #include "wf_heat.cuh"
+#include "wf_integrate.cuh"
 #include "wf_mlp.cuh"
 #include "wf_tensor.cuh"
 
@@ -445,15 +446,11 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
 // stress/rho^2), so two at a time keep the kernel near 64 registers; the pass
 // is bound by L1 throughput rather than by gather latency.
 constexpr int kAccelBatch = 2;
-__global__ void __launch_bounds__(128) k_accel32(StepParams P, Fields F,
-                                                 const float4* __restrict__ v32b,
-                                                 const float* __restrict__ sigr32,
-                                                 float4* __restrict__ a32,
-                                                 const int32_t* __restrict__ nb,
-                                                 const int32_t* __restrict__ cnt) {
-  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= P.n) return;
-  if (F.perm[i] >= P.n_solid) return;
+__device__ __forceinline__ float4 accel_value(const StepParams& P, const Fields& F,
+                                              const float4* __restrict__ v32b,
+                                              const float* __restrict__ sigr32,
+                                              const int32_t* __restrict__ nb,
+                                              const int32_t* __restrict__ cnt, int64_t i) {
   const float4 pi = F.p32[i];
   const float4 vi = v32b[i];
   const int32_t idi = F.id[i];
@@ -510,7 +507,39 @@ __global__ void __launch_bounds__(128) k_accel32(StepParams P, Fields F,
       }
     }
   }
-  a32[i] = make_float4(ax, ay, az, 0.f);
+  return make_float4(ax, ay, az, 0.f);
+}
+
+__global__ void __launch_bounds__(128) k_accel32(StepParams P, Fields F,
+                                                 const float4* __restrict__ v32b,
+                                                 const float* __restrict__ sigr32,
+                                                 float4* __restrict__ a32,
+                                                 const int32_t* __restrict__ nb,
+                                                 const int32_t* __restrict__ cnt) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= P.n || F.perm[i] >= P.n_solid) return;
+  a32[i] = accel_value(P, F, v32b, sigr32, nb, cnt, i);
+}
+
+// The acceleration pass with the integration of the same slot behind it
+// (no contact stage in between): one pass instead of two, the integration's
+// FP64 work and traffic overlapping the other warps' neighbour gathers.
+// Neighbours' positions are read from F.p32 while the new positions go to
+// p32n (the two are swapped by the host after the launch); the other mirrors
+// written here (v32, th32) are not read by this pass.
+__global__ void __launch_bounds__(128) k_accel_int32(StepParams P, Fields F,
+                                                     const float4* __restrict__ v32b,
+                                                     const float* __restrict__ sigr32,
+                                                     const double4* __restrict__ vd2,
+                                                     const int32_t* __restrict__ nb,
+                                                     const int32_t* __restrict__ cnt,
+                                                     float4* __restrict__ p32n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  // rigid (non-solid) slots: zero acceleration, moved by their BCs
+  const float4 af = F.perm[i] < P.n_solid ? accel_value(P, F, v32b, sigr32, nb, cnt, i)
+                                           : make_float4(0.f, 0.f, 0.f, 0.f);
+  integrate_mixed_one(P, F, vd2, i, af, p32n);
 }
 
 }  // namespace
@@ -535,4 +564,10 @@ void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b
 void launch_fp32_accel(const StepParams& P, const Fields& F, const float4* v32b,
                        const float* sigr32, float4* a32, const NbBuffers& N, cudaStream_t s) {
   k_accel32<<<blocks_for(P.n, 128), 128, 0, s>>>(P, F, v32b, sigr32, a32, N.nb, N.cnt);
+}
+void launch_fp32_accel_integrate(const StepParams& P, const Fields& F, const float4* v32b,
+                                 const float* sigr32, const double4* vd2, const NbBuffers& N,
+                                 cudaStream_t s) {
+  k_accel_int32<<<blocks_for(P.n, 128), 128, 0, s>>>(P, F, v32b, sigr32, vd2, N.nb, N.cnt,
+                                                     F.p32n);
 }
