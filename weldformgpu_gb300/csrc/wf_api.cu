@@ -93,6 +93,7 @@ struct wf_domain {
   double rb_dep = 0.0;
   double k_cond = 0.0;          // conductivity (wf_set_conductivity: uniform)
   int64_t rebuilds = 0;         // neighbour rebuilds inside the step loop
+  int light_rebuilds = 0;       // rebuilds since the state was last moved into cell order
   unsigned long long* d_maxdep = nullptr;
   unsigned long long* h_maxdep = nullptr;
   // MechFraserSolve's CSV snapshots (out_<time>.csv), when a prefix is set
@@ -471,7 +472,9 @@ static int ensure_cells(wf_domain* d, int64_t ncell) {
   return WF_OK;
 }
 
-static int rebuild(wf_domain* d, bool use_current) {
+constexpr int kReorderEvery = 20;   // physical reorder at every 20th rebuild of a solve
+
+static int rebuild(wf_domain* d, bool use_current, bool light = false) {
   KTimer t(d, KID_REBUILD);
   const int64_t n = d->n;
   cudaStream_t s = d->stream;
@@ -496,9 +499,21 @@ static int rebuild(wf_domain* d, bool use_current) {
   device_exclusive_scan(d->cell_count, ncell + 1, d->scan_tmp, s);
   launch_cell_scatter(n, d->cellid, d->cell_count, d->cell_cursor, A.perm, d->s_src, d->s_orig, s);
   launch_cell_sort(ncell, d->cell_count, d->s_src, d->s_orig, s);
-  launch_reorder(n, d->s_src, A, B, d->pf, d->pf2, d->inv, s);
-  d->cur = 1 - d->cur;
-  launch_nblist(n, d->npad, d->pf2, d->grid, d->cell_count, d->nb, d->nbc, d->d_status, s);
+  // The lists hold the same particles in the same order whether or not the
+  // state is moved into the sorted order, so the arithmetic is identical;
+  // moving it keeps warps' particles close in space.  Inside the step loop
+  // the state is moved at every kReorderEvery-th rebuild only (solids move
+  // little in between); otherwise the lists name the particles' current slots.
+  const bool full = !light || ++d->light_rebuilds >= kReorderEvery;
+  if (full) {
+    launch_reorder(n, d->s_src, A, B, d->pf, d->pf2, d->inv, s);
+    d->cur = 1 - d->cur;
+    d->light_rebuilds = 0;
+  } else {
+    launch_gather_pf(n, d->s_src, d->pf, d->pf2, s);
+  }
+  launch_nblist(n, d->npad, d->pf2, d->grid, d->cell_count, full ? nullptr : d->s_src, d->nb,
+                d->nbc, d->d_status, s);
   d->launches += 8;
   if (d->F[d->cur].eps_rb) {       // adaptive rebuild: the strain this list was built at
     k_copy_d<<<nblk(n), 256, 0, s>>>(n, d->F[d->cur].eps_p, d->F[d->cur].eps_rb);
@@ -742,7 +757,7 @@ static int solve_step(wf_domain* d) {
     rb = d->ts_i == 0 && (d->is_yielding || !d->rebuild_after_yield);   // :166-182
   }
   if (rb) {
-    int rc = rebuild(d, d->rebuild_current != 0);
+    int rc = rebuild(d, d->rebuild_current != 0, true);
     if (rc) return rc;
     d->rebuilds++;
   }

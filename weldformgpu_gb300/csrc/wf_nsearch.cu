@@ -204,13 +204,18 @@ __global__ void k_reorder(int64_t n, const int32_t* __restrict__ s_src, const Fi
 }
 
 // kComputeCounts + kNeighborhoodQueryWithCounts in one pass (ELL output)
+// pf holds the positions in sorted order.  slot_of == nullptr: the state was
+// reordered to that order and sorted index = slot; else slot_of[k] is the
+// storage slot of the k-th sorted particle, and rows and entries are slots.
 __global__ void __launch_bounds__(128) k_nblist(int64_t n, int64_t npad, const float4* __restrict__ pf,
                                                 GridDev g, const uint32_t* __restrict__ start,
+                                                const int32_t* __restrict__ slot_of,
                                                 int32_t* __restrict__ nb, int32_t* __restrict__ cnt,
                                                 int* status) {
-  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float4 p = pf[i];
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int64_t i = slot_of ? (int64_t)slot_of[k] : k;
+  const float4 p = pf[k];
   const int cx = cell_coord(p.x, g.gmin[0], g.gdelta[0]);
   const int cy = cell_coord(p.y, g.gmin[1], g.gdelta[1]);
   const int cz = cell_coord(p.z, g.gmin[2], g.gdelta[2]);
@@ -231,7 +236,7 @@ __global__ void __launch_bounds__(128) k_nblist(int64_t n, int64_t npad, const f
         const float dx = __fsub_rn(q.x, p.x), dy = __fsub_rn(q.y, p.y), dz = __fsub_rn(q.z, p.z);
         const float sq = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
         if (sq < r2 && sq > 0.0f) {
-          nb[nb_at(npad, i, count)] = (int32_t)s;
+          nb[nb_at(npad, i, count)] = slot_of ? slot_of[s] : (int32_t)s;
           count++;
           if (count == WF_NB) {
             atomicOr(status, WF_STATUS_NB_CAP);
@@ -246,6 +251,13 @@ done:
   // pad the last block with the particle's own slot (see nb_at)
   for (int k = count; k < ((count + WF_NB_BLK - 1) & ~(WF_NB_BLK - 1)); k++)
     nb[nb_at(npad, i, k)] = (int32_t)i;
+}
+
+// the search positions in sorted order, for a rebuild that keeps the state in place
+__global__ void k_gather_pf(int64_t n, const int32_t* __restrict__ s_src,
+                            const float4* __restrict__ pf, float4* __restrict__ pf2) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k < n) pf2[k] = pf[s_src[k]];
 }
 
 __global__ void k_snapshot(int64_t n, Fields F) {
@@ -317,9 +329,13 @@ void launch_reorder(int64_t n, const int32_t* s_src, const Fields& A, const Fiel
   k_reorder<<<nblocks(n, 256), 256, 0, s>>>(n, s_src, A, B, pf, pf2, inv);
 }
 void launch_nblist(int64_t n, int64_t npad, const float4* pf, const GridDev& g,
-                   const uint32_t* start, int32_t* nb, int32_t* cnt, int* status,
-                   cudaStream_t s) {
-  k_nblist<<<nblocks(n, 128), 128, 0, s>>>(n, npad, pf, g, start, nb, cnt, status);
+                   const uint32_t* start, const int32_t* slot_of, int32_t* nb, int32_t* cnt,
+                   int* status, cudaStream_t s) {
+  k_nblist<<<nblocks(n, 128), 128, 0, s>>>(n, npad, pf, g, start, slot_of, nb, cnt, status);
+}
+void launch_gather_pf(int64_t n, const int32_t* s_src, const float4* pf, float4* pf2,
+                      cudaStream_t s) {
+  k_gather_pf<<<nblocks(n, 256), 256, 0, s>>>(n, s_src, pf, pf2);
 }
 void launch_snapshot(int64_t n, const Fields& F, cudaStream_t s) {
   k_snapshot<<<nblocks(n, 256), 256, 0, s>>>(n, F);

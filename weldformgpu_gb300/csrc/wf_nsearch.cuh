@@ -24,6 +24,8 @@ void launch_cell_sort(int64_t ncell, const uint32_t* start, int32_t* s_src, int3
 void launch_reorder(int64_t n, const int32_t* s_src, const Fields& A, const Fields& B,
                     const float4* pf, float4* pf2, int32_t* inv, cudaStream_t s);
 void launch_nblist(int64_t n, int64_t npad, const float4* pf, const GridDev& g,
-                   const uint32_t* start, int32_t* nb, int32_t* cnt, int* status,
-                   cudaStream_t s);
+                   const uint32_t* start, const int32_t* slot_of, int32_t* nb, int32_t* cnt,
+                   int* status, cudaStream_t s);
+void launch_gather_pf(int64_t n, const int32_t* s_src, const float4* pf, float4* pf2,
+                      cudaStream_t s);
 void launch_snapshot(int64_t n, const Fields& F, cudaStream_t s);
