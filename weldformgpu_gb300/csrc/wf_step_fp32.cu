@@ -37,6 +37,44 @@ __device__ __forceinline__ T3f mul_ref_f(const T3f& a, const T3f& b) {
 }
 
 // ---- A32: density rate + update (InteractionAlt.cu:166-246, Mechanical.cu:198) --
+// Lane groups of the pair passes: kLanes consecutive lanes share one particle;
+// lane g of the group takes entries [8b + g W, 8b + (g + 1) W) of every list
+// block b (W = 8 / kLanes), and the lanes' partial sums are combined by an
+// xor-shuffle tree, which gives every lane of the group the same value.  A
+// warp then covers fewer particles and its gathers touch fewer L1 lines (the
+// neighbours of consecutive sorted particles overlap), and each lane's chain
+// of dependent gathers is shorter.
+template <int W>
+__device__ __forceinline__ void nb_sub(const int32_t* __restrict__ nb, int64_t npad, int64_t i,
+                                       int b, int g, int* js) {
+  const int32_t* q = nb + ((int64_t)b * npad + i) * WF_NB_BLK + g * W;
+  if constexpr (W == 8) {
+    const int4 lo = __ldg(reinterpret_cast<const int4*>(q));
+    const int4 hi = __ldg(reinterpret_cast<const int4*>(q) + 1);
+    js[0] = lo.x; js[1] = lo.y; js[2] = lo.z; js[3] = lo.w;
+    js[4] = hi.x; js[5] = hi.y; js[6] = hi.z; js[7] = hi.w;
+  } else if constexpr (W == 4) {
+    const int4 v = __ldg(reinterpret_cast<const int4*>(q));
+    js[0] = v.x; js[1] = v.y; js[2] = v.z; js[3] = v.w;
+  } else {
+    static_assert(W == 2, "list sub-block of 2, 4 or 8 entries");
+    const int2 v = __ldg(reinterpret_cast<const int2*>(q));
+    js[0] = v.x; js[1] = v.y;
+  }
+}
+
+// lane group of G lanes (a power of two) that share one particle
+template <int G>
+__device__ __forceinline__ unsigned group_mask() {
+  if constexpr (G == 32) return 0xffffffffu;
+  return ((1u << G) - 1u) << ((threadIdx.x & 31u) & ~(unsigned)(G - 1));
+}
+
+// Density + heat pass: one lane per particle (786k particles: 0.199 ms with
+// one lane and 6 blocks per SM, 0.202-0.213 ms with 2 or 4 lanes).
+constexpr int kDensLanes = 1;
+constexpr int kDensMinBlocks = 6;
+
 __global__ void __launch_bounds__(128) k_density32(StepParams P, Fields F,
                                                    double4* __restrict__ vd2,
                                                    float4* __restrict__ v32b,
@@ -92,41 +130,46 @@ __global__ void __launch_bounds__(128) k_density32(StepParams P, Fields F,
 // mirror (T^n, written by the integration kernel), so each thread may update
 // its own FP64 temperature in place.  After a rebuild at the start of step
 // n+1 the heat flux of step n uses the new list (built for these positions).
-__global__ void __launch_bounds__(128) k_density_heat32(StepParams P, Fields F,
+__global__ void __launch_bounds__(128, kDensMinBlocks) k_density_heat32(StepParams P, Fields F,
                                                         double4* __restrict__ vd2,
                                                         float4* __restrict__ v32b,
                                                         const int32_t* __restrict__ nb,
                                                         const int32_t* __restrict__ cnt,
                                                         int first, int plastic_heat) {
-  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  constexpr int W = WF_NB_BLK / kDensLanes;
+  constexpr int NB = W < 4 ? W : 4;   // neighbours gathered per batch
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int g = (int)(t & (kDensLanes - 1));
+  const int64_t i = t / kDensLanes;
   if (i >= P.n) return;
   const float4 pi = F.p32[i];
   const float4 vi = F.v32[i];
   const float2 ti = F.th32[i];
-  const double4 vdi = F.vd[i];
   const bool solid = F.perm[i] < P.n_solid;
   const float invh = P.invhf, C = P.Cf, Ch = P.Chf;
   const int32_t idi = F.id[i];
   float drho = 0.0f, sf = 0.0f;
   const int c = cnt[i];
-  int4 lo = make_int4(0, 0, 0, 0), hi = lo;
-  if (c > 0) nb_block(nb, P.npad, i, 0, lo, hi);
+  int nx[W];
+  if (c > 0) nb_sub<W>(nb, P.npad, i, 0, g, nx);
   for (int b = 0; WF_NB_BLK * b < c; b++) {
-    const int js[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
-    const int m = c - WF_NB_BLK * b;
-    if (m > WF_NB_BLK) nb_block(nb, P.npad, i, b + 1, lo, hi);
+    int js[W];
 #pragma unroll
-    for (int h = 0; h < WF_NB_BLK; h += 4) {
-      float4 pj[4], vj[4];
-      float2 tj[4];
+    for (int q = 0; q < W; q++) js[q] = nx[q];
+    const int m = c - WF_NB_BLK * b - g * W;   // entries of this lane's sub-block in the list
+    if (c > WF_NB_BLK * (b + 1)) nb_sub<W>(nb, P.npad, i, b + 1, g, nx);
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
+    for (int h = 0; h < W; h += NB) {
+      float4 pj[NB], vj[NB];
+      float2 tj[NB];
+#pragma unroll
+      for (int q = 0; q < NB; q++) {
         pj[q] = F.p32[js[h + q]];
         vj[q] = F.v32[js[h + q]];
         tj[q] = F.th32[js[h + q]];
       }
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
+      for (int q = 0; q < NB; q++) {
         if (h + q >= m) continue;
         const float xx = pi.x - pj[q].x, xy = pi.y - pj[q].y, xz = pi.z - pj[q].z;
         const float GK = gk32_r2(xx * xx + xy * xy + xz * xz, invh, Ch, C);
@@ -143,6 +186,16 @@ __global__ void __launch_bounds__(128) k_density_heat32(StepParams P, Fields F,
       }
     }
   }
+  if constexpr (kDensLanes > 1) {
+    const unsigned mask = group_mask<kDensLanes>();
+#pragma unroll
+    for (int o = 1; o < kDensLanes; o <<= 1) {
+      sf += __shfl_xor_sync(mask, sf, o, kDensLanes);
+      drho += __shfl_xor_sync(mask, drho, o, kDensLanes);
+    }
+  }
+  if (g != 0) return;
+  const double4 vdi = F.vd[i];
   // heat of the previous step: rate and leapfrog, own particle only
   const double dTdt = heat_rate_mixed(P, F, i, P.k2f * sf, vdi.w, (double)pi.w, F.T[i], plastic_heat);
   F.dTdt[i] = dTdt;
@@ -442,15 +495,20 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
 }
 
 // ---- C32: acceleration + Monaghan viscosity (InteractionAlt.cu:18-150) ----
-// Neighbours gathered per batch: each carries 64 bytes (position, velocity,
-// stress/rho^2), so two at a time keep the kernel near 64 registers; the pass
-// is bound by L1 throughput rather than by gather latency.
+// Lane groups of kAccelLanes (see nb_sub).  Neighbours are gathered per batch
+// of kAccelBatch: each carries 56 bytes (position, velocity, stress/rho^2).
+// 786k particles: 0.278 ms with one lane per particle, 0.272 ms with two
+// (71 registers, 7 blocks per SM), 0.31-0.39 ms with four.
+constexpr int kAccelLanes = 2;
 constexpr int kAccelBatch = 2;
+static_assert(WF_NB_BLK / kAccelLanes >= kAccelBatch, "batch within the lane's sub-block");
+
 __device__ __forceinline__ float4 accel_value(const StepParams& P, const Fields& F,
                                               const float4* __restrict__ v32b,
                                               const float* __restrict__ sigr32,
                                               const int32_t* __restrict__ nb,
-                                              const int32_t* __restrict__ cnt, int64_t i) {
+                                              const int32_t* __restrict__ cnt, int64_t i, int g) {
+  constexpr int W = WF_NB_BLK / kAccelLanes;
   const float4 pi = F.p32[i];
   const float4 vi = v32b[i];
   const int32_t idi = F.id[i];
@@ -464,14 +522,16 @@ __device__ __forceinline__ float4 accel_value(const StepParams& P, const Fields&
   const bool av = alpha != 0.0f || beta != 0.0f;
   float ax = 0.f, ay = 0.f, az = 0.f;
   const int c = cnt[i];
-  int4 lo = make_int4(0, 0, 0, 0), hi = lo;
-  if (c > 0) nb_block(nb, P.npad, i, 0, lo, hi);
+  int nx[W];
+  if (c > 0) nb_sub<W>(nb, P.npad, i, 0, g, nx);
   for (int b = 0; WF_NB_BLK * b < c; b++) {
-    const int js[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
-    const int m = c - WF_NB_BLK * b;
-    if (m > WF_NB_BLK) nb_block(nb, P.npad, i, b + 1, lo, hi);
+    int js[W];
 #pragma unroll
-    for (int hh = 0; hh < WF_NB_BLK; hh += kAccelBatch) {
+    for (int q = 0; q < W; q++) js[q] = nx[q];
+    const int m = c - WF_NB_BLK * b - g * W;   // entries of this lane's sub-block in the list
+    if (c > WF_NB_BLK * (b + 1)) nb_sub<W>(nb, P.npad, i, b + 1, g, nx);
+#pragma unroll
+    for (int hh = 0; hh < W; hh += kAccelBatch) {
       float4 pj[kAccelBatch], vj[kAccelBatch], t0[kAccelBatch];
       float2 t1[kAccelBatch];
 #pragma unroll
@@ -507,18 +567,36 @@ __device__ __forceinline__ float4 accel_value(const StepParams& P, const Fields&
       }
     }
   }
+  if constexpr (kAccelLanes > 1) {
+    const unsigned mask = group_mask<kAccelLanes>();
+#pragma unroll
+    for (int o = 1; o < kAccelLanes; o <<= 1) {
+      ax += __shfl_xor_sync(mask, ax, o, kAccelLanes);
+      ay += __shfl_xor_sync(mask, ay, o, kAccelLanes);
+      az += __shfl_xor_sync(mask, az, o, kAccelLanes);
+    }
+  }
   return make_float4(ax, ay, az, 0.f);
 }
 
-__global__ void __launch_bounds__(128) k_accel32(StepParams P, Fields F,
+// thread -> (slot, lane within the slot's group)
+__device__ __forceinline__ int64_t accel_slot(int& g) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  g = (int)(t & (kAccelLanes - 1));
+  return t / kAccelLanes;
+}
+
+__global__ void __launch_bounds__(128, 7) k_accel32(StepParams P, Fields F,
                                                  const float4* __restrict__ v32b,
                                                  const float* __restrict__ sigr32,
                                                  float4* __restrict__ a32,
                                                  const int32_t* __restrict__ nb,
                                                  const int32_t* __restrict__ cnt) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int g;
+  const int64_t i = accel_slot(g);
   if (i >= P.n || F.perm[i] >= P.n_solid) return;
-  a32[i] = accel_value(P, F, v32b, sigr32, nb, cnt, i);
+  const float4 af = accel_value(P, F, v32b, sigr32, nb, cnt, i, g);
+  if (g == 0) a32[i] = af;
 }
 
 // The acceleration pass with the integration of the same slot behind it
@@ -527,19 +605,20 @@ __global__ void __launch_bounds__(128) k_accel32(StepParams P, Fields F,
 // Neighbours' positions are read from F.p32 while the new positions go to
 // p32n (the two are swapped by the host after the launch); the other mirrors
 // written here (v32, th32) are not read by this pass.
-__global__ void __launch_bounds__(128) k_accel_int32(StepParams P, Fields F,
+__global__ void __launch_bounds__(128, 7) k_accel_int32(StepParams P, Fields F,
                                                      const float4* __restrict__ v32b,
                                                      const float* __restrict__ sigr32,
                                                      const double4* __restrict__ vd2,
                                                      const int32_t* __restrict__ nb,
                                                      const int32_t* __restrict__ cnt,
                                                      float4* __restrict__ p32n) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int g;
+  const int64_t i = accel_slot(g);
   if (i >= P.n) return;
   // rigid (non-solid) slots: zero acceleration, moved by their BCs
-  const float4 af = F.perm[i] < P.n_solid ? accel_value(P, F, v32b, sigr32, nb, cnt, i)
+  const float4 af = F.perm[i] < P.n_solid ? accel_value(P, F, v32b, sigr32, nb, cnt, i, g)
                                            : make_float4(0.f, 0.f, 0.f, 0.f);
-  integrate_mixed_one(P, F, vd2, i, af, p32n);
+  if (g == 0) integrate_mixed_one(P, F, vd2, i, af, p32n);
 }
 
 }  // namespace
@@ -552,7 +631,7 @@ void launch_fp32_density(const StepParams& P, const Fields& F, double4* vd2, flo
 }
 void launch_fp32_density_heat(const StepParams& P, const Fields& F, double4* vd2, float4* v32b,
                               const NbBuffers& N, int first, int plastic_heat, cudaStream_t s) {
-  k_density_heat32<<<blocks_for(P.n, 128), 128, 0, s>>>(P, F, vd2, v32b, N.nb, N.cnt, first,
+  k_density_heat32<<<blocks_for(P.n * kDensLanes, 128), 128, 0, s>>>(P, F, vd2, v32b, N.nb, N.cnt, first,
                                                         plastic_heat);
 }
 void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b, float* sigr32,
@@ -563,11 +642,11 @@ void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b
 }
 void launch_fp32_accel(const StepParams& P, const Fields& F, const float4* v32b,
                        const float* sigr32, float4* a32, const NbBuffers& N, cudaStream_t s) {
-  k_accel32<<<blocks_for(P.n, 128), 128, 0, s>>>(P, F, v32b, sigr32, a32, N.nb, N.cnt);
+  k_accel32<<<blocks_for(P.n * kAccelLanes, 128), 128, 0, s>>>(P, F, v32b, sigr32, a32, N.nb, N.cnt);
 }
 void launch_fp32_accel_integrate(const StepParams& P, const Fields& F, const float4* v32b,
                                  const float* sigr32, const double4* vd2, const NbBuffers& N,
                                  cudaStream_t s) {
-  k_accel_int32<<<blocks_for(P.n, 128), 128, 0, s>>>(P, F, v32b, sigr32, vd2, N.nb, N.cnt,
+  k_accel_int32<<<blocks_for(P.n * kAccelLanes, 128), 128, 0, s>>>(P, F, v32b, sigr32, vd2, N.nb, N.cnt,
                                                      F.p32n);
 }
