@@ -389,6 +389,49 @@ def test_mixed_fused_heat_matches_separate_heat_pass():
     assert Ts.max() > 20.5
 
 
+def _graph_case(name):
+    if name == "mixed_jc_heat":
+        sc = S.compression_cylinder(material="jc", vz_top=-10.0)
+        sc["k"], sc["cp"] = 167.0, 896.0
+        return sc, {"return_map": 1, "thermal": 1, "taylor_quinney": 0.9, "precision": 1,
+                    "rebuild_every": 5, "rebuild_current_positions": 1, "rebuild_after_yield": 0}
+    if name == "fp64_bilinear":   # status reads until the first yield, then rebuilds
+        return S.compression_cylinder(), {}
+    if name == "contact_law0_mixed":
+        return S.contact_cylinder(mu=(0.3, 0.2)), {"precision": 1}
+    if name == "mixed_jc_network":   # the tcgen05 warm start inside the stress pass
+        sc = S.compression_cylinder(material="jc", vz_top=-10.0)
+        return sc, {"return_map": 1, "precision": 1, "rebuild_after_yield": 0, "mlp": 1}
+    # law 1, rotating tool (bins rebuilt on the GPU every step), periodic rebuilds
+    return S.indent_block(rebuild_increment=0.0, omega=2000.0), {"precision": 1, "rebuild_every": 5}
+
+
+@pytest.mark.parametrize("name", ["mixed_jc_heat", "fp64_bilinear", "contact_law0_mixed",
+                                  "contact_law1_rotating_mixed", "mixed_jc_network"])
+def test_step_graphs_bit_identical_to_direct_launches(name):
+    """The steps between host synchronisation points replayed as one CUDA
+    graph give the directly launched steps' results bit for bit, through
+    uneven calls (segments cut at call ends) and neighbour rebuilds."""
+    from weldformgpu_gb300 import Domain_d, mlp
+    sc, opts = _graph_case(name)
+    doms = []
+    for g in (1, 0):
+        d = Domain_d(sc["n"])
+        if opts.get("mlp"):
+            d.set_mlp_weights(mlp.init_params(3))   # untrained: starts accepted or rejected alike
+        doms.append(S.load(d, sc, dict(opts, graph=g)))
+    graph, direct = doms
+    fields = ("x", "u", "v", "a", "rho", "pl_strain", "sigma_eq", "T")
+    for n in (1, 7, 13, 123):
+        graph.step(n)
+        direct.step(n)
+        for f in fields:
+            assert np.array_equal(graph.get_field(f), direct.get_field(f)), (n, f)
+    assert graph.get_scalar("graph_launches") > 0
+    assert direct.get_scalar("graph_launches") == 0
+    assert graph.get_scalar("rebuilds") == direct.get_scalar("rebuilds")
+
+
 def test_reference_api_mech_fraser_solve_bit_exact():
     """MechFraserSolve(tf, dt_out) through the reference's method names: stale
     (last-output) positions for the rebuilds, outputs every dt_out."""

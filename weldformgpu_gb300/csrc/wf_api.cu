@@ -108,6 +108,11 @@ struct wf_domain {
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_used = 0;
   bool timing = false;         // inside wf_time_steps
+  // step-segment graphs (segment_begin / segment_end)
+  int graph = 1;                // option "graph"
+  bool capturing = false;
+  cudaGraphExec_t gexec = nullptr;
+  int64_t graph_launches = 0, graph_instantiations = 0;
   std::string err;
 };
 
@@ -432,6 +437,69 @@ static StepParams make_params(const wf_domain* d) {
 // ---------------------------------------------------------------------------
 // measurement helpers: optional event pairs around one kernel kind
 // ---------------------------------------------------------------------------
+// Step-segment graphs.  The launches of the steps between two host
+// synchronisation points (a neighbour rebuild, which reads the particle
+// bounds back to size the cell grid; a status read; the end of a call) are
+// recorded by stream capture and replayed as one CUDA graph: capture takes
+// the kernels with the arguments the steps would have launched them with
+// (the position buffers that alternate from step to step included), so the
+// replay does the same work in the same order.  The instantiated graph is
+// kept and updated in place when the next segment has the same launches.
+// Not used with the adaptive rebuild or CSV snapshots (host reads every step).
+static int segment_begin(wf_domain* d) {
+  if (!d->graph || d->capturing || d->rb_dep > 0.0 || d->csv_on) return WF_OK;
+  WF_CUDA_OK(cudaStreamBeginCapture(d->stream, cudaStreamCaptureModeRelaxed));
+  d->capturing = true;
+  return WF_OK;
+}
+
+static int segment_end(wf_domain* d) {
+  if (!d->capturing) return WF_OK;
+  d->capturing = false;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(d->stream, &g);
+  if (e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return wf_cuda_fail(d, e, "cudaStreamEndCapture");
+  }
+  size_t nodes = 0;
+  cudaGraphGetNodes(g, nullptr, &nodes);
+  if (nodes == 0) {
+    cudaGraphDestroy(g);
+    return WF_OK;
+  }
+  bool updated = false;
+  if (d->gexec) {
+    cudaGraphExecUpdateResultInfo info;
+    updated = cudaGraphExecUpdate(d->gexec, g, &info) == cudaSuccess;
+    if (!updated) {
+      cudaGetLastError();   // a failed update is not an error: instantiate anew
+      cudaGraphExecDestroy(d->gexec);
+      d->gexec = nullptr;
+    }
+  }
+  if (!updated) {
+    e = cudaGraphInstantiate(&d->gexec, g, 0);
+    if (e != cudaSuccess) {
+      d->gexec = nullptr;
+      cudaGraphDestroy(g);
+      return wf_cuda_fail(d, e, "cudaGraphInstantiate");
+    }
+    d->graph_instantiations++;
+  }
+  cudaGraphDestroy(g);
+  WF_CUDA_OK(cudaGraphLaunch(d->gexec, d->stream));
+  d->graph_launches++;
+  return WF_OK;
+}
+
+// Inside a step segment the timing events become event-record nodes of the
+// graph (the external flag, valid only while capturing); outside, plain records.
+static void record(wf_domain* d, cudaEvent_t e) {
+  if (d->capturing) cudaEventRecordWithFlags(e, d->stream, cudaEventRecordExternal);
+  else cudaEventRecord(e, d->stream);
+}
+
 struct KTimer {
   wf_domain* d;
   int kid;
@@ -446,12 +514,12 @@ struct KTimer {
           d->ev_pool.push_back(e);
         }
       }
-      cudaEventRecord(d->ev_pool[d->ev_used], d->stream);
+      record(d, d->ev_pool[d->ev_used]);
     }
   }
   ~KTimer() {
     if (on) {
-      cudaEventRecord(d->ev_pool[d->ev_used + 1], d->stream);
+      record(d, d->ev_pool[d->ev_used + 1]);
       d->ev_used += 2;
     }
   }
@@ -475,6 +543,10 @@ static int ensure_cells(wf_domain* d, int64_t ncell) {
 constexpr int kReorderEvery = 20;   // physical reorder at every 20th rebuild of a solve
 
 static int rebuild(wf_domain* d, bool use_current, bool light = false) {
+  {
+    const int rc = segment_end(d);
+    if (rc) return rc;
+  }
   KTimer t(d, KID_REBUILD);
   const int64_t n = d->n;
   cudaStream_t s = d->stream;
@@ -680,6 +752,10 @@ static int check_ready(wf_domain* d) {
 }
 
 static int read_status(wf_domain* d) {
+  {
+    const int rc = segment_end(d);
+    if (rc) return rc;
+  }
   WF_CUDA_OK(cudaMemcpyAsync(d->h_status, d->d_status, 8 * sizeof(int), cudaMemcpyDeviceToHost,
                              d->stream));
   WF_CUDA_OK(cudaStreamSynchronize(d->stream));
@@ -736,7 +812,7 @@ static int solve_begin(wf_domain* d, double dt_out) {
   return WF_OK;
 }
 
-static int solve_step(wf_domain* d) {
+static int solve_step_launches(wf_domain* d) {
   cudaStream_t s = d->stream;
   bool rb;
   if (d->rb_dep > 0.0) {
@@ -760,6 +836,10 @@ static int solve_step(wf_domain* d) {
     int rc = rebuild(d, d->rebuild_current != 0, true);
     if (rc) return rc;
     d->rebuilds++;
+  }
+  {
+    const int rc = segment_begin(d);
+    if (rc) return rc;
   }
   StepParams P = make_params(d);
   const Fields& F = d->F[d->cur];
@@ -838,6 +918,19 @@ static int solve_step(wf_domain* d) {
     if (d->h_status[1]) d->is_yielding = true;
   }
   return WF_OK;
+}
+
+// One Fraser step.  A failure inside a step segment ends the capture and
+// drops the segment, so the stream is usable again.
+static int solve_step(wf_domain* d) {
+  const int rc = solve_step_launches(d);
+  if (rc && d->capturing) {
+    d->capturing = false;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamEndCapture(d->stream, &g) == cudaSuccess && g) cudaGraphDestroy(g);
+    cudaGetLastError();
+  }
+  return rc;
 }
 
 // the last step's heat pass (mixed form), before any result leaves a call
@@ -923,6 +1016,11 @@ int wf_destroy(wf_domain* d) {
   for (void* p : ptrs) if (p) cudaFree(p);
   if (d->h_status) cudaFreeHost(d->h_status);
   for (cudaEvent_t e : d->ev_pool) cudaEventDestroy(e);
+  if (d->capturing) {
+    cudaGraph_t g = nullptr;
+    if (cudaStreamEndCapture(d->stream, &g) == cudaSuccess && g) cudaGraphDestroy(g);
+  }
+  if (d->gexec) cudaGraphExecDestroy(d->gexec);
   if (d->stream) cudaStreamDestroy(d->stream);
   delete d;
   return WF_OK;
@@ -1254,7 +1352,10 @@ int wf_set_option(wf_domain* d, const char* key, double v) {
       WF_CUDA_OK(dalloc(&d->log_count, 1, d->stream));
     }
   }
-  else if (k == "graph") { /* reserved */ }
+  else if (k == "graph") {
+    if (d->capturing) return wf_fail(d, WF_ERR_STATE, "graph option changed inside a step segment");
+    d->graph = v != 0;
+  }
   else return wf_fail(d, WF_ERR_ARG, "unknown option: " + k);
   return WF_OK;
 }
@@ -1491,6 +1592,8 @@ int wf_get_scalar(wf_domain* d, const char* name, double* out) {
   if (s == "isfirst") { *out = d->isfirst; return WF_OK; }
   if (s == "launches") { *out = (double)d->launches; return WF_OK; }
   if (s == "rebuilds") { *out = (double)d->rebuilds; return WF_OK; }
+  if (s == "graph_launches") { *out = (double)d->graph_launches; return WF_OK; }
+  if (s == "graph_instantiations") { *out = (double)d->graph_instantiations; return WF_OK; }
   if (s == "contact_tests32" || s == "contact_tests64") {   // law 1, since creation
     unsigned long long c[2];
     WF_CUDA_OK(cudaMemcpyAsync(c, d->d_cstat, sizeof c, cudaMemcpyDeviceToHost, d->stream));
@@ -1570,6 +1673,7 @@ int wf_time_steps(wf_domain* d, int64_t nsteps, double* elapsed_ms, double* kern
   d->timing = true;
   for (int64_t k = 0; k < nsteps && rc == WF_OK; k++) rc = solve_step(d);
   flush_heat(d);   // the timed steps include their whole heat work
+  if (rc == WF_OK) rc = segment_end(d);
   d->timing = false;
   cudaEventRecord(e1, d->stream);
   WF_CUDA_OK(cudaEventSynchronize(e1));
