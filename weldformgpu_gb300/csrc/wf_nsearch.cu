@@ -203,54 +203,168 @@ __global__ void k_reorder(int64_t n, const int32_t* __restrict__ s_src, const Fi
   pf2[k] = pf[s];
 }
 
-// kComputeCounts + kNeighborhoodQueryWithCounts in one pass (ELL output)
-// pf holds the positions in sorted order.  slot_of == nullptr: the state was
-// reordered to that order and sorted index = slot; else slot_of[k] is the
-// storage slot of the k-th sorted particle, and rows and entries are slots.
-__global__ void __launch_bounds__(128) k_nblist(int64_t n, int64_t npad, const float4* __restrict__ pf,
-                                                GridDev g, const uint32_t* __restrict__ start,
-                                                const int32_t* __restrict__ slot_of,
-                                                int32_t* __restrict__ nb, int32_t* __restrict__ cnt,
-                                                int* status) {
-  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  const int64_t i = slot_of ? (int64_t)slot_of[k] : k;
-  const float4 p = pf[k];
-  const int cx = cell_coord(p.x, g.gmin[0], g.gdelta[0]);
-  const int cy = cell_coord(p.y, g.gmin[1], g.gdelta[1]);
-  const int cz = cell_coord(p.z, g.gmin[2], g.gdelta[2]);
-  const float r2 = g.r2;
-  int count = 0;
-  const int x0 = max(cx - 1, 0), x1 = min(cx + 1, g.dim[0] - 1);
-  for (int z = -1; z < 2; z++) {
-    const int fz = cz + z;
-    if (fz < 0 || fz >= g.dim[2]) continue;
-    for (int y = -1; y < 2; y++) {
-      const int fy = cy + y;
-      if (fy < 0 || fy >= g.dim[1]) continue;
-      if (x0 > x1) continue;
+// Neighbour lists, one warp per cell.  The particles of a cell share its
+// candidate set: the nine rows of three x-adjacent cells around it, each one
+// contiguous range of sorted slots, visited z outer, y, x inner
+// (cuNSearchKernels.cu:170-234).  The warp stages in shared memory, in that
+// order, the candidates that lie within r of the box around its particles
+// (any other one fails the distance test for all of them: the box distance
+// is at most the distance to each particle, and a 1e-4 relative margin
+// covers the FP32 rounding of both).  Then, for each chunk of 32 staged
+// candidates and each particle, the lanes test their candidate against that
+// particle with the float rule and the accepted ones are appended in
+// candidate order (ballot, prefix popcount).  Lists, counts and the 70-entry
+// cap are those of a per-particle scan, entry for entry; the staging halves
+// the distance tests (a CPU model of the jittered lattice keeps 161 of 332
+// candidates per cell) and the warp shares one candidate range, where
+// particles scanned by separate lanes diverge at cell boundaries.  786k
+// particles: 0.348 ms per rebuild against 0.385 for the per-particle scan
+// (the ordered append costs about as many instructions as the tests saved).
+// slot_of == nullptr: the state is in sorted order (sorted index = slot);
+// else slot_of[k] is the storage slot of the k-th sorted particle.
+constexpr int kNbWarps = 4;      // warps (cells in flight) per block
+constexpr int kNbStage = 192;    // staged candidates per warp and round
+
+// Tests the staged candidates against the group's particles (part[j]: position
+// and, in w, the storage slot of particle j, whose count lane j holds) and appends the accepted ones to their lists.  Per chunk of 32
+// candidates and per particle j, one ballot gives the accepting lanes; each
+// writes its candidate at j's count before the chunk plus the accepting lanes
+// below it, so the entries keep candidate order.  The counts advance once per
+// chunk (lane j keeps particle j's mask of the chunk), which leaves no chain
+// between the particles' iterations.
+__device__ __forceinline__ void nb_append_round(int nstaged, const float4* __restrict__ sp,
+                                                const int32_t* __restrict__ sid, int gn,
+                                                const float4* __restrict__ part, float r2,
+                                                int64_t npad, int32_t* __restrict__ nb,
+                                                int& count) {
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  for (int ch = 0; ch < nstaged; ch += 32) {
+    const int t = ch + lane;
+    const bool v = t < nstaged;
+    const float4 q = v ? sp[t] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int32_t qid = v ? sid[t] : 0;
+    unsigned mine = 0u;
+#pragma unroll 4
+    for (int j = 0; j < gn; j++) {
+      const float4 pj = part[j];   // same address on every lane: one broadcast read
+      const int32_t ij = __float_as_int(pj.w);
+      const int base = __shfl_sync(0xffffffffu, count, j);
+      const float dx = __fsub_rn(q.x, pj.x), dy = __fsub_rn(q.y, pj.y), dz = __fsub_rn(q.z, pj.z);
+      const float sq =
+          __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+      const bool acc = v && sq < r2 && sq > 0.0f;
+      const unsigned m = __ballot_sync(0xffffffffu, acc);
+      const int k = base + __popc(m & lt);
+      if (acc && k < WF_NB) nb[nb_at(npad, ij, k)] = qid;
+      mine = lane == j ? m : mine;
+    }
+    count += __popc(mine);
+  }
+}
+
+__global__ void __launch_bounds__(32 * kNbWarps) k_nblist(int64_t ncell, int64_t npad,
+                                                          const float4* __restrict__ pf, GridDev g,
+                                                          const uint32_t* __restrict__ start,
+                                                          const int32_t* __restrict__ slot_of,
+                                                          int32_t* __restrict__ nb,
+                                                          int32_t* __restrict__ cnt, int* status) {
+  __shared__ float4 s_pos[kNbWarps][kNbStage];
+  __shared__ int32_t s_id[kNbWarps][kNbStage];
+  __shared__ float4 s_part[kNbWarps][32];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t c = blockIdx.x * (int64_t)kNbWarps + w;
+  if (c >= ncell) return;                      // whole warps leave together
+  const uint32_t ps = start[c], pe = start[c + 1];
+  if (ps >= pe) return;
+  const int cx = (int)(c % g.dim[0]);
+  const int cy = (int)((c / g.dim[0]) % g.dim[1]);
+  const int cz = (int)(c / ((int64_t)g.dim[0] * g.dim[1]));
+  // row r = 3 (dz + 1) + (dy + 1): slot range [rb, rb + rn) on lane r
+  uint32_t rb = 0, rn = 0;
+  if (lane < 9) {
+    const int fz = cz + lane / 3 - 1, fy = cy + lane % 3 - 1;
+    if (fz >= 0 && fz < g.dim[2] && fy >= 0 && fy < g.dim[1]) {
+      const int x0 = max(cx - 1, 0), x1 = min(cx + 1, g.dim[0] - 1);
       const uint32_t rowc = ((uint32_t)fz * g.dim[1] + fy) * g.dim[0];
-      const uint32_t b = __ldg(start + rowc + x0), e = __ldg(start + rowc + x1 + 1);
-      for (uint32_t s = b; s < e; s++) {
-        const float4 q = pf[s];
-        const float dx = __fsub_rn(q.x, p.x), dy = __fsub_rn(q.y, p.y), dz = __fsub_rn(q.z, p.z);
-        const float sq = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-        if (sq < r2 && sq > 0.0f) {
-          nb[nb_at(npad, i, count)] = slot_of ? slot_of[s] : (int32_t)s;
-          count++;
-          if (count == WF_NB) {
-            atomicOr(status, WF_STATUS_NB_CAP);
-            goto done;
-          }
-        }
-      }
+      rb = start[rowc + x0];
+      rn = start[rowc + x1 + 1] - rb;
     }
   }
-done:
-  cnt[i] = count;
-  // pad the last block with the particle's own slot (see nb_at)
-  for (int k = count; k < ((count + WF_NB_BLK - 1) & ~(WF_NB_BLK - 1)); k++)
-    nb[nb_at(npad, i, k)] = (int32_t)i;
+  const float r2 = g.r2, thr = r2 * 1.0001f;
+  float4* sp = s_pos[w];
+  int32_t* sid = s_id[w];
+  for (uint32_t g0 = ps; g0 < pe; g0 += 32) {
+    const int gn = (int)min(32u, pe - g0);
+    // this group's particles (lane j < gn holds particle g0 + j) and their box
+    float px = 0.f, py = 0.f, pz = 0.f;
+    int32_t myslot = 0;
+    float lo[3], hi[3];
+    if (lane < gn) {
+      const float4 p = pf[g0 + lane];
+      px = p.x; py = p.y; pz = p.z;
+      myslot = slot_of ? slot_of[g0 + lane] : (int32_t)(g0 + lane);
+      s_part[w][lane] = make_float4(px, py, pz, __int_as_float(myslot));
+    }
+    {
+      const float4 p0 = pf[g0];
+      lo[0] = hi[0] = lane < gn ? px : p0.x;
+      lo[1] = hi[1] = lane < gn ? py : p0.y;
+      lo[2] = hi[2] = lane < gn ? pz : p0.z;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+      for (int a = 0; a < 3; a++) {
+        lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+        hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+      }
+    int count = 0;
+    int nstaged = 0;
+    for (int r = 0; r < 9; r++) {
+      const uint32_t b = __shfl_sync(0xffffffffu, rb, r);
+      const uint32_t nr = __shfl_sync(0xffffffffu, rn, r);
+      for (uint32_t t0 = 0; t0 < nr; t0 += 32) {
+        if (nstaged > kNbStage - 32) {          // staging full: test what is staged
+          __syncwarp();
+          nb_append_round(nstaged, sp, sid, gn, s_part[w], r2, npad, nb, count);
+          __syncwarp();
+          nstaged = 0;
+        }
+        const bool v = t0 + lane < nr;
+        const uint32_t s = b + t0 + lane;
+        float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+        int32_t id = (int32_t)s;
+        bool keep = false;
+        if (v) {
+          q = pf[s];
+          if (slot_of) id = slot_of[s];
+          const float ex = fmaxf(0.f, fmaxf(lo[0] - q.x, q.x - hi[0]));
+          const float ey = fmaxf(0.f, fmaxf(lo[1] - q.y, q.y - hi[1]));
+          const float ez = fmaxf(0.f, fmaxf(lo[2] - q.z, q.z - hi[2]));
+          keep = ex * ex + ey * ey + ez * ez < thr;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (keep) {
+          const int at = nstaged + __popc(m & ((1u << lane) - 1u));
+          sp[at] = q;
+          sid[at] = id;
+        }
+        nstaged += __popc(m);
+      }
+    }
+    __syncwarp();
+    nb_append_round(nstaged, sp, sid, gn, s_part[w], r2, npad, nb, count);
+    __syncwarp();
+    if (lane < gn) {
+      if (count >= WF_NB) atomicOr(status, WF_STATUS_NB_CAP);
+      const int cn = min(count, WF_NB);
+      cnt[myslot] = cn;
+      // pad the last block with the particle's own slot (see nb_at)
+      for (int k = cn; k < ((cn + WF_NB_BLK - 1) & ~(WF_NB_BLK - 1)); k++)
+        nb[nb_at(npad, myslot, k)] = myslot;
+    }
+  }
 }
 
 // the search positions in sorted order, for a rebuild that keeps the state in place
@@ -331,7 +445,10 @@ void launch_reorder(int64_t n, const int32_t* s_src, const Fields& A, const Fiel
 void launch_nblist(int64_t n, int64_t npad, const float4* pf, const GridDev& g,
                    const uint32_t* start, const int32_t* slot_of, int32_t* nb, int32_t* cnt,
                    int* status, cudaStream_t s) {
-  k_nblist<<<nblocks(n, 128), 128, 0, s>>>(n, npad, pf, g, start, slot_of, nb, cnt, status);
+  (void)n;
+  const int64_t ncell = (int64_t)g.dim[0] * g.dim[1] * g.dim[2];
+  k_nblist<<<nblocks(ncell, kNbWarps), 32 * kNbWarps, 0, s>>>(ncell, npad, pf, g, start, slot_of,
+                                                               nb, cnt, status);
 }
 void launch_gather_pf(int64_t n, const int32_t* s_src, const float4* pf, float4* pf2,
                       cudaStream_t s) {
