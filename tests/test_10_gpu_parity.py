@@ -69,6 +69,38 @@ def test_neighbors_bit_exact_jittered_lattice():
     assert same_lists(*g.get_neighbors(), *o.get_neighbors())
 
 
+def test_neighbour_lists_dense_clusters_and_cap():
+    """Isolated clusters of 40 particles (cells holding more than a warp's
+    worth of particles) and of 90 (lists truncated at 70 entries, the first 70
+    in search order, as cuNSearch's CUDA_MAX_NEIGHBORS): lists identical to
+    the oracle's, the truncation recorded in bit 2 of the status word."""
+    from weldformgpu_gb300 import Domain_d
+    h = 1.0e-3
+    rng = np.random.default_rng(11)
+    pts = []
+    for a in range(3):
+        for b in range(3):
+            for c in range(3):
+                size = 90 if (a + b + c) % 4 == 0 else 40
+                centre = np.array([a, b, c]) * 3.0 * h    # clusters 2.4 h apart, r = 2 h
+                pts.append(centre + rng.uniform(-0.3 * h, 0.3 * h, (size, 3)))
+    x = np.vstack(pts)
+    n = len(x)
+    g = Domain_d(n)
+    g.set_h(h)
+    g.set_positions(x)
+    g.find_neighbors()
+    o = O.OracleDomain(n)
+    o.set_h(h)
+    o.set_positions(np.ascontiguousarray(x).ravel())
+    o.find_neighbors()
+    gc, gl = g.get_neighbors()
+    oc, ol = o.get_neighbors()
+    assert same_lists(gc, gl, oc, ol)
+    assert gc.max() == 70 and (gc == 39).sum() > 0
+    assert int(g.get_scalar("status")) & 2
+
+
 @pytest.mark.parametrize("case,checkpoints", [("bilinear", [1, 600, 1500]), ("jc", [300]),
                                               ("hollomon", [300])])
 def test_fp64_fraser_loop_bit_exact_vs_reference_golden(case, checkpoints):
