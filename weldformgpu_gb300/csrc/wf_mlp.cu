@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer_umma(const uint4* __restrict_
                                                         const float4* __restrict__ X, int64_t n,
                                                         float* __restrict__ Y, int* status) {
   extern __shared__ __align__(1024) uint8_t smu[];
-  mlp_umma_begin(smu, image, status);
+  mlp_umma_begin(smu, image);
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const bool valid = i < n;
   float f[4] = {0.f, 0.f, 0.f, 0.f};
@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(128) k_mlp_newton_iters(StepParams P, double G
                                                           int32_t* __restrict__ used,
                                                           float* __restrict__ dl_out, int* status) {
   extern __shared__ __align__(1024) uint8_t smu[];
-  mlp_umma_begin(smu, image, status);
+  mlp_umma_begin(smu, image);
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const bool valid = i < n;
   const float4 s = valid ? S[i] : make_float4(1.f, 1e-2f, 1.f, 20.f);

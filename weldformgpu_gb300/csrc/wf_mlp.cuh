@@ -108,11 +108,11 @@ __host__ __device__ __forceinline__ int umma_kmajor_off(int r, int k, int K) {
 // thread starts a bulk copy of the weight image into dynamic shared memory
 // and initialises the mbarriers, and warp 0 allocates the 64 tensor-memory
 // columns; in every case warp 0 gives up the allocation permit so further
-// CTAs can start on the SM.  Ends once the image has arrived.  The image must
-// be 16-byte aligned (WF_UMMA_IMAGE is a multiple of 16).  Returns false
-// (and sets WF_STATUS_MMA_WAIT) if the copy's wait ran out.
-__device__ __forceinline__ bool mlp_umma_begin(uint8_t* sm, const uint4* __restrict__ image,
-                                               int* status) {
+// CTAs can start on the SM.  Does not wait for the copy: it arrives while the
+// block works through its neighbour loops, and mlp_umma_cta waits for it
+// (every block that starts the copy reaches that call).  The image must be
+// 16-byte aligned (WF_UMMA_IMAGE is a multiple of 16).
+__device__ __forceinline__ void mlp_umma_begin(uint8_t* sm, const uint4* __restrict__ image) {
   const uint32_t s0 = umma::smem_addr(sm);
   if (image && threadIdx.x == 0) {
     umma::mbar_init(s0 + WF_UMMA_MBAR, 1);
@@ -126,10 +126,6 @@ __device__ __forceinline__ bool mlp_umma_begin(uint8_t* sm, const uint4* __restr
   umma::fence_before_sync();
   __syncthreads();
   umma::fence_after_sync();
-  if (!image) return true;
-  const bool ok = umma::mbar_wait(s0 + WF_UMMA_MBAR_W, 0, 1 << 20);
-  if (!ok && threadIdx.x == 0) atomicOr(status, WF_STATUS_MMA_WAIT);
-  return ok;
 }
 
 // Block-collective, once per kernel after mlp_umma_begin(sm, image != nullptr):
@@ -143,11 +139,19 @@ static __device__ __forceinline__ float mlp_umma_cta(uint8_t* sm, const float f[
   constexpr uint32_t kId = umma::idesc_bf16_f32(128, 64);
   const int tid = threadIdx.x, warp = tid >> 5;
   const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(sm + WF_UMMA_TSLOT);
+  const uint32_t s0 = umma::smem_addr(sm);
+  // the weight image started by mlp_umma_begin (long arrived by now); every
+  // thread waits, so no block leaves with the copy in flight
+  const bool image_ok = umma::mbar_wait(s0 + WF_UMMA_MBAR_W, 0, kWaitLimit);
+  if (!__syncthreads_and(image_ok)) {
+    if (warp == 0) umma::tmem_dealloc(tmem, 64);
+    if (tid == 0) atomicOr(status, WF_STATUS_MMA_WAIT);
+    return -1.0f;
+  }
   if (!__syncthreads_or(want)) {
     if (warp == 0) umma::tmem_dealloc(tmem, 64);
     return -1.0f;
   }
-  const uint32_t s0 = umma::smem_addr(sm);
   const uint32_t mbar = s0 + WF_UMMA_MBAR;
   uint4* a1 = reinterpret_cast<uint4*>(sm + WF_UMMA_A1 + umma_kmajor_off(tid, 0, 16));
   a1[0] = make_uint4(bf16x2(f[0], f[1]), bf16x2(f[2], f[3]), bf16x2(1.0f, 0.0f), 0u);

@@ -291,7 +291,7 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
   // at once: every thread of the block must reach it, so out-of-range and
   // non-solid threads are predicated rather than returned before that point.
   extern __shared__ __align__(1024) uint8_t smlp[];
-  mlp_umma_begin(smlp, mlp, status);
+  mlp_umma_begin(smlp, mlp);
   const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const bool valid = i0 < P.n;
   const int64_t i = valid ? i0 : 0;
