@@ -14,6 +14,8 @@
 // particle's candidates are 9 ranges, visited in the reference's order.
 // Lists are stored in blocks of 8 entries (nb_at in wf_common.cuh): a thread
 // reads 8 entries with two 16-byte loads and a warp reads contiguous memory.
+#include <algorithm>
+
 #include "wf_common.cuh"
 #include "wf_nsearch.cuh"
 
@@ -38,13 +40,16 @@ __global__ void k_prep_positions(int64_t n, const Fields F, int use_current, flo
 // kComputeMinMax: integer cell bounds of floor(p / r), block-reduced first
 __global__ void k_minmax(int64_t n, const float4* __restrict__ pf, float r, int* mm) {
   __shared__ int smn[3][32], smx[3][32];
-  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   int mn[3] = {INT_MAX, INT_MAX, INT_MAX}, mx[3] = {INT_MIN, INT_MIN, INT_MIN};
-  if (i < n) {
-    float4 p = pf[i];
-    int c0 = (int)floorf(__fdiv_rn(p.x, r)), c1 = (int)floorf(__fdiv_rn(p.y, r)),
-        c2 = (int)floorf(__fdiv_rn(p.z, r));
-    mn[0] = mx[0] = c0; mn[1] = mx[1] = c1; mn[2] = mx[2] = c2;
+  // grid-stride over the particles: one block-reduced atomic per block
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float4 p = pf[i];
+    const int c0 = (int)floorf(__fdiv_rn(p.x, r)), c1 = (int)floorf(__fdiv_rn(p.y, r)),
+              c2 = (int)floorf(__fdiv_rn(p.z, r));
+    mn[0] = min(mn[0], c0); mx[0] = max(mx[0], c0);
+    mn[1] = min(mn[1], c1); mx[1] = max(mx[1], c1);
+    mn[2] = min(mn[2], c2); mx[2] = max(mx[2], c2);
   }
   for (int a = 0; a < 3; a++) {
     for (int o = 16; o > 0; o >>= 1) {
@@ -444,7 +449,7 @@ void launch_prep_positions(int64_t n, const Fields& F, int use_current, float4* 
   k_prep_positions<<<nblocks(n, 256), 256, 0, s>>>(n, F, use_current, pf);
 }
 void launch_minmax(int64_t n, const float4* pf, float r, int* mm, cudaStream_t s) {
-  k_minmax<<<nblocks(n, 256), 256, 0, s>>>(n, pf, r, mm);
+  k_minmax<<<std::min(nblocks(n, 256), 1024), 256, 0, s>>>(n, pf, r, mm);
 }
 void launch_cell_count(int64_t n, const float4* pf, const GridDev& g, uint32_t* cellid,
                        uint32_t* count, int* status, cudaStream_t s) {
