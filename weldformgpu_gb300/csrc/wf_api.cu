@@ -58,6 +58,7 @@ struct wf_domain {
   float* sigr32 = nullptr;
   float* mlp_w = nullptr;      // device MLP parameters (FP32, packed layout of wf_mlp.cuh)
   void* mlp_packed = nullptr;  // BF16 tensor-core fragment image of mlp_w
+  MlpL1 mlp_l1{};              // layer 1 of mlp_w (a kernel parameter of the stress pass)
   bool mlp_loaded = false;
   // return-map log: (features, converged increment) pairs from the plain form
   int64_t log_cap = 0;
@@ -862,7 +863,7 @@ static int solve_step_launches(wf_domain* d) {
     }
     { KTimer t(d, KID_STRESS);
       launch_fp32_stress(P, F, d->v32b, d->sigr32, N, d->d_status,
-                         (d->mlp_on && d->mlp_loaded) ? d->mlp_packed : nullptr, s); }
+                         (d->mlp_on && d->mlp_loaded) ? d->mlp_packed : nullptr, &d->mlp_l1, s); }
     if (!P.contact && d->fuse_integrate) {
       { KTimer t(d, KID_ACCEL); launch_fp32_accel_integrate(P, F, d->v32b, d->sigr32, d->vd2, N, s); }
       std::swap(d->F[d->cur].p32, d->F[d->cur].p32n);   // the new positions become current
@@ -1283,6 +1284,7 @@ int wf_set_mlp_weights(wf_domain* d, const float* params) {
   WF_CUDA_OK(cudaMemcpyAsync(d->mlp_w, params, sizeof(float) * WF_MLP_NPARAM,
                              cudaMemcpyHostToDevice, d->stream));
   if (wf_mlp_pack_device(d->mlp_w, d->mlp_packed, d->stream)) return wf_fail(d, WF_ERR_CUDA, "mlp pack");
+  d->mlp_l1 = mlp_l1_from(params);
   WF_CUDA_OK(cudaStreamSynchronize(d->stream));
   d->mlp_loaded = true;
   return WF_OK;

@@ -278,9 +278,11 @@ void launch_mesh_plane(const StepParams& P, cudaStream_t s);
 // density pass of this step with the previous step's heat pass (mixed form)
 void launch_fp32_density_heat(const StepParams& P, const Fields& F, double4* vd2, float4* v32b,
                               const NbBuffers& N, int first, int plastic_heat, cudaStream_t s);
+struct MlpL1;
+// mlp_packed (the tcgen05 weight image) and mlp_l1 (layer 1) together, or neither
 void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b,
                         float* sigr32, const NbBuffers& N, int* status, const void* mlp_packed,
-                        cudaStream_t s);
+                        const MlpL1* mlp_l1, cudaStream_t s);
 void launch_fp32_accel(const StepParams& P, const Fields& F, const float4* v32b,
                        const float* sigr32, float4* a32, const NbBuffers& N, cudaStream_t s);
 void launch_fp32_accel_integrate(const StepParams& P, const Fields& F, const float4* v32b,

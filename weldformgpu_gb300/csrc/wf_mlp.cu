@@ -20,21 +20,13 @@
 namespace {
 
 // ---- parameter packing for the tensor-core kernels ---------------------------
-// The tcgen05 weight image (mlp_umma_cta): B1 = [W1 | b1 | 0] and B2 = W2 in
-// BF16, K-major core-matrix order, then b2, W3 and b3 in FP32.
+// The tcgen05 weight image (mlp_umma_cta): B2 = W2 in BF16, K-major core-
+// matrix order, then b2, W3 and b3 in FP32 (layer 1 travels as MlpL1).
 __global__ void k_mlp_pack_umma(const float* __restrict__ P, uint8_t* __restrict__ out) {
-  const float* W1 = P + WF_MLP_OFF_W1;
-  const float* b1 = P + WF_MLP_OFF_B1;
   const float* W2 = P + WF_MLP_OFF_W2;
   for (int k = threadIdx.x; k < WF_UMMA_IMAGE / 4; k += blockDim.x)
     reinterpret_cast<uint32_t*>(out)[k] = 0u;
   __syncthreads();
-  for (int e = threadIdx.x; e < WF_MLP_H * 16; e += blockDim.x) {
-    const int n = e / 16, k = e % 16;
-    const float v = k < 4 ? W1[n * 4 + k] : (k == 4 ? b1[n] : 0.0f);
-    *reinterpret_cast<__nv_bfloat16*>(out + WF_UMMA_B1 + umma_kmajor_off(n, k, 16)) =
-        __float2bfloat16_rn(v);
-  }
   for (int e = threadIdx.x; e < WF_MLP_H * WF_MLP_H; e += blockDim.x) {
     const int n = e / WF_MLP_H, k = e % WF_MLP_H;
     *reinterpret_cast<__nv_bfloat16*>(out + WF_UMMA_B2 + umma_kmajor_off(n, k, WF_MLP_H)) =
@@ -49,6 +41,7 @@ __global__ void k_mlp_pack_umma(const float* __restrict__ P, uint8_t* __restrict
 
 // ---- standalone inference ---------------------------------------------------
 __global__ void __launch_bounds__(128) k_mlp_infer_umma(const uint4* __restrict__ image,
+                                                        const MlpL1 l1,
                                                         const float4* __restrict__ X, int64_t n,
                                                         float* __restrict__ Y, int* status) {
   extern __shared__ __align__(1024) uint8_t smu[];
@@ -60,7 +53,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer_umma(const uint4* __restrict_
     const float4 x = X[i];
     f[0] = x.x; f[1] = x.y; f[2] = x.z; f[3] = x.w;
   }
-  const float y = mlp_umma_cta(smu, f, valid, status);
+  const float y = mlp_umma_cta(smu, f, valid, status, l1);
   if (valid) Y[i] = y;
 }
 
@@ -138,6 +131,7 @@ __global__ void k_mlp_synth(StepParams P, double G, int64_t n, uint64_t seed, fl
 // Newton iterations from the radial start (image == nullptr) or the network's start
 __global__ void __launch_bounds__(128) k_mlp_newton_iters(StepParams P, double G,
                                                           const uint4* __restrict__ image,
+                                                          const MlpL1 l1,
                                                           const float4* __restrict__ S, int64_t n,
                                                           int32_t* __restrict__ iters,
                                                           int32_t* __restrict__ used,
@@ -157,7 +151,7 @@ __global__ void __launch_bounds__(128) k_mlp_newton_iters(StepParams P, double G
   if (image) {
     float f[4];
     mlp_features(s.x, (double)s.y, s.z, (float)Th, f);
-    const float y = mlp_umma_cta(smu, f, valid, status);
+    const float y = mlp_umma_cta(smu, f, valid, status, l1);
     const float yc = mlp_accept(y);
     if (yc > 0.0f) { ratio = (double)yc; use = 1; }
   }
@@ -356,7 +350,7 @@ int wf_mlp_infer(const float* params, const float* X, int64_t n, int use_tensor_
     if (!dI || !dS) return WF_ERR_ALLOC;
     cudaMemset(dS, 0, sizeof(int));
     k_mlp_pack_umma<<<1, 256>>>(dP, (uint8_t*)dI);
-    k_mlp_infer_umma<<<nb(n, 128), 128, WF_UMMA_SMEM>>>(dI, dX, n, dY, dS);
+    k_mlp_infer_umma<<<nb(n, 128), 128, WF_UMMA_SMEM>>>(dI, mlp_l1_from(params), dX, n, dY, dS);
     int st = 0;
     cudaMemcpy(&st, dS, sizeof(int), cudaMemcpyDeviceToHost);
     if (st & WF_STATUS_MMA_WAIT) return WF_ERR_CUDA;
@@ -477,8 +471,9 @@ int wf_mlp_newton_iters(const wf_material* mat, double G, const float* params, c
     k_mlp_pack_umma<<<1, 256>>>(dP, (uint8_t*)dW);
   }
   StepParams P = jc_params(mat, rtol);
+  const MlpL1 l1 = params ? mlp_l1_from(params) : MlpL1{};
   k_mlp_newton_iters<<<nb(n, 128), 128, params ? WF_UMMA_SMEM : 0>>>(
-      P, G, params ? dW : nullptr, dS, n, dI, dU, dD, dSt);
+      P, G, params ? dW : nullptr, l1, dS, n, dI, dU, dD, dSt);
   cudaMemcpy(iters, dI, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
   cudaMemcpy(used, dU, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
   if (cudaMemcpy(dl, dD, sizeof(float) * n, cudaMemcpyDeviceToHost) != cudaSuccess) return WF_ERR_CUDA;

@@ -69,34 +69,51 @@ __device__ __forceinline__ uint32_t silu_bf16x2(float z0, float z1) {
 // ---------------------------------------------------------------------------
 // tcgen05 inference: one CTA of 128 threads evaluates the network for its 128
 // particles, row m of every matrix being thread m's particle.
-//   layer 1: D1 (128 x 64, FP32 in tensor memory) = A1 (128 x 16) x B1^T,
-//            A1 row = [f0 f1 f2 f3 1 0 ...], B1 row n = [W1[n][0..3] b1[n] 0 ...]
-//   layer 2: D2 (128 x 64) = A2 (128 x 64) x B2^T, A2 = SiLU(D1) in BF16,
-//            B2 = W2; four MMAs of K = 16 accumulate in the same 64 columns
+//   layer 1: each thread, FP32 on the CUDA cores: h = SiLU(W1 f + b1), written
+//            in BF16 as its row of A2 (128 x 64)
+//   layer 2: D2 (128 x 64, FP32 in tensor memory) = A2 x B2^T, B2 = W2; four
+//            MMAs of K = 16 accumulate in the same 64 columns
 //   layer 3: each thread reads its row of D2, adds b2, applies SiLU and
 //            takes the dot product with W3 (FP32).
 // One thread issues the MMAs and commits them to an mbarrier; every thread
 // waits (bounded) and reads its own row with tcgen05.ld.  The 64 tensor-
-// memory columns are allocated and freed inside the call.
+// memory columns are allocated at kernel entry and freed inside the call.
 //
 // Dynamic shared memory (bytes): the weight image (copied from the packed
-// parameters, MlpUmma), then the two A operands, the mbarrier and the
-// tensor-memory address.  K-major, no swizzle (wf_umma.cuh).
+// parameters, k_mlp_pack_umma), then A2, the mbarriers and the tensor-memory
+// address.  K-major, no swizzle (wf_umma.cuh).
 // ---------------------------------------------------------------------------
 #include "wf_common.cuh"
 #include "wf_umma.cuh"
-#define WF_UMMA_B1 0          // 64 x 16 BF16 (SBO 256)
-#define WF_UMMA_B2 2048       // 64 x 64 BF16 (SBO 1024)
-#define WF_UMMA_BIAS2 10240   // 64 floats
-#define WF_UMMA_W3 10496      // 64 floats
-#define WF_UMMA_B3 10752      // 1 float
-#define WF_UMMA_IMAGE 10880   // bytes of the packed weight image (a multiple of 128)
-#define WF_UMMA_A1 10880      // 128 x 16 BF16 (SBO 256)
-#define WF_UMMA_A2 14976      // 128 x 64 BF16 (SBO 1024)
-#define WF_UMMA_MBAR 31360    // mbarrier of the MMAs, 8 bytes
-#define WF_UMMA_TSLOT 31368   // tensor-memory base address, 4 bytes
-#define WF_UMMA_MBAR_W 31376  // mbarrier of the weight-image copy, 8 bytes
-#define WF_UMMA_SMEM 31488    // dynamic shared memory of a kernel that runs the MLP
+#define WF_UMMA_B2 0          // 64 x 64 BF16 (SBO 1024)
+#define WF_UMMA_BIAS2 8192    // 64 floats
+#define WF_UMMA_W3 8448       // 64 floats
+#define WF_UMMA_B3 8704       // 1 float
+#define WF_UMMA_IMAGE 8832    // bytes of the packed weight image (a multiple of 128)
+#define WF_UMMA_A2 8832       // 128 x 64 BF16 (SBO 1024)
+#define WF_UMMA_MBAR 25216    // mbarrier of the MMAs, 8 bytes
+#define WF_UMMA_TSLOT 25224   // tensor-memory base address, 4 bytes
+#define WF_UMMA_MBAR_W 25232  // mbarrier of the weight-image copy, 8 bytes
+#define WF_UMMA_SMEM 25344    // dynamic shared memory of a kernel that runs the MLP
+
+// Layer 1 (4 -> 64) runs on the CUDA cores in FP32: its weights travel as a
+// kernel parameter, so every multiply-add reads its weight from the constant
+// bank.  On the tensor cores it took a K = 16 MMA of its own (4 features, the
+// bias column, zeros), a block barrier and a completion round trip.
+struct MlpL1 {
+  float w[WF_MLP_H][WF_MLP_IN];
+  float b[WF_MLP_H];
+};
+
+// layer 1 of the packed parameters (W1 row-major out x in, then b1)
+inline MlpL1 mlp_l1_from(const float* P) {
+  MlpL1 l;
+  for (int n = 0; n < WF_MLP_H; n++) {
+    for (int k = 0; k < WF_MLP_IN; k++) l.w[n][k] = P[WF_MLP_OFF_W1 + n * WF_MLP_IN + k];
+    l.b[n] = P[WF_MLP_OFF_B1 + n];
+  }
+  return l;
+}
 
 // byte offset of BF16 element (r, k) of a K-major operand with K columns
 __host__ __device__ __forceinline__ int umma_kmajor_off(int r, int k, int K) {
@@ -134,7 +151,7 @@ __device__ __forceinline__ void mlp_umma_begin(uint8_t* sm, const uint4* __restr
 // or -1 when no thread of the block wants a prediction or a completion wait
 // ran out (then WF_STATUS_MMA_WAIT is set in *status).
 static __device__ __forceinline__ float mlp_umma_cta(uint8_t* sm, const float f[4], bool want,
-                                                     int* status) {
+                                                     int* status, const MlpL1& l1) {
   constexpr int kWaitLimit = 1 << 20;
   constexpr uint32_t kId = umma::idesc_bf16_f32(128, 64);
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -153,28 +170,22 @@ static __device__ __forceinline__ float mlp_umma_cta(uint8_t* sm, const float f[
     return -1.0f;
   }
   const uint32_t mbar = s0 + WF_UMMA_MBAR;
-  uint4* a1 = reinterpret_cast<uint4*>(sm + WF_UMMA_A1 + umma_kmajor_off(tid, 0, 16));
-  a1[0] = make_uint4(bf16x2(f[0], f[1]), bf16x2(f[2], f[3]), bf16x2(1.0f, 0.0f), 0u);
-  a1[8] = make_uint4(0u, 0u, 0u, 0u);            // columns 8..15, the next core matrix
-  umma::fence_async_smem();
-  __syncthreads();
-  umma::fence_after_sync();
-  if (tid == 0) {
-    umma::mma_bf16(tmem, umma::smem_desc(s0 + WF_UMMA_A1, 128, 256),
-                   umma::smem_desc(s0 + WF_UMMA_B1, 128, 256), kId, 0u);
-    umma::commit(mbar);
-  }
-  bool ok = umma::mbar_wait(mbar, 0, kWaitLimit);
-  umma::fence_after_sync();
-  const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);   // this warp's 32 lanes
+  // layer 1 and its SiLU (BF16 pairs) into this thread's row of A2
   uint4* a2 = reinterpret_cast<uint4*>(sm + WF_UMMA_A2 + umma_kmajor_off(tid, 0, 64));
 #pragma unroll
   for (int c = 0; c < 4; c++) {
-    float v[16];
-    umma::ld16(trow + 16 * c, v);
     uint32_t r[8];
 #pragma unroll
-    for (int j = 0; j < 8; j++) r[j] = silu_bf16x2(v[2 * j], v[2 * j + 1]);
+    for (int j = 0; j < 8; j++) {
+      const int n0 = 16 * c + 2 * j;
+      float z0 = l1.b[n0], z1 = l1.b[n0 + 1];
+#pragma unroll
+      for (int k = 0; k < WF_MLP_IN; k++) {
+        z0 = fmaf(l1.w[n0][k], f[k], z0);
+        z1 = fmaf(l1.w[n0 + 1][k], f[k], z1);
+      }
+      r[j] = silu_bf16x2(z0, z1);
+    }
     a2[16 * c] = make_uint4(r[0], r[1], r[2], r[3]);       // columns 16c .. 16c+7
     a2[16 * c + 8] = make_uint4(r[4], r[5], r[6], r[7]);   // columns 16c+8 .. 16c+15
   }
@@ -189,8 +200,9 @@ static __device__ __forceinline__ float mlp_umma_cta(uint8_t* sm, const float f[
                      umma::smem_desc(s0 + WF_UMMA_B2 + 256 * kk, 128, 1024), kId, kk > 0 ? 1u : 0u);
     umma::commit(mbar);
   }
-  ok = umma::mbar_wait(mbar, 1, kWaitLimit) && ok;
+  const bool ok = umma::mbar_wait(mbar, 0, kWaitLimit);
   umma::fence_after_sync();
+  const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);   // this warp's 32 lanes
   const float* bias2 = reinterpret_cast<const float*>(sm + WF_UMMA_BIAS2);
   const float* w3 = reinterpret_cast<const float*>(sm + WF_UMMA_W3);
   float y = 0.0f;

@@ -286,7 +286,8 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
                                                   const int32_t* __restrict__ nb,
                                                   const int32_t* __restrict__ cnt,
                                                   int* __restrict__ status,
-                                                  const uint4* __restrict__ mlp) {
+                                                  const uint4* __restrict__ mlp,
+                                                  const MlpL1 l1) {
   // The MLP runs on the tensor cores (tcgen05) for the block's 128 particles
   // at once: every thread of the block must reach it, so out-of-range and
   // non-solid threads are predicated rather than returned before that point.
@@ -402,7 +403,7 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
     const bool want = solid && jc_newton && st > sy0f;
     float f[4] = {0.f, 0.f, 0.f, 0.f};
     if (want) mlp_features(st / sy0f, eps_p, eff, Th, f);
-    const float y = mlp_umma_cta(smlp, f, want, status);
+    const float y = mlp_umma_cta(smlp, f, want, status, l1);
     const float yc = mlp_accept(y);
     if (want && yc > 0.0f) ratio = (double)yc;
     if (!solid) return;
@@ -635,10 +636,12 @@ void launch_fp32_density_heat(const StepParams& P, const Fields& F, double4* vd2
                                                         plastic_heat);
 }
 void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b, float* sigr32,
-                        const NbBuffers& N, int* status, const void* mlp_packed, cudaStream_t s) {
+                        const NbBuffers& N, int* status, const void* mlp_packed,
+                        const MlpL1* mlp_l1, cudaStream_t s) {
   const uint4* W = reinterpret_cast<const uint4*>(mlp_packed);
+  const MlpL1 l1 = (W && mlp_l1) ? *mlp_l1 : MlpL1{};
   size_t smem = W ? WF_UMMA_SMEM : 0;
-  k_stress32<<<blocks_for(P.n, 128), 128, smem, s>>>(P, F, v32b, sigr32, N.nb, N.cnt, status, W);
+  k_stress32<<<blocks_for(P.n, 128), 128, smem, s>>>(P, F, v32b, sigr32, N.nb, N.cnt, status, W, l1);
 }
 void launch_fp32_accel(const StepParams& P, const Fields& F, const float4* v32b,
                        const float* sigr32, float4* a32, const NbBuffers& N, cudaStream_t s) {
