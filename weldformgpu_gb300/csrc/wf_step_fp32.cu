@@ -74,6 +74,7 @@ __device__ __forceinline__ unsigned group_mask() {
 // one lane and 6 blocks per SM, 0.202-0.213 ms with 2 or 4 lanes).
 constexpr int kDensLanes = 1;
 constexpr int kDensMinBlocks = 6;
+constexpr int kDensBatch = 4;
 
 __global__ void __launch_bounds__(128) k_density32(StepParams P, Fields F,
                                                    double4* __restrict__ vd2,
@@ -137,7 +138,7 @@ __global__ void __launch_bounds__(128, kDensMinBlocks) k_density_heat32(StepPara
                                                         const int32_t* __restrict__ cnt,
                                                         int first, int plastic_heat) {
   constexpr int W = WF_NB_BLK / kDensLanes;
-  constexpr int NB = W < 4 ? W : 4;   // neighbours gathered per batch
+  constexpr int NB = W < kDensBatch ? W : kDensBatch;   // neighbours gathered per batch
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int g = (int)(t & (kDensLanes - 1));
   const int64_t i = t / kDensLanes;
@@ -280,6 +281,9 @@ __device__ __forceinline__ void sigr32_split(T* base, int64_t npad, F4*& a, F2*&
   b = reinterpret_cast<F2*>(base + 4 * npad);
 }
 
+// neighbours gathered per batch in the stress pass (position and velocity)
+constexpr int kStressBatch = 4;
+
 __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
                                                   const float4* __restrict__ v32b,
                                                   float* __restrict__ sigr32,
@@ -314,15 +318,15 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
     const int m = c - WF_NB_BLK * b;
     if (m > WF_NB_BLK) nb_block(nb, P.npad, i, b + 1, lo, hi);
 #pragma unroll
-    for (int h = 0; h < WF_NB_BLK; h += 4) {
-      float4 pj[4], vj[4];
+    for (int h = 0; h < WF_NB_BLK; h += kStressBatch) {
+      float4 pj[kStressBatch], vj[kStressBatch];
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
+      for (int q = 0; q < kStressBatch; q++) {
         pj[q] = F.p32[js[h + q]];
         vj[q] = v32b[js[h + q]];
       }
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
+      for (int q = 0; q < kStressBatch; q++) {
         if (h + q >= m || (P.contact && !pass_j(P, F.id[js[h + q]]))) continue;
         const float xx = pi.x - pj[q].x, xy = pi.y - pj[q].y, xz = pi.z - pj[q].z;
         // w = 2 s of the reference's s = -GK m_j / (2 rho_j); the off-diagonal
