@@ -421,6 +421,42 @@ def test_mixed_fused_heat_matches_separate_heat_pass():
     assert Ts.max() > 20.5
 
 
+def test_setters_from_pinned_host_arrays_match_pageable():
+    """The same scenario and checkpoint loaded from page-locked (pinned) and
+    from pageable host arrays give identical fields, before and after steps
+    (the end-to-end measurement passes pinned arrays)."""
+    torch = pytest.importorskip("torch")
+    from weldformgpu_gb300 import Domain_d
+    sc = S.compression_cylinder(material="jc", vz_top=-10.0)
+    sc["k"], sc["cp"] = 167.0, 896.0
+    opts = {"return_map": 1, "thermal": 1, "taylor_quinney": 0.9, "precision": 1}
+    keep = []
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=getattr(torch, str(a.dtype)), pin_memory=True)
+        keep.append(t)
+        out = t.numpy()
+        out[...] = a
+        return out
+
+    base = gpu(sc, opts)
+    base.step(40)
+    state = base.checkpoint()
+    psc = {k: (pinned(v) if isinstance(v, np.ndarray) else v) for k, v in sc.items()}
+    pstate = {k: (pinned(v) if isinstance(v, np.ndarray) else v) for k, v in state.items()}
+    a = S.load(Domain_d(sc["n"]), sc, opts)
+    b = S.load(Domain_d(sc["n"]), psc, opts)
+    a.restore(state)
+    b.restore(pstate)
+    fields = ("x", "u", "v", "rho", "pl_strain", "sigma_eq", "T")
+    for f in fields:
+        assert np.array_equal(a.get_field(f), b.get_field(f)), f
+    a.step(30)
+    b.step(30)
+    for f in fields:
+        assert np.array_equal(a.get_field(f), b.get_field(f)), f
+
+
 def _graph_case(name):
     if name == "mixed_jc_heat":
         sc = S.compression_cylinder(material="jc", vz_top=-10.0)
