@@ -244,11 +244,17 @@ __global__ void k_reorder(int64_t n, const int32_t* __restrict__ s_src, const Fi
 // the distance tests (a CPU model of the jittered lattice keeps 161 of 332
 // candidates per cell) and the warp shares one candidate range, where
 // particles scanned by separate lanes diverge at cell boundaries.  786k
-// particles: 0.348 ms per rebuild against 0.385 for the per-particle scan
-// (the ordered append costs about as many instructions as the tests saved).
+// particles: 0.295 ms per rebuild against 0.385 for the per-particle scan
+// (0.348 with 64-bit entry indices in the append loop).
 // slot_of == nullptr: the state is in sorted order (sorted index = slot);
 // else slot_of[k] is the storage slot of the k-th sorted particle.
 constexpr int kNbWarps = 4;      // warps (cells in flight) per block
+// List entry index (nb_at) in the index type I: 32-bit when the lists hold
+// fewer than 2^31 entries (fewer than ~29M particles), else 64-bit.
+template <class I>
+__device__ __forceinline__ I nb_at_i(I npad, I i, int k) {
+  return ((I)(k >> 3) * npad + i) * (I)WF_NB_BLK + (I)(k & 7);
+}
 constexpr int kNbStage = 192;    // staged candidates per warp and round
 
 // Tests the staged candidates against the group's particles (part[j]: position
@@ -258,6 +264,7 @@ constexpr int kNbStage = 192;    // staged candidates per warp and round
 // below it, so the entries keep candidate order.  The counts advance once per
 // chunk (lane j keeps particle j's mask of the chunk), which leaves no chain
 // between the particles' iterations.
+template <class I>
 __device__ __forceinline__ void nb_append_round(int nstaged, const float4* __restrict__ sp,
                                                 const int32_t* __restrict__ sid, int gn,
                                                 const float4* __restrict__ part, float r2,
@@ -282,13 +289,14 @@ __device__ __forceinline__ void nb_append_round(int nstaged, const float4* __res
       const bool acc = v && sq < r2 && sq > 0.0f;
       const unsigned m = __ballot_sync(0xffffffffu, acc);
       const int k = base + __popc(m & lt);
-      if (acc && k < WF_NB) nb[nb_at(npad, ij, k)] = qid;
+      if (acc && k < WF_NB) nb[nb_at_i<I>((I)npad, (I)ij, k)] = qid;
       mine = lane == j ? m : mine;
     }
     count += __popc(mine);
   }
 }
 
+template <class I>
 __global__ void __launch_bounds__(32 * kNbWarps) k_nblist(int64_t ncell, int64_t npad,
                                                           const float4* __restrict__ pf, GridDev g,
                                                           const uint32_t* __restrict__ start,
@@ -353,7 +361,7 @@ __global__ void __launch_bounds__(32 * kNbWarps) k_nblist(int64_t ncell, int64_t
       for (uint32_t t0 = 0; t0 < nr; t0 += 32) {
         if (nstaged > kNbStage - 32) {          // staging full: test what is staged
           __syncwarp();
-          nb_append_round(nstaged, sp, sid, gn, s_part[w], r2, npad, nb, count);
+          nb_append_round<I>(nstaged, sp, sid, gn, s_part[w], r2, npad, nb, count);
           __syncwarp();
           nstaged = 0;
         }
@@ -380,7 +388,7 @@ __global__ void __launch_bounds__(32 * kNbWarps) k_nblist(int64_t ncell, int64_t
       }
     }
     __syncwarp();
-    nb_append_round(nstaged, sp, sid, gn, s_part[w], r2, npad, nb, count);
+    nb_append_round<I>(nstaged, sp, sid, gn, s_part[w], r2, npad, nb, count);
     __syncwarp();
     if (lane < gn) {
       if (count >= WF_NB) atomicOr(status, WF_STATUS_NB_CAP);
@@ -473,8 +481,12 @@ void launch_nblist(int64_t n, int64_t npad, const float4* pf, const GridDev& g,
                    int* status, cudaStream_t s) {
   (void)n;
   const int64_t ncell = (int64_t)g.dim[0] * g.dim[1] * g.dim[2];
-  k_nblist<<<nblocks(ncell, kNbWarps), 32 * kNbWarps, 0, s>>>(ncell, npad, pf, g, start, slot_of,
-                                                               nb, cnt, status);
+  if ((int64_t)WF_NB_ALLOC * npad < ((int64_t)1 << 31))
+    k_nblist<uint32_t><<<nblocks(ncell, kNbWarps), 32 * kNbWarps, 0, s>>>(
+        ncell, npad, pf, g, start, slot_of, nb, cnt, status);
+  else
+    k_nblist<int64_t><<<nblocks(ncell, kNbWarps), 32 * kNbWarps, 0, s>>>(
+        ncell, npad, pf, g, start, slot_of, nb, cnt, status);
 }
 void launch_gather_pf(int64_t n, const int32_t* s_src, const float4* pf, float4* pf2,
                       cudaStream_t s) {
