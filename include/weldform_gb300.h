@@ -126,8 +126,9 @@ int wf_add_trimesh(wf_domain* d, const double* nodes, int32_t nn, const int32_t*
                    int32_t ne, const double* normals, int32_t zone_id, int64_t first,
                    const double* vel, const double* angvel);
 
-/* Options with no reference field (precision, return map, rebuild cadence…).
- * Keys are listed in the library documentation; unknown keys fail. */
+/* Options with no reference field (precision, return map, rebuild cadence…):
+ * the keys, defaults and meanings are tabulated in INTEGRATION.md section 2;
+ * unknown keys fail with WF_ERR_ARG. */
 int wf_set_option(wf_domain* d, const char* key, double value);
 
 /* ---- solvers ------------------------------------------------------------ */
