@@ -126,9 +126,16 @@ int wf_add_trimesh(wf_domain* d, const double* nodes, int32_t nn, const int32_t*
                    int32_t ne, const double* normals, int32_t zone_id, int64_t first,
                    const double* vel, const double* angvel);
 
-/* Options with no reference field (precision, return map, rebuild cadence…):
- * the keys, defaults and meanings are tabulated in INTEGRATION.md section 2;
- * unknown keys fail with WF_ERR_ARG. */
+/* Options with no reference field; the defaults reproduce the reference and
+ * unknown keys fail with WF_ERR_ARG.  Keys (default):
+ *   precision (0 FP64, 1 mixed), return_map (0 radial, 1 Newton),
+ *   newton_rtol (1e-10), newton_max_iter (50), mlp (0), log_return_map (0),
+ *   rebuild_every (5), rebuild_after_yield (1), rebuild_current_positions (0),
+ *   rebuild_strain_increment (0), thermal (0), taylor_quinney (0),
+ *   clamp_homologous (1), energy_mode (0), contact_dx (0),
+ *   contact_stiffness (0.1), contact_vreg (1e-3), contact_heat_fraction (1),
+ *   fuse_heat (1), fuse_integrate (1), graph (1), output_interval (1e300),
+ *   resume (0), profile_kernel (0). */
 int wf_set_option(wf_domain* d, const char* key, double value);
 
 /* ---- solvers ------------------------------------------------------------ */
