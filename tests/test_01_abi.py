@@ -148,7 +148,8 @@ def test_nastran_reader_implicit_exponents_and_reference_parser(tmp_path):
     with contextlib.redirect_stdout(io.StringIO()):
         rn, rt = _read_nastran(rr, deck)
     assert np.array_equal(rn, nodes) and np.array_equal(rt, tris)
-    example = "/root/reference/examples/input/tool_metal_cut_mm.nas"
+    from oracle import build_ref
+    example = os.path.join(build_ref.reference_dir(), "examples", "input", "tool_metal_cut_mm.nas")
     if os.path.exists(example):
         a = _read_nastran(rd, example)
         b = _read_nastran(rr, example)
