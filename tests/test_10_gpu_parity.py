@@ -421,6 +421,22 @@ def test_mixed_fused_heat_matches_separate_heat_pass():
     assert Ts.max() > 20.5
 
 
+@pytest.mark.parametrize("graph", [1, 0])
+def test_timed_steps_with_per_launch_events(graph):
+    """wf_time_steps with a kernel's launches timed by CUDA events: inside
+    step graphs the events are event-record nodes, without graphs plain
+    records; both report the launches and their time."""
+    sc = S.compression_cylinder(material="jc", vz_top=-10.0)
+    d = gpu(sc, {"return_map": 1, "precision": 1, "graph": graph, "rebuild_after_yield": 0})
+    d.step(3)
+    d.set_option("profile_kernel", 2)        # the stress pass
+    elapsed, kms, kl, total = d.time_steps(12)
+    d.set_option("profile_kernel", 0)
+    assert kl == 12 and 0.0 < kms < elapsed
+    assert total >= 3 * 12
+    assert (d.get_scalar("graph_launches") > 0) == bool(graph)
+
+
 def test_setters_from_pinned_host_arrays_match_pageable():
     """The same scenario and checkpoint loaded from page-locked (pinned) and
     from pageable host arrays give identical fields, before and after steps
