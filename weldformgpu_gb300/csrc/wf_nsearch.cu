@@ -311,9 +311,13 @@ __global__ void __launch_bounds__(32 * kNbWarps) k_nblist(int64_t ncell, int64_t
   if (c >= ncell) return;                      // whole warps leave together
   const uint32_t ps = start[c], pe = start[c + 1];
   if (ps >= pe) return;
-  const int cx = (int)(c % g.dim[0]);
-  const int cy = (int)((c / g.dim[0]) % g.dim[1]);
-  const int cz = (int)(c / ((int64_t)g.dim[0] * g.dim[1]));
+  // cell coordinates in 32-bit arithmetic (the grid holds at most 2e9 cells;
+  // a 64-bit division is a long software sequence in this issue-bound kernel)
+  const uint32_t cu = (uint32_t)c, dx = (uint32_t)g.dim[0], dy = (uint32_t)g.dim[1];
+  const uint32_t cyz = cu / dx;
+  const int cx = (int)(cu - cyz * dx);
+  const int cy = (int)(cyz % dy);
+  const int cz = (int)(cyz / dy);
   // row r = 3 (dz + 1) + (dy + 1): slot range [rb, rb + rn) on lane r
   uint32_t rb = 0, rn = 0;
   if (lane < 9) {
