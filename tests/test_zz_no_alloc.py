@@ -114,3 +114,30 @@ def test_static_search_rejects_sizes_beyond_its_scratch():
     # a rejected call leaves the entry point usable
     _, small = _cases()
     assert_same(static_lists(small["x"], small["h"]), domain_lists(small["x"], small["h"]))
+
+
+def test_static_search_rejects_a_non_finite_position_in_any_block():
+    """A NaN or Inf in the caller's positions (an ordinary input, it cannot fault
+    the GPU) is rejected with WF_ERR_ARG on every call, wherever the particle
+    sits: the status word that records it is cleared before the launch that
+    checks the positions, not inside it."""
+    torch = _torch()
+    dev = torch.device("cuda:0")
+    big, small = _cases()
+    n = big["n"]
+    assert n > 5000
+    f = _entry()
+    err = C.create_string_buffer(256)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    cd = torch.zeros(n, dtype=torch.int32, device=dev)
+    ld = torch.zeros(n * NB, dtype=torch.int32, device=dev)
+    for k, (idx, bad) in enumerate([(5000, np.nan), (n - 1, np.inf), (5000, np.nan),
+                                    (17, -np.inf), (12345, np.nan)]):
+        x = np.array(big["x"], dtype=np.float64).reshape(-1, 3).copy()
+        x[idx, k % 3] = bad
+        xd = torch.from_numpy(x.reshape(-1)).to(dev)
+        rc = f(xd.data_ptr(), n, big["h"], cd.data_ptr(), ld.data_ptr(), stream, err, 256)
+        assert rc == -1, (idx, rc, err.value)
+        assert b"not finite" in err.value
+    # and a clean call right after gives the domain search's lists
+    assert_same(static_lists(small["x"], small["h"]), domain_lists(small["x"], small["h"]))

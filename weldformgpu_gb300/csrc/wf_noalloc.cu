@@ -61,16 +61,19 @@ __device__ __forceinline__ int static_cell(float p, float gmin, float gdelta) {
   return (int)floorf(__fmul_rn(__fsub_rn(p, gmin), gdelta));
 }
 
-// float positions from the caller's double3 array; thread 0 also resets the
-// grid bounds and the status word left by the previous call
+// resets the grid bounds and the status word left by the previous call; a
+// launch of its own, so that it is ordered (by the stream) before every block
+// of k_static_prep, whose blocks may flag a non-finite position in any order
+__global__ void k_static_clear(int* __restrict__ hdr) {
+  hdr[kHdrBounds + 0] = hdr[kHdrBounds + 1] = hdr[kHdrBounds + 2] = INT_MAX;
+  hdr[kHdrBounds + 3] = hdr[kHdrBounds + 4] = hdr[kHdrBounds + 5] = INT_MIN;
+  hdr[kHdrStatus] = 0;
+}
+
+// float positions from the caller's double3 array; flags non-finite ones
 __global__ void k_static_prep(int64_t n, const double* __restrict__ x, float4* __restrict__ pf,
                               int* __restrict__ hdr) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i == 0) {
-    hdr[kHdrBounds + 0] = hdr[kHdrBounds + 1] = hdr[kHdrBounds + 2] = INT_MAX;
-    hdr[kHdrBounds + 3] = hdr[kHdrBounds + 4] = hdr[kHdrBounds + 5] = INT_MIN;
-    hdr[kHdrStatus] = 0;
-  }
   if (i >= n) return;
   const double x0 = x[3 * i], x1 = x[3 * i + 1], x2 = x[3 * i + 2];
   if (!isfinite(x0) || !isfinite(x1) || !isfinite(x2)) atomicOr(hdr + kHdrStatus, WF_STATUS_GRID);
@@ -248,6 +251,7 @@ extern "C" int wf_find_neighbors_static(const double* x, int64_t n, double h, in
   // grid bounds (cuNSearch kComputeMinMax, cuNSearchKernels.cu:41-71), read
   // back to size the cell arrays as computeCellInformation does
   const float r = (float)(2.0 * h);
+  k_static_clear<<<1, 1, 0, s>>>(hdr);
   k_static_prep<<<blocks_for(n, 256), 256, 0, s>>>(n, x, pf, hdr);
   launch_minmax(n, pf, r, hdr + kHdrBounds, s);
   int head[kHdrStatus + 1];
