@@ -81,6 +81,8 @@ int wf_set_free(wf_domain* d, const uint8_t* is_free);   /* SetFreePart :307 */
 int wf_set_id(wf_domain* d, const int32_t* id);          /* SetID       :317 */
 
 /* ---- public fields the reference's main writes directly --------------- */
+/* rejects non-finite positions (WF_ERR_ARG, nothing written); after a solve
+ * has started, the next step rebuilds the lists for the new positions */
 int wf_set_positions(wf_domain* d, const double* x);     /* cudaMemcpy x, WeldFormGPU.cu:704 */
 int wf_set_velocities(wf_domain* d, const double* v);    /* cudaMemcpy v, WeldFormGPU.cu:711 */
 int wf_set_mass(wf_domain* d, const double* m);          /* cudaMemcpy m, WeldFormGPU.cu:822 */
@@ -91,6 +93,10 @@ int wf_set_artificial_viscosity(wf_domain* d, double alpha, double beta); /* Alp
 int wf_set_material(wf_domain* d, const wf_material* mat);    /* materials[0], WeldFormGPU.cu:749-800 */
 int wf_add_velocity_bc(wf_domain* d, int32_t zone_id,
                        double vx, double vy, double vz);  /* bConds, WeldFormGPU.cu:457-485 */
+/* Changes the velocity of BC number `index` (0-based, in wf_add_velocity_bc
+ * order), e.g. from a callback between steps: the reference's UserAcc
+ * (src/WeldFormGPU.cu:78-140) writes bConds[bc].value each step. */
+int wf_set_velocity_bc(wf_domain* d, int32_t index, double vx, double vy, double vz);
 int wf_set_temperature(wf_domain* d, const double* T);   /* T (Domain_d::CopyData, Domain_d.cu:490) */
 int wf_set_thermal_bc(wf_domain* d, const int32_t* bc_t); /* BC_T: 0 none, 1 convection */
 int wf_set_convection(wf_domain* d, double h_conv, double T_inf); /* h_conv_double, T_inf */
@@ -129,7 +135,13 @@ int wf_add_trimesh(wf_domain* d, const double* nodes, int32_t nn, const int32_t*
 /* Options with no reference field; the defaults reproduce the reference and
  * unknown keys fail with WF_ERR_ARG.  Keys (default):
  *   precision (0 FP64, 1 mixed), return_map (0 radial, 1 Newton),
- *   newton_rtol (1e-10), newton_max_iter (50), mlp (0), log_return_map (0),
+ *   newton_rtol (1e-10), newton_max_iter (50, >= 1; a return map that stops
+ *   there unconverged is counted ("newton_capped") and the call returns
+ *   WF_ERR_NUMERIC, the state advanced with the unconverged increments),
+ *   mlp (0), log_return_map (0),
+ *   output_every_step (0: output rows at output times only), print_outputs
+ *   (0: 1 prints MechFraserSolve's lines at output times), output_series_cap
+ *   (65536 rows),
  *   rebuild_every (5), rebuild_after_yield (1), rebuild_current_positions (0),
  *   rebuild_strain_increment (0), thermal (0), taylor_quinney (0),
  *   clamp_homologous (1), energy_mode (0), contact_dx (0),
@@ -137,6 +149,18 @@ int wf_add_trimesh(wf_domain* d, const double* nodes, int32_t nn, const int32_t*
  *   fuse_heat (1), fuse_integrate (1), graph (1), output_interval (1e300),
  *   resume (0), profile_kernel (0). */
 int wf_set_option(wf_domain* d, const char* key, double value);
+
+/* The per-step BC hook: Domain_d::GeneralAfter (src/cuda/Domain_d.cuh:402,
+ * set to UserAcc at src/WeldFormGPU.cu:688).  `fn` runs on the calling host
+ * thread after every step of a solve (wf_mech_fraser_solve, wf_step,
+ * wf_time_steps), when the step's device work is ordered before any later
+ * call on the handle; d->time is then the time of the next step.  It may call
+ * the getters and setters of this handle (wf_get_field, wf_set_velocity_bc,
+ * wf_set_field, ...) but not its solvers.  A non-zero return ends the solve
+ * with WF_ERR_STATE.  While a callback is set the steps are launched one by
+ * one (no step graphs).  fn = NULL removes it. */
+typedef int (*wf_after_fn)(wf_domain* d, void* user);
+int wf_set_callback(wf_domain* d, wf_after_fn fn, void* user);
 
 /* ---- solvers ------------------------------------------------------------ */
 /* Domain_d::MechFraserSolve (src/cuda/SolverFraser.cu:30-409). */
@@ -191,13 +215,46 @@ int wf_get_field_i32(wf_domain* d, const char* name, int32_t* out);
 int wf_get_neighbors(wf_domain* d, int32_t* counts, int32_t* lists);
 /* "time", "step", "is_yielding", "isfirst", "launches", "rebuilds" (neighbour
  * rebuilds inside the step loop), "newton_iters", "newton_calls", "mlp_used",
- * "status", "int_energy_sum", "contact_tests32" / "contact_tests64" (contact
+ * "newton_capped" (return maps that stopped at newton_max_iter), "status",
+ * "int_energy_sum", "contact_tests32" / "contact_tests64" (contact
  * law 1: triangle tests in the FP32 search and the FP64 decision, since
- * creation). */
+ * creation); from the last output row: "max_disp_x|y|z", "max_pl_strain",
+ * "cont_force_sum", "cont_force_x|y|z", "int_energy_total",
+ * "reaction_x|y|z" (BC 0). */
 int wf_get_scalar(wf_domain* d, const char* name, double* out);
+
+/* ---- output reductions ------------------------------------------------------
+ * MechFraserSolve reduces the state on the host at every output time
+ * (src/cuda/SolverFraser.cu:350-388: max displacement, max plastic strain,
+ * the contact force sum over free-surface particles).  Here the same values
+ * and the load each velocity BC carries are reduced on the device in FP64, in
+ * an order fixed by the particle count alone (original ids, fixed blocks),
+ * into one row per output time (every step with option output_every_step):
+ *   [0] time, [1] step, [2..4] max u_x, u_y, u_z (from 0, as the reference),
+ *   [5] max pl_strain, [6] sum of |contforce| over ID == 1 particles,
+ *   [7..9] contact force vector sum, [10] internal energy sum,
+ *   [11 + 3b .. 13 + 3b] BC b's reaction: the sum over its zone of m a
+ *   before the BC zeroes a (the force the rest of the body puts on the zone;
+ *   the platen supplies its negative).
+ * Rows of a solve are kept in order (up to output_series_cap, later rows are
+ * dropped and status bit 32 set); a solve that does not resume starts a new
+ * series.  With CSV output on (wf_set_csv_output), MechFraserSolve writes
+ * the series to <prefix>outputs.csv at its end. */
+#define WF_ROW_FIXED_COLUMNS 11
+/* the last row recorded (cap values at most); *width = row width.  WF_ERR_STATE
+ * before the first row. */
+int wf_get_output_row(wf_domain* d, double* row, int64_t cap, int64_t* width);
+/* up to cap_rows rows of the series, row-major; *n_rows = rows copied (with
+ * cap_rows = 0: rows stored) */
+int wf_get_output_series(wf_domain* d, double* rows, int64_t cap_rows, int64_t* n_rows,
+                         int64_t* width);
+/* BC `bc_index`'s reaction (3 doubles) from the last row */
+int wf_get_reaction(wf_domain* d, int32_t bc_index, double* force);
 /* Checkpoint / restart (no reference counterpart: the reference's CSV
  * snapshots are not restartable).  wf_set_field writes a state field in the
- * caller's order (names as wf_get_field); wf_set_scalar sets "time",
+ * caller's order (names as wf_get_field; "x" goes through wf_set_positions,
+ * which rejects non-finite values, and after the first solve step makes the
+ * next step rebuild the neighbour lists); wf_set_scalar sets "time",
  * "step", "isfirst" or "is_yielding"; with wf_set_option("resume", 1) the
  * next solve keeps time and velocities instead of restarting from rest. */
 int wf_set_field(wf_domain* d, const char* name, const double* in);

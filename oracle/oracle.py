@@ -180,6 +180,21 @@ class OracleDomain:
     def run_stage(self, name):
         self._ck(self.L.wfo_run_stage(self.h, name.encode()), "run_stage " + name)
 
+    def set_velocity_bc(self, index, vx, vy, vz):
+        self._ck(self.L.wfo_set_velocity_bc(self.h, int(index), float(vx), float(vy), float(vz)),
+                 "set_velocity_bc")
+
+    def get_output_series(self):
+        """Output rows (time, step, maxima, contact sums, energy, BC reactions)."""
+        n, w = C.c_int64(), C.c_int64()
+        self._ck(self.L.wfo_get_output_series(self.h, None, 0, C.byref(n), C.byref(w)),
+                 "get_output_series")
+        rows = np.empty((n.value, w.value), dtype=np.float64)
+        if n.value:
+            self._ck(self.L.wfo_get_output_series(self.h, _p(rows), n.value, C.byref(n),
+                                                  C.byref(w)), "get_output_series")
+        return rows
+
 
 # ---- generators -----------------------------------------------------------
 def gen_cylinder_ref(start, R, L, r, density):

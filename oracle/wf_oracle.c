@@ -96,7 +96,13 @@ struct wfo_domain {
   /* solver state */
   int started, ts_i, is_yielding, isfirst_step, nb_built;
   double time, t_out, dt_out, max_pl_strain, int_energy_sum;
-  int64_t step, newton_calls, newton_iters, mlp_used, rebuilds;
+  int64_t step, newton_calls, newton_iters, mlp_used, rebuilds, newton_capped;
+  /* output rows (no reference counterpart beyond the values SolverFraser.cu:350-388
+   * prints): recorded at output times, or every step with output_every_step */
+  int out_every_step;
+  d3* fr;                          /* m a before the BCs, BC-zone particles, on row steps */
+  double* series;                  /* rows of 11 + 3 nbc values */
+  int64_t series_n, series_cap, series_alloc;
   char err[256];
 };
 
@@ -531,8 +537,8 @@ static double newton_return(const wfo_domain* d, const hard_t* hc, double st, do
  * the reference, or the consistent Newton return map (option return_map=1). */
 static void stage_stress(wfo_domain* d) {
   const wf_material* mt = &d->mat;
-  int64_t calls = 0, iters = 0, used = 0;
-#pragma omp parallel for schedule(static) reduction(+ : calls, iters, used)
+  int64_t calls = 0, iters = 0, used = 0, capped = 0;
+#pragma omp parallel for schedule(static) reduction(+ : calls, iters, used, capped)
   for (int64_t i = 0; i < d->n_solid; i++) {
     t3 S = t3_from_sym(d->shearstress + 6 * i);
     t3 D = t3_from_sym(d->strrate + 6 * i);
@@ -602,6 +608,7 @@ static void stage_stress(wfo_domain* d) {
         int it = 0;
         dep = newton_return(d, &hc, st, G3, d->pl_strain[i], sy0, dl0, &it);
         calls++; iters += it;
+        if (it >= d->newton_max_iter) capped++;   /* stopped before the tolerance */
         double sy1, dsy1;
         hard_eval(&hc, d->pl_strain[i], dep, &sy1, &dsy1);
         S = t3_scale(S, sy1 / st);
@@ -622,6 +629,7 @@ static void stage_stress(wfo_domain* d) {
   d->newton_calls += calls;
   d->newton_iters += iters;
   d->mlp_used += used;
+  d->newton_capped += capped;
 }
 
 /* Domain_d::CalcAccel (InteractionAlt.cu:18-150), KernelType 0, XSPH 0 */
@@ -1026,8 +1034,50 @@ static int solve_begin(wfo_domain* d, double dt_out) {
   d->ts_i = 0;
   d->is_yielding = 0;
   d->max_pl_strain = 0.0;
+  d->series_n = 0;
   d->started = 1;
   return WF_OK;
+}
+
+/* One output row, FP64, particles in index order (SolverFraser.cu:350-388:
+ * max displacement from 0, max plastic strain, the sum of |contforce| over
+ * free-surface particles), plus the contact force vector sum, the internal
+ * energy sum and each BC zone's load. */
+static void record_row(wfo_domain* d) {
+  const int64_t w = 11 + 3 * (int64_t)d->nbc;
+  if (d->series_n >= d->series_cap) return;
+  if (d->series_n >= d->series_alloc) {
+    int64_t na = d->series_alloc ? 2 * d->series_alloc : 256;
+    if (na > d->series_cap) na = d->series_cap;
+    d->series = (double*)realloc(d->series, sizeof(double) * (size_t)(na * w));
+    d->series_alloc = na;
+  }
+  double* r = d->series + d->series_n * w;
+  memset(r, 0, sizeof(double) * (size_t)w);
+  r[0] = d->time;
+  r[1] = (double)(d->step + 1);
+  for (int64_t i = 0; i < d->n; i++) {
+    if (d->u[i].x > r[2]) r[2] = d->u[i].x;
+    if (d->u[i].y > r[3]) r[3] = d->u[i].y;
+    if (d->u[i].z > r[4]) r[4] = d->u[i].z;
+    if (d->pl_strain[i] > r[5]) r[5] = d->pl_strain[i];
+    if (d->contact) {
+      const d3 f = d->contforce[i];
+      if (d->ID[i] == d->id_free_surf) r[6] += sqrt(f.x * f.x + f.y * f.y + f.z * f.z);
+      r[7] += f.x;
+      r[8] += f.y;
+      r[9] += f.z;
+    }
+    r[10] += d->int_energy[i];
+  }
+  for (int b = 0; b < d->nbc; b++)
+    for (int64_t i = 0; i < d->n; i++)
+      if (d->ID[i] == d->bc_zone[b]) {
+        r[11 + 3 * b] += d->fr[i].x;
+        r[12 + 3 * b] += d->fr[i].y;
+        r[13 + 3 * b] += d->fr[i].z;
+      }
+  d->series_n++;
 }
 
 static int solve_step(wfo_domain* d) {
@@ -1064,6 +1114,11 @@ static int solve_step(wfo_domain* d) {
       if (d->pl_strain[i] > d->max_pl_strain) d->max_pl_strain = d->pl_strain[i];
     if (d->max_pl_strain > MIN_PS_FOR_NBSEARCH) d->is_yielding = 1;
   }
+  const int row_due = d->out_every_step || d->time + d->dt >= d->t_out;
+  if (row_due)              /* the load each BC zone carries: m a before the BC zeroes a */
+    for (int64_t i = 0; i < d->n; i++)
+      for (int b = 0; b < d->nbc; b++)
+        if (d->ID[i] == d->bc_zone[b]) d->fr[i] = d3_scale(d->a[i], d->m[i]);
   stage_bc(d);              /* :273 */
   stage_update_pos(d);      /* :275 */
   stage_update_vel(d);      /* :278 */
@@ -1079,6 +1134,7 @@ static int solve_step(wfo_domain* d) {
   }
   d->isfirst_step = 0;      /* :320 */
   d->time += d->dt;
+  if (row_due) record_row(d);                          /* :350-388 */
   if (d->time >= d->t_out) {                           /* :323-368 */
     memcpy(d->x_h, d->x, sizeof(d3) * d->n);
     d->t_out += d->dt_out;
@@ -1183,8 +1239,9 @@ int wfo_create(wfo_domain** out, int64_t n) {
   A(dep, n); A(ID, n); A(is_free, n); A(not_write, n);
   A(T, n); A(Ta, n); A(Tb, n); A(dTdt, n); A(k_T, n); A(cp_T, n); A(BC_T, n);
   A(nb_count, n); A(nb, (size_t)n * NBMAX);
-  A(cont_cnt, n); A(cont_nb, (size_t)n * CONT_MAX_NB); A(qf, n); A(eps_rb, n);
+  A(cont_cnt, n); A(cont_nb, (size_t)n * CONT_MAX_NB); A(qf, n); A(eps_rb, n); A(fr, n);
 #undef A
+  d->series_cap = 65536;
   d->id_free_surf = 1;
   d->c_kappa = 0.1;
   d->c_vreg = 1.0e-3;
@@ -1216,7 +1273,7 @@ int wfo_destroy(wfo_domain* d) {
                   d->shearstress, d->strain, d->sigma_eq, d->pl_strain, d->sigma_y,
                   d->eff_strain_rate, d->int_energy, d->dep, d->ID, d->is_free, d->not_write,
                   d->T, d->Ta, d->Tb, d->dTdt, d->k_T, d->cp_T, d->BC_T, d->nb_count, d->nb,
-                  d->cont_cnt, d->cont_nb, d->qf, d->eps_rb};
+                  d->cont_cnt, d->cont_nb, d->qf, d->eps_rb, d->fr, d->series};
   for (size_t k = 0; k < sizeof ptrs / sizeof ptrs[0]; k++) free(ptrs[k]);
   for (int mi = 0; mi < d->trimesh_count; mi++) {
     free(d->mesh[mi].node); free(d->mesh[mi].node_v); free(d->mesh[mi].centroid);
@@ -1296,6 +1353,21 @@ int wfo_set_material(wfo_domain* d, const wf_material* mt) {
   d->has_mat = 1;
   return WF_OK;
 }
+int wfo_set_velocity_bc(wfo_domain* d, int32_t index, double vx, double vy, double vz) {
+  if (!d || index < 0 || index >= d->nbc) return WF_ERR_ARG;
+  d->bc_v[index] = v3(vx, vy, vz);
+  return WF_OK;
+}
+int wfo_get_output_series(wfo_domain* d, double* rows, int64_t cap_rows, int64_t* n_rows,
+                          int64_t* width) {
+  if (!d || !n_rows || (cap_rows > 0 && !rows)) return WF_ERR_ARG;
+  const int64_t w = 11 + 3 * (int64_t)d->nbc;
+  if (width) *width = w;
+  const int64_t m = d->series_n < cap_rows ? d->series_n : cap_rows;
+  if (m > 0) memcpy(rows, d->series, sizeof(double) * (size_t)(m * w));
+  *n_rows = cap_rows > 0 ? m : d->series_n;
+  return WF_OK;
+}
 int wfo_add_velocity_bc(wfo_domain* d, int32_t zone, double vx, double vy, double vz) {
   if (!d) return WF_ERR_ARG;
   if (d->nbc >= WFO_MAX_BC) return fail(d, WF_ERR_ARG, "too many boundary conditions");
@@ -1330,7 +1402,15 @@ int wfo_set_option(wfo_domain* d, const char* key, double v) {
   else if (!strcmp(key, "return_map")) d->return_map = (int)v;
   else if (!strcmp(key, "energy_mode")) d->energy_mode = (int)v;
   else if (!strcmp(key, "newton_rtol")) d->newton_rtol = v;
-  else if (!strcmp(key, "newton_max_iter")) d->newton_max_iter = (int)v;
+  else if (!strcmp(key, "newton_max_iter")) {
+    if (!(v >= 1.0)) return fail(d, WF_ERR_ARG, "newton_max_iter must be >= 1");
+    d->newton_max_iter = (int)v;
+  }
+  else if (!strcmp(key, "output_every_step")) d->out_every_step = v != 0;
+  else if (!strcmp(key, "output_series_cap")) {
+    if (!(v >= 1.0)) return fail(d, WF_ERR_ARG, "output_series_cap must be >= 1");
+    d->series_cap = (int64_t)v;
+  }
   else if (!strcmp(key, "taylor_quinney")) d->chi = v;
   else if (!strcmp(key, "output_interval")) d->output_interval = v;
   else if (!strcmp(key, "clamp_homologous")) d->clamp_homologous = v != 0.0;
@@ -1542,6 +1622,7 @@ int wfo_get_scalar(wfo_domain* d, const char* name, double* out) {
   else if (!strcmp(name, "newton_iters")) *out = (double)d->newton_iters;
   else if (!strcmp(name, "mlp_used")) *out = (double)d->mlp_used;
   else if (!strcmp(name, "rebuilds")) *out = (double)d->rebuilds;
+  else if (!strcmp(name, "newton_capped")) *out = (double)d->newton_capped;
   else if (!strcmp(name, "totmass")) *out = d->totmass;
   else return fail(d, WF_ERR_ARG, "unknown scalar");
   return WF_OK;

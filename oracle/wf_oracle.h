@@ -50,6 +50,10 @@ int wfo_set_time_step(wfo_domain* d, double dt);
 int wfo_set_artificial_viscosity(wfo_domain* d, double alpha, double beta);
 int wfo_set_material(wfo_domain* d, const wf_material* mat);
 int wfo_add_velocity_bc(wfo_domain* d, int32_t zone_id, double vx, double vy, double vz);
+int wfo_set_velocity_bc(wfo_domain* d, int32_t index, double vx, double vy, double vz);
+/* output rows (same layout as wf_get_output_series), FP64 sums in index order */
+int wfo_get_output_series(wfo_domain* d, double* rows, int64_t cap_rows, int64_t* n_rows,
+                          int64_t* width);
 int wfo_set_temperature(wfo_domain* d, const double* T);
 int wfo_set_thermal_bc(wfo_domain* d, const int32_t* bc_t);
 int wfo_set_convection(wfo_domain* d, double h_conv, double T_inf);

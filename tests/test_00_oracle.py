@@ -86,7 +86,7 @@ def test_generators_match_between_oracle_and_library():
     l1 = P.gen_cylinder_lattice(0.005, 0.010, 0.0005, 0.01, 1)
     l2 = O.gen_cylinder_lattice(0.005, 0.010, 0.0005, 0.01, 1)
     assert np.array_equal(l1, l2)
-    assert 6000 < len(l1) < 6600                # BASELINE config 1: ~6.3k particles
+    assert 6000 < len(l1) < 6600                # R 5 mm, H 10 mm lattice: ~6.3k particles
     ids1 = np.zeros(len(l1), np.int32)
     ids2 = np.zeros(len(l1), np.int32)
     nw1 = np.zeros(len(l1), np.uint8)
@@ -457,3 +457,36 @@ def test_oracle_matches_reference_live_config1_neighbors_and_steps():
     d2.step(50)
     for f in ("x", "v", "sigma", "rho", "int_energy"):
         assert np.array_equal(R.get(f), d2.get_field(f)), f
+
+
+def test_oracle_output_rows_are_the_reductions_of_its_fields():
+    """The oracle's output rows (every step) are the plain reductions of its
+    own fields: maxima of u and pl_strain from 0, the energy sum, and each BC
+    zone's load m a before the BC; the platen load of a compression run is
+    compressive on the body (the top zone is pushed up: +z on the body's zone
+    particles) and grows with the plastic strain."""
+    sc = S.compression_cylinder(R=0.003, H=0.006)
+    d = _oracle(sc, {"output_every_step": 1})
+    d.step(60)
+    rows = d.get_output_series()
+    assert rows.shape == (60, 11 + 6)
+    assert np.array_equal(rows[:, 1], np.arange(1, 61))
+    u, ps, e = d.get_field("u"), d.get_field("pl_strain"), d.get_field("int_energy")
+    last = rows[-1]
+    assert last[2] == max(0.0, u[:, 0].max()) and last[4] == max(0.0, u[:, 2].max())
+    assert last[5] == max(0.0, ps.max())
+    assert abs(last[10] - e.sum()) <= 1e-12 * np.abs(e).sum()
+    assert np.all(rows[:, 6:10] == 0.0)                 # no contact
+    fz_top = rows[:, 11 + 3 + 2]
+    assert fz_top[-1] > 0.0 and fz_top[-1] > fz_top[5]
+
+
+def test_oracle_newton_cap_counted():
+    sc = S.compression_cylinder(R=0.003, H=0.006, material="jc", vz_top=-10.0)
+    d = _oracle(sc, {"return_map": 1, "newton_max_iter": 1})
+    d.step(200)
+    assert d.get_scalar("newton_calls") > 0
+    assert d.get_scalar("newton_capped") == d.get_scalar("newton_calls")
+    ok = _oracle(sc, {"return_map": 1})
+    ok.step(200)
+    assert ok.get_scalar("newton_capped") == 0

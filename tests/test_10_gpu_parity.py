@@ -126,7 +126,7 @@ def test_fp64_fraser_loop_bit_exact_vs_reference_golden(case, checkpoints):
 
 
 def test_fp64_config1_lattice_vs_oracle_with_rebuilds():
-    """BASELINE config 1 (jittered lattice, 0.4h/c, rebuild every 10 steps) for 400 steps."""
+    """R 5 mm, H 10 mm jittered lattice, dt 0.4h/c, rebuild every 10 steps, for 400 steps."""
     sc = S.compression_cylinder(R=0.005, H=0.010, generator="lattice", dt_rule="baseline")
     opts = {"rebuild_every": 10, "rebuild_current_positions": 1, "rebuild_after_yield": 0}
     g = gpu(sc, opts)

@@ -83,6 +83,8 @@ SIGNATURES = {
     "set_artificial_viscosity": (C.c_int, [_vp, _d, _d]),
     "set_material": (C.c_int, [_vp, C.POINTER(WfMaterial)]),
     "add_velocity_bc": (C.c_int, [_vp, _i32, _d, _d, _d]),
+    "set_velocity_bc": (C.c_int, [_vp, _i32, _d, _d, _d]),
+    "get_output_series": (C.c_int, [_vp, _pd, _i64, C.POINTER(_i64), C.POINTER(_i64)]),
     "set_temperature": (C.c_int, [_vp, _pd]),
     "set_thermal_bc": (C.c_int, [_vp, _pi32]),
     "set_convection": (C.c_int, [_vp, _d, _d]),
@@ -110,9 +112,21 @@ PRODUCT_ONLY = {
     "version": (C.c_char_p, []),
     "mech_solve": (C.c_int, [_vp, _d, _d]),
     "write_csv": (C.c_int, [_vp, _cs]),
+    "set_csv_output": (C.c_int, [_vp, _cs]),
     "set_scalar": (C.c_int, [_vp, _cs, _d]),
     "time_steps": (C.c_int, [_vp, _i64, _pd, _pd, C.POINTER(_i64), C.POINTER(_i64)]),
+    "get_output_row": (C.c_int, [_vp, _pd, _i64, C.POINTER(_i64)]),
+    "get_reaction": (C.c_int, [_vp, _i32, _pd]),
+    "set_callback": (C.c_int, [_vp, _vp, _vp]),
 }
+
+# int (*wf_after_fn)(wf_domain*, void*): the per-step host hook
+AFTER_FN = C.CFUNCTYPE(C.c_int, _vp, _vp)
+
+# columns of an output row before the per-BC reactions (WF_ROW_FIXED_COLUMNS)
+ROW_FIXED = 11
+ROW_COLUMNS = ("time", "step", "max_ux", "max_uy", "max_uz", "max_pl_strain", "cont_force_sum",
+               "cont_fx", "cont_fy", "cont_fz", "int_energy")
 
 FIELD_COMPONENTS = {
     "x": 3, "v": 3, "a": 3, "u": 3, "normal": 3, "contforce": 3,

@@ -21,9 +21,10 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
           "--expt-relaxed-constexpr"]
 # units whose FP64 arithmetic must round like the reference / the CPU oracle
-NO_FMA = {"wf_step_fp64.cu", "wf_integrate.cu", "wf_contact.cu"}
+NO_FMA = {"wf_step_fp64.cu", "wf_integrate.cu", "wf_contact.cu", "wf_outputs.cu"}
 SOURCES = ["wf_api.cu", "wf_nsearch.cu", "wf_step_fp64.cu", "wf_step_fp32.cu", "wf_integrate.cu",
-           "wf_mlp.cu", "wf_setup.cpp", "wf_noalloc.cu", "wf_contact.cu", "wf_json.cpp"]
+           "wf_mlp.cu", "wf_setup.cpp", "wf_noalloc.cu", "wf_contact.cu", "wf_json.cpp",
+           "wf_outputs.cu"]
 
 
 def nvcc():

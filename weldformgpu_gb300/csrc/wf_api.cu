@@ -24,6 +24,11 @@
 // wf_mlp.cu
 int wf_mlp_pack_device(const float* dparams, void* dpacked, cudaStream_t s);
 size_t wf_mlp_packed_bytes();
+// wf_outputs.cu
+int wf_out_partial_words(int nbc);
+void launch_output_row(const StepParams& P, const Fields& F, double* part, double time,
+                       double step, double* last, double* series, int64_t cap,
+                       unsigned long long* count, int append, int* status, cudaStream_t s);
 
 #define WF_VERSION "weldform-gb300 0.1 (sm_103a)"
 
@@ -71,8 +76,22 @@ struct wf_domain {
   int64_t cell_cap = 0, scan_cap = 0;
   int32_t *s_src = nullptr, *s_orig = nullptr;
   int* d_mm = nullptr;
-  int* d_status = nullptr;     // [0] bits, [1] yield flag, [2..3] newton iters, [4..5] calls
+  int* d_status = nullptr;     // WF_STATUS_WORDS words (wf_common.cuh)
   int* h_status = nullptr;     // pinned mirror
+  // FP64 output rows (wf_outputs.cu): recorded at output times, or every step
+  // with option output_every_step; the series holds up to series_cap rows
+  double4* fr = nullptr;       // m a before the BCs at BC-zone slots (written on row steps)
+  double* out_part = nullptr;  // per-block partials of the row reduction
+  double* out_last = nullptr;  // the last row recorded
+  double* series = nullptr;
+  int64_t series_cap = 65536, series_width = 0;
+  unsigned long long* series_count = nullptr;
+  bool out_every_step = false, row_recorded = false, print_outputs = false;
+  bool lists_stale = false;    // positions replaced mid-run: rebuild at the next step
+  // the per-step host hook (GeneralAfter)
+  wf_after_fn after_fn = nullptr;
+  void* after_user = nullptr;
+  bool in_callback = false;
   unsigned long long* d_cstat = nullptr;   // contact law 1 triangle-test counters
   double* d_stage = nullptr;   // staging for ABI copies (6 doubles per particle)
   // solver state
@@ -319,7 +338,10 @@ static void layout_arena(wf_domain* d, Arena& A) {
   A.take(&d->vd2, n); A.take(&d->v32b, n); A.take(&d->a32, n); A.take(&d->sigr32, 8 * n);
   A.take(&d->nb, (int64_t)WF_NB_ALLOC * n); A.take(&d->nbc, n); A.take(&d->inv, n);
   A.take(&d->pf, n); A.take(&d->pf2, n); A.take(&d->cellid, n); A.take(&d->s_src, n);
-  A.take(&d->s_orig, n); A.take(&d->d_mm, 8); A.take(&d->d_status, 8); A.take(&d->d_cstat, 2);
+  A.take(&d->s_orig, n); A.take(&d->d_mm, 8); A.take(&d->d_status, WF_STATUS_WORDS);
+  A.take(&d->d_cstat, 2);
+  A.take(&d->fr, n); A.take(&d->out_part, wf_out_partial_words(WF_MAX_BC));
+  A.take(&d->out_last, WF_ROW_FIXED + 3 * WF_MAX_BC); A.take(&d->series_count, 1);
   A.take(&d->d_stage, 6 * n); A.take(&d->mlp_w, WF_MLP_NPARAM);
   A.take(&d->mlp_packed, (int64_t)wf_mlp_packed_bytes());
 }
@@ -448,7 +470,7 @@ static StepParams make_params(const wf_domain* d) {
 // kept and updated in place when the next segment has the same launches.
 // Not used with the adaptive rebuild or CSV snapshots (host reads every step).
 static int segment_begin(wf_domain* d) {
-  if (!d->graph || d->capturing || d->rb_dep > 0.0 || d->csv_on) return WF_OK;
+  if (!d->graph || d->capturing || d->rb_dep > 0.0 || d->csv_on || d->after_fn) return WF_OK;
   WF_CUDA_OK(cudaStreamBeginCapture(d->stream, cudaStreamCaptureModeRelaxed));
   d->capturing = true;
   return WF_OK;
@@ -757,8 +779,8 @@ static int read_status(wf_domain* d) {
     const int rc = segment_end(d);
     if (rc) return rc;
   }
-  WF_CUDA_OK(cudaMemcpyAsync(d->h_status, d->d_status, 8 * sizeof(int), cudaMemcpyDeviceToHost,
-                             d->stream));
+  WF_CUDA_OK(cudaMemcpyAsync(d->h_status, d->d_status, WF_STATUS_WORDS * sizeof(int),
+                             cudaMemcpyDeviceToHost, d->stream));
   WF_CUDA_OK(cudaStreamSynchronize(d->stream));
   return WF_OK;
 }
@@ -771,6 +793,30 @@ static int write_snapshot(wf_domain* d) {
   char name[64];
   snprintf(name, sizeof name, "out_%.6f.csv", d->time);
   return wf_write_csv(d, (d->csv_prefix + name).c_str());
+}
+
+static int write_series_csv(wf_domain* d, const char* path);
+
+// MechFraserSolve's lines at an output time (SolverFraser.cu:369-388), from
+// the device-reduced row, plus each BC zone's force
+static int print_output_row(wf_domain* d) {
+  const int rc = segment_end(d);
+  if (rc) return rc;
+  const int nbc = (int)d->bc_zone.size();
+  std::vector<double> r(WF_ROW_FIXED + 3 * nbc);
+  WF_CUDA_OK(cudaMemcpyAsync(r.data(), d->out_last, sizeof(double) * r.size(),
+                             cudaMemcpyDeviceToHost, d->stream));
+  WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+  printf("-------------------------\nTime %g\n", r[0]);
+  printf("Current step: %lld, time: %g\n", (long long)r[1], d->dt);
+  printf("Max disp: %g, %g, %g\n", r[2], r[3], r[4]);
+  printf("Max pl_strain: %g\n", r[5]);
+  if (!d->meshes.empty()) printf("Contact Force Sum: %g\n", r[6]);
+  for (int b = 0; b < nbc; b++)
+    printf("BC %d (zone %d) force: %g, %g, %g\n", b, d->bc_zone[b], r[WF_ROW_FIXED + 3 * b],
+           r[WF_ROW_FIXED + 3 * b + 1], r[WF_ROW_FIXED + 3 * b + 2]);
+  fflush(stdout);
+  return WF_OK;
 }
 
 static int solve_begin(wf_domain* d, double dt_out) {
@@ -786,7 +832,24 @@ static int solve_begin(wf_domain* d, double dt_out) {
   d->dt_out = dt_out;
   d->ts_i = 0;
   d->is_yielding = false;
-  WF_CUDA_OK(cudaMemsetAsync(d->d_status, 0, 8 * sizeof(int), d->stream));
+  {
+    const int64_t width = WF_ROW_FIXED + 3 * (int64_t)d->bc_zone.size();
+    if (!d->series || width != d->series_width) {
+      if (d->series) cudaFree(d->series);
+      d->series = nullptr;
+      if (dalloc(&d->series, d->series_cap * width, d->stream) != cudaSuccess) {
+        d->series = nullptr;
+        return wf_fail(d, WF_ERR_ALLOC, "output series");
+      }
+      d->series_width = width;
+      WF_CUDA_OK(cudaMemsetAsync(d->series_count, 0, sizeof(unsigned long long), d->stream));
+    }
+    if (!resume) {
+      WF_CUDA_OK(cudaMemsetAsync(d->series_count, 0, sizeof(unsigned long long), d->stream));
+      d->row_recorded = false;
+    }
+  }
+  WF_CUDA_OK(cudaMemsetAsync(d->d_status, 0, WF_STATUS_WORDS * sizeof(int), d->stream));
   launch_snapshot(d->n, d->F[d->cur], d->stream);               // x_h = x, :56
   rc = rebuild(d, false);                                       // :109
   if (rc) return rc;
@@ -833,7 +896,15 @@ static int solve_step_launches(wf_domain* d) {
   } else {
     rb = d->ts_i == 0 && (d->is_yielding || !d->rebuild_after_yield);   // :166-182
   }
-  if (rb) {
+  if (d->lists_stale) {
+    // positions were replaced after the solve started (wf_set_positions or a
+    // checkpoint restore): new lists for them before this step
+    launch_snapshot(d->n, d->F[d->cur], s);
+    int rc = rebuild(d, false, true);
+    if (rc) return rc;
+    d->lists_stale = false;
+    d->rebuilds++;
+  } else if (rb) {
     int rc = rebuild(d, d->rebuild_current != 0, true);
     if (rc) return rc;
     d->rebuilds++;
@@ -843,6 +914,9 @@ static int solve_step_launches(wf_domain* d) {
     if (rc) return rc;
   }
   StepParams P = make_params(d);
+  // an output row is due after this step: the integration records the BC forces
+  const bool row_due = d->out_every_step || d->time + d->dt >= d->t_out;
+  if (row_due) P.fr = d->fr;
   const Fields& F = d->F[d->cur];
   NbBuffers N{d->nb, d->nbc};
   const bool mixed = d->precision == 1;
@@ -900,12 +974,22 @@ static int solve_step_launches(wf_domain* d) {
   }
   d->isfirst = false;
   d->time += d->dt;
+  if (row_due) {                                                                      // :350-388
+    launch_output_row(P, F, d->out_part, d->time, (double)(d->step + 1), d->out_last, d->series,
+                      d->series_cap, d->series_count, 1, d->d_status, s);
+    d->launches += 2;
+    d->row_recorded = true;
+  }
   if (d->time >= d->t_out) {                                                          // :323-368
     launch_snapshot(d->n, F, s);
     d->launches += 1;
     d->t_out += d->dt_out;
     if (d->csv_on) {
       int rc = write_snapshot(d);
+      if (rc) return rc;
+    }
+    if (d->print_outputs) {
+      int rc = print_output_row(d);
       if (rc) return rc;
     }
   }
@@ -922,7 +1006,10 @@ static int solve_step_launches(wf_domain* d) {
 }
 
 // One Fraser step.  A failure inside a step segment ends the capture and
-// drops the segment, so the stream is usable again.
+// drops the segment, so the stream is usable again.  Then the host hook, if
+// one is set (GeneralAfter, called by the reference around the integration
+// of every step, SolverFraser.cu:273-281): the step's heat pass is completed
+// first, so that the hook sees the whole state of the step.
 static int solve_step(wf_domain* d) {
   const int rc = solve_step_launches(d);
   if (rc && d->capturing) {
@@ -931,7 +1018,13 @@ static int solve_step(wf_domain* d) {
     if (cudaStreamEndCapture(d->stream, &g) == cudaSuccess && g) cudaGraphDestroy(g);
     cudaGetLastError();
   }
-  return rc;
+  if (rc || !d->after_fn) return rc;
+  flush_heat(d);
+  d->in_callback = true;
+  const int r = d->after_fn(d, d->after_user);
+  d->in_callback = false;
+  if (r) return wf_fail(d, WF_ERR_STATE, "step callback returned " + std::to_string(r));
+  return WF_OK;
 }
 
 // the last step's heat pass (mixed form), before any result leaves a call
@@ -954,6 +1047,14 @@ static int finish(wf_domain* d) {
   if (d->h_status[0] & WF_STATUS_NAN) return wf_fail(d, WF_ERR_NUMERIC, "non-finite stress detected");
   if (d->h_status[0] & WF_STATUS_MMA_WAIT)
     return wf_fail(d, WF_ERR_CUDA, "a tensor-core completion wait ran out (warm-start network)");
+  if (d->h_status[0] & WF_STATUS_NEWTON) {
+    unsigned long long capped;
+    memcpy(&capped, d->h_status + 8, sizeof capped);
+    return wf_fail(d, WF_ERR_NUMERIC,
+                   "Newton return map stopped at newton_max_iter = " +
+                       std::to_string(d->newton_max_iter) + " without meeting newton_rtol in " +
+                       std::to_string(capped) + " return maps (state advanced with them)");
+  }
   return WF_OK;
 }
 
@@ -991,7 +1092,8 @@ int wf_create(wf_domain** out, int64_t n) {
     place.base = reinterpret_cast<uintptr_t>(d->arena);
     layout_arena(d, place);
   }
-  if (cudaMallocHost((void**)&d->h_status, 8 * sizeof(int)) != cudaSuccess) return bail(WF_ERR_ALLOC);
+  if (cudaMallocHost((void**)&d->h_status, WF_STATUS_WORDS * sizeof(int)) != cudaSuccess)
+    return bail(WF_ERR_ALLOC);
   k_iota<<<nblk(n), 256, 0, d->stream>>>(n, d->F[0].perm, d->inv);
   k_fill_d<<<nblk(n), 256, 0, d->stream>>>(n, -1.0, d->F[0].pwn, 1, 0);
   if (cudaStreamSynchronize(d->stream) != cudaSuccess) return bail(WF_ERR_CUDA);
@@ -1013,7 +1115,7 @@ int wf_destroy(wf_domain* d) {
   if (d->cnb) cudaFree(d->cnb);
   if (d->ccnt) cudaFree(d->ccnt);
   void* ptrs[] = {d->log_x, d->log_y, d->log_count, d->cell_count, d->cell_cursor,
-                  d->scan_tmp, d->arena};
+                  d->scan_tmp, d->series, d->arena};
   for (void* p : ptrs) if (p) cudaFree(p);
   if (d->h_status) cudaFreeHost(d->h_status);
   for (cudaEvent_t e : d->ev_pool) cudaEventDestroy(e);
@@ -1114,6 +1216,7 @@ int wf_set_positions(wf_domain* d, const double* x) {
   WF_CUDA_OK(cudaStreamSynchronize(d->stream));
   if (bad) return wf_fail(d, WF_ERR_ARG, "non-finite position");
   d->x_set = true;
+  if (d->started) d->lists_stale = true;   // the lists were built for the old positions
   k_scatter_d<<<nblk(d->n), 256, 0, d->stream>>>(d->n, d->inv, d->d_stage, 3, (double*)CF(d).xm,
                                                   4, 0);
   WF_CUDA_OK(cudaStreamSynchronize(d->stream));
@@ -1162,6 +1265,22 @@ int wf_add_velocity_bc(wf_domain* d, int32_t zone, double vx, double vy, double 
   if ((int)d->bc_zone.size() >= WF_MAX_BC) return wf_fail(d, WF_ERR_ARG, "too many boundary conditions");
   d->bc_zone.push_back(zone);
   d->bc_v.push_back({vx, vy, vz});
+  return WF_OK;
+}
+int wf_set_velocity_bc(wf_domain* d, int32_t index, double vx, double vy, double vz) {
+  if (!d) return WF_ERR_ARG;
+  if (index < 0 || index >= (int32_t)d->bc_zone.size())
+    return wf_fail(d, WF_ERR_ARG, "no velocity BC with index " + std::to_string(index));
+  if (!std::isfinite(vx) || !std::isfinite(vy) || !std::isfinite(vz))
+    return wf_fail(d, WF_ERR_ARG, "non-finite BC velocity");
+  d->bc_v[index] = {vx, vy, vz};
+  return WF_OK;
+}
+int wf_set_callback(wf_domain* d, wf_after_fn fn, void* user) {
+  if (!d) return WF_ERR_ARG;
+  if (d->in_callback) return wf_fail(d, WF_ERR_STATE, "the callback cannot be changed from itself");
+  d->after_fn = fn;
+  d->after_user = fn ? user : nullptr;
   return WF_OK;
 }
 int wf_set_csv_output(wf_domain* d, const char* prefix) {
@@ -1336,7 +1455,21 @@ int wf_set_option(wf_domain* d, const char* key, double v) {
   }
   else if (k == "taylor_quinney") d->chi = v;
   else if (k == "newton_rtol") d->newton_rtol = v;
-  else if (k == "newton_max_iter") d->newton_max_iter = (int)v;
+  else if (k == "newton_max_iter") {
+    if (!(v >= 1.0)) return wf_fail(d, WF_ERR_ARG, "newton_max_iter must be >= 1");
+    d->newton_max_iter = (int)v;
+  }
+  else if (k == "output_every_step") d->out_every_step = v != 0;
+  else if (k == "print_outputs") d->print_outputs = v != 0;
+  else if (k == "output_series_cap") {
+    if (!(v >= 1.0) || v > 1.0e9) return wf_fail(d, WF_ERR_ARG, "output_series_cap must be in [1, 1e9]");
+    if ((int64_t)v != d->series_cap) {
+      if (d->series) cudaFree(d->series);
+      d->series = nullptr;          // reallocated at the next solve start
+      d->series_width = 0;
+      d->series_cap = (int64_t)v;
+    }
+  }
   else if (k == "energy_mode") d->energy_mode = (int)v;
   else if (k == "output_interval") d->output_interval = v;
   else if (k == "clamp_homologous") d->clamp_homologous = v != 0;
@@ -1364,6 +1497,7 @@ int wf_set_option(wf_domain* d, const char* key, double v) {
 
 int wf_find_neighbors(wf_domain* d) {
   if (!d) return WF_ERR_ARG;
+  if (d->in_callback) return wf_fail(d, WF_ERR_STATE, "solvers cannot be called from the step callback");
   if (!d->h_set || !d->x_set) return wf_fail(d, WF_ERR_STATE, "h and positions required");
   launch_snapshot(d->n, CF(d), d->stream);
   int rc = rebuild(d, false);
@@ -1373,6 +1507,7 @@ int wf_find_neighbors(wf_domain* d) {
 
 int wf_step(wf_domain* d, int64_t nsteps) {
   if (!d || nsteps < 0) return WF_ERR_ARG;
+  if (d->in_callback) return wf_fail(d, WF_ERR_STATE, "solvers cannot be called from the step callback");
   if (!d->started) {
     int rc = solve_begin(d, d->output_interval);
     if (rc) return rc;
@@ -1386,24 +1521,28 @@ int wf_step(wf_domain* d, int64_t nsteps) {
 
 int wf_mech_fraser_solve(wf_domain* d, double tf, double dt_out) {
   if (!d || !(dt_out > 0)) return WF_ERR_ARG;
+  if (d->in_callback) return wf_fail(d, WF_ERR_STATE, "solvers cannot be called from the step callback");
   int rc = solve_begin(d, dt_out);
   if (rc) return rc;
   while (d->time < tf) {
     rc = solve_step(d);
     if (rc) return rc;
   }
-  return finish(d);
+  rc = finish(d);
+  if (rc == WF_OK && d->csv_on) rc = write_series_csv(d, (d->csv_prefix + "outputs.csv").c_str());
+  return rc;
 }
 
 int wf_mech_solve(wf_domain* d, double tf, double dt_out) { return wf_mech_fraser_solve(d, tf, dt_out); }
 
 int wf_thermal_solve(wf_domain* d, double tf) {
   if (!d) return WF_ERR_ARG;
+  if (d->in_callback) return wf_fail(d, WF_ERR_STATE, "solvers cannot be called from the step callback");
   if (!d->h_set || !d->x_set || !d->m_set || !d->rho_set || !(d->dt > 0))
     return wf_fail(d, WF_ERR_STATE, "h, positions, masses, density and time step required");
   d->time = 0.0;
   d->isfirst = true;
-  WF_CUDA_OK(cudaMemsetAsync(d->d_status, 0, 8 * sizeof(int), d->stream));
+  WF_CUDA_OK(cudaMemsetAsync(d->d_status, 0, WF_STATUS_WORDS * sizeof(int), d->stream));
   int rc = rebuild(d, true);
   if (rc) return rc;
   if (d->precision == 1) k_mixed_init<<<nblk(d->n), 256, 0, d->stream>>>(d->n, CF(d));
@@ -1439,7 +1578,7 @@ int wf_set_field(wf_domain* d, const char* name, const double* in) {
   Fields& F = CF(d);
   std::string s(name);
   int rc;
-  if (s == "x") { d->x_set = true; rc = upload_d(d, in, 3, (double*)F.xm, 4, 0); }
+  if (s == "x") rc = wf_set_positions(d, in);   // finite check; new lists at the next step
   else if (s == "m") { d->m_set = true; rc = upload_d(d, in, 1, (double*)F.xm, 4, 3); }
   else if (s == "v") rc = upload_d(d, in, 3, (double*)F.vd, 4, 0);
   else if (s == "rho") rc = upload_d(d, in, 1, (double*)F.vd, 4, 3);
@@ -1603,14 +1742,34 @@ int wf_get_scalar(wf_domain* d, const char* name, double* out) {
     *out = (double)c[s == "contact_tests32" ? 0 : 1];
     return WF_OK;
   }
-  if (s == "newton_iters" || s == "newton_calls" || s == "mlp_used" || s == "status") {
+  if (s == "newton_iters" || s == "newton_calls" || s == "mlp_used" || s == "status" ||
+      s == "newton_capped") {
     int rc = read_status(d);
     if (rc) return rc;
     unsigned long long v;
     if (s == "status") { *out = d->h_status[0]; return WF_OK; }
-    memcpy(&v, d->h_status + (s == "newton_iters" ? 2 : (s == "newton_calls" ? 4 : 6)), sizeof v);
+    const int w = s == "newton_iters" ? 2 : (s == "newton_calls" ? 4 : (s == "mlp_used" ? 6 : 8));
+    memcpy(&v, d->h_status + w, sizeof v);
     *out = (double)v;
     return WF_OK;
+  }
+  {  // values of the last output row
+    static const char* names[] = {"max_disp_x", "max_disp_y", "max_disp_z", "max_pl_strain",
+                                  "cont_force_sum", "cont_force_x", "cont_force_y",
+                                  "cont_force_z", "int_energy_total", "reaction_x",
+                                  "reaction_y", "reaction_z"};
+    for (int k = 0; k < 12; k++) {
+      if (s != names[k]) continue;
+      if (k >= 9 && d->bc_zone.empty()) return wf_fail(d, WF_ERR_STATE, "no velocity BC");
+      double r[3];
+      const int rc = wf_get_output_row(d, r, 0, nullptr);   // WF_ERR_STATE before any row
+      if (rc) return rc;
+      const int col = k < 9 ? 2 + k : WF_ROW_FIXED + (k - 9);
+      WF_CUDA_OK(cudaMemcpyAsync(out, d->out_last + col, sizeof(double), cudaMemcpyDeviceToHost,
+                                 d->stream));
+      WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+      return WF_OK;
+    }
   }
   if (s == "int_energy_sum") {
     std::vector<double> e(d->n);
@@ -1623,6 +1782,89 @@ int wf_get_scalar(wf_domain* d, const char* name, double* out) {
   }
   return wf_fail(d, WF_ERR_ARG, "unknown scalar: " + s);
 }
+
+int wf_get_output_row(wf_domain* d, double* row, int64_t cap, int64_t* width) {
+  if (!d || (cap > 0 && !row)) return WF_ERR_ARG;
+  const int64_t w = WF_ROW_FIXED + 3 * (int64_t)d->bc_zone.size();
+  if (width) *width = w;
+  if (!d->row_recorded)
+    return wf_fail(d, WF_ERR_STATE,
+                   "no output row yet: rows are recorded at output times, or every step with "
+                   "option output_every_step");
+  {
+    const int rc = segment_end(d);
+    if (rc) return rc;
+  }
+  if (cap > 0) {
+    WF_CUDA_OK(cudaMemcpyAsync(row, d->out_last, sizeof(double) * std::min(cap, w),
+                               cudaMemcpyDeviceToHost, d->stream));
+    WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+  }
+  return WF_OK;
+}
+
+int wf_get_output_series(wf_domain* d, double* rows, int64_t cap_rows, int64_t* n_rows,
+                         int64_t* width) {
+  if (!d || !n_rows || (cap_rows > 0 && !rows)) return WF_ERR_ARG;
+  const int64_t w = WF_ROW_FIXED + 3 * (int64_t)d->bc_zone.size();
+  if (width) *width = w;
+  *n_rows = 0;
+  if (!d->series || d->series_width != w) return WF_OK;
+  {
+    const int rc = segment_end(d);
+    if (rc) return rc;
+  }
+  unsigned long long c = 0;
+  WF_CUDA_OK(cudaMemcpyAsync(&c, d->series_count, sizeof c, cudaMemcpyDeviceToHost, d->stream));
+  WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+  const int64_t m = std::min<int64_t>((int64_t)c, cap_rows);
+  if (m > 0) {
+    WF_CUDA_OK(cudaMemcpyAsync(rows, d->series, sizeof(double) * m * w, cudaMemcpyDeviceToHost,
+                               d->stream));
+    WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+  }
+  *n_rows = cap_rows > 0 ? m : (int64_t)c;
+  return WF_OK;
+}
+
+int wf_get_reaction(wf_domain* d, int32_t bc_index, double* force) {
+  if (!d || !force) return WF_ERR_ARG;
+  if (bc_index < 0 || bc_index >= (int32_t)d->bc_zone.size())
+    return wf_fail(d, WF_ERR_ARG, "no velocity BC with index " + std::to_string(bc_index));
+  int rc = wf_get_output_row(d, nullptr, 0, nullptr);
+  if (rc) return rc;
+  WF_CUDA_OK(cudaMemcpyAsync(force, d->out_last + WF_ROW_FIXED + 3 * bc_index, 3 * sizeof(double),
+                             cudaMemcpyDeviceToHost, d->stream));
+  WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+  return WF_OK;
+}
+
+}  // extern "C"
+
+// the output series as CSV, one row per recorded output
+static int write_series_csv(wf_domain* d, const char* path) {
+  int64_t n = 0, w = 0;
+  int rc = wf_get_output_series(d, nullptr, 0, &n, &w);
+  if (rc) return rc;
+  std::vector<double> rows((size_t)std::max<int64_t>(n, 1) * w);
+  rc = wf_get_output_series(d, rows.data(), n, &n, &w);
+  if (rc) return rc;
+  FILE* f = fopen(path, "w");
+  if (!f) return wf_fail(d, WF_ERR_IO, std::string("cannot open ") + path);
+  fprintf(f, "time, step, max_ux, max_uy, max_uz, max_pl_strain, cont_force_sum, CFx, CFy, CFz, "
+             "int_energy");
+  for (size_t b = 0; b < d->bc_zone.size(); b++)
+    fprintf(f, ", BC%zu_Fx, BC%zu_Fy, BC%zu_Fz", b, b, b);
+  fprintf(f, "\n");
+  for (int64_t r = 0; r < n; r++) {
+    for (int64_t k = 0; k < w; k++)
+      fprintf(f, k == 1 ? "%.0f" : "%.9e", rows[(size_t)(r * w + k)]), fputs(k + 1 < w ? ", " : "\n", f);
+  }
+  fclose(f);
+  return WF_OK;
+}
+
+extern "C" {
 
 // Domain_d::WriteCSV (src/cuda/Domain_d.cu:556-587): same header and format.
 int wf_write_csv(wf_domain* d, const char* path) {
@@ -1660,6 +1902,7 @@ int wf_write_csv(wf_domain* d, const char* path) {
 int wf_time_steps(wf_domain* d, int64_t nsteps, double* elapsed_ms, double* kernel_ms,
                   int64_t* kernel_launches, int64_t* total_launches) {
   if (!d || nsteps < 0) return WF_ERR_ARG;
+  if (d->in_callback) return wf_fail(d, WF_ERR_STATE, "solvers cannot be called from the step callback");
   if (!d->started) {
     int rc = solve_begin(d, d->output_interval);
     if (rc) return rc;

@@ -44,6 +44,20 @@ __device__ __forceinline__ void nb_block(const int32_t* __restrict__ nb, int64_t
 #define WF_STATUS_NB_CAP    2   // some particle hit WF_MAX_NEIGHBORS (list truncated)
 #define WF_STATUS_GRID      4   // a particle fell outside the search grid
 #define WF_STATUS_MMA_WAIT  8   // a tensor-core completion wait ran out (result discarded)
+#define WF_STATUS_NEWTON   16   // a Newton return map stopped at newton_max_iter unconverged
+#define WF_STATUS_SERIES   32   // the output series was full: rows were dropped
+
+// Status words (int d_status[WF_STATUS_WORDS]): [0] bits, [1] yield flag,
+// 64-bit counters at [2] Newton iterations, [4] plastic return maps, [6]
+// network starts taken, [8] return maps that hit newton_max_iter.
+#define WF_STATUS_WORDS 16
+
+// Output row (wf_get_output_series), all FP64, reduced over the particles in a
+// fixed order: [time, step, max u_x, max u_y, max u_z, max pl_strain,
+// contact-force sum (|contforce| over free-surface particles), contact force
+// vector sum (3), internal energy sum, then per velocity BC the sum of m a
+// over its zone before the BC is imposed (3 each)].
+#define WF_ROW_FIXED 11
 
 // All per-slot arrays that move with the particles at a reorder.
 struct Fields {
@@ -163,6 +177,8 @@ struct StepParams {
   int nbc;
   int32_t bc_zone[WF_MAX_BC];
   double bc_v[WF_MAX_BC][3];
+  double4* fr;          // when not null (an output row is due this step): m a before the
+                        // BCs are imposed, written at the slots of BC-zone particles
   int mlp_on;           // MLP warm start of the Newton return map
   int refresh_pow;      // recompute eps_p^n with pow() this step (bounds series drift)
   int64_t log_cap;      // return-map log (training pairs for the MLP): capacity
@@ -219,17 +235,24 @@ __device__ __forceinline__ float gk32_r2(float r2, float invh, float Ch, float C
 // plastic calls, MLP starts taken) and the yielding flag (word 1), summed over
 // the warp's active lanes first: one atomic per warp instead of one per
 // particle, which would serialise on one L2 address.
+// A return map that stopped at newton_max_iter without meeting its tolerance
+// (capped) adds to the counter at word 8 and sets WF_STATUS_NEWTON.
 __device__ __forceinline__ void warp_count(int* status, unsigned iters, unsigned calls,
-                                           unsigned mlp_used, bool yielding) {
+                                           unsigned mlp_used, bool capped, bool yielding) {
   const unsigned mask = __activemask();
   const unsigned si = __reduce_add_sync(mask, iters);
   const unsigned sc = __reduce_add_sync(mask, calls);
   const unsigned sm = __reduce_add_sync(mask, mlp_used);
+  const unsigned sk = __reduce_add_sync(mask, capped ? 1u : 0u);
   const bool y = __any_sync(mask, yielding);
   if ((int)(threadIdx.x & 31) == __ffs(mask) - 1) {
     if (si) atomicAdd((unsigned long long*)(status + 2), (unsigned long long)si);
     if (sc) atomicAdd((unsigned long long*)(status + 4), (unsigned long long)sc);
     if (sm) atomicAdd((unsigned long long*)(status + 6), (unsigned long long)sm);
+    if (sk) {
+      atomicAdd((unsigned long long*)(status + 8), (unsigned long long)sk);
+      atomicOr(status, WF_STATUS_NEWTON);
+    }
     if (y) status[1] = 1;
   }
 }

@@ -28,6 +28,7 @@ __global__ void __launch_bounds__(256) k_integrate(StepParams P, Fields F,
   const double4 a4 = F.a[i];
   const int32_t id = F.id[i];
   double vx = v4.x, vy = v4.y, vz = v4.z, ax = a4.x, ay = a4.y, az = a4.z;
+  record_bc_force(P, i, id, xm.w, ax, ay, az);
   apply_bc(P, id, vx, vy, vz, ax, ay, az);
   const double dt = P.dt;
   const double ux = vx * dt + ((ax * 0.5) * dt) * dt;

@@ -8,6 +8,16 @@
 #pragma once
 #include "wf_common.cuh"
 
+// The force m a on a BC-zone particle before its BC zeroes a: the load its
+// boundary carries.  Written only when an output row is due this step.
+__device__ __forceinline__ void record_bc_force(const StepParams& P, int64_t i, int32_t id,
+                                                double m, double ax, double ay, double az) {
+  if (!P.fr) return;
+  bool in_bc = false;
+  for (int b = 0; b < P.nbc; b++) in_bc |= id == P.bc_zone[b];
+  if (in_bc) P.fr[i] = make_double4(m * ax, m * ay, m * az, 0.0);
+}
+
 __device__ __forceinline__ void apply_bc(const StepParams& P, int32_t id, double& vx, double& vy,
                                          double& vz, double& ax, double& ay, double& az) {
   for (int b = 0; b < P.nbc; b++)
@@ -28,6 +38,7 @@ __device__ __forceinline__ void integrate_mixed_one(const StepParams& P, const F
   const double4 v4 = vd2[i];
   const int32_t id = F.id[i];
   double vx = v4.x, vy = v4.y, vz = v4.z, ax = af.x, ay = af.y, az = af.z;
+  record_bc_force(P, i, id, xm.w, ax, ay, az);
   apply_bc(P, id, vx, vy, vz, ax, ay, az);
   const float dtf = P.dtf, hdt2 = __fmul_rn(__fmul_rn(0.5f, P.dtf), P.dtf);
   const float fax = (float)ax, fay = (float)ay, faz = (float)az;

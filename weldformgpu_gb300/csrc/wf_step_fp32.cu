@@ -413,6 +413,7 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
     if (!solid) return;
   }
   unsigned n_it = 0u, n_call = 0u, n_mlp = 0u;   // this particle's return-map counters
+  bool capped = false;                            // Newton stopped at newton_max_iter
   if (P.return_map == 0) {
     // reference one-shot radial return (Mechanical.cu:503-536)
     if (sy < (double)st) scale = (float)(sy / (double)st);
@@ -439,6 +440,7 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
                        &it);
     }
     F.pwn[i] = pwn;
+    capped = it >= P.newton_max_iter;
     if (dep > 0.0) {
       scale = inc32 ? sy1f / st : (float)(sy1 / (double)st);
       eps_p += dep;
@@ -458,6 +460,7 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
       const double G3 = 3.0 * P.G;
       int it = 0;
       dep = newton_return(P, H, (double)st, G3, eps_p, sy0, ((double)st - sy0) / G3, &it);
+      capped = it >= P.newton_max_iter;
       double sy1, dsy1;
       hard_eval(M, H, eps_p, dep, &sy1, &dsy1);
       scale = (float)(sy1 / (double)st);
@@ -495,7 +498,7 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
                     (Sn.xx * Dxx + Sn.yy * Dyy + Sn.zz * Dzz +
                      2.0f * (Sn.xy * Dxy + Sn.yz * Dyz + Sn.xz * Dxz));
   F.eint[i] += (double)def * P.dt;
-  warp_count(status, n_it, n_call, n_mlp, eps_p > 1.e-6);
+  warp_count(status, n_it, n_call, n_mlp, capped, eps_p > 1.e-6);
   if (!isfinite(st)) atomicOr(status, WF_STATUS_NAN);
 }
 

@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(128) k_stress64(StepParams P, Fields F,
   if (!isfinite(out.seq)) atomicOr(status, WF_STATUS_NAN);
   // Newton counters and the is_yielding flag (eps_p > 1e-6), one atomic per warp
   warp_count(status, (unsigned)out.newton_iters, out.newton_iters > 0 ? 1u : 0u, 0u,
-             st.eps_p > 1.e-6);
+             P.return_map == 1 && out.newton_iters >= P.newton_max_iter, st.eps_p > 1.e-6);
 }
 
 // ---- C: Domain_d::CalcAccel (src/cuda/InteractionAlt.cu:18-150) ---------

@@ -93,6 +93,29 @@ class Domain_d:
         self._ck(self.L.wf_add_velocity_bc(self.h, int(zone), float(vx), float(vy), float(vz)),
                  "wf_add_velocity_bc")
 
+    def set_velocity_bc(self, index, vx, vy, vz):
+        """Velocity of BC `index` (wf_add_velocity_bc order), e.g. from the step callback."""
+        self._ck(self.L.wf_set_velocity_bc(self.h, int(index), float(vx), float(vy), float(vz)),
+                 "wf_set_velocity_bc")
+
+    def set_callback(self, fn):
+        """Per-step host hook (the reference's GeneralAfter): fn(domain) after every step;
+        a non-zero return ends the solve.  None removes it."""
+        if fn is None:
+            self._cb = None
+            self._ck(self.L.wf_set_callback(self.h, None, None), "wf_set_callback")
+            return
+
+        def tramp(_h, _u):
+            try:
+                r = fn(self)
+                return int(r or 0)
+            except Exception:          # an exception in the hook ends the solve
+                return 1
+        self._cb = _abi.AFTER_FN(tramp)
+        self._ck(self.L.wf_set_callback(self.h, C.cast(self._cb, C.c_void_p), None),
+                 "wf_set_callback")
+
     def set_contact(self, mu_static, mu_dynamic, law=0):
         self._ck(self.L.wf_set_contact(self.h, float(mu_static), float(mu_dynamic), int(law)),
                  "wf_set_contact")
@@ -240,10 +263,44 @@ class Domain_d:
                  "wf_get_neighbors")
         return cnt, lst.reshape(self.n, _abi.WF_MAX_NEIGHBORS)
 
+    def get_output_series(self):
+        """The output rows recorded by the solve (n_rows x width, FP64): time, step,
+        max u (3), max pl_strain, contact force sum, contact force vector (3),
+        internal energy, then per velocity BC the reaction of its zone (3)."""
+        n, w = C.c_int64(), C.c_int64()
+        self._ck(self.L.wf_get_output_series(self.h, None, 0, C.byref(n), C.byref(w)),
+                 "wf_get_output_series")
+        rows = np.empty((n.value, w.value), dtype=np.float64)
+        if n.value:
+            self._ck(self.L.wf_get_output_series(self.h, _ptr(rows, C.c_double), n.value,
+                                                 C.byref(n), C.byref(w)), "wf_get_output_series")
+        return rows
+
+    def get_output_row(self):
+        w = C.c_int64()
+        self._ck(self.L.wf_get_output_row(self.h, None, 0, C.byref(w)), "wf_get_output_row")
+        row = np.empty(w.value, dtype=np.float64)
+        self._ck(self.L.wf_get_output_row(self.h, _ptr(row, C.c_double), w.value, C.byref(w)),
+                 "wf_get_output_row")
+        return row
+
+    def get_reaction(self, bc_index=0):
+        f = np.empty(3, dtype=np.float64)
+        self._ck(self.L.wf_get_reaction(self.h, int(bc_index), _ptr(f, C.c_double)),
+                 "wf_get_reaction")
+        return f
+
     def get_scalar(self, name):
         out = C.c_double()
         self._ck(self.L.wf_get_scalar(self.h, name.encode(), C.byref(out)), "wf_get_scalar(%s)" % name)
         return out.value
+
+    def set_csv_output(self, prefix):
+        """MechFraserSolve's snapshots: <prefix>out_<time>.csv at the solve start and at
+        every output time, and the output rows to <prefix>outputs.csv at its end;
+        None turns them off."""
+        p = None if prefix is None else str(prefix).encode()
+        self._ck(self.L.wf_set_csv_output(self.h, p), "wf_set_csv_output")
 
     def write_csv(self, path):
         self._ck(self.L.wf_write_csv(self.h, str(path).encode()), "wf_write_csv")

@@ -16,7 +16,7 @@ from . import setup as S
 def compression_cylinder(R=0.0025, H=0.005, dx=0.0005, generator="reference", vz_top=-1.0,
                          material="bilinear", jitter=0.01, seed=1, layers=2, dt_rule="reference"):
     """Elastoplastic cylinder compression (the reference's Compression example
-    shape; BASELINE config 1 at R=5 mm, H=10 mm).  Bottom `layers` layers are
+    shape; the 5,000-step benchmark case is R=5 mm, H=10 mm).  Bottom `layers` layers are
     fixed (zone 2), top `layers` layers move at vz_top (zone 3)."""
     r = dx / 2.0
     rho = 2700.0
@@ -38,7 +38,7 @@ def compression_cylinder(R=0.0025, H=0.005, dx=0.0005, generator="reference", vz
                               m_hol=0.2)
         sy = 300e6
         T0 = 20.0
-    else:  # Johnson-Cook, BASELINE config 3 constants (aluminium)
+    else:  # Johnson-Cook aluminium: A 324 MPa, B 114 MPa, n 0.42, C 0.002, m 1.34, Tm 582 C
         E, nu = 70e9, 0.33
         mat = _abi.WfMaterial(model=_abi.WF_JOHNSON_COOK, E=E, nu=nu, sy0=324e6, A=324e6,
                               B=114e6, n=0.42, C=0.002, eps0=1.0, m=1.34, Tm=582.0, Tt=20.0)
@@ -50,7 +50,7 @@ def compression_cylinder(R=0.0025, H=0.005, dx=0.0005, generator="reference", vz
     h = 1.2 * dx
     if dt_rule == "reference":       # src/WeldFormGPU.cu:906, VMAX = 10
         dt = 0.4 * h / (Cs + 10.0)
-    else:                            # BASELINE config 1: 0.4 h / c
+    else:                            # 0.4 h / c (c = sqrt(K / rho))
         dt = 0.4 * h / Cs
     ids = np.zeros(n, np.int32)
     nw = np.zeros(n, np.uint8)
@@ -100,7 +100,7 @@ def contact_cylinder(R=0.005, H=0.010, dx=0.0005, dens=10, v_plane=-10.0, gap=1.
 def indent_block(L=(0.008, 0.008, 0.003), dx=0.00025, R=0.003, level=3, v_tool=-5.0, mu=0.3,
                  gap=1.0e-7, thermal=True, zone=7, rebuild_increment=0.05, omega=0.0):
     """A block indented by a rigid lower-half icosphere (the shape of the
-    2M-particle contact benchmark, BASELINE config 5: block 200 x 200 x 50 dx,
+    2M-particle contact benchmark: block 200 x 200 x 50 dx,
     dx = 0.25 mm, R = 10 mm, ~10k triangles, -5 m/s): contact law 1 (penalty
     0.1 K / dx, friction mu, cell-binned triangle query, frictional heat), JC
     aluminium, neighbour rebuild at a plastic-strain increment.  The bottom
@@ -177,7 +177,7 @@ def load(dom, sc, options=None):
 
 
 def heat_box(n_side=20, dx=1.0e-4, hot=500.0, T0=20.0, sigma=1.0e-3):
-    """Heat conduction only (BASELINE config 2 shape at n_side^3 particles):
+    """Heat conduction only (the 100^3-particle heat box's shape at n_side^3 particles):
     steel cube, Gaussian hot spot at the centre, convection on the outer layer."""
     rho, cp, k = 7850.0, 460.0, 50.0
     L = n_side * dx
@@ -210,7 +210,7 @@ def load_heat(dom, sc):
 
 
 def jc_compression(R=0.025, H=0.050, dx=0.0005, jitter=0.01, seed=1, vz_top=-10.0, layers=2):
-    """Coupled thermo-mechanical Johnson-Cook compression (BASELINE configs 3/4):
+    """Coupled thermo-mechanical Johnson-Cook compression (R 25 mm, H 50 mm, dx 0.5 mm):
     R = 25 mm, H = 50 mm, dx = 0.5 mm (~0.79M particles), jitter +-0.01 dx,
     JC A=324 MPa, B=114 MPa, n=0.42, C=0.002, m=1.34, eps0=1/s, Tref=20 C,
     Tmelt=582 C; k=167 W/mK, cp=896 J/kgK, Taylor-Quinney 0.9 (set as an
