@@ -1,6 +1,6 @@
 """Benchmark of the explicit SPH step: particle-steps/s on one GB300.
 
-Workload (BASELINE configs 3/4): coupled thermo-mechanical Johnson-Cook
+Workload: coupled thermo-mechanical Johnson-Cook
 cylinder compression, R = 25 mm, H = 50 mm, dx = 0.5 mm, seeded jittered
 lattice (~0.79M particles), consistent Newton return map, Taylor-Quinney
 plastic heat, platen at -10 m/s.  A "step" is one pass of the Fraser loop
@@ -13,6 +13,11 @@ when trained weights are loaded) with inputs resident in HBM; `plain_fp64`
 is the plain-FP64 form of the same code; `e2e` times the drop-in call
 (create, setters from host arrays, solve, read-back of the output fields)
 with host clocks.  `cpu_baseline` times the FP64 CPU oracle on the host cores.
+`rel_l2_vs_fp64` compares the two forms from the same plastic state after the
+timed steps; `rel_l2_vs_fp64_from_rest` over a 5,000-step run from rest of a
+smaller cylinder of the same material and loading; `fp64_ceiling` puts the
+plain form against the measured FP64 FMA throughput; `heat` and `indentation`
+are the 1M-particle heat-only and 2M-particle contact workloads.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -45,6 +50,7 @@ BYTES_MODEL = {
 }
 NB_INDEX_BYTES = 4  # per neighbour per pair pass
 KERNEL_IDS = {"density": 1, "stress": 2, "accel": 3, "integrate": 4, "thermal": 5}
+TOP_FZ = 11 + 3 * 1 + 2     # output-row column: BC 1 (the moving platen zone), z component
 PAIR_KERNELS = ("density", "stress", "accel", "thermal")
 
 
@@ -188,9 +194,10 @@ def train_mlp(sc, state, log_steps=5, cap=1 << 20):
     return params, info
 
 
-def run_form(sc, form, steps, warmup, state, mlp_params=None):
+def run_form(sc, form, steps, warmup, state, mlp_params=None, extra_opts=None):
     opts = base_options()
     opts["precision"] = 1 if form == "mixed" else 0
+    opts.update(extra_opts or {})
     d = build_domain(sc, opts)
     d.restore(state)
     if mlp_params is not None:
@@ -208,7 +215,12 @@ def run_form(sc, form, steps, warmup, state, mlp_params=None):
     d.set_option("profile_kernel", 0)
     it1, c1 = d.get_scalar("newton_iters"), d.get_scalar("newton_calls")
     u1 = d.get_scalar("mlp_used")
+    # 20 more steps with an output row every step: the reaction curve of both forms
+    d.set_option("output_every_step", 1)
+    d.step(20)
+    rows = d.get_output_series()[-20:]
     fields = {f: d.get_field(f) for f in ("u", "pl_strain", "sigma_eq", "T")}
+    fields["reaction_force"] = rows[:, TOP_FZ]
     d.close()
     return dict(elapsed_ms=elapsed, kernel_ms=kernel_ms, kernel_launches=kernel_launches,
                 launches=launches, dominant=dominant, per_kernel_ms=kms, clocks=clk.summary(),
@@ -296,6 +308,71 @@ def cpu_baseline(sc, budget_s=12.0):
 def rel_l2(a, b):
     den = np.linalg.norm(b)
     return float(np.linalg.norm(a - b) / (den if den > 0 else 1.0))
+
+
+FROM_REST = {"R": 0.010, "H": 0.020, "steps": 5000}
+
+
+def from_rest_errors(mlp_params=None):
+    """Both forms from rest on a smaller cylinder of the same material, dx,
+    loading and options (R = 10 mm, H = 20 mm, ~50k particles) for 5,000 steps
+    (12 % height reduction): relative L2 error of the mixed form (with the
+    network when given) against the plain FP64 form on the output fields and
+    on the platen's reaction curve (an output row every step)."""
+    from weldformgpu_gb300 import scenarios as S
+    sc = S.jc_compression(R=FROM_REST["R"], H=FROM_REST["H"])
+    out = {}
+    for form in ("fp64", "mixed"):
+        opts = base_options()
+        opts["precision"] = 1 if form == "mixed" else 0
+        opts["output_every_step"] = 1
+        d = build_domain(sc, opts)
+        if form == "mixed" and mlp_params is not None:
+            d.set_mlp_weights(mlp_params)
+            d.set_option("mlp", 1)
+        t0 = time.perf_counter()
+        d.step(FROM_REST["steps"])
+        out[form] = {f: d.get_field(f) for f in ("u", "pl_strain", "sigma_eq", "T")}
+        out[form]["reaction_force"] = d.get_output_series()[:, TOP_FZ]
+        out[form]["_s"] = time.perf_counter() - t0
+        out[form]["_max_ps"] = float(out[form]["pl_strain"].max())
+        d.close()
+    errs = {f: rel_l2(out["mixed"][f] - (20.0 if f == "T" else 0.0),
+                      out["fp64"][f] - (20.0 if f == "T" else 0.0))
+            for f in ("u", "pl_strain", "sigma_eq", "T", "reaction_force")}
+    errs.update({"steps": FROM_REST["steps"], "particles": sc["n"],
+                 "workload": "jc_thermomech_compression_R10mm_H20mm_dx0.5mm from rest",
+                 "max_pl_strain": out["fp64"]["_max_ps"],
+                 "fp64_run_s": out["fp64"]["_s"], "mixed_run_s": out["mixed"]["_s"],
+                 "mlp": mlp_params is not None})
+    return errs
+
+
+def fp64_ceiling(plain_per_kernel_ms, n):
+    """The plain form against the measured FP64 FMA throughput: FP64 flops per
+    particle of each pair kernel (ncu instruction counts, profiles/fp64_flops.json:
+    2 per DFMA, 1 per DADD / DMUL) over its event-timed duration."""
+    import ctypes as C
+    from weldformgpu_gb300 import domain as D
+    g, ms = C.c_double(), C.c_double()
+    rc = D.lib().wf_fp64_fma_peak(C.byref(g), C.byref(ms))
+    if rc != 0:
+        return None
+    out = {"peak_gflops": g.value, "peak_kind": "measured (wf_fp64_fma_peak: FMA chains on every SM)"}
+    fp = os.path.join(ROOT, "profiles", "fp64_flops.json")
+    if os.path.exists(fp):
+        with open(fp) as f:
+            flops = json.load(f)["fp64"]
+        per = {}
+        for k, fpp in flops.items():
+            if k in plain_per_kernel_ms and plain_per_kernel_ms[k] > 0:
+                a = fpp * n / (plain_per_kernel_ms[k] / 1e3) / 1e9
+                per[k] = {"flops_per_particle": fpp, "achieved_gflops": a,
+                          "frac": a / g.value}
+        out["kernels"] = per
+        tot = sum(flops.values())
+        out["flops_per_particle_step"] = tot
+    return out
 
 
 def dist_setup(n_gpus):
@@ -400,7 +477,7 @@ def bench_indentation(args):
         line["rel_l2_vs_fp64_after_20_steps"] = {
             f: rel_l2(fields["mixed"][f] - (20.0 if f == "T" else 0.0),
                       fields["fp64"][f] - (20.0 if f == "T" else 0.0)) for f in fields["mixed"]}
-    print(json.dumps(line))
+    return line
 
 
 def bench_heat(args):
@@ -437,7 +514,7 @@ def bench_heat(args):
             "mixed": out["mixed"], "plain_fp64": out["fp64"],
             "speedup_vs_plain_fp64": out["mixed"]["value"] / out["fp64"]["value"],
             "rel_l2_vs_fp64": rel_l2(T["mixed"] - sc["T"], T["fp64"] - sc["T"])}
-    print(json.dumps(line))
+    return line
 
 
 def main():
@@ -454,6 +531,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-oracle baseline")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end arm")
     ap.add_argument("--no-mlp", action="store_true", help="time the mixed form without the MLP")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the from-rest error run, the FP64 ceiling and the heat / "
+                         "indentation workloads")
     ap.add_argument("--preload", type=int, default=4000,
                     help="steps run (mixed form) before the timed runs, to reach plasticity")
     ap.add_argument("--workload", default="compression",
@@ -466,16 +546,22 @@ def main():
     if args.workload in ("indentation", "heat"):
         from weldformgpu_gb300 import build as Bld
         Bld.build()
-        (bench_indentation if args.workload == "indentation" else bench_heat)(args)
+        print(json.dumps((bench_indentation if args.workload == "indentation" else bench_heat)(args)))
         return
     rank, ws, dist = dist_setup(args.gpus)
 
-    from weldformgpu_gb300 import build as B
-    B.build()
     from weldformgpu_gb300 import scenarios as S
     size = "small" if args.small else args.size
-    sc = {"full": lambda: S.jc_compression(), "medium": lambda: S.jc_compression(R=0.015, H=0.030),
-          "small": lambda: S.jc_compression(R=0.006, H=0.012)}[size]()
+    dims = {"full": {}, "medium": {"R": 0.015, "H": 0.030}, "small": {"R": 0.006, "H": 0.012}}[size]
+    if args.impl == "reference":
+        # the reference arm builds the same workload with the oracle's generator
+        # twins: it neither builds nor loads the CUDA library
+        from oracle import oracle as O
+        sc = S.jc_compression(gen=O, **dims)
+    else:
+        from weldformgpu_gb300 import build as B
+        B.build()
+        sc = S.jc_compression(**dims)
     n = sc["n"]
     config = {"workload": WORKLOAD if size == "full" else WORKLOAD + "_" + size, "particles": n,
               "dx_m": sc["dx"], "dt_s": sc["dt"], "nnb": 56, "rebuild_every": 5,
@@ -501,12 +587,17 @@ def main():
 
     state = preload(sc, args.preload)
     forms = args.forms.split(",")
+    if "fp64" not in forms or "mixed" not in forms:
+        # a profiling run of one form (e.g. under ncu)
+        form = "mixed" if "mixed" in forms else "fp64"
+        mlp = None if (args.no_mlp or form == "fp64") else train_mlp(sc, state)[0]
+        r = run_form(sc, form, args.steps, warmup, state, mlp)
+        print(json.dumps({"profiling_run": True, "form": form,
+                          "ms_per_step": r["elapsed_ms"] / args.steps,
+                          "per_kernel_ms": r["per_kernel_ms"], "particles": n}))
+        return
     mlp, mlp_info = (None, None) if args.no_mlp else train_mlp(sc, state)
     mixed = run_form(sc, "mixed", args.steps, warmup, state, mlp)
-    if "fp64" not in forms:
-        print(json.dumps({"profiling_run": True, "ms_per_step": mixed["elapsed_ms"] / args.steps,
-                          "per_kernel_ms": mixed["per_kernel_ms"], "particles": n}))
-        return
     mixed_nomlp = run_form(sc, "mixed", args.steps, warmup, state) if mlp is not None else None
     plain = run_form(sc, "fp64", args.steps, warmup, state)
     t_mixed = reduce_max(dist, mixed["elapsed_ms"])
@@ -515,7 +606,7 @@ def main():
     plain_value = ws * n * args.steps / (t_plain / 1e3)
     errs = {f: rel_l2(mixed["fields"][f] - (20.0 if f == "T" else 0.0),
                       plain["fields"][f] - (20.0 if f == "T" else 0.0))
-            for f in ("u", "pl_strain", "sigma_eq", "T")}
+            for f in ("u", "pl_strain", "sigma_eq", "T", "reaction_force")}
     e2e_steps = max(args.steps, 100)
     e2e_v, h2d, d2h = (0.0, 0, 0) if args.no_e2e else run_e2e(sc, "mixed", e2e_steps, state, mlp)
     e2e_v = reduce_max(dist, e2e_v) * ws if dist else e2e_v
@@ -548,6 +639,10 @@ def main():
                        "newton_iters_per_plastic_particle": plain["newton_iters_per_call"]},
         "speedup_vs_plain_fp64": value / plain_value,
         "rel_l2_vs_fp64": errs,
+        "rel_l2_vs_fp64_note": "both forms restored from the same %d-step plastic state; "
+                               "fields after the warm-up, profiled and timed steps (%d steps), "
+                               "reaction_force = the platen's curve over 20 further steps"
+                               % (args.preload, warmup + 5 * 20 + args.steps + 20),
         "mlp_warm_start": mlp is not None,
         "mlp": None if mlp is None else dict(
             mlp_info,
@@ -571,6 +666,11 @@ def main():
         "gpu_launches": mixed["launches"],
         "clocks": mixed["clocks"],
     }
+    if not args.no_extra and rank == 0:
+        line["rel_l2_vs_fp64_from_rest"] = from_rest_errors(mlp)
+        line["fp64_ceiling"] = fp64_ceiling(plain["per_kernel_ms"], n)
+        line["heat"] = bench_heat(args)
+        line["indentation"] = bench_indentation(args)
     if rank == 0:
         line["cpu_baseline"] = None if args.no_cpu else cpu_baseline(sc)
         print(json.dumps(line))

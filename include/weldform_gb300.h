@@ -146,7 +146,9 @@ int wf_add_trimesh(wf_domain* d, const double* nodes, int32_t nn, const int32_t*
  *   rebuild_strain_increment (0), thermal (0), taylor_quinney (0),
  *   clamp_homologous (1), energy_mode (0), contact_dx (0),
  *   contact_stiffness (0.1), contact_vreg (1e-3), contact_heat_fraction (1),
- *   fuse_heat (1), fuse_integrate (1), graph (1), output_interval (1e300),
+ *   fuse_heat (1), fuse_integrate (1), tile_staging (0; 1: the mixed pair passes
+ *   read neighbours from per-tile halos in shared memory; same results),
+ *   tile_cap_max (2048: largest halo staged), graph (1), output_interval (1e300),
  *   resume (0), profile_kernel (0). */
 int wf_set_option(wf_domain* d, const char* key, double value);
 
@@ -370,6 +372,11 @@ int wf_mlp_newton_iters(const wf_material* mat, double G, const float* params,
 int wf_time_steps(wf_domain* d, int64_t nsteps, double* elapsed_ms,
                   double* kernel_ms, int64_t* kernel_launches,
                   int64_t* total_launches);
+/* Throughput of the FP64 fused multiply-add pipe of the current device in
+ * GFLOP/s (2 flops per FMA), measured with CUDA events over independent FMA
+ * chains on every SM: the arithmetic ceiling of the plain FP64 form (no
+ * reference counterpart). */
+int wf_fp64_fma_peak(double* gflops, double* ms_per_launch);
 
 #ifdef __cplusplus
 }

@@ -23,13 +23,65 @@ def reference_dir():
     return os.environ.get("WF_REFERENCE_DIR", "/root/reference")
 
 
+# Thermal.cu's kernels, taken verbatim: the file also holds host functions that
+# launch kernels with <<< >>>, which g++ cannot parse, so only these functions
+# are written into the build directory for ref_domain.cpp to #include.
+THERMAL_KERNELS = ("TempCalcLeapfrogFirst", "TempCalcLeapfrog", "CalcConvHeatKernel",
+                   "ThermalSolveKernel")
+
+
+def extract_kernels(path, names):
+    """The text of each `__global__` function definition named in `names` (the
+    overload whose parameter list is not a single PartData_d pointer), from
+    its start line to its matching closing brace."""
+    text = open(path).read()
+    out = []
+    for name in names:
+        pos = 0
+        found = False
+        while True:
+            k = text.find(name, pos)
+            if k < 0:
+                break
+            pos = k + len(name)
+            line_start = text.rfind("\n", 0, k) + 1
+            head = text[line_start:k]
+            if "__global__" not in head or text[pos:].lstrip()[:1] != "(":
+                continue
+            brace = text.find("{", pos)
+            semi = text.find(";", pos)
+            if brace < 0 or (0 <= semi < brace):        # a declaration, not a definition
+                continue
+            if "PartData_d" in text[pos:brace]:
+                continue
+            depth, q = 0, brace
+            while True:
+                if text[q] == "{":
+                    depth += 1
+                elif text[q] == "}":
+                    depth -= 1
+                    if depth == 0:
+                        break
+                q += 1
+            out.append(text[line_start:q + 1])
+            found = True
+            break
+        if not found:
+            raise RuntimeError("kernel %s not found in %s" % (name, path))
+    return "namespace SPH {\n" + "\n\n".join(out) + "\n}  // namespace SPH\n"
+
+
 def build(verbose=False):
     ref = reference_dir()
     src = os.path.join(ref, "src")
     if not os.path.isdir(os.path.join(src, "cuda")):
         return None
+    os.makedirs(OUT_DIR, exist_ok=True)
+    with open(os.path.join(OUT_DIR, "thermal_kernels.inc"), "w") as f:
+        f.write(extract_kernels(os.path.join(src, "cuda", "Thermal.cu"), THERMAL_KERNELS))
     cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
     inc = [
+        "-I" + OUT_DIR,
         "-I" + os.path.join(HERE, "ref_shim"),
         "-I" + os.path.join(src, "cuda"),
         "-I" + src,
@@ -41,7 +93,6 @@ def build(verbose=False):
     ]
     flags = ["-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-w",
              "-DTHRUST_DEVICE_SYSTEM=THRUST_DEVICE_SYSTEM_CPP", "-Wno-cpp"]
-    os.makedirs(OUT_DIR, exist_ok=True)
     objs = []
     for tu in ("ref_domain.cpp", "ref_nsearch.cpp", "ref_nastran.cpp"):
         obj = os.path.join(OUT_DIR, tu.replace(".cpp", ".o"))

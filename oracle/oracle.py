@@ -314,6 +314,8 @@ def ref_lib():
         pd = C.POINTER(C.c_double)
         L.wfr_add_trimesh.argtypes = [C.c_void_p, pd, C.c_int, C.POINTER(C.c_int32), C.c_int, pd,
                                       C.c_int, C.c_int64, pd, pd]
+        L.wfr_thermal_solve.argtypes = [C.c_void_p, C.c_int64, pd, pd, C.POINTER(C.c_int32),
+                                        C.c_double, C.c_double]
         _ref = L
     return _ref
 
@@ -381,6 +383,20 @@ class RefDomain:
 
     def begin(self):
         self.L.wfr_begin(self.h)
+
+    def thermal_solve(self, sc, nsteps):
+        """Domain_d::ThermalSolve's loop (Thermal.cu:188-260) for nsteps steps on a
+        heat scenario (positions, masses, density, h, k, c_p, T, BC_T, h_conv, T_inf)."""
+        n = self.n
+        from weldformgpu_gb300 import _abi as A
+        mat = A.WfMaterial(model=A.WF_BILINEAR, E=1.0, nu=0.3)
+        self.setup(sc["x"], sc["m"], np.zeros(n, np.int32), sc["h"], sc["rho"], 1.0, 1.0, 1.0,
+                   sc["dt"], 1.0, 0.0, mat, T=sc["T"])
+        k = np.full(n, float(sc["k"]))
+        cp = np.full(n, float(sc["cp"]))
+        bc = np.ascontiguousarray(sc["bc_t"], dtype=np.int32)
+        self.L.wfr_thermal_solve(self.h, int(nsteps), _p(k), _p(cp), _p(bc, C.c_int32),
+                                 float(sc["h_conv"]), float(sc["T_inf"]))
 
     def step(self, k):
         self.L.wfr_step(self.h, int(k))

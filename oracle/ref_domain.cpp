@@ -6,7 +6,8 @@
  *
  * The member functions called here (CalcDensInc, UpdateDensity,
  * CalcRateTensors, StressStrainOne, CalcAccel, ApplyBCVel, UpdatePosFraser,
- * UpdateVel, CalcIntEnergy) and the kernel PressureKernelExt are the
+ * UpdateVel, CalcIntEnergy) and the kernels PressureKernelExt,
+ * ThermalSolveKernel, CalcConvHeatKernel and TempCalcLeapfrog[First] are the
  * reference's, included verbatim from src/cuda/.  This file only allocates
  * the Domain_d arrays on the host, runs each kernel as a sequential loop
  * over its thread index, and calls them in MechFraserSolve's order
@@ -33,6 +34,10 @@
 #include "Mechanical.cu"
 #include "InteractionAlt.cu"
 #include "Energy.cu"   /* Mechanical.cu brings Geometry.cu, Contact.cu and Mesh.cu */
+/* Thermal.cu's four kernels, extracted verbatim by oracle/build_ref.py into the
+ * build directory (the file's host functions launch kernels with <<< >>>,
+ * which a host compiler cannot parse) */
+#include "thermal_kernels.inc"
 
 using namespace SPH;
 
@@ -129,6 +134,8 @@ void* wfr_create(int64_t n) {
   d->sigma_eq = alloc<double>(n); d->pl_strain = alloc<double>(n); d->sigma_y = alloc<double>(n);
   d->eff_strain_rate = alloc<double>(n); d->int_energy = alloc<double>(n);
   d->T = alloc<double>(n);
+  d->Ta = alloc<double>(n); d->Tb = alloc<double>(n); d->dTdt = alloc<double>(n);
+  d->k_T = alloc<double>(n); d->cp_T = alloc<double>(n); d->BC_T = alloc<int>(n);
   d->IsFree = alloc<bool>(n); d->NoSlip = alloc<bool>(n); d->ID = alloc<int>(n);
   /* contact arrays (WeldFormGPU.cu:503-511, Domain_d.cu:160-170) */
   d->not_write_surf_ID = alloc<bool>(n);
@@ -161,6 +168,7 @@ void wfr_destroy(void* h) {
                   d->h, d->m, d->rho, d->rho_0, d->p, d->PresEq, d->Cs, d->P0, d->FPMassC,
                   d->G, d->drho, d->sigma, d->strrate, d->rotrate, d->shearstress, d->strain,
                   d->sigma_eq, d->pl_strain, d->sigma_y, d->eff_strain_rate, d->int_energy, d->T,
+                  d->Ta, d->Tb, d->dTdt, d->k_T, d->cp_T, d->BC_T,
                   d->IsFree, d->NoSlip, d->ID, d->mat, r->x_h, d->not_write_surf_ID,
                   d->contneib_count, d->contneib_part, d->mesh_id, d->contact_surf_id,
                   d->first_fem_particle_idx};
@@ -361,6 +369,43 @@ void wfr_step(void* h, int64_t nsteps) {
   }
 }
 
+/* Domain_d::ThermalSolve (Thermal.cu:188-260) for `nsteps` steps: the
+ * neighbour lists of the current positions as CSR (neib_part / neib_offs,
+ * which main builds before the call), then per step the array form of
+ * ThermalSolveKernel (:101-142), CalcConvHeatKernel (:36-64) with the
+ * domain's T_inf and the h_conv given (ThermalSolve passes its local
+ * h_conv = 100), and TempCalcLeapfrogFirst / TempCalcLeapfrog (:16-31). */
+void wfr_thermal_solve(void* h, int64_t nsteps, const double* k, const double* cp,
+                       const int32_t* bc_t, double h_conv, double T_inf) {
+  RefDom* r = (RefDom*)h;
+  Domain_d* d = r->dom;
+  const int64_t N = r->n;
+  for (int64_t i = 0; i < N; i++) {
+    d->k_T[i] = k[i];
+    d->cp_T[i] = cp[i];
+    d->BC_T[i] = bc_t[i];
+  }
+  d->T_inf = T_inf;
+  rebuild(r, d->x);
+  std::vector<int> offs(N + 1), part(r->nbl.size());
+  for (int64_t i = 0; i < N; i++) offs[i] = (int)r->nbo[i];
+  offs[N] = (int)(r->nbo[N - 1] + r->nbc[N - 1]);
+  for (size_t q = 0; q < part.size(); q++) part[q] = (int)r->nbl[q];
+  d->isfirst_step = true;
+  for (int64_t s = 0; s < nsteps; s++) {
+    launch_seq(N, [&] { ThermalSolveKernel(d->dTdt, d->x, d->h, d->m, d->rho, d->T, d->k_T,
+                                           d->cp_T, part.data(), offs.data(), (int)N); });
+    launch_seq(N, [&] { CalcConvHeatKernel(d->dTdt, d->m, d->rho, d->cp_T, d->T, d->T_inf,
+                                           d->BC_T, h_conv, (int)N); });
+    if (d->isfirst_step) {
+      launch_seq(N, [&] { TempCalcLeapfrogFirst(d->T, d->Ta, d->Tb, d->dTdt, d->deltat, (int)N); });
+      d->isfirst_step = false;
+    } else {
+      launch_seq(N, [&] { TempCalcLeapfrog(d->T, d->Ta, d->Tb, d->dTdt, d->deltat, (int)N); });
+    }
+  }
+}
+
 /* copies a named field out, layout as in the product ABI */
 int wfr_get(void* h, const char* name, double* out) {
   RefDom* r = (RefDom*)h;
@@ -389,6 +434,10 @@ int wfr_get(void* h, const char* name, double* out) {
   else if (s == "int_energy") cp(d->int_energy, 1);
   else if (s == "normal") cp3(d->normal);
   else if (s == "contforce") cp3(d->contforce);
+  else if (s == "T") cp(d->T, 1);
+  else if (s == "Ta") cp(d->Ta, 1);
+  else if (s == "Tb") cp(d->Tb, 1);
+  else if (s == "dTdt") cp(d->dTdt, 1);
   else return -1;
   return 0;
 }

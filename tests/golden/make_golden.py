@@ -2,7 +2,7 @@
 
 The reference's own kernel sources (cuNSearch's neighbour kernels and
 Domain_d's CalcDensInc / CalcRateTensors / StressStrainOne / CalcAccel /
-UpdatePosFraser / ... ) are compiled for the CPU by oracle/build_ref.py and
+UpdatePosFraser / ..., Thermal.cu's heat kernels) are compiled for the CPU by oracle/build_ref.py and
 run sequentially in MechFraserSolve's order (oracle/ref_domain.cpp).  This
 script drives them on small seeded scenarios and stores the outputs, so that
 the oracle (and through it the GPU path) can be checked on machines without
@@ -59,6 +59,18 @@ def run_fraser(sc, checkpoints):
 CONTACT_FIELDS = ["u", "normal", "contforce"]
 
 
+def run_thermal(checkpoints):
+    """ThermalSolve on the 16^3 heat box, one fresh run per checkpoint (steps)."""
+    hb = S.heat_box(n_side=16)
+    out = {}
+    for k in checkpoints:
+        R = O.RefDomain(hb["n"])
+        R.thermal_solve(hb, k)
+        for f in ("T", "Ta", "Tb", "dTdt"):
+            out["s%d_%s" % (k, f)] = R.get(f)
+    return out
+
+
 def main():
     lib = build_ref.build()
     if lib is None:
@@ -90,6 +102,10 @@ def main():
     ct = S.contact_cylinder(R=0.0025, H=0.005, dens=6, mu=(0.3, 0.2))
     np.savez_compressed(os.path.join(HERE, "fraser_contact.npz"),
                         **run_fraser(ct, [1, 200, 600]))
+    # 7. heat conduction only (ThermalSolve): 16^3 steel box, Gaussian hot
+    #    spot, convection on the outer layer; the reference's ThermalSolveKernel,
+    #    CalcConvHeatKernel and TempCalcLeapfrog[First] (src/cuda/Thermal.cu:16-142)
+    np.savez_compressed(os.path.join(HERE, "thermal_box.npz"), **run_thermal([1, 100, 500]))
     print("golden vectors written to", HERE)
     return 0
 

@@ -490,3 +490,32 @@ def test_oracle_newton_cap_counted():
     ok = _oracle(sc, {"return_map": 1})
     ok.step(200)
     assert ok.get_scalar("newton_capped") == 0
+
+
+@pytest.mark.parametrize("k", [1, 100, 500])
+def test_heat_oracle_matches_reference_thermal_golden(k):
+    """Heat only (ThermalSolve): the oracle's conduction, convection and
+    leapfrog on the 16^3 heat box against the reference's own Thermal.cu
+    kernels (golden vectors), bit for bit at steps 1, 100 and 500."""
+    g = np.load(os.path.join(GOLDEN, "thermal_box.npz"))
+    hb = S.heat_box(n_side=16)
+    o = S.load_heat(O.OracleDomain(hb["n"]), hb)
+    o.thermal_solve((k - 0.5) * hb["dt"])
+    assert o.get_scalar("step") == k
+    for f in ("T", "Ta", "Tb", "dTdt"):
+        assert np.array_equal(o.get_field(f), g["s%d_%s" % (k, f)]), f
+
+
+def test_heat_oracle_matches_reference_thermal_live():
+    """The same against the reference's Thermal.cu kernels run here (skipped
+    where the reference tree is absent)."""
+    O._ref = None
+    if build_ref.build() is None or O.ref_lib() is None:
+        pytest.skip("reference tree not present")
+    hb = S.heat_box(n_side=12)
+    R = O.RefDomain(hb["n"])
+    R.thermal_solve(hb, 200)
+    o = S.load_heat(O.OracleDomain(hb["n"]), hb)
+    o.thermal_solve(199.5 * hb["dt"])
+    for f in ("T", "Ta", "Tb", "dTdt"):
+        assert np.array_equal(o.get_field(f), R.get(f)), f

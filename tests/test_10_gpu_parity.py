@@ -178,6 +178,27 @@ def test_heat_fp64_vs_oracle():
     np.testing.assert_allclose(g.get_field("T"), o.get_field("T"), rtol=1e-12)
 
 
+@pytest.mark.parametrize("k", [1, 100, 500])
+def test_heat_fp64_vs_reference_thermal_golden(k):
+    """Heat only on the GPU (plain FP64) against the reference's own
+    Thermal.cu kernels (golden vectors, 16^3 box with convection): T, Ta, Tb
+    within 1e-12 relative (CUDA's pow in the convection term may differ from
+    the host's in the last bit); the rate dT/dt, a sum of differences of
+    nearly equal temperatures that amplifies those bits, within the plain
+    form's 1e-9."""
+    g = np.load(os.path.join(GOLDEN, "thermal_box.npz"))
+    sc = S.heat_box(n_side=16)
+    from weldformgpu_gb300 import Domain_d
+    d = S.load_heat(Domain_d(sc["n"]), sc)
+    d.thermal_solve((k - 0.5) * sc["dt"])
+    assert d.get_scalar("step") == k
+    for f in ("T", "Ta", "Tb"):
+        np.testing.assert_allclose(d.get_field(f), g["s%d_%s" % (k, f)], rtol=1e-12, atol=0)
+    ref = g["s%d_dTdt" % k]
+    np.testing.assert_allclose(d.get_field("dTdt"), ref, rtol=1e-9,
+                               atol=1e-9 * np.abs(ref).max())
+
+
 def test_heat_mixed_flux_vs_fp64():
     sc = S.heat_box(n_side=16)
     from weldformgpu_gb300 import Domain_d
@@ -399,6 +420,41 @@ def test_mixed_fused_integration_bit_identical_to_separate_pass():
         for f in ("x", "u", "v", "a", "rho", "pl_strain", "sigma_eq", "T"):
             assert np.array_equal(fused.get_field(f), sep.get_field(f)), (n, f)
     assert sep.get_field("pl_strain").max() > 0.0
+
+
+@pytest.mark.parametrize("cap_max", [2048, 700])
+def test_tile_staging_bit_identical_to_global_gathers(cap_max):
+    """The mixed pair passes reading neighbours from per-tile halos in shared
+    memory give the same bits as the passes gathering from global memory:
+    JC with coupled heat and the tensor-core network, 300 steps with light
+    rebuilds and a periodic reorder.  With tile_cap_max 700 part of the tiles
+    exceed the halo capacity and gather from global memory inside the same
+    launches."""
+    from weldformgpu_gb300 import mlp
+    sc = S.jc_compression(R=0.006, H=0.012)
+    opts = {"return_map": 1, "thermal": 1, "taylor_quinney": 0.9, "rebuild_every": 5,
+            "rebuild_current_positions": 1, "rebuild_after_yield": 0, "precision": 1,
+            "tile_cap_max": cap_max}
+    runs = []
+    for staging in (1, 0):
+        d = gpu(sc, dict(opts, tile_staging=staging))
+        d.set_mlp_weights(mlp.init_params(3))
+        d.set_option("mlp", 1)
+        d.step(300)
+        runs.append({f: d.get_field(f) for f in ("x", "v", "u", "shearstress", "pl_strain",
+                                                 "sigma_eq", "T", "rho")})
+        if staging:
+            tiles = (sc["n"] + 127) // 128
+            staged = d.get_scalar("tiles_staged")
+            hmax = d.get_scalar("tile_halo_max")
+            if cap_max == 2048:
+                assert staged == tiles, (staged, tiles)
+            else:
+                assert 0 < staged < tiles and hmax > cap_max, (staged, tiles, hmax)
+        else:
+            assert d.get_scalar("tile_cap") == 0
+    for f in runs[0]:
+        assert np.array_equal(runs[0][f], runs[1][f]), f
 
 
 def test_mixed_fused_heat_matches_separate_heat_pass():

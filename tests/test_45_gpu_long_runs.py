@@ -1,0 +1,82 @@
+"""GPU: full-length runs from rest.
+
+  - The 5,000-step bilinear compression (R 5 mm, H 10 mm, dx 0.5 mm jittered
+    lattice, ~6.3k particles, dt 0.4 h/c, neighbour rebuild every 10 steps):
+    the plain FP64 form against the oracle over all 5,000 steps, bit for bit
+    (np.array_equal), with the output rows' maxima equal and their sums within
+    1e-12 of the summed magnitudes.
+  - A reduced Johnson-Cook thermo-mechanical compression (R 6 mm, H 12 mm,
+    dx 0.5 mm jittered lattice, platen -10 m/s, Taylor-Quinney 0.9, consistent
+    Newton return map, coupled heat, rebuild every 5 steps) from rest for
+    5,000 steps (20 % height reduction): the mixed form against the plain FP64
+    form of the same code within 1e-3 relative L2 on u, pl_strain, sigma_eq,
+    the temperature rise and the top platen's reaction curve (every step).
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests import scenarios as S
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu(sc, options=None):
+    from weldformgpu_gb300 import Domain_d
+    return S.load(Domain_d(sc["n"]), sc, options)
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, dtype=np.float64).ravel()
+    b = np.asarray(b, dtype=np.float64).ravel()
+    den = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (den if den > 0 else 1.0)
+
+
+def test_bilinear_compression_5000_steps_fp64_bit_exact_vs_oracle():
+    sc = S.compression_cylinder(R=0.005, H=0.010, generator="lattice", dt_rule="baseline")
+    assert 6000 < sc["n"] < 6600
+    opts = {"rebuild_every": 10, "rebuild_current_positions": 1, "rebuild_after_yield": 0,
+            "output_interval": 500 * sc["dt"]}
+    g = gpu(sc, opts)
+    O.set_threads(0)
+    o = S.load(O.OracleDomain(sc["n"]), sc, opts)
+    g.step(5000)
+    o.step(5000)
+    assert o.get_field("pl_strain").max() > 0.01            # well into the plastic range
+    for f in ("x", "u", "v", "rho", "sigma", "pl_strain", "sigma_eq", "sigma_y", "int_energy"):
+        assert np.array_equal(g.get_field(f), o.get_field(f)), f
+    assert g.get_scalar("rebuilds") == o.get_scalar("rebuilds") == 500
+    rg, ro = g.get_output_series(), o.get_output_series()
+    assert len(rg) == len(ro) >= 9
+    np.testing.assert_array_equal(rg[:, :6], ro[:, :6])
+    zones = [int((sc["ids"] == z).sum()) for z, _ in sc["bcs"]]
+    for k in range(6, rg.shape[1]):
+        b = (k - 11) // 3 if k >= 11 else None
+        scale = np.abs(ro[:, 11 + 3 * b:14 + 3 * b]).max() if b is not None else np.abs(ro[:, k]).max()
+        terms = zones[b] if b is not None else sc["n"]
+        assert np.max(np.abs(rg[:, k] - ro[:, k])) <= 1e-12 * scale * terms, k
+
+
+def test_jc_thermomech_from_rest_5000_steps_mixed_within_1e3_of_fp64():
+    sc = S.jc_compression(R=0.006, H=0.012)
+    opts = {"return_map": 1, "thermal": 1, "taylor_quinney": 0.9, "rebuild_every": 5,
+            "rebuild_current_positions": 1, "rebuild_after_yield": 0, "energy_mode": 1,
+            "output_every_step": 1}
+    a = gpu(sc, dict(opts, precision=0))
+    b = gpu(sc, dict(opts, precision=1))
+    a.step(5000)
+    b.step(5000)
+    ps = a.get_field("pl_strain")
+    assert ps.max() > 0.1 and np.mean(ps > 0) > 0.5          # large plastic flow
+    errs = {}
+    for f in ("u", "pl_strain", "sigma_eq"):
+        errs[f] = rel_l2(b.get_field(f), a.get_field(f))
+    errs["T"] = rel_l2(b.get_field("T") - 20.0, a.get_field("T") - 20.0)
+    ra, rb = a.get_output_series(), b.get_output_series()
+    assert ra.shape == rb.shape == (5000, 11 + 6)
+    top = 11 + 3 * 1 + 2                                     # BC 1 (the platen), z
+    assert ra[-1, top] > 0.0
+    errs["reaction_curve"] = rel_l2(rb[:, top], ra[:, top])
+    for f, e in errs.items():
+        assert e <= 1e-3, (f, e, errs)

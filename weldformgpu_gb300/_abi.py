@@ -118,6 +118,7 @@ PRODUCT_ONLY = {
     "get_output_row": (C.c_int, [_vp, _pd, _i64, C.POINTER(_i64)]),
     "get_reaction": (C.c_int, [_vp, _i32, _pd]),
     "set_callback": (C.c_int, [_vp, _vp, _vp]),
+    "fp64_fma_peak": (C.c_int, [_pd, _pd]),
 }
 
 # int (*wf_after_fn)(wf_domain*, void*): the per-step host hook

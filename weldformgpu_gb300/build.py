@@ -24,7 +24,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=o
 NO_FMA = {"wf_step_fp64.cu", "wf_integrate.cu", "wf_contact.cu", "wf_outputs.cu"}
 SOURCES = ["wf_api.cu", "wf_nsearch.cu", "wf_step_fp64.cu", "wf_step_fp32.cu", "wf_integrate.cu",
            "wf_mlp.cu", "wf_setup.cpp", "wf_noalloc.cu", "wf_contact.cu", "wf_json.cpp",
-           "wf_outputs.cu"]
+           "wf_outputs.cu", "wf_measure.cu", "wf_tiles.cu"]
 
 
 def nvcc():

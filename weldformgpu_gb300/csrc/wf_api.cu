@@ -20,6 +20,7 @@
 #include "wf_common.cuh"
 #include "wf_mlp.cuh"
 #include "wf_nsearch.cuh"
+#include "wf_tiles.cuh"
 
 // wf_mlp.cu
 int wf_mlp_pack_device(const float* dparams, void* dpacked, cudaStream_t s);
@@ -88,6 +89,14 @@ struct wf_domain {
   unsigned long long* series_count = nullptr;
   bool out_every_step = false, row_recorded = false, print_outputs = false;
   bool lists_stale = false;    // positions replaced mid-run: rebuild at the next step
+  // tile halos of the staged mixed pair passes (wf_tiles.cuh), rebuilt with the lists
+  int32_t *t_hoff = nullptr, *t_hcnt = nullptr, *t_halo = nullptr;
+  uint16_t* t_nbl = nullptr;
+  int64_t t_halo_cap = 0;
+  int tile_staging = 0;        // option "tile_staging" (off: measured slower, see the design notes)
+  int tile_cap_max = WF_TILE_HALO_MAX;   // option "tile_cap_max": largest halo staged
+  int tile_cap = 0;            // halo capacity the current tiles were built for (0: none)
+  int tile_hmax = 0;           // largest halo of the last build (read at the next rebuild)
   // the per-step host hook (GeneralAfter)
   wf_after_fn after_fn = nullptr;
   void* after_user = nullptr;
@@ -341,6 +350,9 @@ static void layout_arena(wf_domain* d, Arena& A) {
   A.take(&d->s_orig, n); A.take(&d->d_mm, 8); A.take(&d->d_status, WF_STATUS_WORDS);
   A.take(&d->d_cstat, 2);
   A.take(&d->fr, n); A.take(&d->out_part, wf_out_partial_words(WF_MAX_BC));
+  d->t_halo_cap = 10 * n;      // halo entries: ~7 per slot on cell-sorted lattices
+  A.take(&d->t_hoff, n / WF_TILE); A.take(&d->t_hcnt, n / WF_TILE);
+  A.take(&d->t_halo, d->t_halo_cap); A.take(&d->t_nbl, (int64_t)WF_NB_ALLOC * n);
   A.take(&d->out_last, WF_ROW_FIXED + 3 * WF_MAX_BC); A.take(&d->series_count, 1);
   A.take(&d->d_stage, 6 * n); A.take(&d->mlp_w, WF_MLP_NPARAM);
   A.take(&d->mlp_packed, (int64_t)wf_mlp_packed_bytes());
@@ -580,9 +592,10 @@ static int rebuild(wf_domain* d, bool use_current, bool light = false) {
   WF_CUDA_OK(cudaMemcpyAsync(d->d_mm, mm_init, sizeof mm_init, cudaMemcpyHostToDevice, s));
   const float r = (float)(2.0 * d->h);                // SolverFraser.cu:72-82
   launch_minmax(n, d->pf, r, d->d_mm, s);
-  int mm[6];
+  int mm[8];   // bounds, then the largest halo of the previous tile build
   WF_CUDA_OK(cudaMemcpyAsync(mm, d->d_mm, sizeof mm, cudaMemcpyDeviceToHost, s));
   WF_CUDA_OK(cudaStreamSynchronize(s));
+  if (d->tile_cap > 0) d->tile_hmax = mm[6];
   grid_from_minmax(mm, r, &d->grid);
   const int64_t ncell = (int64_t)d->grid.dim[0] * d->grid.dim[1] * d->grid.dim[2];
   if (ncell > (int64_t)2000000000) return wf_fail(d, WF_ERR_NUMERIC, "neighbour grid too large");
@@ -610,6 +623,18 @@ static int rebuild(wf_domain* d, bool use_current, bool light = false) {
   launch_nblist(n, d->npad, d->pf2, d->grid, d->cell_count, full ? nullptr : d->s_src, d->nb,
                 d->nbc, d->d_status, s);
   d->launches += 8;
+  // tile halos for the staged mixed passes, sized by the previous build's
+  // largest halo (tiles with larger halos gather from global memory)
+  d->tile_cap = 0;
+  if (d->precision == 1 && d->tile_staging && d->meshes.empty()) {
+    int cap = d->tile_hmax > 0 ? ((d->tile_hmax + 64 + 63) / 64) * 64 : 1536;
+    cap = std::min(std::max(cap, std::min(256, d->tile_cap_max)), d->tile_cap_max);
+    WF_CUDA_OK(cudaMemsetAsync(d->d_mm + 6, 0, 2 * sizeof(int), s));
+    launch_tile_halo(n, d->npad, d->nb, d->nbc, d->t_hoff, d->t_hcnt, d->t_halo, d->t_halo_cap,
+                     d->t_nbl, cap, reinterpret_cast<unsigned*>(d->d_mm + 7), d->d_mm + 6, s);
+    d->tile_cap = cap;
+    d->launches += 1;
+  }
   if (d->F[d->cur].eps_rb) {       // adaptive rebuild: the strain this list was built at
     k_copy_d<<<nblk(n), 256, 0, s>>>(n, d->F[d->cur].eps_p, d->F[d->cur].eps_rb);
     d->launches += 1;
@@ -921,6 +946,8 @@ static int solve_step_launches(wf_domain* d) {
   NbBuffers N{d->nb, d->nbc};
   const bool mixed = d->precision == 1;
   bool integrated = false;
+  const TileHalo TH{d->t_hoff, d->t_hcnt, d->t_halo, d->t_nbl,
+                    (mixed && d->tile_staging && !P.contact) ? d->tile_cap : 0};
   if (!mixed) {
     { KTimer t(d, KID_DENSITY); launch_fp64_density(P, F, d->vd2, N, s); }          // :193-202
     { KTimer t(d, KID_STRESS); launch_fp64_stress(P, F, d->vd2, N, d->d_status, s); }  // :204-218
@@ -930,16 +957,16 @@ static int solve_step_launches(wf_domain* d) {
       KTimer t(d, KID_DENSITY);
       if (d->heat_pending)
         launch_fp32_density_heat(P, F, d->vd2, d->v32b, N, d->heat_pending_first ? 1 : 0,
-                                 d->chi > 0.0 ? 1 : 0, s);
+                                 d->chi > 0.0 ? 1 : 0, TH, s);
       else
         launch_fp32_density(P, F, d->vd2, d->v32b, N, s);
       d->heat_pending = false;
     }
     { KTimer t(d, KID_STRESS);
       launch_fp32_stress(P, F, d->v32b, d->sigr32, N, d->d_status,
-                         (d->mlp_on && d->mlp_loaded) ? d->mlp_packed : nullptr, &d->mlp_l1, s); }
+                         (d->mlp_on && d->mlp_loaded) ? d->mlp_packed : nullptr, &d->mlp_l1, TH, s); }
     if (!P.contact && d->fuse_integrate) {
-      { KTimer t(d, KID_ACCEL); launch_fp32_accel_integrate(P, F, d->v32b, d->sigr32, d->vd2, N, s); }
+      { KTimer t(d, KID_ACCEL); launch_fp32_accel_integrate(P, F, d->v32b, d->sigr32, d->vd2, N, TH, s); }
       std::swap(d->F[d->cur].p32, d->F[d->cur].p32n);   // the new positions become current
       integrated = true;
     } else {
@@ -1487,6 +1514,12 @@ int wf_set_option(wf_domain* d, const char* key, double v) {
       WF_CUDA_OK(dalloc(&d->log_count, 1, d->stream));
     }
   }
+  else if (k == "tile_staging") d->tile_staging = v != 0;   // takes effect at the next rebuild
+  else if (k == "tile_cap_max") {
+    if (!(v >= 1.0) || v > WF_TILE_HALO_MAX)
+      return wf_fail(d, WF_ERR_ARG, "tile_cap_max must be in [1, 2048]");
+    d->tile_cap_max = (int)v;
+  }
   else if (k == "graph") {
     if (d->capturing) return wf_fail(d, WF_ERR_STATE, "graph option changed inside a step segment");
     d->graph = v != 0;
@@ -1770,6 +1803,25 @@ int wf_get_scalar(wf_domain* d, const char* name, double* out) {
       WF_CUDA_OK(cudaStreamSynchronize(d->stream));
       return WF_OK;
     }
+  }
+  if (s == "tiles_staged" || s == "tile_halo_max" || s == "tile_cap") {
+    // the tiles of the last neighbour rebuild: how many were staged, the largest halo
+    if (s == "tile_cap") { *out = d->tile_cap; return WF_OK; }
+    if (d->tile_cap == 0) { *out = 0.0; return WF_OK; }
+    int rc = segment_end(d);
+    if (rc) return rc;
+    const int64_t tiles = d->npad / WF_TILE;
+    std::vector<int32_t> hc(tiles);
+    int mx = 0;
+    WF_CUDA_OK(cudaMemcpyAsync(hc.data(), d->t_hcnt, sizeof(int32_t) * tiles,
+                               cudaMemcpyDeviceToHost, d->stream));
+    WF_CUDA_OK(cudaMemcpyAsync(&mx, d->d_mm + 6, sizeof(int), cudaMemcpyDeviceToHost, d->stream));
+    WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+    if (s == "tile_halo_max") { *out = mx; return WF_OK; }
+    int64_t staged = 0;
+    for (int32_t h : hc) staged += h > 0;
+    *out = (double)staged;
+    return WF_OK;
   }
   if (s == "int_energy_sum") {
     std::vector<double> e(d->n);

@@ -298,16 +298,19 @@ void launch_contact_stage(const StepParams& P, const Fields& F, const NbBuffers&
                           float4* a32, cudaStream_t s);
 void launch_mesh_update(const StepParams& P, const Fields& F, int mixed, cudaStream_t s);
 void launch_mesh_plane(const StepParams& P, cudaStream_t s);
+struct TileHalo;
 // density pass of this step with the previous step's heat pass (mixed form)
 void launch_fp32_density_heat(const StepParams& P, const Fields& F, double4* vd2, float4* v32b,
-                              const NbBuffers& N, int first, int plastic_heat, cudaStream_t s);
+                              const NbBuffers& N, int first, int plastic_heat, const TileHalo& T,
+                              cudaStream_t s);
 struct MlpL1;
-// mlp_packed (the tcgen05 weight image) and mlp_l1 (layer 1) together, or neither
+// mlp_packed (the tcgen05 weight image) and mlp_l1 (layer 1) together, or neither;
+// T: the tiles' halos (T.cap = 0: every block gathers from global memory)
 void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b,
                         float* sigr32, const NbBuffers& N, int* status, const void* mlp_packed,
-                        const MlpL1* mlp_l1, cudaStream_t s);
+                        const MlpL1* mlp_l1, const TileHalo& T, cudaStream_t s);
 void launch_fp32_accel(const StepParams& P, const Fields& F, const float4* v32b,
                        const float* sigr32, float4* a32, const NbBuffers& N, cudaStream_t s);
 void launch_fp32_accel_integrate(const StepParams& P, const Fields& F, const float4* v32b,
                                  const float* sigr32, const double4* vd2, const NbBuffers& N,
-                                 cudaStream_t s);
+                                 const TileHalo& T, cudaStream_t s);

@@ -14,6 +14,7 @@
 #include "wf_integrate.cuh"
 #include "wf_mlp.cuh"
 #include "wf_tensor.cuh"
+#include "wf_tiles.cuh"
 
 namespace {
 
@@ -131,43 +132,47 @@ __global__ void __launch_bounds__(128) k_density32(StepParams P, Fields F,
 // mirror (T^n, written by the integration kernel), so each thread may update
 // its own FP64 temperature in place.  After a rebuild at the start of step
 // n+1 the heat flux of step n uses the new list (built for these positions).
-__global__ void __launch_bounds__(128, kDensMinBlocks) k_density_heat32(StepParams P, Fields F,
-                                                        double4* __restrict__ vd2,
-                                                        float4* __restrict__ v32b,
-                                                        const int32_t* __restrict__ nb,
-                                                        const int32_t* __restrict__ cnt,
-                                                        int first, int plastic_heat) {
+// The pair loop of the density + heat pass: kStaged reads the neighbours'
+// records from the tile's halo in shared memory through the local list (one
+// lane per particle), else from global memory through the slot list.
+template <bool kStaged>
+__device__ __forceinline__ void density_heat_pairs(const StepParams& P, const Fields& F,
+                                                   const float4* __restrict__ gp,
+                                                   const float4* __restrict__ gv,
+                                                   const float2* __restrict__ gt,
+                                                   const int32_t* __restrict__ nb,
+                                                   const uint16_t* __restrict__ nbl, int64_t i,
+                                                   int g, int c, float4 pi, float4 vi, float2 ti,
+                                                   bool solid, int32_t idi, float& drho_out,
+                                                   float& sf_out) {
   constexpr int W = WF_NB_BLK / kDensLanes;
   constexpr int NB = W < kDensBatch ? W : kDensBatch;   // neighbours gathered per batch
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int g = (int)(t & (kDensLanes - 1));
-  const int64_t i = t / kDensLanes;
-  if (i >= P.n) return;
-  const float4 pi = F.p32[i];
-  const float4 vi = F.v32[i];
-  const float2 ti = F.th32[i];
-  const bool solid = F.perm[i] < P.n_solid;
+  static_assert(!kStaged || kDensLanes == 1, "staged lists are read one lane per particle");
   const float invh = P.invhf, C = P.Cf, Ch = P.Chf;
-  const int32_t idi = F.id[i];
   float drho = 0.0f, sf = 0.0f;
-  const int c = cnt[i];
   int nx[W];
-  if (c > 0) nb_sub<W>(nb, P.npad, i, 0, g, nx);
+  if (c > 0) {
+    if constexpr (kStaged) nbl_block(nbl, P.npad, i, 0, nx);
+    else nb_sub<W>(nb, P.npad, i, 0, g, nx);
+  }
   for (int b = 0; WF_NB_BLK * b < c; b++) {
     int js[W];
 #pragma unroll
     for (int q = 0; q < W; q++) js[q] = nx[q];
     const int m = c - WF_NB_BLK * b - g * W;   // entries of this lane's sub-block in the list
-    if (c > WF_NB_BLK * (b + 1)) nb_sub<W>(nb, P.npad, i, b + 1, g, nx);
+    if (c > WF_NB_BLK * (b + 1)) {
+      if constexpr (kStaged) nbl_block(nbl, P.npad, i, b + 1, nx);
+      else nb_sub<W>(nb, P.npad, i, b + 1, g, nx);
+    }
 #pragma unroll
     for (int h = 0; h < W; h += NB) {
       float4 pj[NB], vj[NB];
       float2 tj[NB];
 #pragma unroll
       for (int q = 0; q < NB; q++) {
-        pj[q] = F.p32[js[h + q]];
-        vj[q] = F.v32[js[h + q]];
-        tj[q] = F.th32[js[h + q]];
+        pj[q] = gp[js[h + q]];
+        vj[q] = gv[js[h + q]];
+        tj[q] = gt[js[h + q]];
       }
 #pragma unroll
       for (int q = 0; q < NB; q++) {
@@ -180,13 +185,65 @@ __global__ void __launch_bounds__(128, kDensMinBlocks) k_density_heat32(StepPara
         const float dT = (ti.x - tj[q].x) + (ti.y - tj[q].y);
         sf += mr * dT * GK;
         // density rate (solid particles, contact filter)
-        if (solid && !(P.contact && !pass_ij(P, idi, F.id[js[h + q]]))) {
+        bool pass = solid;
+        if constexpr (!kStaged) pass = pass && !(P.contact && !pass_ij(P, idi, F.id[js[h + q]]));
+        if (pass) {
           const float vx = vi.x - vj[q].x, vy = vi.y - vj[q].y, vz = vi.z - vj[q].z;
           drho += mr * vi.w * ((vx * xx + vy * xy + vz * xz) * GK);
         }
       }
     }
   }
+  drho_out = drho;
+  sf_out = sf;
+}
+
+__global__ void __launch_bounds__(128, kDensMinBlocks) k_density_heat32(StepParams P, Fields F,
+                                                        double4* __restrict__ vd2,
+                                                        float4* __restrict__ v32b,
+                                                        const int32_t* __restrict__ nb,
+                                                        const int32_t* __restrict__ cnt,
+                                                        int first, int plastic_heat,
+                                                        const TileHalo T) {
+  // tile staging (one lane per particle: a block of 128 threads is one tile)
+  extern __shared__ __align__(16) uint8_t sdh[];
+  float4* sp = reinterpret_cast<float4*>(sdh);
+  float4* sv = sp + T.cap;
+  float2* st = reinterpret_cast<float2*>(sv + T.cap);
+  int staged = -1;
+  if (kDensLanes == 1 && T.cap > 0) {
+    float4* dst[2] = {sp, sv};
+    const float4* src[2] = {F.p32, F.v32};
+    const int H = T.hcnt[blockIdx.x];
+    if (H >= 0 && H <= T.cap) {                 // uniform over the block
+      const int32_t* hs = T.halo + T.hoff[blockIdx.x];
+      for (int k = threadIdx.x; k < H; k += blockDim.x) {
+        const int s = hs[k];
+        cp_async16(dst[0] + k, src[0] + s);
+        cp_async16(dst[1] + k, src[1] + s);
+        cp_async8(st + k, F.th32 + s);
+      }
+      cp_async_wait_all();
+      __syncthreads();
+      staged = H;
+    }
+  }
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int g = (int)(t & (kDensLanes - 1));
+  const int64_t i = t / kDensLanes;
+  if (i >= P.n) return;
+  const float4 pi = F.p32[i];
+  const float4 vi = F.v32[i];
+  const float2 ti = F.th32[i];
+  const bool solid = F.perm[i] < P.n_solid;
+  const int32_t idi = F.id[i];
+  float drho, sf;
+  const int c = cnt[i];
+  if (staged >= 0)
+    density_heat_pairs<true>(P, F, sp, sv, st, nb, T.nbl, i, g, c, pi, vi, ti, solid, idi, drho, sf);
+  else
+    density_heat_pairs<false>(P, F, F.p32, F.v32, F.th32, nb, T.nbl, i, g, c, pi, vi, ti, solid,
+                              idi, drho, sf);
   if constexpr (kDensLanes > 1) {
     const unsigned mask = group_mask<kDensLanes>();
 #pragma unroll
@@ -284,50 +341,61 @@ __device__ __forceinline__ void sigr32_split(T* base, int64_t npad, F4*& a, F2*&
 // neighbours gathered per batch in the stress pass (position and velocity)
 constexpr int kStressBatch = 4;
 
-__global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
-                                                  const float4* __restrict__ v32b,
-                                                  float* __restrict__ sigr32,
-                                                  const int32_t* __restrict__ nb,
-                                                  const int32_t* __restrict__ cnt,
-                                                  int* __restrict__ status,
-                                                  const uint4* __restrict__ mlp,
-                                                  const MlpL1 l1) {
-  // The MLP runs on the tensor cores (tcgen05) for the block's 128 particles
-  // at once: every thread of the block must reach it, so out-of-range and
-  // non-solid threads are predicated rather than returned before that point.
-  extern __shared__ __align__(1024) uint8_t smlp[];
-  mlp_umma_begin(smlp, mlp);
-  const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const bool valid = i0 < P.n;
-  const int64_t i = valid ? i0 : 0;
-  const float4 pi = F.p32[i];
-  const float4 vi = v32b[i];
-  const double rho_new = F.vd[i].w + P.dt * F.drho[i];
-  const double p = 0.0 + (P.Cs * P.Cs) * (rho_new - P.rho0);   // FP64: small density change
-  if (valid) F.p[i] = p;
-  const bool solid = valid && F.perm[i] < P.n_solid;
-  if (!mlp && !solid) return;
+// The rate-tensor pair loop of the stress pass (CalcRateTensors,
+// InteractionAlt.cu:262-383, in FP32): kStaged reads the neighbours' records
+// from the tile's halo in shared memory (gp, gv) through the local list, else
+// from global memory through the slot list.  acc = D xx yy zz xy yz xz, W xy
+// yz xz, with the off-diagonal sums doubled (halved by the caller).
+template <bool kStaged>
+__device__ __forceinline__ void stress_pairs(const StepParams& P, const Fields& F,
+                                             const float4* __restrict__ gp,
+                                             const float4* __restrict__ gv,
+                                             const int32_t* __restrict__ nb,
+                                             const uint16_t* __restrict__ nbl, int64_t i, int c,
+                                             float4 pi, float4 vi, float* acc) {
   const float invh = P.invhf, C = P.Cf, Ch = P.Chf;
   float Dxx = 0.f, Dyy = 0.f, Dzz = 0.f, Dxy = 0.f, Dyz = 0.f, Dxz = 0.f;
   float Wxy = 0.f, Wyz = 0.f, Wxz = 0.f;
-  const int c = solid ? cnt[i] : 0;
-  int4 lo = make_int4(0, 0, 0, 0), hi = lo;
-  if (c > 0) nb_block(nb, P.npad, i, 0, lo, hi);
+  int nx[8];
+  if (c > 0) {
+    if constexpr (kStaged) {
+      nbl_block(nbl, P.npad, i, 0, nx);
+    } else {
+      int4 lo, hi;
+      nb_block(nb, P.npad, i, 0, lo, hi);
+      nx[0] = lo.x; nx[1] = lo.y; nx[2] = lo.z; nx[3] = lo.w;
+      nx[4] = hi.x; nx[5] = hi.y; nx[6] = hi.z; nx[7] = hi.w;
+    }
+  }
   for (int b = 0; WF_NB_BLK * b < c; b++) {
-    const int js[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+    int js[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) js[q] = nx[q];
     const int m = c - WF_NB_BLK * b;
-    if (m > WF_NB_BLK) nb_block(nb, P.npad, i, b + 1, lo, hi);
+    if (m > WF_NB_BLK) {
+      if constexpr (kStaged) {
+        nbl_block(nbl, P.npad, i, b + 1, nx);
+      } else {
+        int4 lo, hi;
+        nb_block(nb, P.npad, i, b + 1, lo, hi);
+        nx[0] = lo.x; nx[1] = lo.y; nx[2] = lo.z; nx[3] = lo.w;
+        nx[4] = hi.x; nx[5] = hi.y; nx[6] = hi.z; nx[7] = hi.w;
+      }
+    }
 #pragma unroll
     for (int h = 0; h < WF_NB_BLK; h += kStressBatch) {
       float4 pj[kStressBatch], vj[kStressBatch];
 #pragma unroll
       for (int q = 0; q < kStressBatch; q++) {
-        pj[q] = F.p32[js[h + q]];
-        vj[q] = v32b[js[h + q]];
+        pj[q] = gp[js[h + q]];
+        vj[q] = gv[js[h + q]];
       }
 #pragma unroll
       for (int q = 0; q < kStressBatch; q++) {
-        if (h + q >= m || (P.contact && !pass_j(P, F.id[js[h + q]]))) continue;
+        if (h + q >= m) continue;
+        if constexpr (!kStaged) {
+          if (P.contact && !pass_j(P, F.id[js[h + q]])) continue;
+        }
         const float xx = pi.x - pj[q].x, xy = pi.y - pj[q].y, xz = pi.z - pj[q].z;
         // w = 2 s of the reference's s = -GK m_j / (2 rho_j); the off-diagonal
         // sums carry the factor 2 and are halved after the loop
@@ -352,6 +420,69 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
       }
     }
   }
+  acc[0] = Dxx; acc[1] = Dyy; acc[2] = Dzz; acc[3] = Dxy; acc[4] = Dyz; acc[5] = Dxz;
+  acc[6] = Wxy; acc[7] = Wyz; acc[8] = Wxz;
+}
+
+// Copies the tile's halo records into shared memory (every thread of the
+// block takes part; asynchronous 16-byte copies, then one barrier).  Returns
+// the halo size, or -1 when the tile is not staged (the block then gathers
+// from global memory).  n_arr arrays: dst[a][k] = src[a][halo[k]].
+__device__ __forceinline__ int stage_halo16(const TileHalo& T, int tile, int n_arr,
+                                            float4* const* dst, const float4* const* src) {
+  const int H = T.cap > 0 ? T.hcnt[tile] : -1;
+  if (H < 0 || H > T.cap) return -1;        // uniform over the block
+  const int32_t* hs = T.halo + T.hoff[tile];
+  for (int k = threadIdx.x; k < H; k += blockDim.x) {
+    const int s = hs[k];
+    for (int a = 0; a < n_arr; a++) cp_async16(dst[a] + k, src[a] + s);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  return H;
+}
+
+__global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
+                                                  const float4* __restrict__ v32b,
+                                                  float* __restrict__ sigr32,
+                                                  const int32_t* __restrict__ nb,
+                                                  const int32_t* __restrict__ cnt,
+                                                  int* __restrict__ status,
+                                                  const uint4* __restrict__ mlp,
+                                                  const MlpL1 l1, const TileHalo T) {
+  // The MLP runs on the tensor cores (tcgen05) for the block's 128 particles
+  // at once: every thread of the block must reach it, so out-of-range and
+  // non-solid threads are predicated rather than returned before that point.
+  // Dynamic shared memory: the network's region (when it runs), then the
+  // tile's halo records (positions, velocities) when the tile is staged.
+  extern __shared__ __align__(1024) uint8_t smlp[];
+  mlp_umma_begin(smlp, mlp);
+  float4* sp = reinterpret_cast<float4*>(smlp + (mlp ? WF_UMMA_SMEM : 0));
+  float4* sv = sp + T.cap;
+  int staged;
+  {
+    float4* dst[2] = {sp, sv};
+    const float4* src[2] = {F.p32, v32b};
+    staged = stage_halo16(T, blockIdx.x, 2, dst, src);
+  }
+  const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool valid = i0 < P.n;
+  const int64_t i = valid ? i0 : 0;
+  const float4 pi = F.p32[i];
+  const float4 vi = v32b[i];
+  const double rho_new = F.vd[i].w + P.dt * F.drho[i];
+  const double p = 0.0 + (P.Cs * P.Cs) * (rho_new - P.rho0);   // FP64: small density change
+  if (valid) F.p[i] = p;
+  const bool solid = valid && F.perm[i] < P.n_solid;
+  if (!mlp && !solid) return;
+  const int c = solid ? cnt[i] : 0;
+  float acc[9];
+  if (staged >= 0)
+    stress_pairs<true>(P, F, sp, sv, nb, T.nbl, i, c, pi, vi, acc);
+  else
+    stress_pairs<false>(P, F, F.p32, v32b, nb, T.nbl, i, c, pi, vi, acc);
+  float Dxx = acc[0], Dyy = acc[1], Dzz = acc[2], Dxy = acc[3], Dyz = acc[4], Dxz = acc[5];
+  float Wxy = acc[6], Wyz = acc[7], Wxz = acc[8];
   Dxy *= 0.5f; Dxz *= 0.5f; Dyz *= 0.5f;
   Wxy *= 0.5f; Wxz *= 0.5f; Wyz *= 0.5f;
   // Jaumann update with the reference's product
@@ -511,11 +642,33 @@ constexpr int kAccelLanes = 2;
 constexpr int kAccelBatch = 2;
 static_assert(WF_NB_BLK / kAccelLanes >= kAccelBatch, "batch within the lane's sub-block");
 
+// sub-block of lane g (entries 8b + g W .. 8b + g W + W - 1) of slot i's local list
+template <int W>
+__device__ __forceinline__ void nbl_sub(const uint16_t* __restrict__ nbl, int64_t npad, int64_t i,
+                                        int b, int g, int* js) {
+  const uint16_t* q = nbl + ((int64_t)b * npad + i) * WF_NB_BLK + g * W;
+  static_assert(W == 4, "local sub-blocks of 4 entries");
+  const uint2 v = __ldg(reinterpret_cast<const uint2*>(q));
+  js[0] = (int)(v.x & 0xffffu); js[1] = (int)(v.x >> 16);
+  js[2] = (int)(v.y & 0xffffu); js[3] = (int)(v.y >> 16);
+}
+
+// Neighbour records of the acceleration pass, from global memory (the slot
+// arrays) or from the tile's halo in shared memory (indexed by local list).
+struct AccelSrc {
+  const float4* p;
+  const float4* v;
+  const float4* sa;
+  const float2* sb;
+};
+
+template <bool kStaged>
 __device__ __forceinline__ float4 accel_value(const StepParams& P, const Fields& F,
                                               const float4* __restrict__ v32b,
                                               const float* __restrict__ sigr32,
                                               const int32_t* __restrict__ nb,
-                                              const int32_t* __restrict__ cnt, int64_t i, int g) {
+                                              const int32_t* __restrict__ cnt, int64_t i, int g,
+                                              const AccelSrc& src, const uint16_t* nbl) {
   constexpr int W = WF_NB_BLK / kAccelLanes;
   const float4 pi = F.p32[i];
   const float4 vi = v32b[i];
@@ -531,13 +684,19 @@ __device__ __forceinline__ float4 accel_value(const StepParams& P, const Fields&
   float ax = 0.f, ay = 0.f, az = 0.f;
   const int c = cnt[i];
   int nx[W];
-  if (c > 0) nb_sub<W>(nb, P.npad, i, 0, g, nx);
+  if (c > 0) {
+    if constexpr (kStaged) nbl_sub<W>(nbl, P.npad, i, 0, g, nx);
+    else nb_sub<W>(nb, P.npad, i, 0, g, nx);
+  }
   for (int b = 0; WF_NB_BLK * b < c; b++) {
     int js[W];
 #pragma unroll
     for (int q = 0; q < W; q++) js[q] = nx[q];
     const int m = c - WF_NB_BLK * b - g * W;   // entries of this lane's sub-block in the list
-    if (c > WF_NB_BLK * (b + 1)) nb_sub<W>(nb, P.npad, i, b + 1, g, nx);
+    if (c > WF_NB_BLK * (b + 1)) {
+      if constexpr (kStaged) nbl_sub<W>(nbl, P.npad, i, b + 1, g, nx);
+      else nb_sub<W>(nb, P.npad, i, b + 1, g, nx);
+    }
 #pragma unroll
     for (int hh = 0; hh < W; hh += kAccelBatch) {
       float4 pj[kAccelBatch], vj[kAccelBatch], t0[kAccelBatch];
@@ -545,14 +704,17 @@ __device__ __forceinline__ float4 accel_value(const StepParams& P, const Fields&
 #pragma unroll
       for (int q = 0; q < kAccelBatch; q++) {
         const int j = js[hh + q];
-        pj[q] = F.p32[j];
-        vj[q] = v32b[j];
-        t0[q] = sga[j];
-        t1[q] = sgb[j];
+        pj[q] = src.p[j];
+        vj[q] = src.v[j];
+        t0[q] = src.sa[j];
+        t1[q] = src.sb[j];
       }
 #pragma unroll
       for (int q = 0; q < kAccelBatch; q++) {
-        if (hh + q >= m || (P.contact && !pass_ij(P, idi, F.id[js[hh + q]]))) continue;
+        if (hh + q >= m) continue;
+        if constexpr (!kStaged) {
+          if (P.contact && !pass_ij(P, idi, F.id[js[hh + q]])) continue;
+        }
         const float xx = pi.x - pj[q].x, xy = pi.y - pj[q].y, xz = pi.z - pj[q].z;
         const float r2 = xx * xx + xy * xy + xz * xz;
         const float GK = gk32_r2(r2, invh, Ch, C) * pj[q].w;
@@ -603,7 +765,11 @@ __global__ void __launch_bounds__(128, 7) k_accel32(StepParams P, Fields F,
   int g;
   const int64_t i = accel_slot(g);
   if (i >= P.n || F.perm[i] >= P.n_solid) return;
-  const float4 af = accel_value(P, F, v32b, sigr32, nb, cnt, i, g);
+  const float4* sga;
+  const float2* sgb;
+  sigr32_split(sigr32, P.npad, sga, sgb);
+  const AccelSrc src{F.p32, v32b, sga, sgb};
+  const float4 af = accel_value<false>(P, F, v32b, sigr32, nb, cnt, i, g, src, nullptr);
   if (g == 0) a32[i] = af;
 }
 
@@ -623,9 +789,64 @@ __global__ void __launch_bounds__(128, 7) k_accel_int32(StepParams P, Fields F,
   int g;
   const int64_t i = accel_slot(g);
   if (i >= P.n) return;
+  const float4* sga;
+  const float2* sgb;
+  sigr32_split(sigr32, P.npad, sga, sgb);
+  const AccelSrc src{F.p32, v32b, sga, sgb};
   // rigid (non-solid) slots: zero acceleration, moved by their BCs
-  const float4 af = F.perm[i] < P.n_solid ? accel_value(P, F, v32b, sigr32, nb, cnt, i, g)
-                                           : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 af = F.perm[i] < P.n_solid
+                        ? accel_value<false>(P, F, v32b, sigr32, nb, cnt, i, g, src, nullptr)
+                        : make_float4(0.f, 0.f, 0.f, 0.f);
+  if (g == 0) integrate_mixed_one(P, F, vd2, i, af, p32n);
+}
+
+// The same pass for staged tiles: a block of 2 x 128 threads is one tile;
+// it copies the halo's positions, velocities and stress / rho^2 records into
+// shared memory, then reads the neighbours from there through the local
+// lists.  Tiles that are not staged gather from global memory.
+__global__ void __launch_bounds__(2 * WF_TILE, 3) k_accel_int32_tiles(
+    StepParams P, Fields F, const float4* __restrict__ v32b, const float* __restrict__ sigr32,
+    const double4* __restrict__ vd2, const int32_t* __restrict__ nb,
+    const int32_t* __restrict__ cnt, float4* __restrict__ p32n, const TileHalo T) {
+  static_assert(kAccelLanes == 2, "one tile per block of 2 lanes per slot");
+  extern __shared__ __align__(16) uint8_t sac[];
+  const float4* sga;
+  const float2* sgb;
+  sigr32_split(sigr32, P.npad, sga, sgb);
+  float4* sp = reinterpret_cast<float4*>(sac);
+  float4* sv = sp + T.cap;
+  float4* ssa = sv + T.cap;
+  float2* ssb = reinterpret_cast<float2*>(ssa + T.cap);
+  int staged = -1;
+  {
+    const int H = T.cap > 0 ? T.hcnt[blockIdx.x] : -1;
+    if (H >= 0 && H <= T.cap) {                 // uniform over the block
+      const int32_t* hs = T.halo + T.hoff[blockIdx.x];
+      for (int k = threadIdx.x; k < H; k += blockDim.x) {
+        const int s = hs[k];
+        cp_async16(sp + k, F.p32 + s);
+        cp_async16(sv + k, v32b + s);
+        cp_async16(ssa + k, sga + s);
+        cp_async8(ssb + k, sgb + s);
+      }
+      cp_async_wait_all();
+      __syncthreads();
+      staged = H;
+    }
+  }
+  int g;
+  const int64_t i = accel_slot(g);
+  if (i >= P.n) return;
+  float4 af = make_float4(0.f, 0.f, 0.f, 0.f);   // rigid (non-solid) slots: moved by their BCs
+  if (F.perm[i] < P.n_solid) {
+    if (staged >= 0) {
+      const AccelSrc src{sp, sv, ssa, ssb};
+      af = accel_value<true>(P, F, v32b, sigr32, nb, cnt, i, g, src, T.nbl);
+    } else {
+      const AccelSrc src{F.p32, v32b, sga, sgb};
+      af = accel_value<false>(P, F, v32b, sigr32, nb, cnt, i, g, src, nullptr);
+    }
+  }
   if (g == 0) integrate_mixed_one(P, F, vd2, i, af, p32n);
 }
 
@@ -638,17 +859,26 @@ void launch_fp32_density(const StepParams& P, const Fields& F, double4* vd2, flo
   k_density32<<<blocks_for(P.n, 128), 128, 0, s>>>(P, F, vd2, v32b, N.nb, N.cnt);
 }
 void launch_fp32_density_heat(const StepParams& P, const Fields& F, double4* vd2, float4* v32b,
-                              const NbBuffers& N, int first, int plastic_heat, cudaStream_t s) {
-  k_density_heat32<<<blocks_for(P.n * kDensLanes, 128), 128, 0, s>>>(P, F, vd2, v32b, N.nb, N.cnt, first,
-                                                        plastic_heat);
+                              const NbBuffers& N, int first, int plastic_heat, const TileHalo& T,
+                              cudaStream_t s) {
+  TileHalo Tl = T;
+  if (kDensLanes != 1) Tl.cap = 0;
+  const size_t smem = (2 * sizeof(float4) + sizeof(float2)) * (size_t)Tl.cap;
+  static size_t opted[64] = {};     // per device: dynamic shared memory opted in so far
+  opt_in_smem(k_density_heat32, smem, opted);
+  k_density_heat32<<<blocks_for(P.n * kDensLanes, 128), 128, smem, s>>>(
+      P, F, vd2, v32b, N.nb, N.cnt, first, plastic_heat, Tl);
 }
 void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b, float* sigr32,
                         const NbBuffers& N, int* status, const void* mlp_packed,
-                        const MlpL1* mlp_l1, cudaStream_t s) {
+                        const MlpL1* mlp_l1, const TileHalo& T, cudaStream_t s) {
   const uint4* W = reinterpret_cast<const uint4*>(mlp_packed);
   const MlpL1 l1 = (W && mlp_l1) ? *mlp_l1 : MlpL1{};
-  size_t smem = W ? WF_UMMA_SMEM : 0;
-  k_stress32<<<blocks_for(P.n, 128), 128, smem, s>>>(P, F, v32b, sigr32, N.nb, N.cnt, status, W, l1);
+  const size_t smem = (W ? WF_UMMA_SMEM : 0) + 2 * sizeof(float4) * (size_t)T.cap;
+  static size_t opted[64] = {};     // per device: dynamic shared memory opted in so far
+  opt_in_smem(k_stress32, smem, opted);
+  k_stress32<<<blocks_for(P.n, 128), 128, smem, s>>>(P, F, v32b, sigr32, N.nb, N.cnt, status, W, l1,
+                                                     T);
 }
 void launch_fp32_accel(const StepParams& P, const Fields& F, const float4* v32b,
                        const float* sigr32, float4* a32, const NbBuffers& N, cudaStream_t s) {
@@ -656,7 +886,15 @@ void launch_fp32_accel(const StepParams& P, const Fields& F, const float4* v32b,
 }
 void launch_fp32_accel_integrate(const StepParams& P, const Fields& F, const float4* v32b,
                                  const float* sigr32, const double4* vd2, const NbBuffers& N,
-                                 cudaStream_t s) {
+                                 const TileHalo& T, cudaStream_t s) {
+  if (T.cap > 0) {
+    const size_t smem = (3 * sizeof(float4) + sizeof(float2)) * (size_t)T.cap;
+    static size_t opted[64] = {};
+    opt_in_smem(k_accel_int32_tiles, smem, opted);
+    k_accel_int32_tiles<<<blocks_for(P.n * kAccelLanes, 2 * WF_TILE), 2 * WF_TILE, smem, s>>>(
+        P, F, v32b, sigr32, vd2, N.nb, N.cnt, F.p32n, T);
+    return;
+  }
   k_accel_int32<<<blocks_for(P.n * kAccelLanes, 128), 128, 0, s>>>(P, F, v32b, sigr32, vd2, N.nb, N.cnt,
                                                      F.p32n);
 }

@@ -1,0 +1,70 @@
+// wf_tiles.cuh — neighbour halos of slot tiles, for the staged pair passes.
+//
+// A tile is WF_TILE consecutive slots, the particles of one block of a mixed
+// pair pass.  Its halo is the ascending list of distinct slots that its
+// particles' neighbour lists name (its own slots included).  The block copies
+// the halo's gathered records (positions, velocities, ...) into shared memory
+// once, with asynchronous 16-byte copies, and its threads then read their
+// neighbours from shared memory through local lists: 16-bit indices into the
+// halo, stored like the slot lists (blocks of 8 entries, nb_at).  The
+// neighbours are the same, in the same order, so the FP32 sums are those of
+// the unstaged passes bit for bit.
+#pragma once
+#include "wf_common.cuh"
+
+#define WF_TILE 128                 // slots per tile
+#define WF_TILE_HALO_MAX 2048       // largest halo a pass stages (records in shared memory)
+#define WF_TILE_WIN_WORDS 8192      // bitmap words of the builder: a window of 262,144 slots
+
+struct TileHalo {
+  const int32_t* hoff;    // [tiles] offset of the tile's halo in `halo` (a multiple of 4)
+  const int32_t* hcnt;    // [tiles] halo size; -1: not staged (the pass gathers from global)
+  const int32_t* halo;    // halo slots, ascending per tile
+  const uint16_t* nbl;    // local lists, layout of nb (nb_at)
+  int cap;                // halo size the passes' shared memory holds (0: staging off)
+};
+
+// Builds the halos and local lists of every tile from the slot lists (nb,
+// cnt) for halos of at most `cap` slots; tiles whose halo is larger, or whose
+// slots span more than the builder's window, get hcnt = -1.  The largest halo
+// found (staged or not) is atomicMax-ed into *hmax.  `halo` holds
+// `halo_cap` entries; tiles that find it full are not staged.
+void launch_tile_halo(int64_t n, int64_t npad, const int32_t* nb, const int32_t* cnt,
+                      int32_t* hoff, int32_t* hcnt, int32_t* halo, int64_t halo_cap,
+                      uint16_t* nbl, int cap, unsigned* halo_used, int* hmax, cudaStream_t s);
+
+// Lets `kernel` use `bytes` of dynamic shared memory on the current device
+// (the attribute is per device; set once per device and larger size).
+template <class K>
+inline void opt_in_smem(K kernel, size_t bytes, size_t* opted /* [64] */) {
+  if (bytes <= 48 * 1024) return;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+  if (bytes <= opted[dev]) return;
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) ==
+      cudaSuccess)
+    opted[dev] = bytes;
+}
+
+// asynchronous global -> shared copies (cp.async; both addresses aligned to the size)
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+// block b (entries 8b .. 8b+7) of slot i's local list as one 16-byte load
+__device__ __forceinline__ void nbl_block(const uint16_t* __restrict__ nbl, int64_t npad,
+                                          int64_t i, int b, int js[8]) {
+  const uint4 q = __ldg(reinterpret_cast<const uint4*>(nbl + ((int64_t)b * npad + i) * WF_NB_BLK));
+  js[0] = (int)(q.x & 0xffffu); js[1] = (int)(q.x >> 16);
+  js[2] = (int)(q.y & 0xffffu); js[3] = (int)(q.y >> 16);
+  js[4] = (int)(q.z & 0xffffu); js[5] = (int)(q.z >> 16);
+  js[6] = (int)(q.w & 0xffffu); js[7] = (int)(q.w >> 16);
+}

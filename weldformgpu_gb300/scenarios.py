@@ -11,13 +11,18 @@ import numpy as np
 
 from . import _abi
 from . import setup as S
+from . import setup as _gen
 
 
 def compression_cylinder(R=0.0025, H=0.005, dx=0.0005, generator="reference", vz_top=-1.0,
-                         material="bilinear", jitter=0.01, seed=1, layers=2, dt_rule="reference"):
+                         material="bilinear", jitter=0.01, seed=1, layers=2, dt_rule="reference",
+                         gen=None):
     """Elastoplastic cylinder compression (the reference's Compression example
     shape; the 5,000-step benchmark case is R=5 mm, H=10 mm).  Bottom `layers` layers are
-    fixed (zone 2), top `layers` layers move at vz_top (zone 3)."""
+    fixed (zone 2), top `layers` layers move at vz_top (zone 3).  `gen` supplies
+    gen_cylinder_ref / gen_cylinder_lattice / assign_zone (default: the
+    library's; any module with the same functions, e.g. a CPU twin)."""
+    S = gen if gen is not None else _gen
     r = dx / 2.0
     rho = 2700.0
     if generator == "reference":
@@ -209,7 +214,8 @@ def load_heat(dom, sc):
     return dom
 
 
-def jc_compression(R=0.025, H=0.050, dx=0.0005, jitter=0.01, seed=1, vz_top=-10.0, layers=2):
+def jc_compression(R=0.025, H=0.050, dx=0.0005, jitter=0.01, seed=1, vz_top=-10.0, layers=2,
+                   gen=None):
     """Coupled thermo-mechanical Johnson-Cook compression (R 25 mm, H 50 mm, dx 0.5 mm):
     R = 25 mm, H = 50 mm, dx = 0.5 mm (~0.79M particles), jitter +-0.01 dx,
     JC A=324 MPa, B=114 MPa, n=0.42, C=0.002, m=1.34, eps0=1/s, Tref=20 C,
@@ -217,6 +223,7 @@ def jc_compression(R=0.025, H=0.050, dx=0.0005, jitter=0.01, seed=1, vz_top=-10.
     option by the caller); top `layers` layers at vz_top, bottom ones fixed;
     dt = 0.4 h / c."""
     sc = compression_cylinder(R=R, H=H, dx=dx, generator="lattice", jitter=jitter, seed=seed,
-                              vz_top=vz_top, material="jc", layers=layers, dt_rule="baseline")
+                              vz_top=vz_top, material="jc", layers=layers, dt_rule="baseline",
+                              gen=gen)
     sc["k"], sc["cp"] = 167.0, 896.0
     return sc
