@@ -531,6 +531,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-oracle baseline")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end arm")
     ap.add_argument("--no-mlp", action="store_true", help="time the mixed form without the MLP")
+    ap.add_argument("--tiles", type=int, default=None,
+                    help="profiling runs: option tile_staging for the timed form")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the from-rest error run, the FP64 ceiling and the heat / "
                          "indentation workloads")
@@ -591,7 +593,8 @@ def main():
         # a profiling run of one form (e.g. under ncu)
         form = "mixed" if "mixed" in forms else "fp64"
         mlp = None if (args.no_mlp or form == "fp64") else train_mlp(sc, state)[0]
-        r = run_form(sc, form, args.steps, warmup, state, mlp)
+        extra = None if args.tiles is None else {"tile_staging": args.tiles}
+        r = run_form(sc, form, args.steps, warmup, state, mlp, extra_opts=extra)
         print(json.dumps({"profiling_run": True, "form": form,
                           "ms_per_step": r["elapsed_ms"] / args.steps,
                           "per_kernel_ms": r["per_kernel_ms"], "particles": n}))

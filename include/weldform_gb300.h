@@ -271,6 +271,7 @@ int wf_set_csv_output(wf_domain* d, const char* prefix);
 /* ---- the reference's input-file driver ---------------------------------
  * main of src/WeldFormGPU.cu:142-926: reads the reference's JSON keys
  * (Configuration, Materials, DomainBlocks Box / Cylinder, DomainZones,
+ * DomainBlocks File (an LS-DYNA keyword deck, wf_read_lsdyna),
  * RigidBodies Plane / File (Nastran), Contact, BoundaryConditions), builds and sets up the
  * domain as main does, runs MechFraserSolve(simTime, outTime) writing
  * out_<time>.csv into out_dir and test.csv at the end.  err (optional,
@@ -326,6 +327,19 @@ int64_t wf_gen_icosphere(double R, const double* center, int level, int lower_ha
  * unknown node id) and *n_nodes; with nodes (3 n_nodes) and tris (3 per
  * triangle, node positions) not NULL, fills them. */
 int64_t wf_read_nastran(const char* path, double* nodes, int32_t* tris, int64_t* n_nodes);
+/* Domain_d::ReadFromLSdyna (src/cuda/Domain_d.cu:236-281; the reference reads
+ * through the LSDynaReader submodule, absent from its tree, so this follows
+ * the public LS-DYNA keyword format): one particle per *ELEMENT_SPH card (NID,
+ * PID, MASS in fields of 8, 8, 16 characters, or comma-separated), in card
+ * order, at the position of its *NODE card (NID, X, Y, Z in fields of 8, 16,
+ * 16, 16, or comma-separated), with the card's mass; a particle whose node is
+ * listed in a *SET_NODE_LIST[_TITLE] (SID on its first card, node ids in
+ * fields of 10 on the following cards) takes the set's id, a later set
+ * overriding an earlier one, others 0.  '$' lines are comments.  Two-call
+ * protocol: with x, mass and ids NULL returns the particle count.  Negative:
+ * WF_ERR_IO (missing file, unreadable card), WF_ERR_ARG (no SPH element, an
+ * element naming an unknown node). */
+int64_t wf_read_lsdyna(const char* path, double* x, double* mass, int32_t* ids);
 /* Domain::AssignZone (src/Domain.cpp:989-1005): tags particles inside the
  * inclusive box [start, end]; returns how many. */
 int64_t wf_assign_zone(const double* x, int64_t n, const double* start, const double* end,

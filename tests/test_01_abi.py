@@ -162,3 +162,66 @@ def test_header_documents_reference_citations():
     for name in ("Set_h", "SetDensity", "SetShearModulus", "SetSigmay", "SetCs", "SetFreePart",
                  "SetID", "MechFraserSolve", "ThermalSolve", "WriteCSV"):
         assert name in text, name
+
+
+def _lsdyna_deck(path):
+    """An LS-DYNA keyword deck: *NODE in fixed fields (8, 16, 16, 16) and in
+    free format, *ELEMENT_SPH (fields 8, 8, 16; one free-format card), two node
+    sets (the second, titled, overrides the first for a shared node), comments,
+    keywords the reader skips, a node that no SPH element uses."""
+    lines = ["*KEYWORD", "$ SPH particles written by the test", "*NODE",
+             "$    nid               x               y               z",
+             "%8d%16s%16s%16s" % (7, "0.0", "0.0", "0.0"),
+             "%8d%16s%16s%16s" % (9, "1.0e-3", "-2.5E-4", "0.125"),
+             "12, 2.0e-3, 0.0, 1.0e-3",
+             "%8d%16s%16s%16s" % (15, "-1.5", "3.0", "4.0"),
+             "%8d%16s%16s%16s" % (99, "9.0", "9.0", "9.0"),
+             "*PART", "this card is skipped", "         1         1",
+             "*ELEMENT_SPH",
+             "$    nid     pid            mass",
+             "%8d%8d%16s" % (9, 1, "2.5e-6"),
+             "%8d%8d%16s" % (7, 1, "1.0e-6"),
+             "15, 1, 4.0e-6",
+             "%8d%8d%16s" % (12, 1, "3.0e-6"),
+             "*SET_NODE_LIST",
+             "%10d%10s%10s%10s%10s" % (2, "0.0", "0.0", "0.0", "0.0"),
+             "%10d%10d" % (7, 12),
+             "*SET_NODE_LIST_TITLE",
+             "top platen",
+             "%10d" % 3,
+             "%10d%10d%10d" % (12, 15, 99),
+             "*END"]
+    path.write_text("\n".join(lines) + "\n")
+    x = np.array([[1.0e-3, -2.5e-4, 0.125], [0.0, 0.0, 0.0], [-1.5, 3.0, 4.0], [2.0e-3, 0.0, 1.0e-3]])
+    m = np.array([2.5e-6, 1.0e-6, 4.0e-6, 3.0e-6])
+    ids = np.array([0, 2, 3, 3], np.int32)
+    return x, m, ids
+
+
+def test_lsdyna_reader_known_answer(tmp_path):
+    from weldformgpu_gb300.domain import lib
+    L = lib()
+    fn = L.wf_read_lsdyna
+    fn.restype = ctypes.c_int64
+    fn.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double),
+                   ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int32)]
+    deck = tmp_path / "particles.k"
+    ex, em, eid = _lsdyna_deck(deck)
+    n = fn(str(deck).encode(), None, None, None)
+    assert n == 4
+    x = np.empty(3 * n)
+    m = np.empty(n)
+    ids = np.empty(n, np.int32)
+    assert fn(str(deck).encode(), x.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+              m.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+              ids.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))) == 4
+    assert np.array_equal(x.reshape(-1, 3), ex) and np.array_equal(m, em)
+    assert np.array_equal(ids, eid)
+    assert fn(str(tmp_path / "none.k").encode(), None, None, None) == -6
+    bad = tmp_path / "bad.k"
+    bad.write_text("*NODE\n       1             0.0             0.0             0.0\n"
+                   "*ELEMENT_SPH\n       5       1          1.0e-6\n")
+    assert fn(str(bad).encode(), None, None, None) == -1        # element on an unknown node
+    empty = tmp_path / "empty.k"
+    empty.write_text("*NODE\n       1             0.0             0.0             0.0\n")
+    assert fn(str(empty).encode(), None, None, None) == -1      # no SPH element

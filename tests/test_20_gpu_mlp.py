@@ -43,6 +43,49 @@ def test_tensor_core_inference_close_to_fp64():
     assert np.corrcoef(ytc, y64)[0, 1] > 0.999
 
 
+def _bf16(x):
+    """Round float32 values to the nearest BF16 (ties to even), as float32."""
+    b = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    r = (b + 0x7FFF + ((b >> 16) & 1)) & 0xFFFF0000
+    return r.astype(np.uint32).view(np.float32)
+
+
+def test_tensor_core_inference_matches_bf16_forward():
+    """The tcgen05 path against a CPU forward that rounds like it: layer 1 in
+    FP32, its SiLU (h + h tanh h, h = z/2) rounded to BF16, W2 in BF16, layer 2
+    accumulated exactly, layer 3 in FP64.  Per sample the difference is
+    bounded by what the GPU rounds differently: its tanh.approx.bf16x2 in
+    layer 1 may land one BF16 step (2^-8 relative) away, and its
+    tanh.approx.f32 in layer 3 carries a relative error below 2^-10 -- so
+    |dy| <= sum_j |w3_j| (2^-10 |s_j| + 1.1 * 2^-7 sum_k |W2_jk| |a_k|) + 1e-6,
+    about a hundred times tighter than the FP64 comparison above."""
+    from weldformgpu_gb300 import mlp
+    rng = np.random.default_rng(7)
+    P = mlp.init_params(5).astype(np.float32)
+    P[256:320] = rng.normal(0.0, 0.2, 64)        # non-zero biases b1, b2
+    P[4416:4480] = rng.normal(0.0, 0.2, 64)
+    X = rng.uniform(-1, 1, (4096, 4)).astype(np.float32)
+    W1 = P[:256].reshape(64, 4).astype(np.float64)
+    b1 = P[256:320].astype(np.float64)
+    W2 = _bf16(P[320:4416]).reshape(64, 64).astype(np.float64)
+    b2 = P[4416:4480].astype(np.float64)
+    W3 = P[4480:4544].astype(np.float64)
+    b3 = float(P[4544])
+    z1 = (X.astype(np.float64) @ W1.T + b1).astype(np.float32)
+    h = _bf16(0.5 * z1).astype(np.float64)
+    t = _bf16(np.tanh(h).astype(np.float32)).astype(np.float64)
+    a = _bf16((h * t + h).astype(np.float32)).astype(np.float64)
+    v = a @ W2.T + b2
+    sv = 0.5 * v
+    y_emu = (W3 * (sv * np.tanh(sv) + sv)).sum(axis=1) + b3
+    bound = (np.abs(W3) * (2.0 ** -10 * np.abs(sv) +
+                           1.1 * 2.0 ** -7 * (np.abs(a) @ np.abs(W2).T))).sum(axis=1) + 1e-6
+    ytc = mlp.infer(P, X, tensor_cores=True).astype(np.float64)
+    err = np.abs(ytc - y_emu)
+    assert np.all(err <= bound), (err.max(), bound[np.argmax(err / bound)], (err / bound).max())
+    assert np.median(err) < 0.1 * np.median(bound)
+
+
 def _gain(mat, G, steps):
     from weldformgpu_gb300 import mlp
     P, loss = mlp.train_jc_warm_start(mat, G, n_synth=131072, steps=steps)

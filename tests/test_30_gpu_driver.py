@@ -235,3 +235,43 @@ def test_json_driver_contact_law1(tmp_path):
     inp.write_text(json.dumps(cfg))
     assert L.wf_run_json(str(inp).encode(), str(out).encode(), err, 512) != 0
     assert b"law" in err.value
+
+
+def test_json_driver_lsdyna_particle_file(tmp_path):
+    """DomainBlocks "File" (main's ReadFromLSdyna path, src/WeldFormGPU.cu:378-398):
+    the cylinder's particles written as an LS-DYNA keyword deck (*NODE,
+    *ELEMENT_SPH with masses, the fixed bottom zone as a *SET_NODE_LIST of id
+    2) give the run of the generator-built input, state for state."""
+    from weldformgpu_gb300.domain import LIB_PATH, lib
+    lib()
+    L = ctypes.CDLL(LIB_PATH)
+    L.wf_run_json.restype = ctypes.c_int
+    L.wf_run_json.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int64]
+    x, mass = P.gen_cylinder_ref((0.0, 0.0, 0.0), R, H, r, rho)
+    ns = len(x)
+    ids = np.zeros(ns, np.int32)
+    P.assign_zone(x, (-1, -1, -1), (1, 1, 0.0004), 2, ids, np.zeros(ns, np.uint8))
+    lines = ["*KEYWORD", "*NODE"]
+    lines += ["%d, %.17g, %.17g, %.17g" % (1000 + i, x[i, 0], x[i, 1], x[i, 2]) for i in range(ns)]
+    lines.append("*ELEMENT_SPH")
+    lines += ["%d, 1, %.17g" % (1000 + i, mass) for i in range(ns)]
+    lines += ["*SET_NODE_LIST", "2"]
+    zone = [1000 + i for i in range(ns) if ids[i] == 2]
+    lines += [", ".join(str(v) for v in zone[k:k + 8]) for k in range(0, len(zone), 8)]
+    lines.append("*END")
+    (tmp_path / "particles.k").write_text("\n".join(lines) + "\n")
+    cfg, zp = _inputs()
+    cfg["DomainBlocks"] = [{"type": "File", "fileName": "particles.k"}]
+    cfg.pop("DomainZones")
+    inp = tmp_path / "from_file.json"
+    inp.write_text(json.dumps(cfg, indent=1))
+    out = tmp_path / "run"
+    out.mkdir()
+    err = ctypes.create_string_buffer(512)
+    assert L.wf_run_json(str(inp).encode(), str(out).encode(), err, 512) == 0, err.value
+    head, rows = _csv(out / "test.csv")
+    d, n = _api_domain(zp)
+    assert rows.shape == (n, 29)
+    np.testing.assert_allclose(rows[:, 1:4], d.get_field("x"), rtol=2e-6, atol=1e-12)
+    np.testing.assert_allclose(rows[:, 19], d.get_field("pl_strain"), rtol=2e-6, atol=1e-12)
+    assert np.array_equal(rows[:, 0].astype(np.int32), d.get_field_i32("ID"))

@@ -627,7 +627,7 @@ static int rebuild(wf_domain* d, bool use_current, bool light = false) {
   // largest halo (tiles with larger halos gather from global memory)
   d->tile_cap = 0;
   if (d->precision == 1 && d->tile_staging && d->meshes.empty()) {
-    int cap = d->tile_hmax > 0 ? ((d->tile_hmax + 64 + 63) / 64) * 64 : 1536;
+    int cap = d->tile_hmax > 0 ? ((d->tile_hmax + 31) / 32) * 32 : 1536;
     cap = std::min(std::max(cap, std::min(256, d->tile_cap_max)), d->tile_cap_max);
     WF_CUDA_OK(cudaMemsetAsync(d->d_mm + 6, 0, 2 * sizeof(int), s));
     launch_tile_halo(n, d->npad, d->nb, d->nbc, d->t_hoff, d->t_hcnt, d->t_halo, d->t_halo_cap,

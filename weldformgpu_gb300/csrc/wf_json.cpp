@@ -271,6 +271,7 @@ bool run_input(const Json& root, const std::string& out_dir, const std::string& 
   read_vec3(db, "dim", L);
   std::vector<double> x;
   std::vector<int32_t> gen_ids;
+  std::vector<double> masses;              // per particle (a particle file), else `mass`
   double mass = 0.0;
   int64_t ns = 0;
   double slice = 2.0000001 * 3.14159265358979323846;   // the reference's default (:307)
@@ -296,8 +297,22 @@ bool run_input(const Json& root, const std::string& out_dir, const std::string& 
     ns = wf_gen_box(start[0], start[1], start[2], L[0], L[1], L[2], r, rho, nullptr, &mass);
     x.resize(3 * (size_t)ns);
     wf_gen_box(start[0], start[1], start[2], L[0], L[1], L[2], r, rho, x.data(), &mass);
+  } else if (domtype == "File") {
+    // particles from an LS-DYNA keyword deck (:378-398, Domain_d::ReadFromLSdyna)
+    std::string fname;
+    read_str(db, "fileName", fname);
+    if (fname.empty()) return run.fail(WF_ERR_ARG, "a File domain block needs fileName");
+    std::string path = fname;               // as given, else beside the input file
+    if (!std::ifstream(path) && !json_dir.empty()) path = json_dir + "/" + fname;
+    ns = wf_read_lsdyna(path.c_str(), nullptr, nullptr, nullptr);
+    if (ns == WF_ERR_IO) return run.fail(WF_ERR_IO, "cannot read particle file " + path);
+    if (ns <= 0) return run.fail(WF_ERR_ARG, "no SPH particles (or an unknown node) in " + path);
+    x.resize(3 * (size_t)ns);
+    masses.resize((size_t)ns);
+    gen_ids.resize((size_t)ns);
+    wf_read_lsdyna(path.c_str(), x.data(), masses.data(), gen_ids.data());
   } else {
-    return run.fail(WF_ERR_ARG, "domain type must be Box or Cylinder");
+    return run.fail(WF_ERR_ARG, "domain type must be Box, Cylinder or File");
   }
   if (ns <= 0) return run.fail(WF_ERR_ARG, "the domain block holds no particles");
   // DomainZones (:396-412); main then protects every zoned particle (:851-858)
@@ -393,7 +408,7 @@ bool run_input(const Json& root, const std::string& out_dir, const std::string& 
   std::vector<uint8_t> nwa((size_t)n, 0), fr((size_t)n, 1);
   for (int64_t i = 0; i < ns; i++) {
     for (int k = 0; k < 3; k++) xa[3 * i + k] = x[3 * i + k];
-    ma[i] = mass;
+    ma[i] = masses.empty() ? mass : masses[i];
     ida[i] = ids[i];
     nwa[i] = nw[i];
   }

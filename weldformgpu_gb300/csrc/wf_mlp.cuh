@@ -157,16 +157,20 @@ static __device__ __forceinline__ float mlp_umma_cta(uint8_t* sm, const float f[
   const int tid = threadIdx.x, warp = tid >> 5;
   const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(sm + WF_UMMA_TSLOT);
   const uint32_t s0 = umma::smem_addr(sm);
-  // the weight image started by mlp_umma_begin (long arrived by now); every
-  // thread waits, so no block leaves with the copy in flight
+  // No thread of the block wants a prediction: one barrier; warp 0 frees the
+  // tensor memory and thread 0 waits for the weight image started by
+  // mlp_umma_begin (the block must not retire with that copy in flight).
+  if (!__syncthreads_or(want)) {
+    if (warp == 0) umma::tmem_dealloc(tmem, 64);
+    if (tid == 0 && !umma::mbar_wait(s0 + WF_UMMA_MBAR_W, 0, kWaitLimit))
+      atomicOr(status, WF_STATUS_MMA_WAIT);
+    return -1.0f;
+  }
+  // the weight image (long arrived by now); every thread waits
   const bool image_ok = umma::mbar_wait(s0 + WF_UMMA_MBAR_W, 0, kWaitLimit);
   if (!__syncthreads_and(image_ok)) {
     if (warp == 0) umma::tmem_dealloc(tmem, 64);
     if (tid == 0) atomicOr(status, WF_STATUS_MMA_WAIT);
-    return -1.0f;
-  }
-  if (!__syncthreads_or(want)) {
-    if (warp == 0) umma::tmem_dealloc(tmem, 64);
     return -1.0f;
   }
   const uint32_t mbar = s0 + WF_UMMA_MBAR;

@@ -9,6 +9,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <array>
 #include <map>
 #include <string>
 #include <vector>
@@ -326,6 +327,114 @@ int64_t wf_read_nastran(const char* path, double* nodes, int32_t* tris, int64_t*
     }
   }
   return ne;
+}
+
+// LS-DYNA keyword deck with SPH particles: Domain_d::ReadFromLSdyna
+// (src/cuda/Domain_d.cu:236-281) reads it through the LSDynaReader submodule,
+// which the reference tree does not carry; this reader follows the public
+// keyword format.  One particle per *ELEMENT_SPH card, in card order, at its
+// node's *NODE position, with the card's mass; a particle whose node is in a
+// *SET_NODE_LIST takes that set's id (a later set wins), else 0.
+namespace {
+std::string trim(const std::string& t) {
+  size_t a = t.find_first_not_of(" \t\r"), b = t.find_last_not_of(" \t\r");
+  return a == std::string::npos ? std::string() : t.substr(a, b - a + 1);
+}
+// the fields of a data card: comma-separated (free format), else fixed widths
+std::vector<std::string> card_fields(const std::string& line, const std::vector<int>& widths) {
+  std::vector<std::string> f;
+  if (line.find(',') != std::string::npos) {
+    std::string cur;
+    for (char c : line) {
+      if (c == ',') { f.push_back(trim(cur)); cur.clear(); }
+      else cur += c;
+    }
+    f.push_back(trim(cur));
+    return f;
+  }
+  size_t p = 0;
+  for (int w : widths) {
+    f.push_back(p < line.size() ? trim(line.substr(p, (size_t)w)) : std::string());
+    p += (size_t)w;
+  }
+  return f;
+}
+bool to_num(const std::string& t, double* v) {
+  if (t.empty()) { *v = 0.0; return true; }
+  char* e = nullptr;
+  *v = strtod(t.c_str(), &e);
+  return e && *e == '\0';
+}
+}  // namespace
+
+int64_t wf_read_lsdyna(const char* path, double* x, double* mass, int32_t* ids) {
+  if (!path) return WF_ERR_ARG;
+  std::ifstream f(path);
+  if (!f) return WF_ERR_IO;
+  std::map<long long, std::array<double, 3>> node;
+  std::vector<std::pair<long long, double>> sph;   // (node id, mass), card order
+  std::vector<std::pair<long long, std::vector<long long>>> sets;
+  enum { NONE, NODE, SPH, SET_CARD1, SET_NODES, SET_TITLE } sec = NONE;
+  for (std::string line; std::getline(f, line);) {
+    if (!line.empty() && line.back() == '\r') line.pop_back();
+    if (line.empty() || line[0] == '$') continue;
+    if (line[0] == '*') {
+      std::string k = trim(line);
+      for (char& c : k) c = (char)toupper((unsigned char)c);
+      if (k == "*NODE") sec = NODE;
+      else if (k == "*ELEMENT_SPH") sec = SPH;
+      else if (k == "*SET_NODE_LIST") sec = SET_CARD1;
+      else if (k == "*SET_NODE_LIST_TITLE") sec = SET_TITLE;
+      else sec = NONE;
+      continue;
+    }
+    double v[4];
+    if (sec == NODE) {
+      const auto fl = card_fields(line, {8, 16, 16, 16});
+      if (fl.size() < 4 || !to_num(fl[0], &v[0]) || !to_num(fl[1], &v[1]) ||
+          !to_num(fl[2], &v[2]) || !to_num(fl[3], &v[3]))
+        return WF_ERR_IO;
+      node[(long long)v[0]] = {v[1], v[2], v[3]};
+    } else if (sec == SPH) {
+      const auto fl = card_fields(line, {8, 8, 16});
+      if (fl.size() < 3 || !to_num(fl[0], &v[0]) || !to_num(fl[2], &v[2])) return WF_ERR_IO;
+      sph.push_back({(long long)v[0], v[2]});
+    } else if (sec == SET_TITLE) {
+      sec = SET_CARD1;                       // the title line
+    } else if (sec == SET_CARD1) {
+      const auto fl = card_fields(line, {10, 10, 10, 10, 10, 10});
+      if (fl.empty() || !to_num(fl[0], &v[0])) return WF_ERR_IO;
+      sets.push_back({(long long)v[0], {}});
+      sec = SET_NODES;
+    } else if (sec == SET_NODES) {
+      const auto fl = card_fields(line, {10, 10, 10, 10, 10, 10, 10, 10});
+      for (const std::string& t : fl) {
+        if (t.empty()) continue;
+        if (!to_num(t, &v[0])) return WF_ERR_IO;
+        if (v[0] != 0.0) sets.back().second.push_back((long long)v[0]);
+      }
+    }
+  }
+  if (sph.empty()) return WF_ERR_ARG;
+  const int64_t n = (int64_t)sph.size();
+  for (const auto& e : sph)
+    if (node.find(e.first) == node.end()) return WF_ERR_ARG;
+  if (!x && !mass && !ids) return n;
+  std::map<long long, int64_t> particle_of;    // node id -> particle index
+  for (int64_t p = 0; p < n; p++) {
+    auto it = node.find(sph[p].first);
+    particle_of[sph[p].first] = p;
+    if (x) for (int k = 0; k < 3; k++) x[3 * p + k] = it->second[k];
+    if (mass) mass[p] = sph[p].second;
+    if (ids) ids[p] = 0;
+  }
+  if (ids)
+    for (const auto& st : sets)
+      for (long long nid : st.second) {
+        auto it = particle_of.find(nid);
+        if (it != particle_of.end()) ids[it->second] = (int32_t)st.first;
+      }
+  return n;
 }
 
 // TriMesh_d::AxisPlaneMesh (src/cuda/Mesh.cu:48-194), the rigid plane main

@@ -141,7 +141,7 @@ __device__ __forceinline__ void density_heat_pairs(const StepParams& P, const Fi
                                                    const float4* __restrict__ gv,
                                                    const float2* __restrict__ gt,
                                                    const int32_t* __restrict__ nb,
-                                                   const uint16_t* __restrict__ nbl, int64_t i,
+                                                   const uint16_t* sl, int64_t i,
                                                    int g, int c, float4 pi, float4 vi, float2 ti,
                                                    bool solid, int32_t idi, float& drho_out,
                                                    float& sf_out) {
@@ -152,7 +152,7 @@ __device__ __forceinline__ void density_heat_pairs(const StepParams& P, const Fi
   float drho = 0.0f, sf = 0.0f;
   int nx[W];
   if (c > 0) {
-    if constexpr (kStaged) nbl_block(nbl, P.npad, i, 0, nx);
+    if constexpr (kStaged) nbl_block_s(sl, threadIdx.x, 0, nx);
     else nb_sub<W>(nb, P.npad, i, 0, g, nx);
   }
   for (int b = 0; WF_NB_BLK * b < c; b++) {
@@ -161,7 +161,7 @@ __device__ __forceinline__ void density_heat_pairs(const StepParams& P, const Fi
     for (int q = 0; q < W; q++) js[q] = nx[q];
     const int m = c - WF_NB_BLK * b - g * W;   // entries of this lane's sub-block in the list
     if (c > WF_NB_BLK * (b + 1)) {
-      if constexpr (kStaged) nbl_block(nbl, P.npad, i, b + 1, nx);
+      if constexpr (kStaged) nbl_block_s(sl, threadIdx.x, b + 1, nx);
       else nb_sub<W>(nb, P.npad, i, b + 1, g, nx);
     }
 #pragma unroll
@@ -210,6 +210,7 @@ __global__ void __launch_bounds__(128, kDensMinBlocks) k_density_heat32(StepPara
   float4* sp = reinterpret_cast<float4*>(sdh);
   float4* sv = sp + T.cap;
   float2* st = reinterpret_cast<float2*>(sv + T.cap);
+  uint16_t* sl = reinterpret_cast<uint16_t*>(st + T.cap);
   int staged = -1;
   if (kDensLanes == 1 && T.cap > 0) {
     float4* dst[2] = {sp, sv};
@@ -223,6 +224,7 @@ __global__ void __launch_bounds__(128, kDensMinBlocks) k_density_heat32(StepPara
         cp_async16(dst[1] + k, src[1] + s);
         cp_async8(st + k, F.th32 + s);
       }
+      stage_lists(T.nbl, P.npad, blockIdx.x, sl);
       cp_async_wait_all();
       __syncthreads();
       staged = H;
@@ -240,9 +242,9 @@ __global__ void __launch_bounds__(128, kDensMinBlocks) k_density_heat32(StepPara
   float drho, sf;
   const int c = cnt[i];
   if (staged >= 0)
-    density_heat_pairs<true>(P, F, sp, sv, st, nb, T.nbl, i, g, c, pi, vi, ti, solid, idi, drho, sf);
+    density_heat_pairs<true>(P, F, sp, sv, st, nb, sl, i, g, c, pi, vi, ti, solid, idi, drho, sf);
   else
-    density_heat_pairs<false>(P, F, F.p32, F.v32, F.th32, nb, T.nbl, i, g, c, pi, vi, ti, solid,
+    density_heat_pairs<false>(P, F, F.p32, F.v32, F.th32, nb, nullptr, i, g, c, pi, vi, ti, solid,
                               idi, drho, sf);
   if constexpr (kDensLanes > 1) {
     const unsigned mask = group_mask<kDensLanes>();
@@ -340,6 +342,9 @@ __device__ __forceinline__ void sigr32_split(T* base, int64_t npad, F4*& a, F2*&
 
 // neighbours gathered per batch in the stress pass (position and velocity)
 constexpr int kStressBatch = 4;
+// hardening slope over 3G above which the warm-start network is asked: the
+// radial start's relative overshoot must exceed the network's error (~1e-2)
+constexpr float kMlpSteep = 0.02f;
 
 // The rate-tensor pair loop of the stress pass (CalcRateTensors,
 // InteractionAlt.cu:262-383, in FP32): kStaged reads the neighbours' records
@@ -351,7 +356,7 @@ __device__ __forceinline__ void stress_pairs(const StepParams& P, const Fields& 
                                              const float4* __restrict__ gp,
                                              const float4* __restrict__ gv,
                                              const int32_t* __restrict__ nb,
-                                             const uint16_t* __restrict__ nbl, int64_t i, int c,
+                                             const uint16_t* sl, int64_t i, int c,
                                              float4 pi, float4 vi, float* acc) {
   const float invh = P.invhf, C = P.Cf, Ch = P.Chf;
   float Dxx = 0.f, Dyy = 0.f, Dzz = 0.f, Dxy = 0.f, Dyz = 0.f, Dxz = 0.f;
@@ -359,7 +364,7 @@ __device__ __forceinline__ void stress_pairs(const StepParams& P, const Fields& 
   int nx[8];
   if (c > 0) {
     if constexpr (kStaged) {
-      nbl_block(nbl, P.npad, i, 0, nx);
+      nbl_block_s(sl, threadIdx.x, 0, nx);
     } else {
       int4 lo, hi;
       nb_block(nb, P.npad, i, 0, lo, hi);
@@ -374,7 +379,7 @@ __device__ __forceinline__ void stress_pairs(const StepParams& P, const Fields& 
     const int m = c - WF_NB_BLK * b;
     if (m > WF_NB_BLK) {
       if constexpr (kStaged) {
-        nbl_block(nbl, P.npad, i, b + 1, nx);
+        nbl_block_s(sl, threadIdx.x, b + 1, nx);
       } else {
         int4 lo, hi;
         nb_block(nb, P.npad, i, b + 1, lo, hi);
@@ -424,12 +429,14 @@ __device__ __forceinline__ void stress_pairs(const StepParams& P, const Fields& 
   acc[6] = Wxy; acc[7] = Wyz; acc[8] = Wxz;
 }
 
-// Copies the tile's halo records into shared memory (every thread of the
-// block takes part; asynchronous 16-byte copies, then one barrier).  Returns
-// the halo size, or -1 when the tile is not staged (the block then gathers
-// from global memory).  n_arr arrays: dst[a][k] = src[a][halo[k]].
-__device__ __forceinline__ int stage_halo16(const TileHalo& T, int tile, int n_arr,
-                                            float4* const* dst, const float4* const* src) {
+// Copies the tile's halo records and local lists into shared memory (every
+// thread of the block takes part; asynchronous 16-byte copies, then one
+// barrier).  Returns the halo size, or -1 when the tile is not staged (the
+// block then gathers from global memory).  n_arr arrays: dst[a][k] =
+// src[a][halo[k]]; the lists go to sl.
+__device__ __forceinline__ int stage_halo16(const TileHalo& T, int64_t npad, int tile, int n_arr,
+                                            float4* const* dst, const float4* const* src,
+                                            uint16_t* sl) {
   const int H = T.cap > 0 ? T.hcnt[tile] : -1;
   if (H < 0 || H > T.cap) return -1;        // uniform over the block
   const int32_t* hs = T.halo + T.hoff[tile];
@@ -437,6 +444,7 @@ __device__ __forceinline__ int stage_halo16(const TileHalo& T, int tile, int n_a
     const int s = hs[k];
     for (int a = 0; a < n_arr; a++) cp_async16(dst[a] + k, src[a] + s);
   }
+  stage_lists(T.nbl, npad, tile, sl);
   cp_async_wait_all();
   __syncthreads();
   return H;
@@ -459,11 +467,12 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
   mlp_umma_begin(smlp, mlp);
   float4* sp = reinterpret_cast<float4*>(smlp + (mlp ? WF_UMMA_SMEM : 0));
   float4* sv = sp + T.cap;
+  uint16_t* sl = reinterpret_cast<uint16_t*>(sv + T.cap);
   int staged;
   {
     float4* dst[2] = {sp, sv};
     const float4* src[2] = {F.p32, v32b};
-    staged = stage_halo16(T, blockIdx.x, 2, dst, src);
+    staged = stage_halo16(T, P.npad, blockIdx.x, 2, dst, src, sl);
   }
   const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const bool valid = i0 < P.n;
@@ -478,9 +487,9 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
   const int c = solid ? cnt[i] : 0;
   float acc[9];
   if (staged >= 0)
-    stress_pairs<true>(P, F, sp, sv, nb, T.nbl, i, c, pi, vi, acc);
+    stress_pairs<true>(P, F, sp, sv, nb, sl, i, c, pi, vi, acc);
   else
-    stress_pairs<false>(P, F, F.p32, v32b, nb, T.nbl, i, c, pi, vi, acc);
+    stress_pairs<false>(P, F, F.p32, v32b, nb, nullptr, i, c, pi, vi, acc);
   float Dxx = acc[0], Dyy = acc[1], Dzz = acc[2], Dxy = acc[3], Dyz = acc[4], Dxz = acc[5];
   float Wxy = acc[6], Wyz = acc[7], Wxz = acc[8];
   Dxy *= 0.5f; Dxz *= 0.5f; Dyz *= 0.5f;
@@ -533,9 +542,16 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
   }
   double ratio = -1.0;
   if (mlp) {
-    // warm start: sigma_y0 from the cached power (FP32 suffices for the features)
+    // warm start: sigma_y0 from the cached power (FP32 suffices for the features).
+    // The network can only improve on the radial start where that start is
+    // poor: it overshoots the increment by about H' / (3G + H'), with the
+    // hardening slope H' = n B RT eps_p^(n - 1) = n B RT pwn / eps_p.  Where
+    // that is below the network's own prediction error (~1e-2) the radial
+    // start is the better one, and Newton needs one iteration from either.
     const float sy0f = ((float)M.A + (float)M.B * (float)fmax(pwn, 0.0)) * RTf;
-    const bool want = solid && jc_newton && st > sy0f;
+    const bool steep = !(eps_p > 0.0) || !(pwn > 0.0) ||
+                       P.jcnf * P.jcBf * RTf * (float)(pwn / eps_p) > kMlpSteep * P.G3f;
+    const bool want = solid && jc_newton && st > sy0f && steep;
     float f[4] = {0.f, 0.f, 0.f, 0.f};
     if (want) mlp_features(st / sy0f, eps_p, eff, Th, f);
     const float y = mlp_umma_cta(smlp, f, want, status, l1);
@@ -644,11 +660,10 @@ static_assert(WF_NB_BLK / kAccelLanes >= kAccelBatch, "batch within the lane's s
 
 // sub-block of lane g (entries 8b + g W .. 8b + g W + W - 1) of slot i's local list
 template <int W>
-__device__ __forceinline__ void nbl_sub(const uint16_t* __restrict__ nbl, int64_t npad, int64_t i,
-                                        int b, int g, int* js) {
-  const uint16_t* q = nbl + ((int64_t)b * npad + i) * WF_NB_BLK + g * W;
+__device__ __forceinline__ void nbl_sub_s(const uint16_t* sl, int t, int b, int g, int* js) {
+  const uint16_t* q = sl + (b * WF_TILE + t) * WF_NB_BLK + g * W;
   static_assert(W == 4, "local sub-blocks of 4 entries");
-  const uint2 v = __ldg(reinterpret_cast<const uint2*>(q));
+  const uint2 v = *reinterpret_cast<const uint2*>(q);
   js[0] = (int)(v.x & 0xffffu); js[1] = (int)(v.x >> 16);
   js[2] = (int)(v.y & 0xffffu); js[3] = (int)(v.y >> 16);
 }
@@ -685,7 +700,7 @@ __device__ __forceinline__ float4 accel_value(const StepParams& P, const Fields&
   const int c = cnt[i];
   int nx[W];
   if (c > 0) {
-    if constexpr (kStaged) nbl_sub<W>(nbl, P.npad, i, 0, g, nx);
+    if constexpr (kStaged) nbl_sub_s<W>(nbl, (int)(threadIdx.x >> 1), 0, g, nx);
     else nb_sub<W>(nb, P.npad, i, 0, g, nx);
   }
   for (int b = 0; WF_NB_BLK * b < c; b++) {
@@ -694,7 +709,7 @@ __device__ __forceinline__ float4 accel_value(const StepParams& P, const Fields&
     for (int q = 0; q < W; q++) js[q] = nx[q];
     const int m = c - WF_NB_BLK * b - g * W;   // entries of this lane's sub-block in the list
     if (c > WF_NB_BLK * (b + 1)) {
-      if constexpr (kStaged) nbl_sub<W>(nbl, P.npad, i, b + 1, g, nx);
+      if constexpr (kStaged) nbl_sub_s<W>(nbl, (int)(threadIdx.x >> 1), b + 1, g, nx);
       else nb_sub<W>(nb, P.npad, i, b + 1, g, nx);
     }
 #pragma unroll
@@ -817,6 +832,7 @@ __global__ void __launch_bounds__(2 * WF_TILE, 3) k_accel_int32_tiles(
   float4* sv = sp + T.cap;
   float4* ssa = sv + T.cap;
   float2* ssb = reinterpret_cast<float2*>(ssa + T.cap);
+  uint16_t* sl = reinterpret_cast<uint16_t*>(ssb + T.cap);
   int staged = -1;
   {
     const int H = T.cap > 0 ? T.hcnt[blockIdx.x] : -1;
@@ -829,6 +845,7 @@ __global__ void __launch_bounds__(2 * WF_TILE, 3) k_accel_int32_tiles(
         cp_async16(ssa + k, sga + s);
         cp_async8(ssb + k, sgb + s);
       }
+      stage_lists(T.nbl, P.npad, blockIdx.x, sl);
       cp_async_wait_all();
       __syncthreads();
       staged = H;
@@ -841,7 +858,7 @@ __global__ void __launch_bounds__(2 * WF_TILE, 3) k_accel_int32_tiles(
   if (F.perm[i] < P.n_solid) {
     if (staged >= 0) {
       const AccelSrc src{sp, sv, ssa, ssb};
-      af = accel_value<true>(P, F, v32b, sigr32, nb, cnt, i, g, src, T.nbl);
+      af = accel_value<true>(P, F, v32b, sigr32, nb, cnt, i, g, src, sl);
     } else {
       const AccelSrc src{F.p32, v32b, sga, sgb};
       af = accel_value<false>(P, F, v32b, sigr32, nb, cnt, i, g, src, nullptr);
@@ -863,7 +880,8 @@ void launch_fp32_density_heat(const StepParams& P, const Fields& F, double4* vd2
                               cudaStream_t s) {
   TileHalo Tl = T;
   if (kDensLanes != 1) Tl.cap = 0;
-  const size_t smem = (2 * sizeof(float4) + sizeof(float2)) * (size_t)Tl.cap;
+  const size_t smem =
+      Tl.cap > 0 ? (2 * sizeof(float4) + sizeof(float2)) * (size_t)Tl.cap + WF_TILE_LIST_BYTES : 0;
   static size_t opted[64] = {};     // per device: dynamic shared memory opted in so far
   opt_in_smem(k_density_heat32, smem, opted);
   k_density_heat32<<<blocks_for(P.n * kDensLanes, 128), 128, smem, s>>>(
@@ -874,7 +892,8 @@ void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b
                         const MlpL1* mlp_l1, const TileHalo& T, cudaStream_t s) {
   const uint4* W = reinterpret_cast<const uint4*>(mlp_packed);
   const MlpL1 l1 = (W && mlp_l1) ? *mlp_l1 : MlpL1{};
-  const size_t smem = (W ? WF_UMMA_SMEM : 0) + 2 * sizeof(float4) * (size_t)T.cap;
+  const size_t smem = (W ? WF_UMMA_SMEM : 0) +
+                      (T.cap > 0 ? 2 * sizeof(float4) * (size_t)T.cap + WF_TILE_LIST_BYTES : 0);
   static size_t opted[64] = {};     // per device: dynamic shared memory opted in so far
   opt_in_smem(k_stress32, smem, opted);
   k_stress32<<<blocks_for(P.n, 128), 128, smem, s>>>(P, F, v32b, sigr32, N.nb, N.cnt, status, W, l1,
@@ -888,7 +907,7 @@ void launch_fp32_accel_integrate(const StepParams& P, const Fields& F, const flo
                                  const float* sigr32, const double4* vd2, const NbBuffers& N,
                                  const TileHalo& T, cudaStream_t s) {
   if (T.cap > 0) {
-    const size_t smem = (3 * sizeof(float4) + sizeof(float2)) * (size_t)T.cap;
+    const size_t smem = (3 * sizeof(float4) + sizeof(float2)) * (size_t)T.cap + WF_TILE_LIST_BYTES;
     static size_t opted[64] = {};
     opt_in_smem(k_accel_int32_tiles, smem, opted);
     k_accel_int32_tiles<<<blocks_for(P.n * kAccelLanes, 2 * WF_TILE), 2 * WF_TILE, smem, s>>>(

@@ -59,6 +59,25 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
 
+// A staged tile's local lists in shared memory: block b of the tile's t-th
+// slot at sl[(b * WF_TILE + t) * 8] (the global layout with WF_TILE as stride)
+#define WF_TILE_LIST_BYTES (WF_NB_BLOCKS * WF_TILE * WF_NB_BLK * 2)
+
+// Copies the tile's local lists (all WF_NB_BLOCKS blocks, 2 KB each,
+// contiguous in global memory) into shared memory with 16-byte cp.async;
+// the caller waits (cp_async_wait_all + barrier).
+__device__ __forceinline__ void stage_lists(const uint16_t* __restrict__ nbl, int64_t npad,
+                                            int tile, uint16_t* sl);
+
+// block b (entries 8b .. 8b+7) of slot t's local list in shared memory
+__device__ __forceinline__ void nbl_block_s(const uint16_t* sl, int t, int b, int js[8]) {
+  const uint4 q = *reinterpret_cast<const uint4*>(sl + (b * WF_TILE + t) * WF_NB_BLK);
+  js[0] = (int)(q.x & 0xffffu); js[1] = (int)(q.x >> 16);
+  js[2] = (int)(q.y & 0xffffu); js[3] = (int)(q.y >> 16);
+  js[4] = (int)(q.z & 0xffffu); js[5] = (int)(q.z >> 16);
+  js[6] = (int)(q.w & 0xffffu); js[7] = (int)(q.w >> 16);
+}
+
 // block b (entries 8b .. 8b+7) of slot i's local list as one 16-byte load
 __device__ __forceinline__ void nbl_block(const uint16_t* __restrict__ nbl, int64_t npad,
                                           int64_t i, int b, int js[8]) {
@@ -67,4 +86,14 @@ __device__ __forceinline__ void nbl_block(const uint16_t* __restrict__ nbl, int6
   js[2] = (int)(q.y & 0xffffu); js[3] = (int)(q.y >> 16);
   js[4] = (int)(q.z & 0xffffu); js[5] = (int)(q.z >> 16);
   js[6] = (int)(q.w & 0xffffu); js[7] = (int)(q.w >> 16);
+}
+
+__device__ __forceinline__ void stage_lists(const uint16_t* __restrict__ nbl, int64_t npad,
+                                            int tile, uint16_t* sl) {
+  constexpr int kChunks = WF_NB_BLOCKS * WF_TILE;   // 16-byte pieces
+  for (int k = threadIdx.x; k < kChunks; k += blockDim.x) {
+    const int b = k / WF_TILE, t = k - b * WF_TILE;
+    cp_async16(sl + (int64_t)k * WF_NB_BLK,
+               nbl + ((int64_t)b * npad + (int64_t)tile * WF_TILE + t) * WF_NB_BLK);
+  }
 }
