@@ -425,7 +425,8 @@ def test_mixed_fused_integration_bit_identical_to_separate_pass():
 @pytest.mark.parametrize("cap_max", [2048, 700])
 def test_tile_staging_bit_identical_to_global_gathers(cap_max):
     """The mixed pair passes reading neighbours from per-tile halos in shared
-    memory give the same bits as the passes gathering from global memory:
+    memory, and those reading 16-bit lists (offsets from each tile's base
+    slot), give the same bits as the passes gathering through the 32-bit lists:
     JC with coupled heat and the tensor-core network, 300 steps with light
     rebuilds and a periodic reorder.  With tile_cap_max 700 part of the tiles
     exceed the halo capacity and gather from global memory inside the same
@@ -436,8 +437,8 @@ def test_tile_staging_bit_identical_to_global_gathers(cap_max):
             "rebuild_current_positions": 1, "rebuild_after_yield": 0, "precision": 1,
             "tile_cap_max": cap_max}
     runs = []
-    for staging in (1, 0):
-        d = gpu(sc, dict(opts, tile_staging=staging))
+    for staging in (1, 0, 2):                    # 2: global gathers through 16-bit lists
+        d = gpu(sc, dict(opts, tile_staging=1 if staging == 1 else 0, list16=int(staging == 2)))
         d.set_mlp_weights(mlp.init_params(3))
         d.set_option("mlp", 1)
         d.step(300)
@@ -455,6 +456,7 @@ def test_tile_staging_bit_identical_to_global_gathers(cap_max):
             assert d.get_scalar("tile_cap") == 0
     for f in runs[0]:
         assert np.array_equal(runs[0][f], runs[1][f]), f
+        assert np.array_equal(runs[2][f], runs[1][f]), f
 
 
 def test_mixed_fused_heat_matches_separate_heat_pass():

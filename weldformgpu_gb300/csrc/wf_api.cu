@@ -94,6 +94,12 @@ struct wf_domain {
   uint16_t* t_nbl = nullptr;
   int64_t t_halo_cap = 0;
   int tile_staging = 0;        // option "tile_staging" (off: measured slower, see the design notes)
+  int list_prefetch = 1;       // option "list_prefetch"
+  // 16-bit lists of the global gather path (wf_tiles.cuh), rebuilt with the lists
+  int list16 = 0;              // option "list16"
+  bool l16_built = false;
+  int32_t* l16_base = nullptr;
+  uint16_t* l16_off = nullptr;
   int tile_cap_max = WF_TILE_HALO_MAX;   // option "tile_cap_max": largest halo staged
   int tile_cap = 0;            // halo capacity the current tiles were built for (0: none)
   int tile_hmax = 0;           // largest halo of the last build (read at the next rebuild)
@@ -353,6 +359,7 @@ static void layout_arena(wf_domain* d, Arena& A) {
   d->t_halo_cap = 10 * n;      // halo entries: ~7 per slot on cell-sorted lattices
   A.take(&d->t_hoff, n / WF_TILE); A.take(&d->t_hcnt, n / WF_TILE);
   A.take(&d->t_halo, d->t_halo_cap); A.take(&d->t_nbl, (int64_t)WF_NB_ALLOC * n);
+  A.take(&d->l16_base, n / WF_TILE); A.take(&d->l16_off, (int64_t)WF_NB_ALLOC * n);
   A.take(&d->out_last, WF_ROW_FIXED + 3 * WF_MAX_BC); A.take(&d->series_count, 1);
   A.take(&d->d_stage, 6 * n); A.take(&d->mlp_w, WF_MLP_NPARAM);
   A.take(&d->mlp_packed, (int64_t)wf_mlp_packed_bytes());
@@ -416,6 +423,7 @@ static StepParams make_params(const wf_domain* d) {
     for (int c = 0; c < 3; c++) P.bc_v[b][c] = d->bc_v[b][c];
   }
   P.mlp_on = d->mlp_on;
+  P.nb_pf = d->list_prefetch;
   const wf_material& m = d->mat;
   MatParams& M = P.mat;
   M.model = m.model;
@@ -625,6 +633,12 @@ static int rebuild(wf_domain* d, bool use_current, bool light = false) {
   d->launches += 8;
   // tile halos for the staged mixed passes, sized by the previous build's
   // largest halo (tiles with larger halos gather from global memory)
+  d->l16_built = false;
+  if (d->precision == 1 && d->list16) {
+    launch_list16(n, d->npad, d->nb, d->nbc, d->l16_base, d->l16_off, s);
+    d->l16_built = true;
+    d->launches += 1;
+  }
   d->tile_cap = 0;
   if (d->precision == 1 && d->tile_staging && d->meshes.empty()) {
     int cap = d->tile_hmax > 0 ? ((d->tile_hmax + 31) / 32) * 32 : 1536;
@@ -948,6 +962,7 @@ static int solve_step_launches(wf_domain* d) {
   bool integrated = false;
   const TileHalo TH{d->t_hoff, d->t_hcnt, d->t_halo, d->t_nbl,
                     (mixed && d->tile_staging && !P.contact) ? d->tile_cap : 0};
+  const List16 L16{(mixed && d->list16 && d->l16_built) ? d->l16_base : nullptr, d->l16_off};
   if (!mixed) {
     { KTimer t(d, KID_DENSITY); launch_fp64_density(P, F, d->vd2, N, s); }          // :193-202
     { KTimer t(d, KID_STRESS); launch_fp64_stress(P, F, d->vd2, N, d->d_status, s); }  // :204-218
@@ -957,16 +972,18 @@ static int solve_step_launches(wf_domain* d) {
       KTimer t(d, KID_DENSITY);
       if (d->heat_pending)
         launch_fp32_density_heat(P, F, d->vd2, d->v32b, N, d->heat_pending_first ? 1 : 0,
-                                 d->chi > 0.0 ? 1 : 0, TH, s);
+                                 d->chi > 0.0 ? 1 : 0, TH, L16, s);
       else
         launch_fp32_density(P, F, d->vd2, d->v32b, N, s);
       d->heat_pending = false;
     }
     { KTimer t(d, KID_STRESS);
       launch_fp32_stress(P, F, d->v32b, d->sigr32, N, d->d_status,
-                         (d->mlp_on && d->mlp_loaded) ? d->mlp_packed : nullptr, &d->mlp_l1, TH, s); }
+                         (d->mlp_on && d->mlp_loaded) ? d->mlp_packed : nullptr, &d->mlp_l1, TH, L16,
+                         s); }
     if (!P.contact && d->fuse_integrate) {
-      { KTimer t(d, KID_ACCEL); launch_fp32_accel_integrate(P, F, d->v32b, d->sigr32, d->vd2, N, TH, s); }
+      { KTimer t(d, KID_ACCEL);
+        launch_fp32_accel_integrate(P, F, d->v32b, d->sigr32, d->vd2, N, TH, L16, s); }
       std::swap(d->F[d->cur].p32, d->F[d->cur].p32n);   // the new positions become current
       integrated = true;
     } else {
@@ -1515,6 +1532,8 @@ int wf_set_option(wf_domain* d, const char* key, double v) {
     }
   }
   else if (k == "tile_staging") d->tile_staging = v != 0;   // takes effect at the next rebuild
+  else if (k == "list_prefetch") d->list_prefetch = v != 0;
+  else if (k == "list16") d->list16 = v != 0;          // takes effect at the next rebuild
   else if (k == "tile_cap_max") {
     if (!(v >= 1.0) || v > WF_TILE_HALO_MAX)
       return wf_fail(d, WF_ERR_ARG, "tile_cap_max must be in [1, 2048]");

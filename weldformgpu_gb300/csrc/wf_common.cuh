@@ -35,6 +35,16 @@ __device__ __forceinline__ void nb_block(const int32_t* __restrict__ nb, int64_t
   hi = __ldg(q + 1);
 }
 
+// L2 prefetch of list block b of slot i, two blocks ahead of its use, so
+// that the list stream (read once per pass, from DRAM) meets L2 latency when
+// it is loaded; it holds no registers.  One thread of every `group` issues it
+// (a 128-byte line holds the blocks of four consecutive slots).
+__device__ __forceinline__ void nb_prefetch(const int32_t* nb, int64_t npad, int64_t i, int b,
+                                            int group) {
+  if ((threadIdx.x & (group - 1)) == 0)
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(nb + ((int64_t)b * npad + i) * WF_NB_BLK));
+}
+
 #define WF_MAX_BC 16
 #define WF_MAX_MESH 4
 #define WF_PI 3.14159265358979323846
@@ -180,6 +190,7 @@ struct StepParams {
   double4* fr;          // when not null (an output row is due this step): m a before the
                         // BCs are imposed, written at the slots of BC-zone particles
   int mlp_on;           // MLP warm start of the Newton return map
+  int nb_pf;            // L2 prefetch of the neighbour lists two blocks ahead (mixed passes)
   int refresh_pow;      // recompute eps_p^n with pow() this step (bounds series drift)
   int64_t log_cap;      // return-map log (training pairs for the MLP): capacity
   unsigned long long* log_count;
@@ -299,18 +310,21 @@ void launch_contact_stage(const StepParams& P, const Fields& F, const NbBuffers&
 void launch_mesh_update(const StepParams& P, const Fields& F, int mixed, cudaStream_t s);
 void launch_mesh_plane(const StepParams& P, cudaStream_t s);
 struct TileHalo;
-// density pass of this step with the previous step's heat pass (mixed form)
+struct List16;
+// density pass of this step with the previous step's heat pass (mixed form);
+// T: tile halos (T.cap = 0: none), L16: 16-bit lists (L16.base null: none)
 void launch_fp32_density_heat(const StepParams& P, const Fields& F, double4* vd2, float4* v32b,
                               const NbBuffers& N, int first, int plastic_heat, const TileHalo& T,
-                              cudaStream_t s);
+                              const List16& L16, cudaStream_t s);
 struct MlpL1;
 // mlp_packed (the tcgen05 weight image) and mlp_l1 (layer 1) together, or neither;
 // T: the tiles' halos (T.cap = 0: every block gathers from global memory)
 void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b,
                         float* sigr32, const NbBuffers& N, int* status, const void* mlp_packed,
-                        const MlpL1* mlp_l1, const TileHalo& T, cudaStream_t s);
+                        const MlpL1* mlp_l1, const TileHalo& T, const List16& L16,
+                        cudaStream_t s);
 void launch_fp32_accel(const StepParams& P, const Fields& F, const float4* v32b,
                        const float* sigr32, float4* a32, const NbBuffers& N, cudaStream_t s);
 void launch_fp32_accel_integrate(const StepParams& P, const Fields& F, const float4* v32b,
                                  const float* sigr32, const double4* vd2, const NbBuffers& N,
-                                 const TileHalo& T, cudaStream_t s);
+                                 const TileHalo& T, const List16& L16, cudaStream_t s);

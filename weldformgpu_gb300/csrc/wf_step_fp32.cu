@@ -40,29 +40,11 @@ __device__ __forceinline__ T3f mul_ref_f(const T3f& a, const T3f& b) {
 // ---- A32: density rate + update (InteractionAlt.cu:166-246, Mechanical.cu:198) --
 // Lane groups of the pair passes: kLanes consecutive lanes share one particle;
 // lane g of the group takes entries [8b + g W, 8b + (g + 1) W) of every list
-// block b (W = 8 / kLanes), and the lanes' partial sums are combined by an
-// xor-shuffle tree, which gives every lane of the group the same value.  A
-// warp then covers fewer particles and its gathers touch fewer L1 lines (the
-// neighbours of consecutive sorted particles overlap), and each lane's chain
-// of dependent gathers is shorter.
-template <int W>
-__device__ __forceinline__ void nb_sub(const int32_t* __restrict__ nb, int64_t npad, int64_t i,
-                                       int b, int g, int* js) {
-  const int32_t* q = nb + ((int64_t)b * npad + i) * WF_NB_BLK + g * W;
-  if constexpr (W == 8) {
-    const int4 lo = __ldg(reinterpret_cast<const int4*>(q));
-    const int4 hi = __ldg(reinterpret_cast<const int4*>(q) + 1);
-    js[0] = lo.x; js[1] = lo.y; js[2] = lo.z; js[3] = lo.w;
-    js[4] = hi.x; js[5] = hi.y; js[6] = hi.z; js[7] = hi.w;
-  } else if constexpr (W == 4) {
-    const int4 v = __ldg(reinterpret_cast<const int4*>(q));
-    js[0] = v.x; js[1] = v.y; js[2] = v.z; js[3] = v.w;
-  } else {
-    static_assert(W == 2, "list sub-block of 2, 4 or 8 entries");
-    const int2 v = __ldg(reinterpret_cast<const int2*>(q));
-    js[0] = v.x; js[1] = v.y;
-  }
-}
+// block b (W = 8 / kLanes, the list readers' sub<W>), and the lanes' partial
+// sums are combined by an xor-shuffle tree, which gives every lane of the
+// group the same value.  A warp then covers fewer particles and its gathers
+// touch fewer L1 lines (the neighbours of consecutive sorted particles
+// overlap), and each lane's chain of dependent gathers is shorter.
 
 // lane group of G lanes (a power of two) that share one particle
 template <int G>
@@ -132,38 +114,31 @@ __global__ void __launch_bounds__(128) k_density32(StepParams P, Fields F,
 // mirror (T^n, written by the integration kernel), so each thread may update
 // its own FP64 temperature in place.  After a rebuild at the start of step
 // n+1 the heat flux of step n uses the new list (built for these positions).
-// The pair loop of the density + heat pass: kStaged reads the neighbours'
-// records from the tile's halo in shared memory through the local list (one
-// lane per particle), else from global memory through the slot list.
-template <bool kStaged>
+// The pair loop of the density + heat pass over the neighbour list L: its
+// entries are slots (NbList32 / NbList16: records gathered from the global
+// arrays gp, gv, gt) or ranks in the tile's halo (NbListS: the arrays are its
+// shared-memory copies).
+template <class L>
 __device__ __forceinline__ void density_heat_pairs(const StepParams& P, const Fields& F,
                                                    const float4* __restrict__ gp,
                                                    const float4* __restrict__ gv,
-                                                   const float2* __restrict__ gt,
-                                                   const int32_t* __restrict__ nb,
-                                                   const uint16_t* sl, int64_t i,
+                                                   const float2* __restrict__ gt, const L& list,
                                                    int g, int c, float4 pi, float4 vi, float2 ti,
                                                    bool solid, int32_t idi, float& drho_out,
                                                    float& sf_out) {
   constexpr int W = WF_NB_BLK / kDensLanes;
   constexpr int NB = W < kDensBatch ? W : kDensBatch;   // neighbours gathered per batch
-  static_assert(!kStaged || kDensLanes == 1, "staged lists are read one lane per particle");
   const float invh = P.invhf, C = P.Cf, Ch = P.Chf;
   float drho = 0.0f, sf = 0.0f;
   int nx[W];
-  if (c > 0) {
-    if constexpr (kStaged) nbl_block_s(sl, threadIdx.x, 0, nx);
-    else nb_sub<W>(nb, P.npad, i, 0, g, nx);
-  }
+  if (c > 0) list.template sub<W>(0, g, nx);
   for (int b = 0; WF_NB_BLK * b < c; b++) {
     int js[W];
 #pragma unroll
     for (int q = 0; q < W; q++) js[q] = nx[q];
     const int m = c - WF_NB_BLK * b - g * W;   // entries of this lane's sub-block in the list
-    if (c > WF_NB_BLK * (b + 1)) {
-      if constexpr (kStaged) nbl_block_s(sl, threadIdx.x, b + 1, nx);
-      else nb_sub<W>(nb, P.npad, i, b + 1, g, nx);
-    }
+    if (P.nb_pf && c > WF_NB_BLK * (b + 2)) list.prefetch(b + 2, kDensLanes);
+    if (c > WF_NB_BLK * (b + 1)) list.template sub<W>(b + 1, g, nx);
 #pragma unroll
     for (int h = 0; h < W; h += NB) {
       float4 pj[NB], vj[NB];
@@ -186,7 +161,7 @@ __device__ __forceinline__ void density_heat_pairs(const StepParams& P, const Fi
         sf += mr * dT * GK;
         // density rate (solid particles, contact filter)
         bool pass = solid;
-        if constexpr (!kStaged) pass = pass && !(P.contact && !pass_ij(P, idi, F.id[js[h + q]]));
+        if constexpr (L::kSlots) pass = pass && !(P.contact && !pass_ij(P, idi, F.id[js[h + q]]));
         if (pass) {
           const float vx = vi.x - vj[q].x, vy = vi.y - vj[q].y, vz = vi.z - vj[q].z;
           drho += mr * vi.w * ((vx * xx + vy * xy + vz * xz) * GK);
@@ -204,7 +179,7 @@ __global__ void __launch_bounds__(128, kDensMinBlocks) k_density_heat32(StepPara
                                                         const int32_t* __restrict__ nb,
                                                         const int32_t* __restrict__ cnt,
                                                         int first, int plastic_heat,
-                                                        const TileHalo T) {
+                                                        const TileHalo T, const List16 L16) {
   // tile staging (one lane per particle: a block of 128 threads is one tile)
   extern __shared__ __align__(16) uint8_t sdh[];
   float4* sp = reinterpret_cast<float4*>(sdh);
@@ -241,11 +216,16 @@ __global__ void __launch_bounds__(128, kDensMinBlocks) k_density_heat32(StepPara
   const int32_t idi = F.id[i];
   float drho, sf;
   const int c = cnt[i];
+  const int b16 = L16.base ? L16.base[i / WF_TILE] : -1;     // uniform over the block
   if (staged >= 0)
-    density_heat_pairs<true>(P, F, sp, sv, st, nb, sl, i, g, c, pi, vi, ti, solid, idi, drho, sf);
+    density_heat_pairs(P, F, sp, sv, st, NbListS{sl, (int)threadIdx.x}, g, c, pi, vi, ti, solid,
+                       idi, drho, sf);
+  else if (b16 >= 0)
+    density_heat_pairs(P, F, F.p32, F.v32, F.th32, NbList16{L16.off, P.npad, i, b16}, g, c, pi, vi,
+                       ti, solid, idi, drho, sf);
   else
-    density_heat_pairs<false>(P, F, F.p32, F.v32, F.th32, nb, nullptr, i, g, c, pi, vi, ti, solid,
-                              idi, drho, sf);
+    density_heat_pairs(P, F, F.p32, F.v32, F.th32, NbList32{nb, P.npad, i}, g, c, pi, vi, ti, solid,
+                       idi, drho, sf);
   if constexpr (kDensLanes > 1) {
     const unsigned mask = group_mask<kDensLanes>();
 #pragma unroll
@@ -347,46 +327,27 @@ constexpr int kStressBatch = 4;
 constexpr float kMlpSteep = 0.02f;
 
 // The rate-tensor pair loop of the stress pass (CalcRateTensors,
-// InteractionAlt.cu:262-383, in FP32): kStaged reads the neighbours' records
-// from the tile's halo in shared memory (gp, gv) through the local list, else
-// from global memory through the slot list.  acc = D xx yy zz xy yz xz, W xy
-// yz xz, with the off-diagonal sums doubled (halved by the caller).
-template <bool kStaged>
+// InteractionAlt.cu:262-383, in FP32) over the neighbour list L (slots into
+// the global arrays gp, gv, or ranks into the tile's halo in shared memory).
+// acc = D xx yy zz xy yz xz, W xy yz xz, with the off-diagonal sums doubled
+// (halved by the caller).
+template <class L>
 __device__ __forceinline__ void stress_pairs(const StepParams& P, const Fields& F,
                                              const float4* __restrict__ gp,
-                                             const float4* __restrict__ gv,
-                                             const int32_t* __restrict__ nb,
-                                             const uint16_t* sl, int64_t i, int c,
+                                             const float4* __restrict__ gv, const L& list, int c,
                                              float4 pi, float4 vi, float* acc) {
   const float invh = P.invhf, C = P.Cf, Ch = P.Chf;
   float Dxx = 0.f, Dyy = 0.f, Dzz = 0.f, Dxy = 0.f, Dyz = 0.f, Dxz = 0.f;
   float Wxy = 0.f, Wyz = 0.f, Wxz = 0.f;
   int nx[8];
-  if (c > 0) {
-    if constexpr (kStaged) {
-      nbl_block_s(sl, threadIdx.x, 0, nx);
-    } else {
-      int4 lo, hi;
-      nb_block(nb, P.npad, i, 0, lo, hi);
-      nx[0] = lo.x; nx[1] = lo.y; nx[2] = lo.z; nx[3] = lo.w;
-      nx[4] = hi.x; nx[5] = hi.y; nx[6] = hi.z; nx[7] = hi.w;
-    }
-  }
+  if (c > 0) list.block(0, nx);
   for (int b = 0; WF_NB_BLK * b < c; b++) {
     int js[8];
 #pragma unroll
     for (int q = 0; q < 8; q++) js[q] = nx[q];
     const int m = c - WF_NB_BLK * b;
-    if (m > WF_NB_BLK) {
-      if constexpr (kStaged) {
-        nbl_block_s(sl, threadIdx.x, b + 1, nx);
-      } else {
-        int4 lo, hi;
-        nb_block(nb, P.npad, i, b + 1, lo, hi);
-        nx[0] = lo.x; nx[1] = lo.y; nx[2] = lo.z; nx[3] = lo.w;
-        nx[4] = hi.x; nx[5] = hi.y; nx[6] = hi.z; nx[7] = hi.w;
-      }
-    }
+    if (P.nb_pf && m > 2 * WF_NB_BLK) list.prefetch(b + 2, 1);
+    if (m > WF_NB_BLK) list.block(b + 1, nx);
 #pragma unroll
     for (int h = 0; h < WF_NB_BLK; h += kStressBatch) {
       float4 pj[kStressBatch], vj[kStressBatch];
@@ -398,7 +359,7 @@ __device__ __forceinline__ void stress_pairs(const StepParams& P, const Fields& 
 #pragma unroll
       for (int q = 0; q < kStressBatch; q++) {
         if (h + q >= m) continue;
-        if constexpr (!kStaged) {
+        if constexpr (L::kSlots) {
           if (P.contact && !pass_j(P, F.id[js[h + q]])) continue;
         }
         const float xx = pi.x - pj[q].x, xy = pi.y - pj[q].y, xz = pi.z - pj[q].z;
@@ -457,7 +418,8 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
                                                   const int32_t* __restrict__ cnt,
                                                   int* __restrict__ status,
                                                   const uint4* __restrict__ mlp,
-                                                  const MlpL1 l1, const TileHalo T) {
+                                                  const MlpL1 l1, const TileHalo T,
+                                                  const List16 L16) {
   // The MLP runs on the tensor cores (tcgen05) for the block's 128 particles
   // at once: every thread of the block must reach it, so out-of-range and
   // non-solid threads are predicated rather than returned before that point.
@@ -486,10 +448,13 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
   if (!mlp && !solid) return;
   const int c = solid ? cnt[i] : 0;
   float acc[9];
+  const int b16 = L16.base ? L16.base[i0 / WF_TILE] : -1;    // uniform over the block
   if (staged >= 0)
-    stress_pairs<true>(P, F, sp, sv, nb, sl, i, c, pi, vi, acc);
+    stress_pairs(P, F, sp, sv, NbListS{sl, (int)threadIdx.x}, c, pi, vi, acc);
+  else if (b16 >= 0)
+    stress_pairs(P, F, F.p32, v32b, NbList16{L16.off, P.npad, i, b16}, c, pi, vi, acc);
   else
-    stress_pairs<false>(P, F, F.p32, v32b, nb, nullptr, i, c, pi, vi, acc);
+    stress_pairs(P, F, F.p32, v32b, NbList32{nb, P.npad, i}, c, pi, vi, acc);
   float Dxx = acc[0], Dyy = acc[1], Dzz = acc[2], Dxy = acc[3], Dyz = acc[4], Dxz = acc[5];
   float Wxy = acc[6], Wyz = acc[7], Wxz = acc[8];
   Dxy *= 0.5f; Dxz *= 0.5f; Dyz *= 0.5f;
@@ -658,16 +623,6 @@ constexpr int kAccelLanes = 2;
 constexpr int kAccelBatch = 2;
 static_assert(WF_NB_BLK / kAccelLanes >= kAccelBatch, "batch within the lane's sub-block");
 
-// sub-block of lane g (entries 8b + g W .. 8b + g W + W - 1) of slot i's local list
-template <int W>
-__device__ __forceinline__ void nbl_sub_s(const uint16_t* sl, int t, int b, int g, int* js) {
-  const uint16_t* q = sl + (b * WF_TILE + t) * WF_NB_BLK + g * W;
-  static_assert(W == 4, "local sub-blocks of 4 entries");
-  const uint2 v = *reinterpret_cast<const uint2*>(q);
-  js[0] = (int)(v.x & 0xffffu); js[1] = (int)(v.x >> 16);
-  js[2] = (int)(v.y & 0xffffu); js[3] = (int)(v.y >> 16);
-}
-
 // Neighbour records of the acceleration pass, from global memory (the slot
 // arrays) or from the tile's halo in shared memory (indexed by local list).
 struct AccelSrc {
@@ -677,13 +632,12 @@ struct AccelSrc {
   const float2* sb;
 };
 
-template <bool kStaged>
+template <class L>
 __device__ __forceinline__ float4 accel_value(const StepParams& P, const Fields& F,
                                               const float4* __restrict__ v32b,
                                               const float* __restrict__ sigr32,
-                                              const int32_t* __restrict__ nb,
                                               const int32_t* __restrict__ cnt, int64_t i, int g,
-                                              const AccelSrc& src, const uint16_t* nbl) {
+                                              const AccelSrc& src, const L& list) {
   constexpr int W = WF_NB_BLK / kAccelLanes;
   const float4 pi = F.p32[i];
   const float4 vi = v32b[i];
@@ -699,19 +653,14 @@ __device__ __forceinline__ float4 accel_value(const StepParams& P, const Fields&
   float ax = 0.f, ay = 0.f, az = 0.f;
   const int c = cnt[i];
   int nx[W];
-  if (c > 0) {
-    if constexpr (kStaged) nbl_sub_s<W>(nbl, (int)(threadIdx.x >> 1), 0, g, nx);
-    else nb_sub<W>(nb, P.npad, i, 0, g, nx);
-  }
+  if (c > 0) list.template sub<W>(0, g, nx);
   for (int b = 0; WF_NB_BLK * b < c; b++) {
     int js[W];
 #pragma unroll
     for (int q = 0; q < W; q++) js[q] = nx[q];
     const int m = c - WF_NB_BLK * b - g * W;   // entries of this lane's sub-block in the list
-    if (c > WF_NB_BLK * (b + 1)) {
-      if constexpr (kStaged) nbl_sub_s<W>(nbl, (int)(threadIdx.x >> 1), b + 1, g, nx);
-      else nb_sub<W>(nb, P.npad, i, b + 1, g, nx);
-    }
+    if (P.nb_pf && c > WF_NB_BLK * (b + 2)) list.prefetch(b + 2, kAccelLanes);
+    if (c > WF_NB_BLK * (b + 1)) list.template sub<W>(b + 1, g, nx);
 #pragma unroll
     for (int hh = 0; hh < W; hh += kAccelBatch) {
       float4 pj[kAccelBatch], vj[kAccelBatch], t0[kAccelBatch];
@@ -727,7 +676,7 @@ __device__ __forceinline__ float4 accel_value(const StepParams& P, const Fields&
 #pragma unroll
       for (int q = 0; q < kAccelBatch; q++) {
         if (hh + q >= m) continue;
-        if constexpr (!kStaged) {
+        if constexpr (L::kSlots) {
           if (P.contact && !pass_ij(P, idi, F.id[js[hh + q]])) continue;
         }
         const float xx = pi.x - pj[q].x, xy = pi.y - pj[q].y, xz = pi.z - pj[q].z;
@@ -784,7 +733,7 @@ __global__ void __launch_bounds__(128, 7) k_accel32(StepParams P, Fields F,
   const float2* sgb;
   sigr32_split(sigr32, P.npad, sga, sgb);
   const AccelSrc src{F.p32, v32b, sga, sgb};
-  const float4 af = accel_value<false>(P, F, v32b, sigr32, nb, cnt, i, g, src, nullptr);
+  const float4 af = accel_value(P, F, v32b, sigr32, cnt, i, g, src, NbList32{nb, P.npad, i});
   if (g == 0) a32[i] = af;
 }
 
@@ -800,7 +749,7 @@ __global__ void __launch_bounds__(128, 7) k_accel_int32(StepParams P, Fields F,
                                                      const double4* __restrict__ vd2,
                                                      const int32_t* __restrict__ nb,
                                                      const int32_t* __restrict__ cnt,
-                                                     float4* __restrict__ p32n) {
+                                                     float4* __restrict__ p32n, const List16 L16) {
   int g;
   const int64_t i = accel_slot(g);
   if (i >= P.n) return;
@@ -809,9 +758,14 @@ __global__ void __launch_bounds__(128, 7) k_accel_int32(StepParams P, Fields F,
   sigr32_split(sigr32, P.npad, sga, sgb);
   const AccelSrc src{F.p32, v32b, sga, sgb};
   // rigid (non-solid) slots: zero acceleration, moved by their BCs
-  const float4 af = F.perm[i] < P.n_solid
-                        ? accel_value<false>(P, F, v32b, sigr32, nb, cnt, i, g, src, nullptr)
-                        : make_float4(0.f, 0.f, 0.f, 0.f);
+  float4 af = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (F.perm[i] < P.n_solid) {
+    const int b16 = L16.base ? L16.base[i / WF_TILE] : -1;   // uniform over the block
+    if (b16 >= 0)
+      af = accel_value(P, F, v32b, sigr32, cnt, i, g, src, NbList16{L16.off, P.npad, i, b16});
+    else
+      af = accel_value(P, F, v32b, sigr32, cnt, i, g, src, NbList32{nb, P.npad, i});
+  }
   if (g == 0) integrate_mixed_one(P, F, vd2, i, af, p32n);
 }
 
@@ -858,10 +812,10 @@ __global__ void __launch_bounds__(2 * WF_TILE, 3) k_accel_int32_tiles(
   if (F.perm[i] < P.n_solid) {
     if (staged >= 0) {
       const AccelSrc src{sp, sv, ssa, ssb};
-      af = accel_value<true>(P, F, v32b, sigr32, nb, cnt, i, g, src, sl);
+      af = accel_value(P, F, v32b, sigr32, cnt, i, g, src, NbListS{sl, (int)(threadIdx.x >> 1)});
     } else {
       const AccelSrc src{F.p32, v32b, sga, sgb};
-      af = accel_value<false>(P, F, v32b, sigr32, nb, cnt, i, g, src, nullptr);
+      af = accel_value(P, F, v32b, sigr32, cnt, i, g, src, NbList32{nb, P.npad, i});
     }
   }
   if (g == 0) integrate_mixed_one(P, F, vd2, i, af, p32n);
@@ -877,7 +831,7 @@ void launch_fp32_density(const StepParams& P, const Fields& F, double4* vd2, flo
 }
 void launch_fp32_density_heat(const StepParams& P, const Fields& F, double4* vd2, float4* v32b,
                               const NbBuffers& N, int first, int plastic_heat, const TileHalo& T,
-                              cudaStream_t s) {
+                              const List16& L16, cudaStream_t s) {
   TileHalo Tl = T;
   if (kDensLanes != 1) Tl.cap = 0;
   const size_t smem =
@@ -885,11 +839,12 @@ void launch_fp32_density_heat(const StepParams& P, const Fields& F, double4* vd2
   static size_t opted[64] = {};     // per device: dynamic shared memory opted in so far
   opt_in_smem(k_density_heat32, smem, opted);
   k_density_heat32<<<blocks_for(P.n * kDensLanes, 128), 128, smem, s>>>(
-      P, F, vd2, v32b, N.nb, N.cnt, first, plastic_heat, Tl);
+      P, F, vd2, v32b, N.nb, N.cnt, first, plastic_heat, Tl, L16);
 }
 void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b, float* sigr32,
                         const NbBuffers& N, int* status, const void* mlp_packed,
-                        const MlpL1* mlp_l1, const TileHalo& T, cudaStream_t s) {
+                        const MlpL1* mlp_l1, const TileHalo& T, const List16& L16,
+                        cudaStream_t s) {
   const uint4* W = reinterpret_cast<const uint4*>(mlp_packed);
   const MlpL1 l1 = (W && mlp_l1) ? *mlp_l1 : MlpL1{};
   const size_t smem = (W ? WF_UMMA_SMEM : 0) +
@@ -897,7 +852,7 @@ void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b
   static size_t opted[64] = {};     // per device: dynamic shared memory opted in so far
   opt_in_smem(k_stress32, smem, opted);
   k_stress32<<<blocks_for(P.n, 128), 128, smem, s>>>(P, F, v32b, sigr32, N.nb, N.cnt, status, W, l1,
-                                                     T);
+                                                     T, L16);
 }
 void launch_fp32_accel(const StepParams& P, const Fields& F, const float4* v32b,
                        const float* sigr32, float4* a32, const NbBuffers& N, cudaStream_t s) {
@@ -905,7 +860,7 @@ void launch_fp32_accel(const StepParams& P, const Fields& F, const float4* v32b,
 }
 void launch_fp32_accel_integrate(const StepParams& P, const Fields& F, const float4* v32b,
                                  const float* sigr32, const double4* vd2, const NbBuffers& N,
-                                 const TileHalo& T, cudaStream_t s) {
+                                 const TileHalo& T, const List16& L16, cudaStream_t s) {
   if (T.cap > 0) {
     const size_t smem = (3 * sizeof(float4) + sizeof(float2)) * (size_t)T.cap + WF_TILE_LIST_BYTES;
     static size_t opted[64] = {};
@@ -915,5 +870,5 @@ void launch_fp32_accel_integrate(const StepParams& P, const Fields& F, const flo
     return;
   }
   k_accel_int32<<<blocks_for(P.n * kAccelLanes, 128), 128, 0, s>>>(P, F, v32b, sigr32, vd2, N.nb, N.cnt,
-                                                     F.p32n);
+                                                     F.p32n, L16);
 }

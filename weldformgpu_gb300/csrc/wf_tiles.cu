@@ -136,7 +136,50 @@ __global__ void __launch_bounds__(kT) k_tile_halo(int64_t n, int64_t npad,
   }
 }
 
+// 16-bit lists: the tile's window [lo, hi] of named slots; when it spans at
+// most 65,536 slots every entry (padding included) becomes slot - lo.
+__global__ void __launch_bounds__(kT) k_list16(int64_t n, int64_t npad,
+                                               const int32_t* __restrict__ nb,
+                                               const int32_t* __restrict__ cnt,
+                                               int32_t* __restrict__ base,
+                                               uint16_t* __restrict__ off) {
+  __shared__ int s_lo[kWarps], s_hi[kWarps];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t tile = blockIdx.x;
+  const int64_t i = tile * kT + tid;
+  const bool valid = i < n;
+  const int c = valid ? cnt[i] : 0;
+  int lo = valid ? (int)i : INT_MAX, hi = valid ? (int)i : INT_MIN;
+  for (int k = 0; k < c; k++) {
+    const int s = nb[nb_at(npad, i, k)];
+    lo = min(lo, s);
+    hi = max(hi, s);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if (lane == 0) { s_lo[warp] = lo; s_hi[warp] = hi; }
+  __syncthreads();
+  lo = s_lo[0];
+  hi = s_hi[0];
+  for (int w = 1; w < kWarps; w++) { lo = min(lo, s_lo[w]); hi = max(hi, s_hi[w]); }
+  const bool fits = lo <= hi && (int64_t)hi - lo < 65536;
+  if (tid == 0) base[tile] = fits ? lo : -1;
+  if (!fits || !valid) return;
+  const int cend = (c + WF_NB_BLK - 1) & ~(WF_NB_BLK - 1);
+  for (int k = 0; k < cend; k++) {
+    const int s = k < c ? nb[nb_at(npad, i, k)] : (int)i;
+    off[nb_at(npad, i, k)] = (uint16_t)(s - lo);
+  }
+}
+
 }  // namespace
+
+void launch_list16(int64_t n, int64_t npad, const int32_t* nb, const int32_t* cnt, int32_t* base,
+                   uint16_t* off, cudaStream_t s) {
+  k_list16<<<(unsigned)(npad / WF_TILE), WF_TILE, 0, s>>>(n, npad, nb, cnt, base, off);
+}
 
 void launch_tile_halo(int64_t n, int64_t npad, const int32_t* nb, const int32_t* cnt,
                       int32_t* hoff, int32_t* hcnt, int32_t* halo, int64_t halo_cap,

@@ -33,6 +33,17 @@ void launch_tile_halo(int64_t n, int64_t npad, const int32_t* nb, const int32_t*
                       int32_t* hoff, int32_t* hcnt, int32_t* halo, int64_t halo_cap,
                       uint16_t* nbl, int cap, unsigned* halo_used, int* hmax, cudaStream_t s);
 
+// 16-bit neighbour lists for the global gather path: per tile of WF_TILE
+// slots a base slot (the smallest slot its lists name, or -1 when they span
+// more than 65,536 slots: the tile then keeps the 32-bit lists), and entries
+// stored as slot - base in the layout of nb (nb_at).
+struct List16 {
+  const int32_t* base;    // [tiles]
+  const uint16_t* off;    // offsets, layout of nb
+};
+void launch_list16(int64_t n, int64_t npad, const int32_t* nb, const int32_t* cnt, int32_t* base,
+                   uint16_t* off, cudaStream_t s);
+
 // Lets `kernel` use `bytes` of dynamic shared memory on the current device
 // (the attribute is per device; set once per device and larger size).
 template <class K>
@@ -97,3 +108,88 @@ __device__ __forceinline__ void stage_lists(const uint16_t* __restrict__ nbl, in
                nbl + ((int64_t)b * npad + (int64_t)tile * WF_TILE + t) * WF_NB_BLK);
   }
 }
+
+// ---- neighbour-list readers of the mixed pair passes ----------------------
+// block(b, js): entries 8b .. 8b+7 of the particle's list; sub<W>(b, g, js):
+// the W entries of lane g of a lane group (W = 8 / lanes); prefetch(b):
+// brings block b towards L2 two blocks ahead of use.  `kSlots` tells whether
+// the entries are slots (global arrays) or halo ranks (shared memory).
+struct NbList32 {                 // 32-bit slot lists
+  static constexpr bool kSlots = true;
+  const int32_t* nb;
+  int64_t npad, i;
+  __device__ __forceinline__ void block(int b, int* js) const {
+    const int4* q = reinterpret_cast<const int4*>(nb + ((int64_t)b * npad + i) * WF_NB_BLK);
+    const int4 lo = __ldg(q), hi = __ldg(q + 1);
+    js[0] = lo.x; js[1] = lo.y; js[2] = lo.z; js[3] = lo.w;
+    js[4] = hi.x; js[5] = hi.y; js[6] = hi.z; js[7] = hi.w;
+  }
+  template <int W>
+  __device__ __forceinline__ void sub(int b, int g, int* js) const {
+    const int32_t* q = nb + ((int64_t)b * npad + i) * WF_NB_BLK + g * W;
+    if constexpr (W == 8) {
+      block(b, js);
+    } else if constexpr (W == 4) {
+      const int4 v = __ldg(reinterpret_cast<const int4*>(q));
+      js[0] = v.x; js[1] = v.y; js[2] = v.z; js[3] = v.w;
+    } else {
+      static_assert(W == 2, "list sub-block of 2, 4 or 8 entries");
+      const int2 v = __ldg(reinterpret_cast<const int2*>(q));
+      js[0] = v.x; js[1] = v.y;
+    }
+  }
+  // a 128-byte line holds one block of 4 consecutive slots
+  __device__ __forceinline__ void prefetch(int b, int lanes) const {
+    nb_prefetch(nb, npad, i, b, 4 * lanes);
+  }
+};
+
+struct NbList16 {                 // 16-bit offsets from the tile's base slot
+  static constexpr bool kSlots = true;
+  const uint16_t* off;
+  int64_t npad, i;
+  int base;
+  __device__ __forceinline__ void block(int b, int* js) const {
+    const uint4 q = __ldg(reinterpret_cast<const uint4*>(off + ((int64_t)b * npad + i) * WF_NB_BLK));
+    js[0] = base + (int)(q.x & 0xffffu); js[1] = base + (int)(q.x >> 16);
+    js[2] = base + (int)(q.y & 0xffffu); js[3] = base + (int)(q.y >> 16);
+    js[4] = base + (int)(q.z & 0xffffu); js[5] = base + (int)(q.z >> 16);
+    js[6] = base + (int)(q.w & 0xffffu); js[7] = base + (int)(q.w >> 16);
+  }
+  template <int W>
+  __device__ __forceinline__ void sub(int b, int g, int* js) const {
+    if constexpr (W == 8) {
+      block(b, js);
+    } else {
+      static_assert(W == 4, "16-bit sub-blocks of 4 entries");
+      const uint2 v = __ldg(reinterpret_cast<const uint2*>(
+          off + ((int64_t)b * npad + i) * WF_NB_BLK + g * W));
+      js[0] = base + (int)(v.x & 0xffffu); js[1] = base + (int)(v.x >> 16);
+      js[2] = base + (int)(v.y & 0xffffu); js[3] = base + (int)(v.y >> 16);
+    }
+  }
+  // a 128-byte line holds one block of 8 consecutive slots
+  __device__ __forceinline__ void prefetch(int b, int lanes) const {
+    if ((threadIdx.x & (8 * lanes - 1)) == 0)
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(off + ((int64_t)b * npad + i) * WF_NB_BLK));
+  }
+};
+
+struct NbListS {                  // a staged tile's local lists in shared memory
+  static constexpr bool kSlots = false;
+  const uint16_t* sl;
+  int t;                          // the slot's place in its tile
+  __device__ __forceinline__ void block(int b, int* js) const { nbl_block_s(sl, t, b, js); }
+  template <int W>
+  __device__ __forceinline__ void sub(int b, int g, int* js) const {
+    if constexpr (W == 8) {
+      block(b, js);
+    } else {
+      static_assert(W == 4, "local sub-blocks of 4 entries");
+      const uint2 v = *reinterpret_cast<const uint2*>(sl + (b * WF_TILE + t) * WF_NB_BLK + g * W);
+      js[0] = (int)(v.x & 0xffffu); js[1] = (int)(v.x >> 16);
+      js[2] = (int)(v.y & 0xffffu); js[3] = (int)(v.y >> 16);
+    }
+  }
+  __device__ __forceinline__ void prefetch(int, int) const {}
+};
