@@ -444,7 +444,7 @@ def test_tile_staging_bit_identical_to_global_gathers(cap_max):
         d.step(300)
         runs.append({f: d.get_field(f) for f in ("x", "v", "u", "shearstress", "pl_strain",
                                                  "sigma_eq", "T", "rho")})
-        if staging:
+        if staging == 1:
             tiles = (sc["n"] + 127) // 128
             staged = d.get_scalar("tiles_staged")
             hmax = d.get_scalar("tile_halo_max")
@@ -454,6 +454,7 @@ def test_tile_staging_bit_identical_to_global_gathers(cap_max):
                 assert 0 < staged < tiles and hmax > cap_max, (staged, tiles, hmax)
         else:
             assert d.get_scalar("tile_cap") == 0
+        d.close()
     for f in runs[0]:
         assert np.array_equal(runs[0][f], runs[1][f]), f
         assert np.array_equal(runs[2][f], runs[1][f]), f

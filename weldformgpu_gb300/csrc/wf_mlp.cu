@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer_umma(const uint4* __restrict_
     const float4 x = X[i];
     f[0] = x.x; f[1] = x.y; f[2] = x.z; f[3] = x.w;
   }
-  const float y = mlp_umma_cta(smu, f, valid, status, l1);
+  const float y = mlp_umma_cta(smu, image, f, valid, status, l1);
   if (valid) Y[i] = y;
 }
 
@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(128) k_mlp_newton_iters(StepParams P, double G
   if (image) {
     float f[4];
     mlp_features(s.x, (double)s.y, s.z, (float)Th, f);
-    const float y = mlp_umma_cta(smu, f, valid, status, l1);
+    const float y = mlp_umma_cta(smu, image, f, valid, status, l1);
     const float yc = mlp_accept(y);
     if (yc > 0.0f) { ratio = (double)yc; use = 1; }
   }

@@ -122,19 +122,15 @@ __host__ __device__ __forceinline__ int umma_kmajor_off(int r, int k, int K) {
 
 // Kernel entry of every kernel that contains the MLP (all threads of the
 // block, before anything else): with the network on (image != nullptr) one
-// thread starts a bulk copy of the weight image into dynamic shared memory
-// and initialises the mbarriers, and warp 0 allocates the 64 tensor-memory
+// thread initialises the mbarriers and warp 0 allocates the 64 tensor-memory
 // columns; in every case warp 0 gives up the allocation permit so further
-// CTAs can start on the SM.  Does not wait for the copy: it arrives while the
-// block works through its neighbour loops, and mlp_umma_cta waits for it
-// (every block that starts the copy reaches that call).  The image must be
-// 16-byte aligned (WF_UMMA_IMAGE is a multiple of 16).
+// CTAs can start on the SM.  The weight image is copied later, by
+// mlp_umma_cta, and only in blocks where some thread wants a prediction.
 __device__ __forceinline__ void mlp_umma_begin(uint8_t* sm, const uint4* __restrict__ image) {
   const uint32_t s0 = umma::smem_addr(sm);
   if (image && threadIdx.x == 0) {
     umma::mbar_init(s0 + WF_UMMA_MBAR, 1);
     umma::mbar_init(s0 + WF_UMMA_MBAR_W, 1);
-    umma::bulk_load(s0, image, WF_UMMA_IMAGE, s0 + WF_UMMA_MBAR_W);
   }
   if (threadIdx.x < 32) {
     if (image) umma::tmem_alloc(s0 + WF_UMMA_TSLOT, 64);
@@ -150,23 +146,23 @@ __device__ __forceinline__ void mlp_umma_begin(uint8_t* sm, const uint4* __restr
 // tensor memory.  Returns the network output for the calling thread's row,
 // or -1 when no thread of the block wants a prediction or a completion wait
 // ran out (then WF_STATUS_MMA_WAIT is set in *status).
-static __device__ __forceinline__ float mlp_umma_cta(uint8_t* sm, const float f[4], bool want,
-                                                     int* status, const MlpL1& l1) {
+static __device__ __forceinline__ float mlp_umma_cta(uint8_t* sm, const uint4* __restrict__ image,
+                                                     const float f[4], bool want, int* status,
+                                                     const MlpL1& l1) {
   constexpr int kWaitLimit = 1 << 20;
   constexpr uint32_t kId = umma::idesc_bf16_f32(128, 64);
   const int tid = threadIdx.x, warp = tid >> 5;
   const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(sm + WF_UMMA_TSLOT);
   const uint32_t s0 = umma::smem_addr(sm);
-  // No thread of the block wants a prediction: one barrier; warp 0 frees the
-  // tensor memory and thread 0 waits for the weight image started by
-  // mlp_umma_begin (the block must not retire with that copy in flight).
+  // No thread of the block wants a prediction: one barrier, and warp 0 frees
+  // the tensor memory (no weight copy was started).
   if (!__syncthreads_or(want)) {
     if (warp == 0) umma::tmem_dealloc(tmem, 64);
-    if (tid == 0 && !umma::mbar_wait(s0 + WF_UMMA_MBAR_W, 0, kWaitLimit))
-      atomicOr(status, WF_STATUS_MMA_WAIT);
     return -1.0f;
   }
-  // the weight image (long arrived by now); every thread waits
+  // the weight image: one bulk copy into the start of the dynamic shared
+  // memory, completing on its mbarrier; every thread waits (bounded)
+  if (tid == 0) umma::bulk_load(s0, image, WF_UMMA_IMAGE, s0 + WF_UMMA_MBAR_W);
   const bool image_ok = umma::mbar_wait(s0 + WF_UMMA_MBAR_W, 0, kWaitLimit);
   if (!__syncthreads_and(image_ok)) {
     if (warp == 0) umma::tmem_dealloc(tmem, 64);

@@ -519,7 +519,7 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
     const bool want = solid && jc_newton && st > sy0f && steep;
     float f[4] = {0.f, 0.f, 0.f, 0.f};
     if (want) mlp_features(st / sy0f, eps_p, eff, Th, f);
-    const float y = mlp_umma_cta(smlp, f, want, status, l1);
+    const float y = mlp_umma_cta(smlp, mlp, f, want, status, l1);
     const float yc = mlp_accept(y);
     if (want && yc > 0.0f) ratio = (double)yc;
     if (!solid) return;
