@@ -48,6 +48,10 @@ BYTES_MODEL = {
     "mixed": {"density": 216, "stress": 248, "accel": 96, "integrate": 320, "thermal": 88},
     "fp64": {"density": 120, "stress": 416, "accel": 144, "integrate": 264, "thermal": 112},
 }
+# Bytes of one launch of the mixed form's kernels as timed (no contact): the
+# density launch carries the previous step's heat pass (216 + 88) and the
+# acceleration launch the integration of the same slot (96 + 320).
+LAUNCH_BYTES_MIXED = {"density": 216 + 88, "stress": 248, "accel": 96 + 320, "thermal": 88}
 NB_INDEX_BYTES = 4  # per neighbour per pair pass
 KERNEL_IDS = {"density": 1, "stress": 2, "accel": 3, "integrate": 4, "thermal": 5}
 TOP_FZ = 11 + 3 * 1 + 2     # output-row column: BC 1 (the moving platen zone), z component
@@ -617,7 +621,7 @@ def main():
     peak, peak_kind = measured_peaks()
     dom = mixed["dominant"]
     per_launch_ms = mixed["kernel_ms"] / max(mixed["kernel_launches"], 1)
-    alg_bytes = BYTES_MODEL["mixed"][dom] * n
+    alg_bytes = LAUNCH_BYTES_MIXED.get(dom, BYTES_MODEL["mixed"][dom]) * n
     if dom in PAIR_KERNELS:
         alg_bytes_idx = alg_bytes + NB_INDEX_BYTES * 56 * n
     else:

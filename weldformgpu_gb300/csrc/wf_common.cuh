@@ -232,7 +232,9 @@ __device__ __forceinline__ float gradK32(float q, float h, float C) {
 // The mixed form's cubic-spline gradient factor GK (Functions.cu:82-88) from
 // r^2 > 0 (invh = 1/h, Ch = C/h; the q < 1 branch is C/(q h) q (-3 + 9/4 q)
 // without the division): r and C/r from one reciprocal square root, the two
-// branches of the spline selected without a branch.
+// branches of the spline selected without a branch.  r^2 = 0 (a particle and
+// itself: the padding entries of the lists) gives exactly 0: rsqrt(+0) = +inf,
+// q = 0 * inf is NaN and both comparisons fail.
 __device__ __forceinline__ float gk32_r2(float r2, float invh, float Ch, float C) {
   const float ri = rsqrtf(r2);
   const float q = r2 * ri * invh;

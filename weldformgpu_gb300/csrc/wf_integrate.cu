@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(128) k_heat_rate(StepParams P, Fields F,
           const float xx = pi.x - pj[u].x, xy = pi.y - pj[u].y, xz = pi.z - pj[u].z;
           // x.(GK x) / r^2 = GK
           const float GK = gk32_r2(xx * xx + xy * xy + xz * xz, invh, Ch, C);
-          sf += __fdividef(pj[u].w, rj[u]) * dT * GK;
+          sf += __fdividef(pj[u].w, rj[u]) * GK * dT;   // as in k_density_heat32
         }
       }
     }

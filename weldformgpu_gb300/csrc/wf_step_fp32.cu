@@ -95,10 +95,11 @@ __global__ void __launch_bounds__(128) k_density32(StepParams P, Fields F,
           const float xx = pi.x - pj[q].x, xy = pi.y - pj[q].y, xz = pi.z - pj[q].z;
           const float GK = gk32_r2(xx * xx + xy * xy + xz * xz, invh, Ch, C);
           const float vx = vi.x - vj[q].x, vy = vi.y - vj[q].y, vz = vi.z - vj[q].z;
-          drho += pj[q].w * __fdividef(vi.w, vj[q].w) * ((vx * xx + vy * xy + vz * xz) * GK);
+          drho += __fdividef(pj[q].w, vj[q].w) * GK * (vx * xx + vy * xy + vz * xz);
         }
       }
     }
+    drho *= vi.w;                      // rho_i multiplies the sum (as in k_density_heat32)
     F.drho[i] = (double)drho;
     rho_new = vdi.w + P.dt * (double)drho;
   }
@@ -151,25 +152,29 @@ __device__ __forceinline__ void density_heat_pairs(const StepParams& P, const Fi
       }
 #pragma unroll
       for (int q = 0; q < NB; q++) {
-        if (h + q >= m) continue;
+        // Entries past the count are the particle's own slot (list padding):
+        // r^2 = 0 gives GK = 0 exactly (gk32_r2), so they add exact zeros and
+        // need no test, except under the contact filter.
+        if (P.contact && h + q >= m) continue;
         const float xx = pi.x - pj[q].x, xy = pi.y - pj[q].y, xz = pi.z - pj[q].z;
         const float GK = gk32_r2(xx * xx + xy * xy + xz * xz, invh, Ch, C);
-        const float mr = __fdividef(pj[q].w, vj[q].w);   // m_j / rho_j
+        // m_j / rho_j GK, shared by both sums
+        const float mg = __fdividef(pj[q].w, vj[q].w) * GK;
         // heat flux (every particle, no contact filter); the pair
         // conductivity 4 k_i k_j / (k_i + k_j) = 2k multiplies the sum
         const float dT = (ti.x - tj[q].x) + (ti.y - tj[q].y);
-        sf += mr * dT * GK;
-        // density rate (solid particles, contact filter)
+        sf += mg * dT;
+        // density rate (solid particles, contact filter); rho_i multiplies the sum
         bool pass = solid;
         if constexpr (L::kSlots) pass = pass && !(P.contact && !pass_ij(P, idi, F.id[js[h + q]]));
         if (pass) {
           const float vx = vi.x - vj[q].x, vy = vi.y - vj[q].y, vz = vi.z - vj[q].z;
-          drho += mr * vi.w * ((vx * xx + vy * xy + vz * xz) * GK);
+          drho += mg * (vx * xx + vy * xy + vz * xz);
         }
       }
     }
   }
-  drho_out = drho;
+  drho_out = drho * vi.w;
   sf_out = sf;
 }
 
@@ -330,15 +335,17 @@ constexpr float kMlpSteep = 0.02f;
 // InteractionAlt.cu:262-383, in FP32) over the neighbour list L (slots into
 // the global arrays gp, gv, or ranks into the tile's halo in shared memory).
 // acc = D xx yy zz xy yz xz, W xy yz xz, with the off-diagonal sums doubled
-// (halved by the caller).
+// (halved by the caller).  The off-diagonal terms of a pair are a + b (D) and
+// a - b (W) of two products a = s_k x_l, b = s_l x_k: their two sums are
+// accumulated (one FMA each) and combined once after the loop.
 template <class L>
 __device__ __forceinline__ void stress_pairs(const StepParams& P, const Fields& F,
                                              const float4* __restrict__ gp,
                                              const float4* __restrict__ gv, const L& list, int c,
                                              float4 pi, float4 vi, float* acc) {
   const float invh = P.invhf, C = P.Cf, Ch = P.Chf;
-  float Dxx = 0.f, Dyy = 0.f, Dzz = 0.f, Dxy = 0.f, Dyz = 0.f, Dxz = 0.f;
-  float Wxy = 0.f, Wyz = 0.f, Wxz = 0.f;
+  float Dxx = 0.f, Dyy = 0.f, Dzz = 0.f;
+  float Axy = 0.f, Bxy = 0.f, Axz = 0.f, Bxz = 0.f, Ayz = 0.f, Byz = 0.f;
   int nx[8];
   if (c > 0) list.block(0, nx);
   for (int b = 0; WF_NB_BLK * b < c; b++) {
@@ -358,7 +365,10 @@ __device__ __forceinline__ void stress_pairs(const StepParams& P, const Fields& 
       }
 #pragma unroll
       for (int q = 0; q < kStressBatch; q++) {
-        if (h + q >= m) continue;
+        // Entries past the count are the particle's own slot (list padding):
+        // r^2 = 0 gives GK = 0 exactly (gk32_r2), so they add exact zeros and
+        // need no test, except under the contact filter.
+        if (P.contact && h + q >= m) continue;
         if constexpr (L::kSlots) {
           if (P.contact && !pass_j(P, F.id[js[h + q]])) continue;
         }
@@ -372,22 +382,18 @@ __device__ __forceinline__ void stress_pairs(const StepParams& P, const Fields& 
         Dxx += sa * xx;
         Dyy += sb * xy;
         Dzz += sc * xz;
-        float t = sa * xy, u = sb * xx;
-        Dxy += t + u;
-        Wxy += t - u;
-        t = sa * xz;
-        u = sc * xx;
-        Dxz += t + u;
-        Wxz += u - t;
-        t = sb * xz;
-        u = sc * xy;
-        Dyz += t + u;
-        Wyz += t - u;
+        Axy += sa * xy;
+        Bxy += sb * xx;
+        Axz += sa * xz;
+        Bxz += sc * xx;
+        Ayz += sb * xz;
+        Byz += sc * xy;
       }
     }
   }
-  acc[0] = Dxx; acc[1] = Dyy; acc[2] = Dzz; acc[3] = Dxy; acc[4] = Dyz; acc[5] = Dxz;
-  acc[6] = Wxy; acc[7] = Wyz; acc[8] = Wxz;
+  acc[0] = Dxx; acc[1] = Dyy; acc[2] = Dzz;
+  acc[3] = Axy + Bxy; acc[4] = Ayz + Byz; acc[5] = Axz + Bxz;
+  acc[6] = Axy - Bxy; acc[7] = Ayz - Byz; acc[8] = Bxz - Axz;
 }
 
 // Copies the tile's halo records and local lists into shared memory (every
@@ -515,7 +521,8 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
     // start is the better one, and Newton needs one iteration from either.
     const float sy0f = ((float)M.A + (float)M.B * (float)fmax(pwn, 0.0)) * RTf;
     const bool steep = !(eps_p > 0.0) || !(pwn > 0.0) ||
-                       P.jcnf * P.jcBf * RTf * (float)(pwn / eps_p) > kMlpSteep * P.G3f;
+                       P.jcnf * P.jcBf * RTf * __fdividef((float)pwn, (float)eps_p) >
+                           kMlpSteep * P.G3f;
     const bool want = solid && jc_newton && st > sy0f && steep;
     float f[4] = {0.f, 0.f, 0.f, 0.f};
     if (want) mlp_features(st / sy0f, eps_p, eff, Th, f);
@@ -675,7 +682,10 @@ __device__ __forceinline__ float4 accel_value(const StepParams& P, const Fields&
       }
 #pragma unroll
       for (int q = 0; q < kAccelBatch; q++) {
-        if (hh + q >= m) continue;
+        // Entries past the count are the particle's own slot (list padding):
+        // r^2 = 0 gives GK = 0 exactly (gk32_r2), so they add exact zeros and
+        // need no test, except under the contact filter.
+        if (P.contact && hh + q >= m) continue;
         if constexpr (L::kSlots) {
           if (P.contact && !pass_ij(P, idi, F.id[js[hh + q]])) continue;
         }
