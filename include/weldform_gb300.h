@@ -144,7 +144,9 @@ int wf_add_trimesh(wf_domain* d, const double* nodes, int32_t nn, const int32_t*
  *   (65536 rows),
  *   rebuild_every (5), rebuild_after_yield (1), rebuild_current_positions (0),
  *   rebuild_strain_increment (0), thermal (0), taylor_quinney (0),
- *   clamp_homologous (1), energy_mode (0), contact_dx (0),
+ *   clamp_homologous (1), energy_mode (0: particle 0's S:D for every
+ *   particle, as Energy.cu:270-276; 1: each particle's own; both forms),
+ *   contact_dx (0),
  *   contact_stiffness (0.1), contact_vreg (1e-3), contact_heat_fraction (1),
  *   fuse_heat (1), fuse_integrate (1), tile_staging (0; 1: the mixed pair passes
  *   read neighbours from per-tile halos in shared memory; same results),

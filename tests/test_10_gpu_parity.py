@@ -167,6 +167,28 @@ def test_mixed_form_within_1e3_of_fp64_jc_newton():
         assert e <= 1e-3, (f, e)
 
 
+@pytest.mark.parametrize("mode", [0, 1])
+def test_mixed_internal_energy_within_1e3_of_fp64(mode):
+    """CalcIntEnergy in both energy modes: 0 (the reference's: particle 0's
+    S:D for every particle, Energy.cu:270-276) and 1 (each particle's own),
+    the mixed form against plain FP64, and the FP64 form against the oracle."""
+    sc = S.compression_cylinder(material="jc", vz_top=-10.0)
+    opts = {"return_map": 1, "energy_mode": mode}
+    a = gpu(sc, dict(opts, precision=0))
+    b = gpu(sc, dict(opts, precision=1))
+    o = ora(sc, opts)
+    a.step(300)
+    b.step(300)
+    o.step(300)
+    ea, eb, eo = a.get_field("int_energy"), b.get_field("int_energy"), o.get_field("int_energy")
+    assert np.abs(ea).max() > 0
+    if mode == 0:      # one S0:D0 per step for every particle, scaled by each m/rho
+        assert np.ptp(ea) <= 0.05 * np.abs(ea).max()
+    np.testing.assert_allclose(ea, eo, rtol=1e-9, atol=1e-9 * np.abs(eo).max())
+    e = rel_l2(eb, ea)
+    assert e <= 1e-3, e
+
+
 def test_heat_fp64_vs_oracle():
     sc = S.heat_box(n_side=16)
     from weldformgpu_gb300 import Domain_d

@@ -1,0 +1,137 @@
+"""Edge cases of the SPH step on the GPU against the oracle: a single particle,
+isolated particles (empty lists), coincident particles (zero distance: the
+neighbour rule's `0 < d^2` excludes the pair), and particle counts that leave
+ragged warps, blocks and list blocks.
+
+Tolerances as in the parity tests: neighbour lists identical; plain FP64 with
+the bilinear law bit-exact against the oracle; mixed form within 1e-3
+relative L2 of plain FP64 (or, where every field is exactly 0 or untouched,
+equal to it).
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests import scenarios as S
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("x", "u", "v", "a", "rho", "sigma", "pl_strain", "sigma_eq", "int_energy")
+
+
+def gpu(sc, options=None):
+    from weldformgpu_gb300 import Domain_d
+    return S.load(Domain_d(sc["n"]), sc, options)
+
+
+def ora(sc, options=None):
+    return S.load(O.OracleDomain(sc["n"]), sc, options)
+
+
+def same_lists(c1, l1, c2, l2):
+    if not np.array_equal(c1, c2):
+        return False
+    return all(np.array_equal(l1[i, :c1[i]], l2[i, :c2[i]]) for i in range(len(c1)))
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64).ravel()
+    b = np.asarray(b, np.float64).ravel()
+    den = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (den if den > 0 else 1.0)
+
+
+def with_positions(x, zones=True, vz_top=-1.0):
+    """The bilinear compression material and time step on the particles x;
+    with `zones`, the lowest layer is fixed (zone 2) and the highest moves at
+    vz_top (zone 3), as in the compression cylinder."""
+    base = S.compression_cylinder(vz_top=vz_top)
+    x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
+    n = len(x)
+    sc = dict(base)
+    sc.update(n=n, x=x, m=np.full(n, base["m"][0]), ids=np.zeros(n, np.int32),
+              not_write=np.zeros(n, np.uint8), T=np.full(n, base["T"][0]))
+    if zones and n > 1:
+        z = x[:, 2]
+        sc["ids"][z <= z.min() + 1e-12] = 2
+        sc["ids"][z >= z.max() - 1e-12] = 3
+    else:
+        sc["bcs"] = []
+    return sc
+
+
+def check_fp64_and_mixed(sc, steps):
+    g = gpu(sc, {"precision": 0})
+    o = ora(sc)
+    g.find_neighbors()
+    o.find_neighbors()
+    assert same_lists(*g.get_neighbors(), *o.get_neighbors())
+    g.step(steps)
+    o.step(steps)
+    for f in FIELDS:
+        assert np.array_equal(g.get_field(f), o.get_field(f)), f
+    m = gpu(sc, {"precision": 1})
+    m.step(steps)
+    for f in FIELDS:
+        got, ref = m.get_field(f), g.get_field(f)
+        assert np.all(np.isfinite(got)), f
+        assert rel_l2(got, ref) <= 1e-3, (f, rel_l2(got, ref))
+    return g, m
+
+
+def test_single_particle():
+    """One particle: an empty list in a grid of 4 x 4 x 4 cells and 127
+    padding slots in its block; at rest and without BCs nothing moves."""
+    sc = with_positions(np.array([[1.0e-3, -2.0e-3, 3.0e-3]]), zones=False)
+    g, m = check_fp64_and_mixed(sc, 20)
+    c, _ = g.get_neighbors()
+    assert c.tolist() == [0]
+    assert np.array_equal(np.ravel(m.get_field("x")), sc["x"].ravel())
+
+
+def test_isolated_particles_have_empty_lists():
+    """A lattice at 2.5 h spacing (support radius 2 h): every list empty; the
+    top layer still moves under its velocity BC and nothing else changes."""
+    h = S.compression_cylinder()["h"]
+    s = 2.5 * h
+    g3 = np.stack(np.meshgrid(np.arange(5), np.arange(4), np.arange(6), indexing="ij"), -1)
+    x = g3.reshape(-1, 3) * s
+    sc = with_positions(x, zones=True, vz_top=-2.0)
+    g, m = check_fp64_and_mixed(sc, 30)
+    c, _ = g.get_neighbors()
+    assert (c == 0).all()
+    top = sc["ids"] == 3
+    dz = g.get_field("u").reshape(-1, 3)[:, 2]
+    assert (dz[top] < 0).all() and (dz[~top] == 0).all()
+
+
+def test_coincident_particles_exclude_each_other():
+    """Duplicates at exactly the same position as existing particles of the
+    cylinder: the pair is not in either list (zero distance), each duplicate
+    is in its neighbours' lists, and the step matches the oracle."""
+    base = S.compression_cylinder()
+    x = base["x"]
+    rng = np.random.default_rng(5)
+    dup = rng.choice(len(x), 12, replace=False)
+    xx = np.vstack([x, x[dup]])
+    sc = with_positions(xx, zones=True, vz_top=-5.0)
+    g, _ = check_fp64_and_mixed(sc, 60)
+    c, lst = g.get_neighbors()
+    n0 = len(x)
+    for k, i in enumerate(dup):
+        j = n0 + k
+        assert j not in set(lst[i, :c[i]].tolist())
+        assert i not in set(lst[j, :c[j]].tolist())
+        assert c[j] == c[i]
+
+
+@pytest.mark.parametrize("n", [2, 31, 33, 129, 257])
+def test_ragged_particle_counts(n):
+    """Counts that leave partial warps, blocks of 128 and list blocks of 8:
+    the n particles nearest the cylinder's centre."""
+    base = S.compression_cylinder()
+    x = base["x"]
+    c = 0.5 * (x.min(0) + x.max(0))
+    x = x[np.argsort(((x - c) ** 2).sum(1), kind="stable")[:n]]
+    sc = with_positions(x, zones=True, vz_top=-5.0)
+    check_fp64_and_mixed(sc, 40)

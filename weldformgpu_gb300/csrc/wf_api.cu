@@ -82,6 +82,7 @@ struct wf_domain {
   // FP64 output rows (wf_outputs.cu): recorded at output times, or every step
   // with option output_every_step; the series holds up to series_cap rows
   double4* fr = nullptr;       // m a before the BCs at BC-zone slots (written on row steps)
+  double* e0 = nullptr;        // mixed form, energy_mode 0: particle 0's S:D (one word)
   double* out_part = nullptr;  // per-block partials of the row reduction
   double* out_last = nullptr;  // the last row recorded
   double* series = nullptr;
@@ -356,6 +357,7 @@ static void layout_arena(wf_domain* d, Arena& A) {
   A.take(&d->s_orig, n); A.take(&d->d_mm, 8); A.take(&d->d_status, WF_STATUS_WORDS);
   A.take(&d->d_cstat, 2);
   A.take(&d->fr, n); A.take(&d->out_part, wf_out_partial_words(WF_MAX_BC));
+  A.take(&d->e0, 1);
   d->t_halo_cap = 10 * n;      // halo entries: ~7 per slot on cell-sorted lattices
   A.take(&d->t_hoff, n / WF_TILE); A.take(&d->t_hcnt, n / WF_TILE);
   A.take(&d->t_halo, d->t_halo_cap); A.take(&d->t_nbl, (int64_t)WF_NB_ALLOC * n);
@@ -397,6 +399,7 @@ static StepParams make_params(const wf_domain* d) {
   P.newton_rtol = d->newton_rtol;
   P.clamp_homologous = d->clamp_homologous;
   P.energy_mode = d->energy_mode;
+  P.e0 = d->e0;
   P.inv = d->inv;
   P.contact = d->meshes.empty() ? 0 : 1;
   P.ncsid = (int)d->meshes.size();

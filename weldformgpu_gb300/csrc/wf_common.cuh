@@ -171,6 +171,7 @@ struct StepParams {
   double newton_rtol;
   int clamp_homologous;
   int energy_mode;      // 0 reference (particle 0's tensors), 1 per particle
+  double* e0;           // mixed form, energy_mode 0: particle 0's S:D of this step
   const int32_t* inv;   // inv[original id] = slot (particle 0's slot for energy_mode 0)
   int contact;          // contact pass filter active
   int ncsid;

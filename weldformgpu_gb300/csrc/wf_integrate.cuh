@@ -56,6 +56,9 @@ __device__ __forceinline__ void integrate_mixed_one(const StepParams& P, const F
   F.vd[i] = make_double4(vx, vy, vz, v4.w);
   F.u[i] = u;
   F.a[i] = make_double4(ax, ay, az, 0.0);
+  // energy_mode 0: particle 0's S:D of this step (written by the stress pass)
+  // for every particle, as k_integrate's FP64 form
+  if (P.energy_mode == 0) F.eint[i] += xm.w / v4.w * *P.e0 * P.dt;
   p32_out[i] = make_float4((float)xm.x, (float)xm.y, (float)xm.z, (float)xm.w);
   F.v32[i] = make_float4((float)vx, (float)vy, (float)vz, (float)v4.w);
   const double T = F.T[i];

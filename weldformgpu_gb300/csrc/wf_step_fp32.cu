@@ -612,11 +612,18 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
   F.seq[i] = seq;
   F.dep[i] = dep;
   F.eff[i] = (double)eff;
-  // CalcIntEnergy with the particle's own tensors, accumulated in FP64
-  const float def = __fdividef(pi.w, rf) *
-                    (Sn.xx * Dxx + Sn.yy * Dyy + Sn.zz * Dzz +
-                     2.0f * (Sn.xy * Dxy + Sn.yz * Dyz + Sn.xz * Dxz));
-  F.eint[i] += (double)def * P.dt;
+  // CalcIntEnergy, accumulated in FP64: energy_mode 1 with the particle's own
+  // tensors; energy_mode 0 (the reference's, Energy.cu:270-276) with particle
+  // 0's for every particle: its S:D goes to *P.e0 and the integration adds
+  // m/rho S0:D0 dt to each particle
+  const float sd = Sn.xx * Dxx + Sn.yy * Dyy + Sn.zz * Dzz +
+                   2.0f * (Sn.xy * Dxy + Sn.yz * Dyz + Sn.xz * Dxz);
+  if (P.energy_mode != 0) {
+    const float def = __fdividef(pi.w, rf) * sd;
+    F.eint[i] += (double)def * P.dt;
+  } else if (i == (int64_t)P.inv[0]) {
+    *P.e0 = (double)sd;
+  }
   warp_count(status, n_it, n_call, n_mlp, capped, eps_p > 1.e-6);
   if (!isfinite(st)) atomicOr(status, WF_STATUS_NAN);
 }
