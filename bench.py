@@ -178,9 +178,16 @@ def preload(sc, steps):
     return st
 
 
-def train_mlp(sc, state, log_steps=5, cap=1 << 20):
-    """Warm-start network for this material: pairs logged by the plain FP64
-    form from the checkpoint plus synthetic states, trained on the GPU."""
+MLP_SYNTH = 1 << 21          # synthetic states (targets from an FP64 Newton on the GPU)
+MLP_STEPS = 8000             # Adam steps of 4,096 pairs (~3 passes over ~10.5M pairs)
+
+
+def train_mlp(sc, state, log_steps=12, cap=1 << 23):
+    """Warm-start network for this material: ~10M training pairs, the
+    (state, converged increment) pairs the plain FP64 form logs over
+    `log_steps` steps from the checkpoint (up to `cap`, ~0.7M plastic
+    particles per step at 786k) plus MLP_SYNTH synthetic states, trained on
+    the GPU."""
     from weldformgpu_gb300 import mlp
     t0 = time.perf_counter()
     opts = base_options()
@@ -191,10 +198,11 @@ def train_mlp(sc, state, log_steps=5, cap=1 << 20):
     d.step(log_steps)
     logged = d.get_return_map_log(cap)
     d.close()
-    params, loss = mlp.train_jc_warm_start(sc["mat"], sc["G"], n_synth=262144, logged=logged,
-                                           steps=4000, batch=4096)
-    info = {"train_loss_mse": loss, "logged_pairs": int(len(logged[0])), "synthetic_pairs": 262144,
-            "train_steps": 4000, "batch": 4096, "train_s": time.perf_counter() - t0}
+    params, loss = mlp.train_jc_warm_start(sc["mat"], sc["G"], n_synth=MLP_SYNTH, logged=logged,
+                                           steps=MLP_STEPS, batch=4096)
+    info = {"train_loss_mse": loss, "logged_pairs": int(len(logged[0])),
+            "synthetic_pairs": MLP_SYNTH, "train_steps": MLP_STEPS, "batch": 4096,
+            "train_s": time.perf_counter() - t0}
     return params, info
 
 
