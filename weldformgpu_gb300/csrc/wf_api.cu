@@ -96,6 +96,7 @@ struct wf_domain {
   int64_t t_halo_cap = 0;
   int tile_staging = 0;        // option "tile_staging" (off: measured slower, see the design notes)
   int list_prefetch = 1;       // option "list_prefetch"
+  int state_prefetch = 1;      // option "state_prefetch"
   // 16-bit lists of the global gather path (wf_tiles.cuh), rebuilt with the lists
   int list16 = 0;              // option "list16"
   bool l16_built = false;
@@ -427,6 +428,7 @@ static StepParams make_params(const wf_domain* d) {
   }
   P.mlp_on = d->mlp_on;
   P.nb_pf = d->list_prefetch;
+  P.state_pf = d->state_prefetch;
   const wf_material& m = d->mat;
   MatParams& M = P.mat;
   M.model = m.model;
@@ -1536,6 +1538,7 @@ int wf_set_option(wf_domain* d, const char* key, double v) {
   }
   else if (k == "tile_staging") d->tile_staging = v != 0;   // takes effect at the next rebuild
   else if (k == "list_prefetch") d->list_prefetch = v != 0;
+  else if (k == "state_prefetch") d->state_prefetch = v != 0;
   else if (k == "list16") d->list16 = v != 0;          // takes effect at the next rebuild
   else if (k == "tile_cap_max") {
     if (!(v >= 1.0) || v > WF_TILE_HALO_MAX)

@@ -45,6 +45,13 @@ __device__ __forceinline__ void nb_prefetch(const int32_t* nb, int64_t npad, int
     asm volatile("prefetch.global.L2 [%0];" ::"l"(nb + ((int64_t)b * npad + i) * WF_NB_BLK));
 }
 
+// Brings the line holding p towards L2 (a hint: no registers held).  The
+// mixed pair passes issue it for the per-particle state their tail reads
+// after the pair loop, so that the tail's loads hit L2.
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 #define WF_MAX_BC 16
 #define WF_MAX_MESH 4
 #define WF_PI 3.14159265358979323846
@@ -192,6 +199,7 @@ struct StepParams {
                         // BCs are imposed, written at the slots of BC-zone particles
   int mlp_on;           // MLP warm start of the Newton return map
   int nb_pf;            // L2 prefetch of the neighbour lists two blocks ahead (mixed passes)
+  int state_pf;         // L2 prefetch of the state a mixed pass reads after its pair loop
   int refresh_pow;      // recompute eps_p^n with pow() this step (bounds series drift)
   int64_t log_cap;      // return-map log (training pairs for the MLP): capacity
   unsigned long long* log_count;

@@ -219,6 +219,10 @@ __global__ void __launch_bounds__(128, kDensMinBlocks) k_density_heat32(StepPara
   const float2 ti = F.th32[i];
   const bool solid = F.perm[i] < P.n_solid;
   const int32_t idi = F.id[i];
+  if (P.state_pf && g == 0) {
+    prefetch_l2(F.vd + i); prefetch_l2(F.T + i); prefetch_l2(F.cpT + i);
+    prefetch_l2(F.dep + i); prefetch_l2(F.sy + i); prefetch_l2(F.Ta + i);
+  }
   float drho, sf;
   const int c = cnt[i];
   const int b16 = L16.base ? L16.base[i / WF_TILE] : -1;     // uniform over the block
@@ -452,6 +456,10 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
   if (valid) F.p[i] = p;
   const bool solid = valid && F.perm[i] < P.n_solid;
   if (!mlp && !solid) return;
+  if (P.state_pf && solid) {
+    prefetch_l2(F.ss32 + 6 * i); prefetch_l2(F.eps_p + i); prefetch_l2(F.sy + i);
+    prefetch_l2(F.pwn + i); prefetch_l2(F.T + i); prefetch_l2(F.eint + i);
+  }
   const int c = solid ? cnt[i] : 0;
   float acc[9];
   const int b16 = L16.base ? L16.base[i0 / WF_TILE] : -1;    // uniform over the block
@@ -774,6 +782,9 @@ __global__ void __launch_bounds__(128, 7) k_accel_int32(StepParams P, Fields F,
   const float2* sgb;
   sigr32_split(sigr32, P.npad, sga, sgb);
   const AccelSrc src{F.p32, v32b, sga, sgb};
+  if (P.state_pf && g == 0) {
+    prefetch_l2(F.xm + i); prefetch_l2(vd2 + i); prefetch_l2(F.u + i); prefetch_l2(F.T + i);
+  }
   // rigid (non-solid) slots: zero acceleration, moved by their BCs
   float4 af = make_float4(0.f, 0.f, 0.f, 0.f);
   if (F.perm[i] < P.n_solid) {
