@@ -152,7 +152,10 @@ int wf_add_trimesh(wf_domain* d, const double* nodes, int32_t nn, const int32_t*
  *   read neighbours from per-tile halos in shared memory; same results),
  *   tile_cap_max (2048: largest halo staged), list_prefetch (1: L2 prefetch of
  *   the neighbour lists two blocks ahead), state_prefetch (1: L2 prefetch, before
- *   the pair loop, of the state each mixed pass reads after it), list16 (0; 1: 16-bit list offsets for
+ *   the pair loop, of the state each mixed pass reads after it), wave_prefetch
+ *   (2: L2 prefetch of the prologue and first 2 list blocks of the slot one
+ *   resident wave of blocks later; 0 off), wave_prefetch_distance (1.0, in
+ *   resident waves), list16 (0; 1: 16-bit list offsets for
  *   the mixed passes' global gathers; same results), graph (1), output_interval (1e300),
  *   resume (0), profile_kernel (0). */
 int wf_set_option(wf_domain* d, const char* key, double value);

@@ -97,6 +97,8 @@ struct wf_domain {
   int tile_staging = 0;        // option "tile_staging" (off: measured slower, see the design notes)
   int list_prefetch = 1;       // option "list_prefetch"
   int state_prefetch = 1;      // option "state_prefetch"
+  int wave_prefetch = 2;       // option "wave_prefetch"
+  double wave_dist = 1.0;      // option "wave_prefetch_distance"
   // 16-bit lists of the global gather path (wf_tiles.cuh), rebuilt with the lists
   int list16 = 0;              // option "list16"
   bool l16_built = false;
@@ -429,6 +431,8 @@ static StepParams make_params(const wf_domain* d) {
   P.mlp_on = d->mlp_on;
   P.nb_pf = d->list_prefetch;
   P.state_pf = d->state_prefetch;
+  P.wave_pf = d->wave_prefetch;
+  P.wave_dist = d->wave_dist;
   const wf_material& m = d->mat;
   MatParams& M = P.mat;
   M.model = m.model;
@@ -1539,6 +1543,8 @@ int wf_set_option(wf_domain* d, const char* key, double v) {
   else if (k == "tile_staging") d->tile_staging = v != 0;   // takes effect at the next rebuild
   else if (k == "list_prefetch") d->list_prefetch = v != 0;
   else if (k == "state_prefetch") d->state_prefetch = v != 0;
+  else if (k == "wave_prefetch") d->wave_prefetch = (int)v;
+  else if (k == "wave_prefetch_distance") d->wave_dist = v;
   else if (k == "list16") d->list16 = v != 0;          // takes effect at the next rebuild
   else if (k == "tile_cap_max") {
     if (!(v >= 1.0) || v > WF_TILE_HALO_MAX)

@@ -200,6 +200,10 @@ struct StepParams {
   int mlp_on;           // MLP warm start of the Newton return map
   int nb_pf;            // L2 prefetch of the neighbour lists two blocks ahead (mixed passes)
   int state_pf;         // L2 prefetch of the state a mixed pass reads after its pair loop
+  int wave_pf;          // L2 prefetch of the prologue of the slot one resident wave later
+                        // and of the first wave_pf blocks of its list (0: none)
+  int64_t pf_ahead;     // that distance in slots (set per launch; 0: none)
+  double wave_dist;     // the distance in resident waves (host side)
   int refresh_pow;      // recompute eps_p^n with pow() this step (bounds series drift)
   int64_t log_cap;      // return-map log (training pairs for the MLP): capacity
   unsigned long long* log_count;

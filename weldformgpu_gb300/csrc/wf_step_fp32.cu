@@ -223,6 +223,14 @@ __global__ void __launch_bounds__(128, kDensMinBlocks) k_density_heat32(StepPara
     prefetch_l2(F.vd + i); prefetch_l2(F.T + i); prefetch_l2(F.cpT + i);
     prefetch_l2(F.dep + i); prefetch_l2(F.sy + i); prefetch_l2(F.Ta + i);
   }
+  if (P.pf_ahead > 0 && g == 0) {
+    const int64_t ia = i + P.pf_ahead;      // the slot this thread's successor will take
+    if (ia < P.n) {
+      prefetch_l2(F.p32 + ia); prefetch_l2(F.v32 + ia); prefetch_l2(F.th32 + ia);
+      prefetch_l2(cnt + ia); prefetch_l2(F.perm + ia);
+      for (int b = 0; b < P.wave_pf && b < WF_NB_BLOCKS; b++) nb_prefetch(nb, P.npad, ia, b, 4);
+    }
+  }
   float drho, sf;
   const int c = cnt[i];
   const int b16 = L16.base ? L16.base[i / WF_TILE] : -1;     // uniform over the block
@@ -459,6 +467,14 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
   if (P.state_pf && solid) {
     prefetch_l2(F.ss32 + 6 * i); prefetch_l2(F.eps_p + i); prefetch_l2(F.sy + i);
     prefetch_l2(F.pwn + i); prefetch_l2(F.T + i); prefetch_l2(F.eint + i);
+  }
+  if (P.pf_ahead > 0) {
+    const int64_t ia = i0 + P.pf_ahead;     // the slot this thread's successor will take
+    if (ia < P.n) {
+      prefetch_l2(F.p32 + ia); prefetch_l2(v32b + ia); prefetch_l2(F.vd + ia);
+      prefetch_l2(F.drho + ia); prefetch_l2(cnt + ia); prefetch_l2(F.perm + ia);
+      for (int b = 0; b < P.wave_pf && b < WF_NB_BLOCKS; b++) nb_prefetch(nb, P.npad, ia, b, 4);
+    }
   }
   const int c = solid ? cnt[i] : 0;
   float acc[9];
@@ -785,6 +801,15 @@ __global__ void __launch_bounds__(128, 7) k_accel_int32(StepParams P, Fields F,
   if (P.state_pf && g == 0) {
     prefetch_l2(F.xm + i); prefetch_l2(vd2 + i); prefetch_l2(F.u + i); prefetch_l2(F.T + i);
   }
+  if (P.pf_ahead > 0 && g == 0) {
+    const int64_t ia = i + P.pf_ahead;      // the slot this thread's successor will take
+    if (ia < P.n) {
+      prefetch_l2(F.p32 + ia); prefetch_l2(v32b + ia); prefetch_l2(sga + ia);
+      prefetch_l2(sgb + ia); prefetch_l2(cnt + ia); prefetch_l2(F.perm + ia);
+      prefetch_l2(F.id + ia);
+      for (int b = 0; b < P.wave_pf && b < WF_NB_BLOCKS; b++) nb_prefetch(nb, P.npad, ia, b, 2 * kAccelLanes);
+    }
+  }
   // rigid (non-solid) slots: zero acceleration, moved by their BCs
   float4 af = make_float4(0.f, 0.f, 0.f, 0.f);
   if (F.perm[i] < P.n_solid) {
@@ -853,6 +878,24 @@ __global__ void __launch_bounds__(2 * WF_TILE, 3) k_accel_int32_tiles(
 
 static inline int blocks_for(int64_t n, int t) { return (int)((n + t - 1) / t); }
 
+// Slots one resident wave ahead for `kernel` (SMs x resident blocks x threads
+// per block / lanes per slot): block b + (resident blocks) starts about when
+// block b ends, so the prologue a block prefetches for the slots that far on
+// is in L2 when their block starts.  Cached per dynamic shared memory size.
+template <class K>
+static int64_t wave_slots(K kernel, int threads, size_t smem, int lanes, size_t* c_smem,
+                          int64_t* c_val) {
+  if (*c_val > 0 && *c_smem == smem) return *c_val;
+  int dev = 0, sms = 0, per = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem) != cudaSuccess)
+    return 0;
+  *c_smem = smem;
+  *c_val = (int64_t)sms * per * threads / lanes;
+  return *c_val;
+}
+
 void launch_fp32_density(const StepParams& P, const Fields& F, double4* vd2, float4* v32b,
                          const NbBuffers& N, cudaStream_t s) {
   k_density32<<<blocks_for(P.n, 128), 128, 0, s>>>(P, F, vd2, v32b, N.nb, N.cnt);
@@ -866,8 +909,13 @@ void launch_fp32_density_heat(const StepParams& P, const Fields& F, double4* vd2
       Tl.cap > 0 ? (2 * sizeof(float4) + sizeof(float2)) * (size_t)Tl.cap + WF_TILE_LIST_BYTES : 0;
   static size_t opted[64] = {};     // per device: dynamic shared memory opted in so far
   opt_in_smem(k_density_heat32, smem, opted);
+  static size_t c_smem = 0;
+  static int64_t c_val = 0;
+  StepParams Q = P;
+  Q.pf_ahead = !P.wave_pf ? 0 : (int64_t)(P.wave_dist * (double)wave_slots(
+      k_density_heat32, 128, smem, kDensLanes, &c_smem, &c_val));
   k_density_heat32<<<blocks_for(P.n * kDensLanes, 128), 128, smem, s>>>(
-      P, F, vd2, v32b, N.nb, N.cnt, first, plastic_heat, Tl, L16);
+      Q, F, vd2, v32b, N.nb, N.cnt, first, plastic_heat, Tl, L16);
 }
 void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b, float* sigr32,
                         const NbBuffers& N, int* status, const void* mlp_packed,
@@ -879,7 +927,12 @@ void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b
                       (T.cap > 0 ? 2 * sizeof(float4) * (size_t)T.cap + WF_TILE_LIST_BYTES : 0);
   static size_t opted[64] = {};     // per device: dynamic shared memory opted in so far
   opt_in_smem(k_stress32, smem, opted);
-  k_stress32<<<blocks_for(P.n, 128), 128, smem, s>>>(P, F, v32b, sigr32, N.nb, N.cnt, status, W, l1,
+  static size_t c_smem = 0;
+  static int64_t c_val = 0;
+  StepParams Q = P;
+  Q.pf_ahead = !P.wave_pf ? 0 : (int64_t)(P.wave_dist * (double)wave_slots(
+      k_stress32, 128, smem, 1, &c_smem, &c_val));
+  k_stress32<<<blocks_for(P.n, 128), 128, smem, s>>>(Q, F, v32b, sigr32, N.nb, N.cnt, status, W, l1,
                                                      T, L16);
 }
 void launch_fp32_accel(const StepParams& P, const Fields& F, const float4* v32b,
@@ -897,6 +950,11 @@ void launch_fp32_accel_integrate(const StepParams& P, const Fields& F, const flo
         P, F, v32b, sigr32, vd2, N.nb, N.cnt, F.p32n, T);
     return;
   }
-  k_accel_int32<<<blocks_for(P.n * kAccelLanes, 128), 128, 0, s>>>(P, F, v32b, sigr32, vd2, N.nb, N.cnt,
-                                                     F.p32n, L16);
+  static size_t c_smem = 0;
+  static int64_t c_val = 0;
+  StepParams Q = P;
+  Q.pf_ahead = !P.wave_pf ? 0 : (int64_t)(P.wave_dist * (double)wave_slots(
+      k_accel_int32, 128, 0, kAccelLanes, &c_smem, &c_val));
+  k_accel_int32<<<blocks_for(P.n * kAccelLanes, 128), 128, 0, s>>>(Q, F, v32b, sigr32, vd2, N.nb,
+                                                                   N.cnt, F.p32n, L16);
 }
