@@ -150,8 +150,8 @@ int wf_add_trimesh(wf_domain* d, const double* nodes, int32_t nn, const int32_t*
  *   contact_stiffness (0.1), contact_vreg (1e-3), contact_heat_fraction (1),
  *   fuse_heat (1), fuse_integrate (1), tile_staging (0; 1: the mixed pair passes
  *   read neighbours from per-tile halos in shared memory; same results),
- *   tile_cap_max (2048: largest halo staged), list_prefetch (1: L2 prefetch of
- *   the neighbour lists two blocks ahead), state_prefetch (1: L2 prefetch, before
+ *   tile_cap_max (2048: largest halo staged), list_prefetch (2: L2 prefetch of
+ *   the neighbour lists that many blocks ahead; 0 off), state_prefetch (1: L2 prefetch, before
  *   the pair loop, of the state each mixed pass reads after it), wave_prefetch
  *   (2: L2 prefetch of the prologue and first 2 list blocks of the slot one
  *   resident wave of blocks later; 0 off), wave_prefetch_distance (1.0, in

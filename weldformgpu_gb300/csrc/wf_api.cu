@@ -95,7 +95,7 @@ struct wf_domain {
   uint16_t* t_nbl = nullptr;
   int64_t t_halo_cap = 0;
   int tile_staging = 0;        // option "tile_staging" (off: measured slower, see the design notes)
-  int list_prefetch = 1;       // option "list_prefetch"
+  int list_prefetch = 2;       // option "list_prefetch" (blocks ahead)
   int state_prefetch = 1;      // option "state_prefetch"
   int wave_prefetch = 2;       // option "wave_prefetch"
   double wave_dist = 1.0;      // option "wave_prefetch_distance"
@@ -1541,7 +1541,7 @@ int wf_set_option(wf_domain* d, const char* key, double v) {
     }
   }
   else if (k == "tile_staging") d->tile_staging = v != 0;   // takes effect at the next rebuild
-  else if (k == "list_prefetch") d->list_prefetch = v != 0;
+  else if (k == "list_prefetch") d->list_prefetch = std::max(0, std::min((int)v, WF_NB_BLOCKS));
   else if (k == "state_prefetch") d->state_prefetch = v != 0;
   else if (k == "wave_prefetch") d->wave_prefetch = (int)v;
   else if (k == "wave_prefetch_distance") d->wave_dist = v;

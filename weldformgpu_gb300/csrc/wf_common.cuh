@@ -198,7 +198,7 @@ struct StepParams {
   double4* fr;          // when not null (an output row is due this step): m a before the
                         // BCs are imposed, written at the slots of BC-zone particles
   int mlp_on;           // MLP warm start of the Newton return map
-  int nb_pf;            // L2 prefetch of the neighbour lists two blocks ahead (mixed passes)
+  int nb_pf;            // L2 prefetch of the neighbour lists nb_pf blocks ahead (mixed passes; 0 off)
   int state_pf;         // L2 prefetch of the state a mixed pass reads after its pair loop
   int wave_pf;          // L2 prefetch of the prologue of the slot one resident wave later
                         // and of the first wave_pf blocks of its list (0: none)

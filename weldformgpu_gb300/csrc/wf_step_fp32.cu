@@ -138,7 +138,7 @@ __device__ __forceinline__ void density_heat_pairs(const StepParams& P, const Fi
 #pragma unroll
     for (int q = 0; q < W; q++) js[q] = nx[q];
     const int m = c - WF_NB_BLK * b - g * W;   // entries of this lane's sub-block in the list
-    if (P.nb_pf && c > WF_NB_BLK * (b + 2)) list.prefetch(b + 2, kDensLanes);
+    if (P.nb_pf && c > WF_NB_BLK * (b + P.nb_pf)) list.prefetch(b + P.nb_pf, kDensLanes);
     if (c > WF_NB_BLK * (b + 1)) list.template sub<W>(b + 1, g, nx);
 #pragma unroll
     for (int h = 0; h < W; h += NB) {
@@ -365,7 +365,7 @@ __device__ __forceinline__ void stress_pairs(const StepParams& P, const Fields& 
 #pragma unroll
     for (int q = 0; q < 8; q++) js[q] = nx[q];
     const int m = c - WF_NB_BLK * b;
-    if (P.nb_pf && m > 2 * WF_NB_BLK) list.prefetch(b + 2, 1);
+    if (P.nb_pf && m > P.nb_pf * WF_NB_BLK) list.prefetch(b + P.nb_pf, 1);
     if (m > WF_NB_BLK) list.block(b + 1, nx);
 #pragma unroll
     for (int h = 0; h < WF_NB_BLK; h += kStressBatch) {
@@ -697,7 +697,7 @@ __device__ __forceinline__ float4 accel_value(const StepParams& P, const Fields&
 #pragma unroll
     for (int q = 0; q < W; q++) js[q] = nx[q];
     const int m = c - WF_NB_BLK * b - g * W;   // entries of this lane's sub-block in the list
-    if (P.nb_pf && c > WF_NB_BLK * (b + 2)) list.prefetch(b + 2, kAccelLanes);
+    if (P.nb_pf && c > WF_NB_BLK * (b + P.nb_pf)) list.prefetch(b + P.nb_pf, kAccelLanes);
     if (c > WF_NB_BLK * (b + 1)) list.template sub<W>(b + 1, g, nx);
 #pragma unroll
     for (int hh = 0; hh < W; hh += kAccelBatch) {
