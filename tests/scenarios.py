@@ -1,5 +1,7 @@
 """Scenario helpers for the tests: the package's scenario builders plus the
 loader for the reference compiled for the CPU (oracle/_ref)."""
+import numpy as np
+
 from weldformgpu_gb300.scenarios import *  # noqa: F401,F403
 from weldformgpu_gb300.scenarios import compression_cylinder, heat_box, load, load_heat  # noqa: F401
 
@@ -64,3 +66,20 @@ def one_particle_under_triangle(x0, tri_nodes, v_tool, mu=0.3, dx=1.0e-3, dt=1.0
         s = mu * fn / max(np.linalg.norm(vt), 1.0e-3)
         return fn * n - s * vt, s * (vt @ vt), n
     return sc, expected
+
+
+def support_radius_pairs(h=1.0e-3, seed=3):
+    """4,000 isolated pairs whose distance lies within +-4e-7 (relative, about
+    3 float32 ulps) of the support radius r = 2h."""
+    rng = np.random.default_rng(seed)
+    g = np.stack(np.meshgrid(np.arange(20), np.arange(20), np.arange(10), indexing="ij"),
+                 -1).reshape(-1, 3)
+    a = g * (10.0 * h) + rng.uniform(-0.5 * h, 0.5 * h, g.shape)
+    u = rng.normal(size=g.shape)
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    r = float(np.float32(2.0 * h))
+    e = rng.uniform(-4e-7, 4e-7, len(g))
+    x = np.empty((2 * len(g), 3))
+    x[0::2] = a
+    x[1::2] = a + u * (r * (1.0 + e))[:, None]
+    return x

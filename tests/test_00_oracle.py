@@ -35,6 +35,29 @@ def test_neighbors_small_match_reference_cunsearch():
         assert np.array_equal(lst[i, :cnt[i]], g["lists"][i, :cnt[i]])
 
 
+def test_neighbour_rule_at_the_support_radius_matches_float32():
+    """Pairs within ~3 float32 ulps of r = 2h: the oracle's lists are those of
+    the float rule evaluated with numpy float32 (rounded differences, squares
+    and sum, no fused multiply-add; d^2 < r^2), about half the pairs in."""
+    h = 1.0e-3
+    x = S.support_radius_pairs(h)
+    n = len(x)
+    d = O.OracleDomain(n)
+    d.set_h(h)
+    d.set_positions(np.ascontiguousarray(x).ravel())
+    d.find_neighbors()
+    cnt, lst = d.get_neighbors()
+    xf = x.astype(np.float32)
+    dd = xf[1::2] - xf[0::2]
+    s = (dd[:, 0] * dd[:, 0] + dd[:, 1] * dd[:, 1]) + dd[:, 2] * dd[:, 2]
+    r = np.float32(2.0 * h)
+    inside = s < r * r
+    assert s.dtype == np.float32
+    assert np.array_equal(cnt[0::2] == 1, inside) and np.array_equal(cnt[1::2] == 1, inside)
+    assert np.array_equal(lst[0::2, 0][inside], np.arange(1, n, 2)[inside])
+    assert 0.3 < inside.mean() < 0.7
+
+
 def test_neighbors_config1_digest():
     g = np.load(os.path.join(GOLDEN, "nb_c1.npz"))
     c1 = S.compression_cylinder(R=0.005, H=0.010)

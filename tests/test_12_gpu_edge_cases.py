@@ -135,3 +135,27 @@ def test_ragged_particle_counts(n):
     x = x[np.argsort(((x - c) ** 2).sum(1), kind="stable")[:n]]
     sc = with_positions(x, zones=True, vz_top=-5.0)
     check_fp64_and_mixed(sc, 40)
+
+
+def test_neighbour_rule_at_the_support_radius():
+    """Pairs within a few float32 ulps of the support radius: the lists follow
+    the float rule (FP32 differences, squares and their sum each rounded to
+    nearest, then d^2 < r^2) exactly as the oracle's; about half the pairs are
+    accepted, so a last-bit difference in the rule moves some of them."""
+    from weldformgpu_gb300 import Domain_d
+    h = 1.0e-3
+    x = S.support_radius_pairs(h)
+    n = len(x)
+    g = Domain_d(n)
+    g.set_h(h)
+    g.set_positions(x)
+    g.find_neighbors()
+    o = O.OracleDomain(n)
+    o.set_h(h)
+    o.set_positions(np.ascontiguousarray(x).ravel())
+    o.find_neighbors()
+    gc, gl = g.get_neighbors()
+    oc, ol = o.get_neighbors()
+    assert same_lists(gc, gl, oc, ol)
+    acc = int((gc[0::2] == 1).sum())
+    assert 0.3 * (n // 2) < acc < 0.7 * (n // 2), acc

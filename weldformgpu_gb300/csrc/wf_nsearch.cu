@@ -258,17 +258,12 @@ __device__ __forceinline__ I nb_at_i(I npad, I i, int k) {
 constexpr int kNbStage = 192;    // staged candidates per warp and round
 
 // Tests the staged candidates against the group's particles (part[j]: position
-// and, in w, the storage slot of particle j, whose count lane j holds) and
-// appends the accepted ones to their lists.  Per chunk of 64 candidates (two
-// per lane: t and t + 32) and per particle j, two ballots give the accepting
-// lanes; each writes its candidate at j's count before the chunk plus the
-// accepted candidates before it in staging order (the first half's, then the
-// second half's below its lane), so the entries keep candidate order.  The two
-// candidates' distances are computed with packed FP32 operations, each
-// component rounded like the scalar rule (__fadd2_rn / __fmul2_rn behave per
-// component as __fadd_rn / __fmul_rn; q - p is q + (-p)).  The counts advance
-// once per chunk (lane j keeps particle j's masks of the chunk), which leaves
-// no chain between the particles' iterations.
+// and, in w, the storage slot of particle j, whose count lane j holds) and appends the accepted ones to their lists.  Per chunk of 32
+// candidates and per particle j, one ballot gives the accepting lanes; each
+// writes its candidate at j's count before the chunk plus the accepting lanes
+// below it, so the entries keep candidate order.  The counts advance once per
+// chunk (lane j keeps particle j's mask of the chunk), which leaves no chain
+// between the particles' iterations.
 template <class I>
 __device__ __forceinline__ void nb_append_round(int nstaged, const float4* __restrict__ sp,
                                                 const int32_t* __restrict__ sid, int gn,
@@ -277,37 +272,27 @@ __device__ __forceinline__ void nb_append_round(int nstaged, const float4* __res
                                                 int& count) {
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
-  for (int ch = 0; ch < nstaged; ch += 64) {
-    const int t0 = ch + lane, t1 = t0 + 32;
-    const bool v0 = t0 < nstaged, v1 = t1 < nstaged;
-    const float4 q0 = v0 ? sp[t0] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 q1 = v1 ? sp[t1] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const int32_t id0 = v0 ? sid[t0] : 0, id1 = v1 ? sid[t1] : 0;
-    const float2 qx = make_float2(q0.x, q1.x), qy = make_float2(q0.y, q1.y),
-                 qz = make_float2(q0.z, q1.z);
-    unsigned mine0 = 0u, mine1 = 0u;
-#pragma unroll 2
+  for (int ch = 0; ch < nstaged; ch += 32) {
+    const int t = ch + lane;
+    const bool v = t < nstaged;
+    const float4 q = v ? sp[t] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int32_t qid = v ? sid[t] : 0;
+    unsigned mine = 0u;
+#pragma unroll 4
     for (int j = 0; j < gn; j++) {
       const float4 pj = part[j];   // same address on every lane: one broadcast read
       const int32_t ij = __float_as_int(pj.w);
       const int base = __shfl_sync(0xffffffffu, count, j);
-      const float2 dx = __fadd2_rn(qx, make_float2(-pj.x, -pj.x));
-      const float2 dy = __fadd2_rn(qy, make_float2(-pj.y, -pj.y));
-      const float2 dz = __fadd2_rn(qz, make_float2(-pj.z, -pj.z));
-      const float2 sq = __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)),
-                                   __fmul2_rn(dz, dz));
-      const bool a0 = v0 && sq.x < r2 && sq.x > 0.0f;
-      const bool a1 = v1 && sq.y < r2 && sq.y > 0.0f;
-      const unsigned m0 = __ballot_sync(0xffffffffu, a0);
-      const unsigned m1 = __ballot_sync(0xffffffffu, a1);
-      const int k0 = base + __popc(m0 & lt);
-      const int k1 = base + __popc(m0) + __popc(m1 & lt);
-      if (a0 && k0 < WF_NB) nb[nb_at_i<I>((I)npad, (I)ij, k0)] = id0;
-      if (a1 && k1 < WF_NB) nb[nb_at_i<I>((I)npad, (I)ij, k1)] = id1;
-      mine0 = lane == j ? m0 : mine0;
-      mine1 = lane == j ? m1 : mine1;
+      const float dx = __fsub_rn(q.x, pj.x), dy = __fsub_rn(q.y, pj.y), dz = __fsub_rn(q.z, pj.z);
+      const float sq =
+          __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+      const bool acc = v && sq < r2 && sq > 0.0f;
+      const unsigned m = __ballot_sync(0xffffffffu, acc);
+      const int k = base + __popc(m & lt);
+      if (acc && k < WF_NB) nb[nb_at_i<I>((I)npad, (I)ij, k)] = qid;
+      mine = lane == j ? m : mine;
     }
-    count += __popc(mine0) + __popc(mine1);
+    count += __popc(mine);
   }
 }
 
