@@ -65,7 +65,12 @@ typedef struct wf_domain wf_domain;
 /* Domain_d::SetDimension (src/cuda/Domain_d.cu:19-234): allocates the SoA
  * arena for `particle_count` particles; solid_part_count = particle_count. */
 int         wf_create(wf_domain** out, int64_t particle_count);
+/* Domain_d::~Domain_d.  The domain's device arena (one allocation for every
+ * per-particle array) is kept for the next wf_create on the same device whose
+ * layout needs between 80 and 100 % of it (zeroed there like a fresh one);
+ * wf_release_cache() returns it to the driver. */
 int         wf_destroy(wf_domain* d);
+int         wf_release_cache(void);
 const char* wf_last_error(const wf_domain* d);
 const char* wf_version(void);
 

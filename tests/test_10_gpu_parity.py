@@ -554,6 +554,43 @@ def test_setters_from_pinned_host_arrays_match_pageable():
         assert np.array_equal(a.get_field(f), b.get_field(f)), f
 
 
+def test_cached_arena_gives_a_fresh_domain():
+    """wf_destroy keeps the arena for the next wf_create: a domain built on a
+    reused arena (same size, and a smaller layout in the larger block) runs
+    exactly as one built on fresh memory, after the old one was run hot."""
+    from weldformgpu_gb300 import Domain_d, domain as D
+    sc = S.compression_cylinder(material="jc", vz_top=-10.0)
+    opts = {"return_map": 1, "precision": 1, "energy_mode": 1}
+    small = dict(sc)                     # the first 520 particles: a slightly smaller layout
+    m = 520
+    small.update(n=m, x=sc["x"][:m], m=sc["m"][:m], ids=sc["ids"][:m],
+                 not_write=sc["not_write"][:m], T=sc["T"][:m])
+    assert 0.9 * sc["n"] < m < sc["n"]
+    fields = ("x", "u", "v", "rho", "sigma", "pl_strain", "sigma_eq", "int_energy")
+
+    def run(scn):
+        d = S.load(Domain_d(scn["n"]), scn, opts)
+        d.step(60)
+        out = {f: d.get_field(f) for f in fields}
+        st = int(d.get_scalar("status"))
+        d.close()
+        return out, st
+
+    assert D.lib().wf_release_cache() == 0
+    fresh, st0 = run(sc)                 # on a fresh allocation
+    again, st1 = run(sc)                 # on the arena the first run left
+    assert D.lib().wf_release_cache() == 0
+    fresh_small, _ = run(small)
+    big, _ = run(sc)                     # leaves the larger block cached
+    reused_small, _ = run(small)         # the smaller layout in it
+    assert st0 == st1 == 0
+    for f in fields:
+        assert np.array_equal(fresh[f], again[f]), f
+        assert np.array_equal(fresh[f], big[f]), f
+        assert np.array_equal(fresh_small[f], reused_small[f]), f
+    assert D.lib().wf_release_cache() == 0
+
+
 def _graph_case(name):
     if name == "mixed_jc_heat":
         sc = S.compression_cylinder(material="jc", vz_top=-10.0)

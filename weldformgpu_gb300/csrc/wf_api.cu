@@ -13,6 +13,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -40,8 +41,15 @@ enum { KID_NONE = 0, KID_DENSITY = 1, KID_STRESS = 2, KID_ACCEL = 3, KID_INTEGRA
 struct wf_domain {
   int64_t n = 0, n_solid = 0, npad = 0;
   cudaStream_t stream = nullptr;
+  int dev = 0;                  // the device the domain was created on
   char* arena = nullptr;        // fixed-size device arrays, one allocation
-  size_t arena_bytes = 0;
+  size_t arena_bytes = 0;       // bytes the layout uses
+  size_t arena_alloc = 0;       // bytes of the allocation (a cached one may be larger)
+  // host -> device copies of the setters: two staging buffers filled on
+  // cstream, each scattered on `stream` (ev_full: copy done, ev_free: scatter done)
+  cudaStream_t cstream = nullptr;
+  cudaEvent_t ev_full[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
+  int stage_next = 0;
   // uniform scalars (the reference's setters fill every particle with one value)
   double h = 0, rho0 = 0, G = 0, Cs = 0, dt = 0, alpha = 1.0, beta = 0.0;
   double h_conv = 100.0, T_inf = 0.0;
@@ -113,6 +121,7 @@ struct wf_domain {
   bool in_callback = false;
   unsigned long long* d_cstat = nullptr;   // contact law 1 triangle-test counters
   double* d_stage = nullptr;   // staging for ABI copies (6 doubles per particle)
+  double* d_stage2 = nullptr;  // the setters' second staging buffer
   // solver state
   bool started = false, nb_built = false, is_yielding = false, isfirst = true;
   // mixed form: the heat pass of the last step runs inside the next step's
@@ -366,7 +375,7 @@ static void layout_arena(wf_domain* d, Arena& A) {
   A.take(&d->t_halo, d->t_halo_cap); A.take(&d->t_nbl, (int64_t)WF_NB_ALLOC * n);
   A.take(&d->l16_base, n / WF_TILE); A.take(&d->l16_off, (int64_t)WF_NB_ALLOC * n);
   A.take(&d->out_last, WF_ROW_FIXED + 3 * WF_MAX_BC); A.take(&d->series_count, 1);
-  A.take(&d->d_stage, 6 * n); A.take(&d->mlp_w, WF_MLP_NPARAM);
+  A.take(&d->d_stage, 6 * n); A.take(&d->d_stage2, 6 * n); A.take(&d->mlp_w, WF_MLP_NPARAM);
   A.take(&d->mlp_packed, (int64_t)wf_mlp_packed_bytes());
 }
 
@@ -380,6 +389,61 @@ static void free_fields(Fields& F) {
 // ---------------------------------------------------------------------------
 // parameters
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
+// arena cache
+// ---------------------------------------------------------------------------
+// wf_destroy keeps the last domain's arena (and its page-locked status words)
+// here instead of freeing them, and the next wf_create on the same device
+// whose layout needs between 80 and 100 % of it takes it over (zeroed on its
+// stream like a fresh one).  cudaMalloc and cudaFree of the ~1 GB arena of a
+// 786k-particle domain cost ~0.5 ms each, paid by every drop-in call that
+// creates and destroys its domain.  A cached block that does not fit is freed
+// before the new allocation; wf_release_cache() frees the cache.
+struct ArenaCache {
+  char* arena = nullptr;
+  size_t bytes = 0;
+  int dev = -1;
+  int* h_status = nullptr;
+};
+static std::mutex g_cache_mu;
+static ArenaCache g_cache;
+
+static void cache_free_locked() {
+  if (g_cache.arena) {
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(g_cache.dev);
+    cudaFree(g_cache.arena);
+    cudaSetDevice(cur);
+  }
+  if (g_cache.h_status) cudaFreeHost(g_cache.h_status);
+  g_cache = ArenaCache{};
+}
+static void cache_take(wf_domain* d) {
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  if (!g_cache.arena) return;
+  if (g_cache.dev != d->dev || g_cache.bytes < d->arena_bytes ||
+      g_cache.bytes > d->arena_bytes + d->arena_bytes / 4) {
+    cache_free_locked();
+    return;
+  }
+  d->arena = g_cache.arena;
+  d->arena_alloc = g_cache.bytes;
+  d->h_status = g_cache.h_status;
+  g_cache = ArenaCache{};
+}
+static void cache_put(wf_domain* d) {
+  if (!d->arena) return;
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  cache_free_locked();                       // keep the most recent one
+  g_cache.arena = d->arena;
+  g_cache.bytes = d->arena_alloc;
+  g_cache.dev = d->dev;
+  g_cache.h_status = d->h_status;
+  d->arena = nullptr;
+  d->h_status = nullptr;
+}
+
 static StepParams make_params(const wf_domain* d) {
   StepParams P;
   memset(&P, 0, sizeof P);
@@ -1129,15 +1193,25 @@ int wf_create(wf_domain** out, int64_t n) {
   d->npad = (n + 127) / 128 * 128;
   int rc = WF_OK;
   auto bail = [&](int code) { wf_destroy(d); return code; };
-  if (cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaGetDevice(&d->dev) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&d->cstream, cudaStreamNonBlocking) != cudaSuccess)
     return bail(WF_ERR_CUDA);
+  for (int b = 0; b < 2; b++)
+    if (cudaEventCreateWithFlags(&d->ev_full[b], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&d->ev_free[b], cudaEventDisableTiming) != cudaSuccess)
+      return bail(WF_ERR_CUDA);
   {
     Arena size;
     layout_arena(d, size);
     d->arena_bytes = size.off;
-    if (cudaMalloc((void**)&d->arena, d->arena_bytes) != cudaSuccess) {
-      d->arena = nullptr;
-      return bail(WF_ERR_ALLOC);
+    cache_take(d);
+    if (!d->arena) {
+      if (cudaMalloc((void**)&d->arena, d->arena_bytes) != cudaSuccess) {
+        d->arena = nullptr;
+        return bail(WF_ERR_ALLOC);
+      }
+      d->arena_alloc = d->arena_bytes;
     }
     if (cudaMemsetAsync(d->arena, 0, d->arena_bytes, d->stream) != cudaSuccess)
       return bail(WF_ERR_CUDA);
@@ -1145,7 +1219,8 @@ int wf_create(wf_domain** out, int64_t n) {
     place.base = reinterpret_cast<uintptr_t>(d->arena);
     layout_arena(d, place);
   }
-  if (cudaMallocHost((void**)&d->h_status, WF_STATUS_WORDS * sizeof(int)) != cudaSuccess)
+  if (!d->h_status &&
+      cudaMallocHost((void**)&d->h_status, WF_STATUS_WORDS * sizeof(int)) != cudaSuccess)
     return bail(WF_ERR_ALLOC);
   k_iota<<<nblk(n), 256, 0, d->stream>>>(n, d->F[0].perm, d->inv);
   k_fill_d<<<nblk(n), 256, 0, d->stream>>>(n, -1.0, d->F[0].pwn, 1, 0);
@@ -1156,7 +1231,9 @@ int wf_create(wf_domain** out, int64_t n) {
 
 int wf_destroy(wf_domain* d) {
   if (!d) return WF_OK;
+  if (d->cstream) cudaStreamSynchronize(d->cstream);
   if (d->stream) cudaStreamSynchronize(d->stream);
+  cache_put(d);                // the arena and status words, for the next domain
   for (int k = 0; k < 2; k++) free_fields(d->F[k]);
   for (MeshDev& M : d->meshes) {
     void* mp[] = {M.node, M.node_v, M.centroid, M.normal, M.elnode, M.pplane, M.cstart, M.ctri,
@@ -1177,31 +1254,67 @@ int wf_destroy(wf_domain* d) {
     if (cudaStreamEndCapture(d->stream, &g) == cudaSuccess && g) cudaGraphDestroy(g);
   }
   if (d->gexec) cudaGraphExecDestroy(d->gexec);
+  for (int b = 0; b < 2; b++) {
+    if (d->ev_full[b]) cudaEventDestroy(d->ev_full[b]);
+    if (d->ev_free[b]) cudaEventDestroy(d->ev_free[b]);
+  }
+  if (d->cstream) cudaStreamDestroy(d->cstream);
   if (d->stream) cudaStreamDestroy(d->stream);
   delete d;
+  return WF_OK;
+}
+
+int wf_release_cache(void) {
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  cache_free_locked();
   return WF_OK;
 }
 
 }  // extern "C"
 
 // ---- scatter helpers ----------------------------------------------------
-static int upload_d(wf_domain* d, const double* src, int comps, double* dst, int stride, int off) {
-  WF_CUDA_OK(cudaMemcpyAsync(d->d_stage, src, sizeof(double) * comps * d->n, cudaMemcpyHostToDevice,
-                             d->stream));
-  k_scatter_d<<<nblk(d->n), 256, 0, d->stream>>>(d->n, d->inv, d->d_stage, comps, dst, stride, off);
-  WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+// A setter's host array goes to one of two staging buffers on the copy
+// stream and is scattered into slot order on the domain's stream; the call
+// returns once the copy is done (the caller may then reuse its array), while
+// the scatter runs on behind it and overlaps the next setter's copy.  A copy
+// into a buffer waits for the scatter that last read it.
+static double* stage_copy(wf_domain* d, const void* src, size_t bytes, int* b_out) {
+  const int b = d->stage_next;
+  d->stage_next ^= 1;
+  double* stage = b ? d->d_stage2 : d->d_stage;
+  if (cudaStreamWaitEvent(d->cstream, d->ev_free[b], 0) != cudaSuccess ||
+      cudaMemcpyAsync(stage, src, bytes, cudaMemcpyHostToDevice, d->cstream) != cudaSuccess ||
+      cudaEventRecord(d->ev_full[b], d->cstream) != cudaSuccess ||
+      cudaStreamWaitEvent(d->stream, d->ev_full[b], 0) != cudaSuccess)
+    return nullptr;
+  *b_out = b;
+  return stage;
+}
+static int stage_done(wf_domain* d, int b) {
+  WF_CUDA_OK(cudaEventRecord(d->ev_free[b], d->stream));
+  WF_CUDA_OK(cudaEventSynchronize(d->ev_full[b]));
   return WF_OK;
+}
+static int upload_d(wf_domain* d, const double* src, int comps, double* dst, int stride, int off) {
+  int b = 0;
+  double* stage = stage_copy(d, src, sizeof(double) * comps * d->n, &b);
+  if (!stage) return wf_fail(d, WF_ERR_CUDA, "host to device copy");
+  k_scatter_d<<<nblk(d->n), 256, 0, d->stream>>>(d->n, d->inv, stage, comps, dst, stride, off);
+  return stage_done(d, b);
 }
 template <class T>
 static int upload_t(wf_domain* d, const T* src, T* dst) {
-  WF_CUDA_OK(cudaMemcpyAsync(d->d_stage, src, sizeof(T) * d->n, cudaMemcpyHostToDevice, d->stream));
-  k_scatter_t<T><<<nblk(d->n), 256, 0, d->stream>>>(d->n, d->inv, (const T*)d->d_stage, dst);
-  WF_CUDA_OK(cudaStreamSynchronize(d->stream));
-  return WF_OK;
+  int b = 0;
+  double* stage = stage_copy(d, src, sizeof(T) * d->n, &b);
+  if (!stage) return wf_fail(d, WF_ERR_CUDA, "host to device copy");
+  k_scatter_t<T><<<nblk(d->n), 256, 0, d->stream>>>(d->n, d->inv, (const T*)stage, dst);
+  return stage_done(d, b);
 }
+// fills need no host synchronisation: later device work and read-backs are
+// ordered behind them on the domain's stream
 static int fill_d(wf_domain* d, double v, double* dst, int stride, int off) {
   k_fill_d<<<nblk(d->n), 256, 0, d->stream>>>(d->n, v, dst, stride, off);
-  WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+  WF_CUDA_OK(cudaGetLastError());
   return WF_OK;
 }
 static Fields& CF(wf_domain* d) { return d->F[d->cur]; }
@@ -1272,7 +1385,8 @@ int wf_set_positions(wf_domain* d, const double* x) {
   if (d->started) d->lists_stale = true;   // the lists were built for the old positions
   k_scatter_d<<<nblk(d->n), 256, 0, d->stream>>>(d->n, d->inv, d->d_stage, 3, (double*)CF(d).xm,
                                                   4, 0);
-  WF_CUDA_OK(cudaStreamSynchronize(d->stream));
+  // a later setter copy into this staging buffer waits for the scatter
+  WF_CUDA_OK(cudaEventRecord(d->ev_free[0], d->stream));
   return WF_OK;
 }
 int wf_set_velocities(wf_domain* d, const double* v) {
