@@ -273,7 +273,7 @@ def e2e_call(sc, form, steps, state, mlp_params=None, outs=None):
     out = [d.get_field(f, out=None if outs is None else outs[f]) for f in fields]
     d.close()
     t1 = time.perf_counter()
-    h2d = n * (3 * 8 + 8 + 4 + 1 + 8 + 8)           # scenario: x, m, id, not_write, Cs, T
+    h2d = n * (3 * 8 + 8 + 4 + 1 + 8)               # scenario: x, m, id, not_write, T (Cs stays on the host)
     h2d += sum(v.nbytes for k, v in state.items() if not k.startswith("_"))
     d2h = sum(a.nbytes for a in out)
     return n * steps / (t1 - t0), h2d / steps, d2h / steps
@@ -285,6 +285,7 @@ def run_e2e(sc, form, steps, state, mlp_params=None, reps=3):
     one untimed warm-up call, then the median of `reps` timed calls (each a
     complete create ... destroy)."""
     psc = {k: (pinned_like(v) if isinstance(v, np.ndarray) else v) for k, v in sc.items()}
+    psc["Cs_particles"] = pinned_like(np.full(sc["n"], sc["Cs"]))
     pstate = {k: (pinned_like(v) if isinstance(v, np.ndarray) else v) for k, v in state.items()}
     n = sc["n"]
     outs = {"u": pinned_like(np.zeros(3 * n)), "pl_strain": pinned_like(np.zeros(n)),

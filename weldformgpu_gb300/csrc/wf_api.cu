@@ -132,7 +132,6 @@ struct wf_domain {
   std::vector<MeshDev> meshes;
   double mu_s = 0.0, mu_d = 0.0, totmass = 0.0;
   int contact_law = 0;
-  std::vector<double> h_mass;      // masses in caller order (totmass, rigid particles)
   int32_t *cnb = nullptr, *ccnt = nullptr;
   // contact law 1 constants; tool bins built at the first solve
   double c_kappa = 0.1, c_dx = 0.0, c_vreg = 1.0e-3, c_eta = 1.0;
@@ -967,8 +966,13 @@ static int solve_begin(wf_domain* d, double dt_out) {
   if (rc) return rc;
   if (!resume) k_setvel0<<<nblk(d->n), 256, 0, d->stream>>>(d->n, d->n_solid, d->F[d->cur]);   // :123
   if (!d->meshes.empty()) {
-    d->totmass = 0.0;                              // WeldFormGPU.cu:808-820, in index order
-    for (double mm : d->h_mass) d->totmass += mm;
+    // WeldFormGPU.cu:808-820: the masses summed in index order (rigid particles
+    // hold mass 0 since wf_add_trimesh placed them)
+    std::vector<double> hm((size_t)d->n);
+    rc = wf_get_field(d, "m", hm.data());
+    if (rc) return rc;
+    d->totmass = 0.0;
+    for (double mm : hm) d->totmass += mm;
     launch_mesh_plane(make_params(d), d->stream);  // CalcSpheresKernel, :129-141
     if (d->contact_law == 1) {
       if (!(d->c_dx > 0.0)) return wf_fail(d, WF_ERR_STATE, "contact law 1 needs the option contact_dx");
@@ -1354,8 +1358,10 @@ int wf_set_heat_cap(wf_domain* d, double cp) {
 }
 int wf_set_cs(wf_domain* d, const double* cs) {
   if (!d || !cs) return WF_ERR_ARG;
-  for (int64_t i = 1; i < d->n; i++)
-    if (cs[i] != cs[0]) return wf_fail(d, WF_ERR_ARG, "per-particle Cs must be uniform");
+  const double c0 = cs[0];
+  bool mixed = false;
+  for (int64_t i = 1; i < d->n; i++) mixed |= cs[i] != c0;   // no early exit: vectorised
+  if (mixed) return wf_fail(d, WF_ERR_ARG, "per-particle Cs must be uniform");
   d->Cs = cs[0];
   d->cs_set = true;
   return WF_OK;
@@ -1396,7 +1402,6 @@ int wf_set_velocities(wf_domain* d, const double* v) {
 int wf_set_mass(wf_domain* d, const double* m) {
   if (!d || !m) return WF_ERR_ARG;
   d->m_set = true;
-  d->h_mass.assign(m, m + d->n);
   return upload_d(d, m, 1, (double*)CF(d).xm, 4, 3);
 }
 int wf_set_not_write_surf_id(wf_domain* d, const uint8_t* f) {
@@ -1540,7 +1545,6 @@ int wf_add_trimesh(wf_domain* d, const double* nodes, int32_t nn, const int32_t*
                                           zone_id, CF(d));
   WF_CUDA_OK(cudaStreamSynchronize(s));
   WF_CUDA_OK(cudaGetLastError());
-  for (int64_t p = first; p < first + ne; p++) d->h_mass[p] = 0.0;
   return WF_OK;
 }
 

@@ -157,7 +157,8 @@ def load(dom, sc, options=None):
     dom.set_density(sc["rho"])
     dom.set_shear_modulus(sc["G"])
     dom.set_sigma_y(sc["sy"])
-    dom.set_cs(np.full(n, sc["Cs"]))
+    cs = sc.get("Cs_particles")          # the per-particle array, when the caller holds one
+    dom.set_cs(cs if cs is not None else np.full(n, sc["Cs"]))
     dom.set_positions(np.ascontiguousarray(sc["x"]).ravel())
     dom.set_mass(sc["m"])
     dom.set_id(sc["ids"])
