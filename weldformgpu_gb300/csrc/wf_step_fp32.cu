@@ -429,7 +429,13 @@ __device__ __forceinline__ int stage_halo16(const TileHalo& T, int64_t npad, int
   return H;
 }
 
-__global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
+// The stress pass, with the warm-start network compiled in (kMlp: kernel
+// k_stress32_mlp, 96 registers, 5 blocks per SM) or without it (k_stress32,
+// held to 80 registers for 6 blocks per SM; 786k particles: 0.222 -> 0.213
+// ms; with the network's 25 KB of shared memory per block, 6 blocks per SM
+// gain nothing: the L1 they leave is too small).
+template <bool kMlp>
+__device__ __forceinline__ void stress32_body(StepParams P, Fields F,
                                                   const float4* __restrict__ v32b,
                                                   float* __restrict__ sigr32,
                                                   const int32_t* __restrict__ nb,
@@ -444,8 +450,8 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
   // Dynamic shared memory: the network's region (when it runs), then the
   // tile's halo records (positions, velocities) when the tile is staged.
   extern __shared__ __align__(1024) uint8_t smlp[];
-  mlp_umma_begin(smlp, mlp);
-  float4* sp = reinterpret_cast<float4*>(smlp + (mlp ? WF_UMMA_SMEM : 0));
+  if constexpr (kMlp) mlp_umma_begin(smlp, mlp);
+  float4* sp = reinterpret_cast<float4*>(smlp + (kMlp ? WF_UMMA_SMEM : 0));
   float4* sv = sp + T.cap;
   uint16_t* sl = reinterpret_cast<uint16_t*>(sv + T.cap);
   int staged;
@@ -463,7 +469,7 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
   const double p = 0.0 + (P.Cs * P.Cs) * (rho_new - P.rho0);   // FP64: small density change
   if (valid) F.p[i] = p;
   const bool solid = valid && F.perm[i] < P.n_solid;
-  if (!mlp && !solid) return;
+  if (!kMlp && !solid) return;
   if (P.state_pf && solid) {
     prefetch_l2(F.ss32 + 6 * i); prefetch_l2(F.eps_p + i); prefetch_l2(F.sy + i);
     prefetch_l2(F.pwn + i); prefetch_l2(F.T + i); prefetch_l2(F.eint + i);
@@ -536,7 +542,7 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
     RTf = (1.0f + P.jcCf * __logf(sr * P.jcinveps0f)) * (1.0f - __powf(Th, P.jcmf));
   }
   double ratio = -1.0;
-  if (mlp) {
+  if constexpr (kMlp) {
     // warm start: sigma_y0 from the cached power (FP32 suffices for the features).
     // The network can only improve on the radial start where that start is
     // poor: it overshoots the increment by about H' / (3G + H'), with the
@@ -652,11 +658,34 @@ __global__ void __launch_bounds__(128) k_stress32(StepParams P, Fields F,
   if (!isfinite(st)) atomicOr(status, WF_STATUS_NAN);
 }
 
+__global__ void __launch_bounds__(128) k_stress32_mlp(StepParams P, Fields F,
+                                                      const float4* __restrict__ v32b,
+                                                      float* __restrict__ sigr32,
+                                                      const int32_t* __restrict__ nb,
+                                                      const int32_t* __restrict__ cnt,
+                                                      int* __restrict__ status,
+                                                      const uint4* __restrict__ mlp,
+                                                      const MlpL1 l1, const TileHalo T,
+                                                      const List16 L16) {
+  stress32_body<true>(P, F, v32b, sigr32, nb, cnt, status, mlp, l1, T, L16);
+}
+__global__ void __launch_bounds__(128, 6) k_stress32(StepParams P, Fields F,
+                                                     const float4* __restrict__ v32b,
+                                                     float* __restrict__ sigr32,
+                                                     const int32_t* __restrict__ nb,
+                                                     const int32_t* __restrict__ cnt,
+                                                     int* __restrict__ status,
+                                                     const TileHalo T, const List16 L16) {
+  stress32_body<false>(P, F, v32b, sigr32, nb, cnt, status, nullptr, MlpL1{}, T, L16);
+}
+
 // ---- C32: acceleration + Monaghan viscosity (InteractionAlt.cu:18-150) ----
 // Lane groups of kAccelLanes (see nb_sub).  Neighbours are gathered per batch
 // of kAccelBatch: each carries 56 bytes (position, velocity, stress/rho^2).
 // 786k particles: 0.278 ms with one lane per particle, 0.272 ms with two
-// (71 registers, 7 blocks per SM), 0.31-0.39 ms with four.
+// (71 registers, 7 blocks per SM), 0.31-0.39 ms with four.  With the L2
+// prefetches the fused pass held to 64 registers (8 blocks per SM, no spill)
+// runs 0.252 -> 0.245 ms; 6 blocks 0.270, 9 blocks spill.
 constexpr int kAccelLanes = 2;
 constexpr int kAccelBatch = 2;
 static_assert(WF_NB_BLK / kAccelLanes >= kAccelBatch, "batch within the lane's sub-block");
@@ -784,7 +813,7 @@ __global__ void __launch_bounds__(128, 7) k_accel32(StepParams P, Fields F,
 // Neighbours' positions are read from F.p32 while the new positions go to
 // p32n (the two are swapped by the host after the launch); the other mirrors
 // written here (v32, th32) are not read by this pass.
-__global__ void __launch_bounds__(128, 7) k_accel_int32(StepParams P, Fields F,
+__global__ void __launch_bounds__(128, 8) k_accel_int32(StepParams P, Fields F,
                                                      const float4* __restrict__ v32b,
                                                      const float* __restrict__ sigr32,
                                                      const double4* __restrict__ vd2,
@@ -925,15 +954,23 @@ void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b
   const MlpL1 l1 = (W && mlp_l1) ? *mlp_l1 : MlpL1{};
   const size_t smem = (W ? WF_UMMA_SMEM : 0) +
                       (T.cap > 0 ? 2 * sizeof(float4) * (size_t)T.cap + WF_TILE_LIST_BYTES : 0);
-  static size_t opted[64] = {};     // per device: dynamic shared memory opted in so far
-  opt_in_smem(k_stress32, smem, opted);
-  static size_t c_smem = 0;
-  static int64_t c_val = 0;
+  static size_t opted[2][64] = {};  // per variant and device: dynamic shared memory opted in
+  static size_t c_smem[2] = {0, 0};
+  static int64_t c_val[2] = {0, 0};
   StepParams Q = P;
-  Q.pf_ahead = !P.wave_pf ? 0 : (int64_t)(P.wave_dist * (double)wave_slots(
-      k_stress32, 128, smem, 1, &c_smem, &c_val));
-  k_stress32<<<blocks_for(P.n, 128), 128, smem, s>>>(Q, F, v32b, sigr32, N.nb, N.cnt, status, W, l1,
-                                                     T, L16);
+  if (W) {
+    opt_in_smem(k_stress32_mlp, smem, opted[1]);
+    Q.pf_ahead = !P.wave_pf ? 0 : (int64_t)(P.wave_dist * (double)wave_slots(
+        k_stress32_mlp, 128, smem, 1, &c_smem[1], &c_val[1]));
+    k_stress32_mlp<<<blocks_for(P.n, 128), 128, smem, s>>>(Q, F, v32b, sigr32, N.nb, N.cnt,
+                                                           status, W, l1, T, L16);
+  } else {
+    opt_in_smem(k_stress32, smem, opted[0]);
+    Q.pf_ahead = !P.wave_pf ? 0 : (int64_t)(P.wave_dist * (double)wave_slots(
+        k_stress32, 128, smem, 1, &c_smem[0], &c_val[0]));
+    k_stress32<<<blocks_for(P.n, 128), 128, smem, s>>>(Q, F, v32b, sigr32, N.nb, N.cnt, status,
+                                                       T, L16);
+  }
 }
 void launch_fp32_accel(const StepParams& P, const Fields& F, const float4* v32b,
                        const float* sigr32, float4* a32, const NbBuffers& N, cudaStream_t s) {
