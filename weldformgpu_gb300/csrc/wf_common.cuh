@@ -334,6 +334,9 @@ void launch_fp32_density_heat(const StepParams& P, const Fields& F, double4* vd2
 struct MlpL1;
 // mlp_packed (the tcgen05 weight image) and mlp_l1 (layer 1) together, or neither;
 // T: the tiles' halos (T.cap = 0: every block gathers from global memory)
+// the mixed heat pass alone (a call's last step; the mixed ThermalSolve)
+void launch_fp32_heat(const StepParams& P, const Fields& F, const NbBuffers& N, int plastic_heat,
+                      cudaStream_t s);
 void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b,
                         float* sigr32, const NbBuffers& N, int* status, const void* mlp_packed,
                         const MlpL1* mlp_l1, const TileHalo& T, const List16& L16,

@@ -157,6 +157,7 @@ void launch_integrate(const StepParams& P, const Fields& F, const double4* vd2,
 
 void launch_thermal(const StepParams& P, const Fields& F, const NbBuffers& N, int first,
                     int plastic_heat, int mixed, cudaStream_t s) {
-  k_heat_rate<<<blocks_for(P.n, 128), 128, 0, s>>>(P, F, N.nb, N.cnt, plastic_heat, mixed);
+  if (mixed) launch_fp32_heat(P, F, N, plastic_heat, s);
+  else k_heat_rate<<<blocks_for(P.n, 128), 128, 0, s>>>(P, F, N.nb, N.cnt, plastic_heat, 0);
   k_heat_leapfrog<<<blocks_for(P.n, 256), 256, 0, s>>>(P, F, first, mixed);
 }

@@ -267,6 +267,76 @@ __global__ void __launch_bounds__(128, kDensMinBlocks) k_density_heat32(StepPara
   v32b[i] = make_float4(vi.x, vi.y, vi.z, (float)rho_new);
 }
 
+// ---- the heat pass alone (ThermalSolveKernel, src/cuda/Thermal.cu:101-142) --
+// A call's last heat pass and every step of the mixed ThermalSolve: the heat
+// sum of density_heat_pairs, the same operations in the same neighbour order
+// (so a separate pass gives the fused pass's sum bit for bit), with the
+// neighbour's density read as one float of its velocity record.
+template <class L>
+__device__ __forceinline__ float heat_pairs(const StepParams& P, const float4* __restrict__ gp,
+                                            const float4* __restrict__ gv,
+                                            const float2* __restrict__ gt, const L& list, int c,
+                                            float4 pi, float2 ti) {
+  constexpr int NB = kDensBatch;
+  const float invh = P.invhf, C = P.Cf, Ch = P.Chf;
+  float sf = 0.0f;
+  int nx[WF_NB_BLK];
+  if (c > 0) list.block(0, nx);
+  for (int b = 0; WF_NB_BLK * b < c; b++) {
+    int js[WF_NB_BLK];
+#pragma unroll
+    for (int q = 0; q < WF_NB_BLK; q++) js[q] = nx[q];
+    if (P.nb_pf && c > WF_NB_BLK * (b + P.nb_pf)) list.prefetch(b + P.nb_pf, 1);
+    if (c > WF_NB_BLK * (b + 1)) list.block(b + 1, nx);
+#pragma unroll
+    for (int h = 0; h < WF_NB_BLK; h += NB) {
+      float4 pj[NB];
+      float rj[NB];
+      float2 tj[NB];
+#pragma unroll
+      for (int q = 0; q < NB; q++) {
+        pj[q] = gp[js[h + q]];
+        rj[q] = __ldg(&gv[js[h + q]].w);
+        tj[q] = gt[js[h + q]];
+      }
+#pragma unroll
+      for (int q = 0; q < NB; q++) {
+        // padding entries (the particle's own slot) add exact zeros (gk32_r2)
+        const float xx = pi.x - pj[q].x, xy = pi.y - pj[q].y, xz = pi.z - pj[q].z;
+        const float GK = gk32_r2(xx * xx + xy * xy + xz * xz, invh, Ch, C);
+        const float mg = __fdividef(pj[q].w, rj[q]) * GK;
+        const float dT = (ti.x - tj[q].x) + (ti.y - tj[q].y);
+        sf += mg * dT;
+      }
+    }
+  }
+  return sf;
+}
+
+__global__ void __launch_bounds__(128, kDensMinBlocks) k_heat32(StepParams P, Fields F,
+                                                               const int32_t* __restrict__ nb,
+                                                               const int32_t* __restrict__ cnt,
+                                                               int plastic_heat) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  if (P.state_pf) {
+    prefetch_l2(F.vd + i); prefetch_l2(F.xm + i); prefetch_l2(F.T + i); prefetch_l2(F.cpT + i);
+    prefetch_l2(F.dep + i); prefetch_l2(F.sy + i);
+  }
+  if (P.pf_ahead > 0) {
+    const int64_t ia = i + P.pf_ahead;      // the slot this thread's successor will take
+    if (ia < P.n) {
+      prefetch_l2(F.p32 + ia); prefetch_l2(F.th32 + ia); prefetch_l2(cnt + ia);
+      for (int b = 0; b < P.wave_pf && b < WF_NB_BLOCKS; b++) nb_prefetch(nb, P.npad, ia, b, 4);
+    }
+  }
+  const float4 pi = F.p32[i];
+  const float2 ti = F.th32[i];
+  const int c = cnt[i];
+  const float sf = heat_pairs(P, F.p32, F.v32, F.th32, NbList32{nb, P.npad, i}, c, pi, ti);
+  F.dTdt[i] = heat_rate_mixed(P, F, i, P.k2f * sf, F.vd[i].w, F.xm[i].w, F.T[i], plastic_heat);
+}
+
 // Johnson-Cook consistent return map of the mixed form, solved for the
 // increment.  With the cached power pwn = ep^n and u = dl / ep,
 //   f(dl) = d0 - 3G dl - B RT pwn ((1 + u)^n - 1),   d0 = st - (A + B pwn) RT,
@@ -945,6 +1015,15 @@ void launch_fp32_density_heat(const StepParams& P, const Fields& F, double4* vd2
       k_density_heat32, 128, smem, kDensLanes, &c_smem, &c_val));
   k_density_heat32<<<blocks_for(P.n * kDensLanes, 128), 128, smem, s>>>(
       Q, F, vd2, v32b, N.nb, N.cnt, first, plastic_heat, Tl, L16);
+}
+void launch_fp32_heat(const StepParams& P, const Fields& F, const NbBuffers& N, int plastic_heat,
+                      cudaStream_t s) {
+  static size_t c_smem = 0;
+  static int64_t c_val = 0;
+  StepParams Q = P;
+  Q.pf_ahead = !P.wave_pf ? 0 : (int64_t)(P.wave_dist * (double)wave_slots(
+      k_heat32, 128, 0, 1, &c_smem, &c_val));
+  k_heat32<<<blocks_for(P.n, 128), 128, 0, s>>>(Q, F, N.nb, N.cnt, plastic_heat);
 }
 void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b, float* sigr32,
                         const NbBuffers& N, int* status, const void* mlp_packed,
