@@ -57,13 +57,14 @@ __global__ void __launch_bounds__(256) k_integrate(StepParams P, Fields F,
 }
 
 // ---- heat: ThermalSolveKernel + plastic heat + CalcConvHeatKernel -------
-// src/cuda/Thermal.cu:101-142 and :36-64.  FP64 form: the reference's
-// arithmetic in its order.  Mixed form: pair flux in FP32 with the
-// temperature difference taken in FP64 first; dT/dt and T stay FP64.
+// src/cuda/Thermal.cu:101-142 and :36-64, FP64 form: the reference's
+// arithmetic in its order.  The mixed form's heat pass is k_heat32
+// (wf_step_fp32.cu): pair flux in FP32 with the temperature difference taken
+// from the (hi, lo) float pair; dT/dt and T stay FP64.
 __global__ void __launch_bounds__(128) k_heat_rate(StepParams P, Fields F,
                                                    const int32_t* __restrict__ nb,
                                                    const int32_t* __restrict__ cnt,
-                                                   int plastic_heat, int mixed) {
+                                                   int plastic_heat) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= P.n) return;
   const double4 xi = F.xm[i];
@@ -71,54 +72,16 @@ __global__ void __launch_bounds__(128) k_heat_rate(StepParams P, Fields F,
   const double Ti = F.T[i], ki = F.kT[i];
   const int c = cnt[i];
   double s = 0.0;
-  if (!mixed) {
-    for (int k = 0; k < c; k++) {
-      const int j = __ldg(nb + nb_at(P.npad, i, k));
-      const double4 xj = F.xm[j];
-      const double rhoj = F.vd[j].w;
-      const double kj = F.kT[j];
-      const double xx = xi.x - xj.x, xy = xi.y - xj.y, xz = xi.z - xj.z;
-      const double nxij = sqrt(xx * xx + xy * xy + xz * xz);
-      const double GK = gradK64(nxij / P.h, P.h, P.gkC);
-      s += xj.w / rhoj * (4.0 * ki * kj / (ki + kj) * (Ti - F.T[j])) *
-           (xx * (xx * GK) + xy * (xy * GK) + xz * (xz * GK)) / (nxij * nxij);
-    }
-  } else {
-    // temperature differences from the (hi, lo) float pair: exact to ~1e-14 of T
-    const float4 pi = F.p32[i];
-    const float2 ti = F.th32[i];
-    const float invh = P.invhf, C = P.Cf, Ch = P.Chf;
-    float sf = 0.0f;
-    int4 lo = make_int4(0, 0, 0, 0), hi = lo;
-    if (c > 0) nb_block(nb, P.npad, i, 0, lo, hi);
-    for (int b = 0; WF_NB_BLK * b < c; b++) {
-      const int js[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
-      const int m = c - WF_NB_BLK * b;
-      if (m > WF_NB_BLK) nb_block(nb, P.npad, i, b + 1, lo, hi);
-#pragma unroll
-      for (int h = 0; h < WF_NB_BLK; h += 4) {
-        float4 pj[4];
-        float2 tj[4];
-        float rj[4];
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-          pj[u] = F.p32[js[h + u]];
-          tj[u] = F.th32[js[h + u]];
-          rj[u] = F.v32[js[h + u]].w;
-        }
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-          if (h + u >= m) continue;
-          const float dT = (ti.x - tj[u].x) + (ti.y - tj[u].y);
-          const float xx = pi.x - pj[u].x, xy = pi.y - pj[u].y, xz = pi.z - pj[u].z;
-          // x.(GK x) / r^2 = GK
-          const float GK = gk32_r2(xx * xx + xy * xy + xz * xz, invh, Ch, C);
-          sf += __fdividef(pj[u].w, rj[u]) * GK * dT;   // as in k_density_heat32
-        }
-      }
-    }
-    F.dTdt[i] = heat_rate_mixed(P, F, i, P.k2f * sf, rhoi, xi.w, Ti, plastic_heat);
-    return;
+  for (int k = 0; k < c; k++) {
+    const int j = __ldg(nb + nb_at(P.npad, i, k));
+    const double4 xj = F.xm[j];
+    const double rhoj = F.vd[j].w;
+    const double kj = F.kT[j];
+    const double xx = xi.x - xj.x, xy = xi.y - xj.y, xz = xi.z - xj.z;
+    const double nxij = sqrt(xx * xx + xy * xy + xz * xz);
+    const double GK = gradK64(nxij / P.h, P.h, P.gkC);
+    s += xj.w / rhoj * (4.0 * ki * kj / (ki + kj) * (Ti - F.T[j])) *
+         (xx * (xx * GK) + xy * (xy * GK) + xz * (xz * GK)) / (nxij * nxij);
   }
   s *= 1. / (rhoi * F.cpT[i]);
   if (plastic_heat && F.perm[i] < P.n_solid) {
@@ -158,6 +121,6 @@ void launch_integrate(const StepParams& P, const Fields& F, const double4* vd2,
 void launch_thermal(const StepParams& P, const Fields& F, const NbBuffers& N, int first,
                     int plastic_heat, int mixed, cudaStream_t s) {
   if (mixed) launch_fp32_heat(P, F, N, plastic_heat, s);
-  else k_heat_rate<<<blocks_for(P.n, 128), 128, 0, s>>>(P, F, N.nb, N.cnt, plastic_heat, 0);
+  else k_heat_rate<<<blocks_for(P.n, 128), 128, 0, s>>>(P, F, N.nb, N.cnt, plastic_heat);
   k_heat_leapfrog<<<blocks_for(P.n, 256), 256, 0, s>>>(P, F, first, mixed);
 }
