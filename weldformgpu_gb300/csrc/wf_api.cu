@@ -1051,7 +1051,7 @@ static int solve_step_launches(wf_domain* d) {
         launch_fp32_density_heat(P, F, d->vd2, d->v32b, N, d->heat_pending_first ? 1 : 0,
                                  d->chi > 0.0 ? 1 : 0, TH, L16, s);
       else
-        launch_fp32_density(P, F, d->vd2, d->v32b, N, s);
+        launch_fp32_density(P, F, d->vd2, d->v32b, N, L16, s);
       d->heat_pending = false;
     }
     { KTimer t(d, KID_STRESS);

@@ -315,8 +315,6 @@ void launch_integrate(const StepParams& P, const Fields& F, const double4* vd2,
 void launch_thermal(const StepParams& P, const Fields& F, const NbBuffers& N, int first,
                     int plastic_heat, int mixed, cudaStream_t s);
 
-void launch_fp32_density(const StepParams& P, const Fields& F, double4* vd2, float4* v32b,
-                         const NbBuffers& N, cudaStream_t s);
 // contact (wf_contact.cu): surface tagging, contact list (when `list`) and
 // penalty forces after the acceleration pass; mesh motion and rigid particles
 // after the integration; plane coefficients at solve start
@@ -326,6 +324,9 @@ void launch_mesh_update(const StepParams& P, const Fields& F, int mixed, cudaStr
 void launch_mesh_plane(const StepParams& P, cudaStream_t s);
 struct TileHalo;
 struct List16;
+// density pass alone (mixed form; a call's first step, or heat off)
+void launch_fp32_density(const StepParams& P, const Fields& F, double4* vd2, float4* v32b,
+                         const NbBuffers& N, const List16& L16, cudaStream_t s);
 // density pass of this step with the previous step's heat pass (mixed form);
 // T: tile halos (T.cap = 0: none), L16: 16-bit lists (L16.base null: none)
 void launch_fp32_density_heat(const StepParams& P, const Fields& F, double4* vd2, float4* v32b,

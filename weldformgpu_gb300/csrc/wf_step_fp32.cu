@@ -59,54 +59,6 @@ constexpr int kDensLanes = 1;
 constexpr int kDensMinBlocks = 6;
 constexpr int kDensBatch = 4;
 
-__global__ void __launch_bounds__(128) k_density32(StepParams P, Fields F,
-                                                   double4* __restrict__ vd2,
-                                                   float4* __restrict__ v32b,
-                                                   const int32_t* __restrict__ nb,
-                                                   const int32_t* __restrict__ cnt) {
-  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= P.n) return;
-  const float4 pi = F.p32[i];
-  const float4 vi = F.v32[i];
-  const double4 vdi = F.vd[i];
-  double rho_new = vdi.w;
-  if (F.perm[i] < P.n_solid) {
-    const float invh = P.invhf, C = P.Cf, Ch = P.Chf;
-    const int32_t idi = F.id[i];
-    float drho = 0.0f;
-    const int c = cnt[i];
-    int4 lo = make_int4(0, 0, 0, 0), hi = lo;
-    if (c > 0) nb_block(nb, P.npad, i, 0, lo, hi);
-    for (int b = 0; WF_NB_BLK * b < c; b++) {
-      const int js[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
-      const int m = c - WF_NB_BLK * b;   // valid entries of this block (capped at 8)
-      if (m > WF_NB_BLK) nb_block(nb, P.npad, i, b + 1, lo, hi);
-#pragma unroll
-      for (int h = 0; h < WF_NB_BLK; h += 4) {
-        float4 pj[4], vj[4];
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          pj[q] = F.p32[js[h + q]];
-          vj[q] = F.v32[js[h + q]];
-        }
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          if (h + q >= m || (P.contact && !pass_ij(P, idi, F.id[js[h + q]]))) continue;
-          const float xx = pi.x - pj[q].x, xy = pi.y - pj[q].y, xz = pi.z - pj[q].z;
-          const float GK = gk32_r2(xx * xx + xy * xy + xz * xz, invh, Ch, C);
-          const float vx = vi.x - vj[q].x, vy = vi.y - vj[q].y, vz = vi.z - vj[q].z;
-          drho += __fdividef(pj[q].w, vj[q].w) * GK * (vx * xx + vy * xy + vz * xz);
-        }
-      }
-    }
-    drho *= vi.w;                      // rho_i multiplies the sum (as in k_density_heat32)
-    F.drho[i] = (double)drho;
-    rho_new = vdi.w + P.dt * (double)drho;
-  }
-  vd2[i] = make_double4(vdi.x, vdi.y, vdi.z, rho_new);
-  v32b[i] = make_float4(vi.x, vi.y, vi.z, (float)rho_new);
-}
-
 // ---- A32 + heat: the previous step's heat pass fused into this density pass.
 // Heat at the end of step n (ThermalSolveKernel + plastic heat + convection +
 // leapfrog, src/cuda/Thermal.cu:16-142) and the density pass of step n+1 read
@@ -119,7 +71,7 @@ __global__ void __launch_bounds__(128) k_density32(StepParams P, Fields F,
 // entries are slots (NbList32 / NbList16: records gathered from the global
 // arrays gp, gv, gt) or ranks in the tile's halo (NbListS: the arrays are its
 // shared-memory copies).
-template <class L>
+template <class L, bool kHeat = true>
 __device__ __forceinline__ void density_heat_pairs(const StepParams& P, const Fields& F,
                                                    const float4* __restrict__ gp,
                                                    const float4* __restrict__ gv,
@@ -148,7 +100,7 @@ __device__ __forceinline__ void density_heat_pairs(const StepParams& P, const Fi
       for (int q = 0; q < NB; q++) {
         pj[q] = gp[js[h + q]];
         vj[q] = gv[js[h + q]];
-        tj[q] = gt[js[h + q]];
+        if constexpr (kHeat) tj[q] = gt[js[h + q]];
       }
 #pragma unroll
       for (int q = 0; q < NB; q++) {
@@ -162,8 +114,10 @@ __device__ __forceinline__ void density_heat_pairs(const StepParams& P, const Fi
         const float mg = __fdividef(pj[q].w, vj[q].w) * GK;
         // heat flux (every particle, no contact filter); the pair
         // conductivity 4 k_i k_j / (k_i + k_j) = 2k multiplies the sum
-        const float dT = (ti.x - tj[q].x) + (ti.y - tj[q].y);
-        sf += mg * dT;
+        if constexpr (kHeat) {
+          const float dT = (ti.x - tj[q].x) + (ti.y - tj[q].y);
+          sf += mg * dT;
+        }
         // density rate (solid particles, contact filter); rho_i multiplies the sum
         bool pass = solid;
         if constexpr (L::kSlots) pass = pass && !(P.contact && !pass_ij(P, idi, F.id[js[h + q]]));
@@ -176,6 +130,50 @@ __device__ __forceinline__ void density_heat_pairs(const StepParams& P, const Fi
   }
   drho_out = drho * vi.w;
   sf_out = sf;
+}
+
+// ---- A32: the density pass without a heat pass to fuse (a call's first
+// step; every step when heat is off): the density sum of density_heat_pairs.
+__global__ void __launch_bounds__(128, kDensMinBlocks) k_density32(StepParams P, Fields F,
+                                                                  double4* __restrict__ vd2,
+                                                                  float4* __restrict__ v32b,
+                                                                  const int32_t* __restrict__ nb,
+                                                                  const int32_t* __restrict__ cnt,
+                                                                  const List16 L16) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  const bool solid = F.perm[i] < P.n_solid;
+  if (P.state_pf) prefetch_l2(F.vd + i);
+  if (P.pf_ahead > 0) {
+    const int64_t ia = i + P.pf_ahead;      // the slot this thread's successor will take
+    if (ia < P.n) {
+      prefetch_l2(F.p32 + ia); prefetch_l2(F.v32 + ia); prefetch_l2(cnt + ia);
+      prefetch_l2(F.perm + ia);
+      for (int b = 0; b < P.wave_pf && b < WF_NB_BLOCKS; b++) nb_prefetch(nb, P.npad, ia, b, 4);
+    }
+  }
+  const float4 pi = F.p32[i];
+  const float4 vi = F.v32[i];
+  const int c = solid ? cnt[i] : 0;
+  const int32_t idi = F.id[i];
+  float drho = 0.0f, sf = 0.0f;
+  const int b16 = L16.base ? L16.base[i / WF_TILE] : -1;     // uniform over the block
+  const float2 t0 = make_float2(0.f, 0.f);
+  if (b16 >= 0)
+    density_heat_pairs<NbList16, false>(P, F, F.p32, F.v32, nullptr,
+                                        NbList16{L16.off, P.npad, i, b16}, 0, c, pi, vi, t0, solid,
+                                        idi, drho, sf);
+  else
+    density_heat_pairs<NbList32, false>(P, F, F.p32, F.v32, nullptr, NbList32{nb, P.npad, i}, 0,
+                                        c, pi, vi, t0, solid, idi, drho, sf);
+  const double4 vdi = F.vd[i];
+  double rho_new = vdi.w;
+  if (solid) {
+    F.drho[i] = (double)drho;
+    rho_new = vdi.w + P.dt * (double)drho;
+  }
+  vd2[i] = make_double4(vdi.x, vdi.y, vdi.z, rho_new);
+  v32b[i] = make_float4(vi.x, vi.y, vi.z, (float)rho_new);
 }
 
 __global__ void __launch_bounds__(128, kDensMinBlocks) k_density_heat32(StepParams P, Fields F,
@@ -996,8 +994,13 @@ static int64_t wave_slots(K kernel, int threads, size_t smem, int lanes, size_t*
 }
 
 void launch_fp32_density(const StepParams& P, const Fields& F, double4* vd2, float4* v32b,
-                         const NbBuffers& N, cudaStream_t s) {
-  k_density32<<<blocks_for(P.n, 128), 128, 0, s>>>(P, F, vd2, v32b, N.nb, N.cnt);
+                         const NbBuffers& N, const List16& L16, cudaStream_t s) {
+  static size_t c_smem = 0;
+  static int64_t c_val = 0;
+  StepParams Q = P;
+  Q.pf_ahead = !P.wave_pf ? 0 : (int64_t)(P.wave_dist * (double)wave_slots(
+      k_density32, 128, 0, 1, &c_smem, &c_val));
+  k_density32<<<blocks_for(P.n, 128), 128, 0, s>>>(Q, F, vd2, v32b, N.nb, N.cnt, L16);
 }
 void launch_fp32_density_heat(const StepParams& P, const Fields& F, double4* vd2, float4* v32b,
                               const NbBuffers& N, int first, int plastic_heat, const TileHalo& T,
