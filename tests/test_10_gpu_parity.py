@@ -482,6 +482,34 @@ def test_tile_staging_bit_identical_to_global_gathers(cap_max):
         assert np.array_equal(runs[2][f], runs[1][f]), f
 
 
+@pytest.mark.parametrize("network", [0, 1])
+def test_prefetch_options_do_not_change_results(network):
+    """The L2 prefetches of the mixed passes (lists ahead, the tail's state,
+    the next wave's prologue) are hints: every field is bit-identical with
+    all of them off, with and without the tensor-core network (two stress
+    kernels), including the call-end heat pass and the first-step density
+    pass of each call."""
+    from weldformgpu_gb300 import mlp
+    sc = S.jc_compression(R=0.006, H=0.012)
+    opts = {"return_map": 1, "thermal": 1, "taylor_quinney": 0.9, "rebuild_every": 5,
+            "rebuild_current_positions": 1, "rebuild_after_yield": 0, "precision": 1}
+    runs = []
+    for pf in ({}, {"list_prefetch": 0, "state_prefetch": 0, "wave_prefetch": 0},
+               {"list_prefetch": 3, "wave_prefetch": 7, "wave_prefetch_distance": 0.5}):
+        d = gpu(sc, dict(opts, **pf))
+        if network:
+            d.set_mlp_weights(mlp.init_params(3))
+            d.set_option("mlp", 1)
+        for n in (1, 37, 62):                    # calls: first-step density, call-end heat
+            d.step(n)
+        runs.append({f: d.get_field(f) for f in ("x", "v", "u", "shearstress", "pl_strain",
+                                                 "sigma_eq", "T", "rho", "int_energy")})
+        d.close()
+    for f in runs[0]:
+        assert np.array_equal(runs[0][f], runs[1][f]), f
+        assert np.array_equal(runs[0][f], runs[2][f]), f
+
+
 def test_mixed_fused_heat_matches_separate_heat_pass():
     """Mixed form: the heat pass fused into the next step's density pass gives
     the temperatures of the separate heat pass (to FP32 rounding), including
