@@ -1,8 +1,9 @@
 """Builds oracle/_ref/libwfref.so: the reference's own kernel sources compiled
 for the CPU, used only to pin the oracle (test infrastructure).
 
-The sources are read where they lie in the reference tree (default
-/root/reference, or $WF_REFERENCE_DIR); nothing is copied.  The reference's
+The sources are read where they lie in the reference tree: $WF_REFERENCE_DIR,
+or else a directory named `reference` beside the repository's root; nothing is
+copied.  The reference's
 CMake build is not used: two translation units written here
 (ref_domain.cpp, ref_nsearch.cpp) #include the reference's kernel files, and
 cuda_host_shim.h stands in for the CUDA built-ins.  Flags keep IEEE
@@ -20,7 +21,11 @@ OUT = os.path.join(OUT_DIR, "libwfref.so")
 
 
 def reference_dir():
-    return os.environ.get("WF_REFERENCE_DIR", "/root/reference")
+    """$WF_REFERENCE_DIR, else `reference` beside the repository's root."""
+    env = os.environ.get("WF_REFERENCE_DIR")
+    if env:
+        return env
+    return os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
 
 
 # Thermal.cu's kernels, taken verbatim: the file also holds host functions that
