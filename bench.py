@@ -426,7 +426,7 @@ def indentation_domain(sc, form, shift_t, state=None):
 
 
 def bench_indentation(args):
-    """Config-5 shape (--size full): block 200 x 200 x 50 at dx = 0.25 mm (2.0M particles;
+    """Indentation workload (--size full): block 200 x 200 x 50 at dx = 0.25 mm (2.0M particles;
     medium 100 x 100 x 50, small 50 x 50 x 25)
     indented by the lower half of a level-5 icosphere (R = 10 mm, 10,304
     triangles) at -5 m/s; contact law 1 (0.1 K/dx penalty, mu = 0.3,
@@ -494,7 +494,7 @@ def bench_indentation(args):
 
 
 def bench_heat(args):
-    """Config-2 shape: heat conduction only (ThermalSolve) in a 100^3-particle
+    """Heat-only workload: heat conduction only (ThermalSolve) in a 100^3-particle
     steel box (dx = 0.1 mm, 1.0M particles), Gaussian hot spot, convection on
     the outer layer, dt = 0.1 dx^2 rho c_p / k.  Plain FP64 against the mixed
     form (FP32 flux, FP64 temperature accumulation).  Each solve call starts

@@ -81,7 +81,7 @@ def main():
     cnt, lst = O.ref_neighbors(sc["x"], sc["h"])
     np.savez_compressed(os.path.join(HERE, "nb_small.npz"), x=sc["x"], h=sc["h"], counts=cnt,
                         lists=lst)
-    # 2. neighbour digest at config-1 size (R = 5 mm, H = 10 mm, 5,244 particles)
+    # 2. neighbour digest of the R = 5 mm, H = 10 mm cylinder (5,244 particles)
     c1 = S.compression_cylinder(R=0.005, H=0.010)
     cnt1, lst1 = O.ref_neighbors(c1["x"], c1["h"])
     s1, s2, dig = list_digest(cnt1, lst1)

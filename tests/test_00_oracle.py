@@ -58,7 +58,7 @@ def test_neighbour_rule_at_the_support_radius_matches_float32():
     assert 0.3 < inside.mean() < 0.7
 
 
-def test_neighbors_config1_digest():
+def test_neighbors_cylinder_r5mm_digest():
     g = np.load(os.path.join(GOLDEN, "nb_c1.npz"))
     c1 = S.compression_cylinder(R=0.005, H=0.010)
     assert c1["n"] == int(g["n"]) == 5244          # reference generator count
@@ -462,8 +462,8 @@ def test_mlp_gradient_check_fp64():
 
 @pytest.mark.skipif(O.ref_lib() is None and build_ref.build() is None,
                     reason="reference tree not present (golden vectors cover this machine)")
-def test_oracle_matches_reference_live_config1_neighbors_and_steps():
-    """Config-1 size (5,244 particles): neighbour lists and 50 Fraser steps,
+def test_oracle_matches_reference_live_cylinder_r5mm_neighbors_and_steps():
+    """The R 5 mm, H 10 mm cylinder (5,244 particles): neighbour lists and 50 Fraser steps,
     reference kernels vs oracle, bit for bit."""
     O._ref = None
     c1 = S.compression_cylinder(R=0.005, H=0.010)

@@ -49,7 +49,7 @@ def same_lists(c1, l1, c2, l2):
     return all(np.array_equal(l1[i, :c1[i]], l2[i, :c2[i]]) for i in range(len(c1)))
 
 
-def test_neighbors_bit_exact_config1():
+def test_neighbors_bit_exact_cylinder_r5mm():
     c1 = S.compression_cylinder(R=0.005, H=0.010)
     g = gpu(c1)
     g.find_neighbors()
@@ -125,9 +125,9 @@ def test_fp64_fraser_loop_bit_exact_vs_reference_golden(case, checkpoints):
                     case, k, f, np.max(np.abs(got - ref)))
 
 
-def test_fp64_config1_lattice_vs_oracle_with_rebuilds():
+def test_fp64_cylinder_r5mm_lattice_vs_oracle_with_rebuilds():
     """R 5 mm, H 10 mm jittered lattice, dt 0.4h/c, rebuild every 10 steps, for 400 steps."""
-    sc = S.compression_cylinder(R=0.005, H=0.010, generator="lattice", dt_rule="baseline")
+    sc = S.compression_cylinder(R=0.005, H=0.010, generator="lattice", dt_rule="sound_speed")
     opts = {"rebuild_every": 10, "rebuild_current_positions": 1, "rebuild_after_yield": 0}
     g = gpu(sc, opts)
     o = ora(sc, opts)
@@ -154,7 +154,7 @@ def test_fp64_newton_jc_vs_oracle():
 
 def test_mixed_form_within_1e3_of_fp64_jc_newton():
     sc = S.compression_cylinder(R=0.004, H=0.008, material="jc", vz_top=-10.0,
-                                generator="lattice", dt_rule="baseline")
+                                generator="lattice", dt_rule="sound_speed")
     opts = {"return_map": 1, "rebuild_every": 10, "rebuild_current_positions": 1,
             "rebuild_after_yield": 0}
     a = gpu(sc, dict(opts, precision=0))
@@ -268,8 +268,8 @@ def test_contact_fp64_bit_exact_vs_reference_golden():
     assert (np.abs(d.get_field("contforce")).sum(axis=1) > 0).sum() > 20
 
 
-def test_contact_config1_fp64_bit_exact_vs_oracle():
-    """Config-1 cylinder (5,244 particles) under a 200-triangle plane at
+def test_contact_cylinder_r5mm_fp64_bit_exact_vs_oracle():
+    """The R 5 mm, H 10 mm cylinder (5,244 particles) under a 200-triangle plane at
     -10 m/s with friction: plain FP64 bit for bit against the oracle."""
     sc = S.contact_cylinder(mu=(0.3, 0.2))
     o, g64 = ora(sc), gpu(sc)

@@ -51,7 +51,7 @@ def assert_rows_match(rg, ro, n_terms):
 
 
 def test_output_rows_fp64_vs_oracle_compression():
-    """Bilinear compression (config-1 cylinder, 400 steps): every-step rows;
+    """Bilinear compression (R 5 mm, H 10 mm cylinder, 400 steps): every-step rows;
     the top platen's reaction grows as the cylinder is loaded."""
     sc = S.compression_cylinder(R=0.005, H=0.010)
     opts = {"output_every_step": 1}
@@ -110,7 +110,7 @@ def test_mixed_reaction_curve_within_1e3_of_fp64():
     """JC compression with heat, mixed form vs plain FP64 of the same code:
     the top platen's reaction curve (every step) within 1e-3 relative L2."""
     sc = S.compression_cylinder(R=0.004, H=0.008, material="jc", vz_top=-10.0,
-                                generator="lattice", dt_rule="baseline")
+                                generator="lattice", dt_rule="sound_speed")
     sc["k"], sc["cp"] = 167.0, 896.0
     opts = {"return_map": 1, "thermal": 1, "taylor_quinney": 0.9, "output_every_step": 1,
             "rebuild_every": 10, "rebuild_current_positions": 1, "rebuild_after_yield": 0}

@@ -138,7 +138,7 @@ def test_mlp_in_solver_same_answer():
     mat, G = jc_mat()
     P, _ = mlp.train_jc_warm_start(mat, G, n_synth=65536, steps=1500)
     sc = S.compression_cylinder(R=0.004, H=0.008, material="jc", vz_top=-10.0,
-                                generator="lattice", dt_rule="baseline")
+                                generator="lattice", dt_rule="sound_speed")
     opts = {"return_map": 1, "precision": 1}
     a = S.load(Domain_d(sc["n"]), sc, opts)
     b = S.load(Domain_d(sc["n"]), sc, opts)

@@ -34,7 +34,7 @@ def rel_l2(a, b):
 
 
 def test_bilinear_compression_5000_steps_fp64_bit_exact_vs_oracle():
-    sc = S.compression_cylinder(R=0.005, H=0.010, generator="lattice", dt_rule="baseline")
+    sc = S.compression_cylinder(R=0.005, H=0.010, generator="lattice", dt_rule="sound_speed")
     assert 6000 < sc["n"] < 6600
     opts = {"rebuild_every": 10, "rebuild_current_positions": 1, "rebuild_after_yield": 0,
             "output_interval": 500 * sc["dt"]}

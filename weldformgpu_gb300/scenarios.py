@@ -224,7 +224,7 @@ def jc_compression(R=0.025, H=0.050, dx=0.0005, jitter=0.01, seed=1, vz_top=-10.
     option by the caller); top `layers` layers at vz_top, bottom ones fixed;
     dt = 0.4 h / c."""
     sc = compression_cylinder(R=R, H=H, dx=dx, generator="lattice", jitter=jitter, seed=seed,
-                              vz_top=vz_top, material="jc", layers=layers, dt_rule="baseline",
+                              vz_top=vz_top, material="jc", layers=layers, dt_rule="sound_speed",
                               gen=gen)
     sc["k"], sc["cp"] = 167.0, 896.0
     return sc
