@@ -7,7 +7,7 @@ Tolerances:
     the FP64 kernels build with -fmad=false and sum neighbours in the
     oracle's order;
   - plain FP64 form with pow/log (Johnson-Cook Newton, convection): 1e-9
-    relative, the benchmark spec's plain-form bound (CUDA's pow/log may differ
+    relative, the plain-form bound (CUDA's pow/log may differ
     from glibc's in the last bit);
   - mixed form: relative L2 error <= 1e-3 per output field against the
     plain FP64 run of the same pipeline.
