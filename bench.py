@@ -324,40 +324,60 @@ def rel_l2(a, b):
 
 
 FROM_REST = {"R": 0.010, "H": 0.020, "steps": 5000}
+FROM_REST_FIELDS = ("u", "pl_strain", "sigma_eq", "T", "reaction_force")
 
 
-def from_rest_errors(mlp_params=None):
+def from_rest_errors(mlp_params=None, steps=None):
     """Both forms from rest on a smaller cylinder of the same material, dx,
-    loading and options (R = 10 mm, H = 20 mm, ~50k particles) for 5,000 steps
-    (12 % height reduction): relative L2 error of the mixed form (with the
-    network when given) against the plain FP64 form on the output fields and
-    on the platen's reaction curve (an output row every step)."""
+    loading and options (R = 10 mm, H = 20 mm, ~50k particles) for `steps`
+    steps (default 5,000: 12 % height reduction; 20,000: 49 %): relative L2
+    error of the mixed form (with the network when given) against the plain
+    FP64 form on the output fields and on the platen's reaction curve (an
+    output row every step), at the end and, for longer runs, every 5,000
+    steps."""
     from weldformgpu_gb300 import scenarios as S
+    steps = steps or FROM_REST["steps"]
     sc = S.jc_compression(R=FROM_REST["R"], H=FROM_REST["H"])
-    out = {}
+    doms, secs = {}, {"fp64": 0.0, "mixed": 0.0}
     for form in ("fp64", "mixed"):
         opts = base_options()
         opts["precision"] = 1 if form == "mixed" else 0
         opts["output_every_step"] = 1
+        opts["output_series_cap"] = steps + 16
         d = build_domain(sc, opts)
         if form == "mixed" and mlp_params is not None:
             d.set_mlp_weights(mlp_params)
             d.set_option("mlp", 1)
-        t0 = time.perf_counter()
-        d.step(FROM_REST["steps"])
-        out[form] = {f: d.get_field(f) for f in ("u", "pl_strain", "sigma_eq", "T")}
-        out[form]["reaction_force"] = d.get_output_series()[:, TOP_FZ]
-        out[form]["_s"] = time.perf_counter() - t0
-        out[form]["_max_ps"] = float(out[form]["pl_strain"].max())
+        doms[form] = d
+    checkpoints, done, max_ps = [], 0, 0.0
+    while done < steps:
+        k = min(5000, steps - done)
+        for form, d in doms.items():
+            t0 = time.perf_counter()
+            d.step(k)
+            secs[form] += time.perf_counter() - t0
+        done += k
+        out = {}
+        for form, d in doms.items():
+            out[form] = {f: d.get_field(f) for f in ("u", "pl_strain", "sigma_eq", "T")}
+            out[form]["reaction_force"] = d.get_output_series()[:, TOP_FZ]
+        errs = {f: rel_l2(out["mixed"][f] - (20.0 if f == "T" else 0.0),
+                          out["fp64"][f] - (20.0 if f == "T" else 0.0)) for f in FROM_REST_FIELDS}
+        max_ps = float(out["fp64"]["pl_strain"].max())
+        errs.update({"steps": done, "max_pl_strain": max_ps,
+                     "height_reduction": float(-out["fp64"]["u"].reshape(-1, 3)[:, 2].min()
+                                               / FROM_REST["H"])})
+        checkpoints.append(errs)
+    for d in doms.values():
         d.close()
-    errs = {f: rel_l2(out["mixed"][f] - (20.0 if f == "T" else 0.0),
-                      out["fp64"][f] - (20.0 if f == "T" else 0.0))
-            for f in ("u", "pl_strain", "sigma_eq", "T", "reaction_force")}
-    errs.update({"steps": FROM_REST["steps"], "particles": sc["n"],
+    errs = {f: checkpoints[-1][f] for f in FROM_REST_FIELDS}
+    errs.update({"steps": steps, "particles": sc["n"],
                  "workload": "jc_thermomech_compression_R10mm_H20mm_dx0.5mm from rest",
-                 "max_pl_strain": out["fp64"]["_max_ps"],
-                 "fp64_run_s": out["fp64"]["_s"], "mixed_run_s": out["mixed"]["_s"],
+                 "max_pl_strain": max_ps, "height_reduction": checkpoints[-1]["height_reduction"],
+                 "fp64_run_s": secs["fp64"], "mixed_run_s": secs["mixed"],
                  "mlp": mlp_params is not None})
+    if len(checkpoints) > 1:
+        errs["checkpoints"] = checkpoints
     return errs
 
 
@@ -544,6 +564,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-oracle baseline")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end arm")
     ap.add_argument("--no-mlp", action="store_true", help="time the mixed form without the MLP")
+    ap.add_argument("--from-rest-steps", type=int, default=None,
+                    help="length of the from-rest mixed-vs-FP64 comparison (default 5000)")
     ap.add_argument("--tiles", type=int, default=None,
                     help="profiling runs: option tile_staging for the timed form")
     ap.add_argument("--no-extra", action="store_true",
@@ -683,7 +705,7 @@ def main():
         "clocks": mixed["clocks"],
     }
     if not args.no_extra and rank == 0:
-        line["rel_l2_vs_fp64_from_rest"] = from_rest_errors(mlp)
+        line["rel_l2_vs_fp64_from_rest"] = from_rest_errors(mlp, args.from_rest_steps)
         line["fp64_ceiling"] = fp64_ceiling(plain["per_kernel_ms"], n)
         line["heat"] = bench_heat(args)
         line["indentation"] = bench_indentation(args)
