@@ -11,6 +11,10 @@
     5,000 steps (20 % height reduction): the mixed form against the plain FP64
     form of the same code within 1e-3 relative L2 on u, pl_strain, sigma_eq,
     the temperature rise and the top platen's reaction curve (every step).
+  - The full-length benchmark run's strain history (20,000 steps from rest at
+    the benchmark's nominal strain rate, ~19 % height reduction) on the same
+    small cylinder, the mixed form with the tensor-core warm-start network,
+    the same 1e-3 bar every 5,000 steps.
 """
 import numpy as np
 import pytest
@@ -80,3 +84,37 @@ def test_jc_thermomech_from_rest_5000_steps_mixed_within_1e3_of_fp64():
     errs["reaction_curve"] = rel_l2(rb[:, top], ra[:, top])
     for f, e in errs.items():
         assert e <= 1e-3, (f, e, errs)
+
+
+def test_jc_thermomech_from_rest_20000_steps_mixed_with_network_within_1e3_of_fp64():
+    """The full-length benchmark run's strain history on a smaller cylinder:
+    20,000 steps from rest at the benchmark's nominal strain rate (platen
+    speed over height, 10 m/s / 50 mm = 2.4 m/s / 12 mm = 200 /s), so the
+    cylinder ends ~19 % shorter like the full-size one; the mixed form with
+    the tensor-core warm-start network against plain FP64, errors checked
+    every 5,000 steps."""
+    from weldformgpu_gb300 import mlp
+    sc = S.jc_compression(R=0.006, H=0.012, vz_top=-2.4)
+    opts = {"return_map": 1, "thermal": 1, "taylor_quinney": 0.9, "rebuild_every": 5,
+            "rebuild_current_positions": 1, "rebuild_after_yield": 0, "energy_mode": 1,
+            "output_every_step": 1}
+    a = gpu(sc, dict(opts, precision=0))
+    b = gpu(sc, dict(opts, precision=1))
+    params, _ = mlp.train_jc_warm_start(sc["mat"], sc["G"], n_synth=65536, steps=1500,
+                                        batch=2048)
+    b.set_mlp_weights(params)
+    b.set_option("mlp", 1)
+    top = 11 + 3 * 1 + 2                                     # BC 1 (the platen), z
+    for k in range(4):
+        a.step(5000)
+        b.step(5000)
+        errs = {f: rel_l2(b.get_field(f), a.get_field(f)) for f in ("u", "pl_strain", "sigma_eq")}
+        errs["T"] = rel_l2(b.get_field("T") - 20.0, a.get_field("T") - 20.0)
+        errs["reaction_curve"] = rel_l2(b.get_output_series()[:, top],
+                                        a.get_output_series()[:, top])
+        for f, e in errs.items():
+            assert e <= 1e-3, (5000 * (k + 1), f, e, errs)
+    assert b.get_scalar("mlp_used") > 0
+    shortening = -a.get_field("u").reshape(-1, 3)[:, 2].min() / 0.012
+    assert 0.15 < shortening < 0.25, shortening
+    assert a.get_field("pl_strain").max() > 0.1
