@@ -72,7 +72,10 @@ __device__ __forceinline__ uint32_t silu_bf16x2(float z0, float z1) {
 //   layer 1: each thread, FP32 on the CUDA cores: h = SiLU(W1 f + b1), written
 //            in BF16 as its row of A2 (128 x 64)
 //   layer 2: D2 (128 x 64, FP32 in tensor memory) = A2 x B2^T, B2 = W2; four
-//            MMAs of K = 16 accumulate in the same 64 columns
+//            MMAs of K = 16 accumulate in the same 64 columns, two per half
+//            of A2 (hidden units 0-31, then 32-63), the halves passing
+//            through one 8 KB buffer: 8 KB less shared memory per block
+//            (more L1 for the pass's gathers) for one more MMA round trip
 //   layer 3: each thread reads its row of D2, adds b2, applies SiLU and
 //            takes the dot product with W3 (FP32).
 // One thread issues the MMAs and commits them to an mbarrier; every thread
@@ -90,11 +93,11 @@ __device__ __forceinline__ uint32_t silu_bf16x2(float z0, float z1) {
 #define WF_UMMA_W3 8448       // 64 floats
 #define WF_UMMA_B3 8704       // 1 float
 #define WF_UMMA_IMAGE 8832    // bytes of the packed weight image (a multiple of 128)
-#define WF_UMMA_A2 8832       // 128 x 64 BF16 (SBO 1024)
-#define WF_UMMA_MBAR 25216    // mbarrier of the MMAs, 8 bytes
-#define WF_UMMA_TSLOT 25224   // tensor-memory base address, 4 bytes
-#define WF_UMMA_MBAR_W 25232  // mbarrier of the weight-image copy, 8 bytes
-#define WF_UMMA_SMEM 25344    // dynamic shared memory of a kernel that runs the MLP
+#define WF_UMMA_A2 8832       // 128 x 32 BF16, one half of A2 at a time (SBO 512)
+#define WF_UMMA_MBAR 17024    // mbarrier of the MMAs, 8 bytes
+#define WF_UMMA_TSLOT 17032   // tensor-memory base address, 4 bytes
+#define WF_UMMA_MBAR_W 17040  // mbarrier of the weight-image copy, 8 bytes
+#define WF_UMMA_SMEM 17152    // dynamic shared memory of a kernel that runs the MLP
 
 // Layer 1 (4 -> 64) runs on the CUDA cores in FP32: its weights travel as a
 // kernel parameter, so every multiply-add reads its weight from the constant
@@ -171,36 +174,50 @@ static __device__ __forceinline__ float mlp_umma_cta(uint8_t* sm, const uint4* _
   }
   const uint32_t mbar = s0 + WF_UMMA_MBAR;
   // layer 1 and its SiLU (BF16 pairs) into this thread's row of A2
-  uint4* a2 = reinterpret_cast<uint4*>(sm + WF_UMMA_A2 + umma_kmajor_off(tid, 0, 64));
+  uint4* a2 = reinterpret_cast<uint4*>(sm + WF_UMMA_A2 + umma_kmajor_off(tid, 0, 32));
+  bool ok = true;
 #pragma unroll
-  for (int c = 0; c < 4; c++) {
-    uint32_t r[8];
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-      const int n0 = 16 * c + 2 * j;
-      float z0 = l1.b[n0], z1 = l1.b[n0 + 1];
-#pragma unroll
-      for (int k = 0; k < WF_MLP_IN; k++) {
-        z0 = fmaf(l1.w[n0][k], f[k], z0);
-        z1 = fmaf(l1.w[n0 + 1][k], f[k], z1);
-      }
-      r[j] = silu_bf16x2(z0, z1);
+  for (int half = 0; half < 2; half++) {
+    if (half == 1) {
+      // the first half's MMAs have read the buffer once their commit arrived
+      ok = umma::mbar_wait(mbar, 0, kWaitLimit);
+      if (!__syncthreads_and(ok)) break;
+      umma::fence_after_sync();
     }
-    a2[16 * c] = make_uint4(r[0], r[1], r[2], r[3]);       // columns 16c .. 16c+7
-    a2[16 * c + 8] = make_uint4(r[4], r[5], r[6], r[7]);   // columns 16c+8 .. 16c+15
-  }
-  umma::fence_async_smem();
-  umma::fence_before_sync();
-  __syncthreads();
-  umma::fence_after_sync();
-  if (tid == 0) {
 #pragma unroll
-    for (int kk = 0; kk < 4; kk++)
-      umma::mma_bf16(tmem, umma::smem_desc(s0 + WF_UMMA_A2 + 256 * kk, 128, 1024),
-                     umma::smem_desc(s0 + WF_UMMA_B2 + 256 * kk, 128, 1024), kId, kk > 0 ? 1u : 0u);
-    umma::commit(mbar);
+    for (int cc = 0; cc < 2; cc++) {
+      const int c = 2 * half + cc;                      // hidden units 16c .. 16c+15
+      uint32_t r[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const int n0 = 16 * c + 2 * j;
+        float z0 = l1.b[n0], z1 = l1.b[n0 + 1];
+#pragma unroll
+        for (int k = 0; k < WF_MLP_IN; k++) {
+          z0 = fmaf(l1.w[n0][k], f[k], z0);
+          z1 = fmaf(l1.w[n0 + 1][k], f[k], z1);
+        }
+        r[j] = silu_bf16x2(z0, z1);
+      }
+      a2[16 * cc] = make_uint4(r[0], r[1], r[2], r[3]);       // columns 16cc .. 16cc+7
+      a2[16 * cc + 8] = make_uint4(r[4], r[5], r[6], r[7]);   // columns 16cc+8 .. 16cc+15
+    }
+    umma::fence_async_smem();
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    if (tid == 0) {
+#pragma unroll
+      for (int kk = 0; kk < 2; kk++) {
+        const int kg = 2 * half + kk;                   // K step of the whole product
+        umma::mma_bf16(tmem, umma::smem_desc(s0 + WF_UMMA_A2 + 256 * kk, 128, 512),
+                       umma::smem_desc(s0 + WF_UMMA_B2 + 256 * kg, 128, 1024), kId,
+                       kg > 0 ? 1u : 0u);
+      }
+      umma::commit(mbar);
+    }
   }
-  const bool ok = umma::mbar_wait(mbar, 0, kWaitLimit);
+  if (ok) ok = umma::mbar_wait(mbar, 1, kWaitLimit);
   umma::fence_after_sync();
   const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);   // this warp's 32 lanes
   const float* bias2 = reinterpret_cast<const float*>(sm + WF_UMMA_BIAS2);

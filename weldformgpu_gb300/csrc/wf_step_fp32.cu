@@ -498,10 +498,10 @@ __device__ __forceinline__ int stage_halo16(const TileHalo& T, int64_t npad, int
 }
 
 // The stress pass, with the warm-start network compiled in (kMlp: kernel
-// k_stress32_mlp, 96 registers, 5 blocks per SM) or without it (k_stress32,
-// held to 80 registers for 6 blocks per SM; 786k particles: 0.222 -> 0.213
-// ms; with the network's 25 KB of shared memory per block, 6 blocks per SM
-// gain nothing: the L1 they leave is too small).
+// k_stress32_mlp) or without it (k_stress32); both held to 80 registers for
+// 6 blocks per SM (786k particles: 0.222 -> 0.213 ms without the network;
+// with it, 6 blocks gained nothing while the network took 25 KB of shared
+// memory per block, and 0.2335 -> 0.226 ms once it took 17 KB).
 template <bool kMlp>
 __device__ __forceinline__ void stress32_body(StepParams P, Fields F,
                                                   const float4* __restrict__ v32b,
@@ -726,7 +726,7 @@ __device__ __forceinline__ void stress32_body(StepParams P, Fields F,
   if (!isfinite(st)) atomicOr(status, WF_STATUS_NAN);
 }
 
-__global__ void __launch_bounds__(128) k_stress32_mlp(StepParams P, Fields F,
+__global__ void __launch_bounds__(128, 6) k_stress32_mlp(StepParams P, Fields F,
                                                       const float4* __restrict__ v32b,
                                                       float* __restrict__ sigr32,
                                                       const int32_t* __restrict__ nb,
