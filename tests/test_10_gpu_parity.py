@@ -699,3 +699,25 @@ def test_write_csv_reference_columns(tmp_path):
     assert lines[0].startswith("ID, X, Y, Z, posX,posY,posZ,Ux, Uy, Uz")
     assert len(lines) == sc["n"] + 1
     assert len(lines[1].split(",")) == 29
+
+
+def test_release_cache_returns_the_arena_to_the_driver():
+    """wf_destroy keeps the arena cached (device memory stays allocated) and
+    wf_release_cache frees it: the free device memory returns to its level
+    before the domain was created."""
+    torch = pytest.importorskip("torch")
+    from weldformgpu_gb300 import Domain_d, domain as D
+    sc = S.jc_compression(R=0.012, H=0.024)          # ~0.1M particles, an arena of ~140 MB
+    assert D.lib().wf_release_cache() == 0
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    d = S.load(Domain_d(sc["n"]), sc, {"precision": 1})
+    d.step(2)
+    d.close()
+    torch.cuda.synchronize()
+    free_cached = torch.cuda.mem_get_info()[0]
+    assert D.lib().wf_release_cache() == 0
+    torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free0 - free_cached > 64 << 20                  # the arena is still held
+    assert abs(free1 - free0) < 32 << 20, (free0, free_cached, free1)
