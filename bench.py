@@ -603,7 +603,9 @@ def main():
     config = {"workload": WORKLOAD if size == "full" else WORKLOAD + "_" + size, "particles": n,
               "dx_m": sc["dx"], "dt_s": sc["dt"], "nnb": 56, "rebuild_every": 5,
               "return_map": "jc_newton_rtol1e-10", "thermal": "coupled, Taylor-Quinney 0.9",
-              "l2": "inputs larger than L2 (state %.0f MB > 129 MB)" % (n * 1100 / 1e6),
+              "l2": (("inputs larger than L2 (state %.0f MB > 129 MB)" if n * 1100 > 129e6 else
+                      "inputs within L2 (state %.0f MB < 129 MB): a reduced case, not a timing run")
+                     % (n * 1100 / 1e6)),
               "parallelism": "replicas" if ws > 1 else "single",
               "preload_steps": args.preload}
 
@@ -611,6 +613,9 @@ def main():
         if rank != 0:
             return
         cb = cpu_baseline(sc, budget_s=max(5.0, min(30.0, 1.5 * args.steps)))
+        # the CPU arm times steps from the generated state (after one set-up
+        # step), not from the preloaded plastic state of the GPU arm
+        config = dict(config, preload_steps=0)
         line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT,
                 "n_gpus": args.gpus, "steps": args.steps, "warmup": warmup,
                 "higher_is_better": True, "data": "synthetic", "dtype": "f64",
