@@ -6,6 +6,7 @@
 // (src/cuda/SolverFraser.cu:30-409) and ThermalSolve (src/cuda/Thermal.cu:188-260)
 // as sequences of kernel launches on one CUDA stream.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <array>
@@ -37,6 +38,11 @@ void launch_output_row(const StepParams& P, const Fields& F, double* part, doubl
 // kernel ids for wf_set_option("profile_kernel", id)
 enum { KID_NONE = 0, KID_DENSITY = 1, KID_STRESS = 2, KID_ACCEL = 3, KID_INTEGRATE = 4,
        KID_THERMAL = 5, KID_REBUILD = 6, KID_CONTACT = 7 };
+// NVTX range names of the stages (a profiler shows the host-side launch of
+// each stage under its name; without a profiler attached a range costs a
+// few nanoseconds)
+static const char* const kStageNames[] = {"wf", "density", "stress", "accel", "integrate",
+                                          "thermal", "rebuild", "contact"};
 
 struct wf_domain {
   int64_t n = 0, n_solid = 0, npad = 0;
@@ -621,6 +627,7 @@ struct KTimer {
   bool on;
   KTimer(wf_domain* d_, int kid_)
       : d(d_), kid(kid_), on(d_->timing && d_->profile_kernel == kid_) {
+    nvtxRangePushA(kStageNames[kid_]);
     if (on) {
       if (d->ev_used + 2 > d->ev_pool.size()) {
         for (int k = 0; k < 64; k++) {
@@ -637,6 +644,7 @@ struct KTimer {
       record(d, d->ev_pool[d->ev_used + 1]);
       d->ev_used += 2;
     }
+    nvtxRangePop();
   }
 };
 
