@@ -162,7 +162,13 @@ int wf_add_trimesh(wf_domain* d, const double* nodes, int32_t nn, const int32_t*
  *   resident wave of blocks later; 0 off), wave_prefetch_distance (1.0, in
  *   resident waves), list16 (0; 1: 16-bit list offsets for
  *   the mixed passes' global gathers; same results), graph (1), output_interval (1e300),
- *   resume (0), profile_kernel (0). */
+ *   resume (0), profile_kernel (0), debug_checks (0; 1: after every rebuild each
+ *   neighbour list is checked before any pass reads it, a bad entry replaced by the
+ *   particle's own slot, and after every step positions and velocities are checked
+ *   for non-finite values; either sets status bit 6 and the call returns
+ *   WF_ERR_STATE), debug_inject_list_error (a particle id: its list's first entry is
+ *   set out of range after the next list build, for testing the checks; only with
+ *   debug_checks = 1). */
 int wf_set_option(wf_domain* d, const char* key, double value);
 
 /* The per-step BC hook: Domain_d::GeneralAfter (src/cuda/Domain_d.cuh:402,

@@ -721,3 +721,32 @@ def test_release_cache_returns_the_arena_to_the_driver():
     free1 = torch.cuda.mem_get_info()[0]
     assert free0 - free_cached > 64 << 20                  # the arena is still held
     assert abs(free1 - free0) < 32 << 20, (free0, free_cached, free1)
+
+
+def test_debug_checks_repair_and_report_an_injected_list_error():
+    """Option debug_checks (the stand-in for a bounds-checking sanitizer):
+    with nothing wrong it changes no bit of the results; a list entry set out
+    of range on the device (host-side injection, between the list build and
+    the check) is repaired before any pass reads it, reported in status bit 6
+    and by the call's return code, and leaves the state finite.  The injection
+    is refused without the checks."""
+    from weldformgpu_gb300.domain import WeldformError
+    sc = S.compression_cylinder(material="jc", vz_top=-10.0)
+    opts = {"return_map": 1, "precision": 1}
+    ref = gpu(sc, opts)
+    ref.step(30)
+    a = gpu(sc, dict(opts, debug_checks=1))
+    a.step(30)
+    for f in ("x", "v", "u", "sigma_eq", "pl_strain"):
+        assert np.array_equal(a.get_field(f), ref.get_field(f)), f
+    assert int(a.get_scalar("status")) & 64 == 0
+    b = gpu(sc, opts)
+    with pytest.raises(WeldformError):
+        b.set_option("debug_inject_list_error", 100)
+    c = gpu(sc, dict(opts, debug_checks=1))
+    c.set_option("debug_inject_list_error", 100)
+    with pytest.raises(WeldformError):
+        c.step(30)
+    assert int(c.get_scalar("status")) & 64
+    for f in ("x", "v", "sigma_eq"):
+        assert np.all(np.isfinite(c.get_field(f))), f

@@ -161,6 +161,8 @@ struct wf_domain {
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_used = 0;
   bool timing = false;         // inside wf_time_steps
+  int debug_checks = 0;        // option "debug_checks"
+  int64_t inject_list_error = -1;   // option "debug_inject_list_error" (original id), -1 off
   // step-segment graphs (segment_begin / segment_end)
   int graph = 1;                // option "graph"
   bool capturing = false;
@@ -319,6 +321,53 @@ __global__ void __launch_bounds__(256) k_max_dep(int64_t n, const double* eps,
 __global__ void k_copy_d(int64_t n, const double* src, double* dst) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) dst[i] = src[i];
+}
+
+// ---- debug checks (option debug_checks) ---------------------------------
+// The stand-in for a bounds-checking sanitizer: after every neighbour
+// rebuild each list is checked before any pair pass reads it (counts within
+// [0, WF_NB], entries of other particles in [0, n), padding entries the
+// particle's own slot); a bad entry is replaced by the own slot (which adds
+// exact zeros) and WF_STATUS_CHECKS is set, so the passes that follow stay in
+// bounds and the call reports the error.  After every step positions and
+// velocities are checked for non-finite values.
+__global__ void k_check_lists(int64_t n, int64_t npad, int32_t* __restrict__ nb,
+                              int32_t* __restrict__ cnt, int* __restrict__ status) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  bool bad = false;
+  int c = cnt[i];
+  if (c < 0 || c > WF_NB) {
+    bad = true;
+    c = c < 0 ? 0 : WF_NB;
+    cnt[i] = c;
+  }
+  const int cend = (c + WF_NB_BLK - 1) & ~(WF_NB_BLK - 1);
+  for (int k = 0; k < cend; k++) {
+    int32_t& e = nb[nb_at(npad, i, k)];
+    const bool ok = k < c ? (e >= 0 && (int64_t)e < n && (int64_t)e != i) : (int64_t)e == i;
+    if (!ok) {
+      e = (int32_t)i;
+      bad = true;
+    }
+  }
+  if (bad) atomicOr(status, WF_STATUS_CHECKS);
+}
+__global__ void k_check_finite(int64_t n, const double4* __restrict__ xm,
+                               const double4* __restrict__ vd, int* __restrict__ status) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double4 x = xm[i], v = vd[i];
+  if (!(isfinite(x.x) && isfinite(x.y) && isfinite(x.z) && isfinite(v.x) && isfinite(v.y) &&
+        isfinite(v.z) && isfinite(v.w)))
+    atomicOr(status, WF_STATUS_CHECKS);
+}
+// fault injection for the checks' test: the first entry of one particle's
+// list is set out of range, between the list build and k_check_lists
+__global__ void k_inject_list_error(int64_t n, int64_t npad, int32_t slot, int32_t* nb,
+                                    const int32_t* cnt) {
+  if (blockIdx.x == 0 && threadIdx.x == 0 && slot >= 0 && slot < n && cnt[slot] > 0)
+    nb[nb_at(npad, slot, 0)] = (int32_t)(n + 7);
 }
 inline int nblk(int64_t n, int t = 256) { return (int)((n + t - 1) / t); }
 }  // namespace
@@ -711,6 +760,18 @@ static int rebuild(wf_domain* d, bool use_current, bool light = false) {
   launch_nblist(n, d->npad, d->pf2, d->grid, d->cell_count, full ? nullptr : d->s_src, d->nb,
                 d->nbc, d->d_status, s);
   d->launches += 8;
+  if (d->debug_checks) {
+    if (d->inject_list_error >= 0) {
+      int32_t slot = -1;
+      WF_CUDA_OK(cudaMemcpyAsync(&slot, d->inv + d->inject_list_error, sizeof slot,
+                                 cudaMemcpyDeviceToHost, s));
+      WF_CUDA_OK(cudaStreamSynchronize(s));
+      k_inject_list_error<<<1, 32, 0, s>>>(n, d->npad, slot, d->nb, d->nbc);
+      d->inject_list_error = -1;                // once
+    }
+    k_check_lists<<<nblk(n), 256, 0, s>>>(n, d->npad, d->nb, d->nbc, d->d_status);
+    d->launches += 1;
+  }
   // tile halos for the staged mixed passes, sized by the previous build's
   // largest halo (tiles with larger halos gather from global memory)
   d->l16_built = false;
@@ -1101,6 +1162,10 @@ static int solve_step_launches(wf_domain* d) {
     launch_mesh_update(P, F, mixed ? 1 : 0, s);
     d->launches += 3 * P.ncsid;
   }
+  if (d->debug_checks) {
+    k_check_finite<<<nblk(d->n), 256, 0, s>>>(d->n, F.xm, F.vd, d->d_status);
+    d->launches += 1;
+  }
   d->isfirst = false;
   d->time += d->dt;
   if (row_due) {                                                                      // :350-388
@@ -1174,6 +1239,10 @@ static int finish(wf_domain* d) {
   if (rc) return rc;
   WF_CUDA_OK(cudaGetLastError());
   if (d->h_status[0] & WF_STATUS_NAN) return wf_fail(d, WF_ERR_NUMERIC, "non-finite stress detected");
+  if (d->h_status[0] & WF_STATUS_CHECKS)
+    return wf_fail(d, WF_ERR_STATE,
+                   "debug checks: a neighbour-list entry out of range (repaired) or a non-finite "
+                   "position or velocity");
   if (d->h_status[0] & WF_STATUS_MMA_WAIT)
     return wf_fail(d, WF_ERR_CUDA, "a tensor-core completion wait ran out (warm-start network)");
   if (d->h_status[0] & WF_STATUS_NEWTON) {
@@ -1669,6 +1738,15 @@ int wf_set_option(wf_domain* d, const char* key, double v) {
   else if (k == "tile_staging") d->tile_staging = v != 0;   // takes effect at the next rebuild
   else if (k == "list_prefetch") d->list_prefetch = std::max(0, std::min((int)v, WF_NB_BLOCKS));
   else if (k == "state_prefetch") d->state_prefetch = v != 0;
+  else if (k == "debug_checks") d->debug_checks = v != 0;
+  else if (k == "debug_inject_list_error") {
+    // the injected entry is repaired by the list check before any pass reads it
+    if (!d->debug_checks)
+      return wf_fail(d, WF_ERR_ARG, "debug_inject_list_error needs debug_checks = 1");
+    if (!(v >= 0.0) || v >= (double)d->n)
+      return wf_fail(d, WF_ERR_ARG, "debug_inject_list_error: a particle id in [0, n)");
+    d->inject_list_error = (int64_t)v;
+  }
   else if (k == "wave_prefetch") d->wave_prefetch = (int)v;
   else if (k == "wave_prefetch_distance") d->wave_dist = v;
   else if (k == "list16") d->list16 = v != 0;          // takes effect at the next rebuild

@@ -63,6 +63,8 @@ __device__ __forceinline__ void prefetch_l2(const void* p) {
 #define WF_STATUS_MMA_WAIT  8   // a tensor-core completion wait ran out (result discarded)
 #define WF_STATUS_NEWTON   16   // a Newton return map stopped at newton_max_iter unconverged
 #define WF_STATUS_SERIES   32   // the output series was full: rows were dropped
+#define WF_STATUS_CHECKS   64   // option debug_checks: a list entry out of range (repaired
+                                // before use) or a non-finite position or velocity
 
 // Status words (int d_status[WF_STATUS_WORDS]): [0] bits, [1] yield flag,
 // 64-bit counters at [2] Newton iterations, [4] plastic return maps, [6]
