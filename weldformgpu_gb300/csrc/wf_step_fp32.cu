@@ -858,7 +858,7 @@ __device__ __forceinline__ int64_t accel_slot(int& g) {
   return t / kAccelLanes;
 }
 
-__global__ void __launch_bounds__(128, 7) k_accel32(StepParams P, Fields F,
+__global__ void __launch_bounds__(128, 8) k_accel32(StepParams P, Fields F,
                                                  const float4* __restrict__ v32b,
                                                  const float* __restrict__ sigr32,
                                                  float4* __restrict__ a32,
@@ -866,10 +866,21 @@ __global__ void __launch_bounds__(128, 7) k_accel32(StepParams P, Fields F,
                                                  const int32_t* __restrict__ cnt) {
   int g;
   const int64_t i = accel_slot(g);
-  if (i >= P.n || F.perm[i] >= P.n_solid) return;
+  if (i >= P.n) return;
   const float4* sga;
   const float2* sgb;
   sigr32_split(sigr32, P.npad, sga, sgb);
+  if (P.pf_ahead > 0 && g == 0) {
+    const int64_t ia = i + P.pf_ahead;      // the slot this thread's successor will take
+    if (ia < P.n) {
+      prefetch_l2(F.p32 + ia); prefetch_l2(v32b + ia); prefetch_l2(sga + ia);
+      prefetch_l2(sgb + ia); prefetch_l2(cnt + ia); prefetch_l2(F.perm + ia);
+      prefetch_l2(F.id + ia);
+      for (int b = 0; b < P.wave_pf && b < WF_NB_BLOCKS; b++)
+        nb_prefetch(nb, P.npad, ia, b, 2 * kAccelLanes);
+    }
+  }
+  if (F.perm[i] >= P.n_solid) return;
   const AccelSrc src{F.p32, v32b, sga, sgb};
   const float4 af = accel_value(P, F, v32b, sigr32, cnt, i, g, src, NbList32{nb, P.npad, i});
   if (g == 0) a32[i] = af;
@@ -1056,7 +1067,12 @@ void launch_fp32_stress(const StepParams& P, const Fields& F, const float4* v32b
 }
 void launch_fp32_accel(const StepParams& P, const Fields& F, const float4* v32b,
                        const float* sigr32, float4* a32, const NbBuffers& N, cudaStream_t s) {
-  k_accel32<<<blocks_for(P.n * kAccelLanes, 128), 128, 0, s>>>(P, F, v32b, sigr32, a32, N.nb, N.cnt);
+  static size_t c_smem = 0;
+  static int64_t c_val = 0;
+  StepParams Q = P;
+  Q.pf_ahead = !P.wave_pf ? 0 : (int64_t)(P.wave_dist * (double)wave_slots(
+      k_accel32, 128, 0, kAccelLanes, &c_smem, &c_val));
+  k_accel32<<<blocks_for(P.n * kAccelLanes, 128), 128, 0, s>>>(Q, F, v32b, sigr32, a32, N.nb, N.cnt);
 }
 void launch_fp32_accel_integrate(const StepParams& P, const Fields& F, const float4* v32b,
                                  const float* sigr32, const double4* vd2, const NbBuffers& N,
