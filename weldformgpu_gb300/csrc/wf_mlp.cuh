@@ -70,7 +70,7 @@ __device__ __forceinline__ uint32_t silu_bf16x2(float z0, float z1) {
 // tcgen05 inference: one CTA of 128 threads evaluates the network for its 128
 // particles, row m of every matrix being thread m's particle.
 //   layer 1: each thread, FP32 on the CUDA cores: h = SiLU(W1 f + b1), written
-//            in BF16 as its row of A2 (128 x 64)
+//            in BF16 as its row of A2 (128 x 64), half a row at a time
 //   layer 2: D2 (128 x 64, FP32 in tensor memory) = A2 x B2^T, B2 = W2; four
 //            MMAs of K = 16 accumulate in the same 64 columns, two per half
 //            of A2 (hidden units 0-31, then 32-63), the halves passing
@@ -78,8 +78,9 @@ __device__ __forceinline__ uint32_t silu_bf16x2(float z0, float z1) {
 //            (more L1 for the pass's gathers) for one more MMA round trip
 //   layer 3: each thread reads its row of D2, adds b2, applies SiLU and
 //            takes the dot product with W3 (FP32).
-// One thread issues the MMAs and commits them to an mbarrier; every thread
-// waits (bounded) and reads its own row with tcgen05.ld.  The 64 tensor-
+// One thread issues each half's two MMAs and commits them to an mbarrier
+// (phase 0, then 1); every thread waits (bounded) before the second half
+// overwrites the buffer and before reading its own row with tcgen05.ld.  The 64 tensor-
 // memory columns are allocated at kernel entry and freed inside the call.
 //
 // Dynamic shared memory (bytes): the weight image (copied from the packed
