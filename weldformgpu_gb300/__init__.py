@@ -9,7 +9,7 @@ from . import _abi  # noqa: F401
 
 def __getattr__(name):
     # lazy: importing the package must not require the CUDA library
-    if name in ("Domain_d", "WeldformError", "lib", "version"):
+    if name in ("Domain_d", "WeldformError", "lib", "version", "release_cache"):
         from . import domain
         return getattr(domain, name)
     raise AttributeError(name)

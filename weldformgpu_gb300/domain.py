@@ -321,5 +321,13 @@ class Domain_d:
     WriteCSV = write_csv
 
 
+def release_cache():
+    """wf_release_cache: frees the device arena that wf_destroy keeps for the
+    next domain (e.g. before handing the GPU's memory to another library)."""
+    rc = lib().wf_release_cache()
+    if rc != 0:
+        raise WeldformError(rc, "wf_release_cache", "")
+
+
 def version():
     return lib().wf_version().decode()
