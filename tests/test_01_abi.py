@@ -225,3 +225,19 @@ def test_lsdyna_reader_known_answer(tmp_path):
     empty = tmp_path / "empty.k"
     empty.write_text("*NODE\n       1             0.0             0.0             0.0\n")
     assert fn(str(empty).encode(), None, None, None) == -1      # no SPH element
+
+
+def test_header_compiles_as_c99_and_cpp():
+    """The boundary is a C ABI: the header alone compiles as C99 and as C++
+    (what a cgo, JNI or plain C caller would include)."""
+    import shutil
+    import subprocess
+    hdr = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                       "weldform_gb300.h")
+    gcc, gxx = shutil.which("gcc"), shutil.which("g++")
+    if gcc is None or gxx is None:
+        pytest.skip("no host compiler")
+    for cmd in ([gcc, "-fsyntax-only", "-x", "c", "-std=c99", "-Wall", "-Werror", hdr],
+                [gxx, "-fsyntax-only", "-x", "c++", "-Wall", "-Werror", hdr]):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, (cmd, r.stderr)
